@@ -1,0 +1,858 @@
+// C ABI of the GB300 G-VOM path (include/gvom_gb300.h): instance state,
+// device memory, stream ordering and the host side of Gvom.__init__,
+// Process_pointcloud and combine_maps (scripts/gvom.py:21-442).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/gvom_gb300.h"
+#include "gvom_internal.cuh"
+
+
+using namespace gvom;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(expr)                                                                         \
+    do {                                                                                       \
+        cudaError_t e__ = (expr);                                                              \
+        if (e__ != cudaSuccess)                                                                \
+            return fail(GVOM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e__));   \
+    } while (0)
+
+struct Slot {
+    int *idx = nullptr;
+    VoxelRec *rec = nullptr;
+    long long cap = 0;
+    double od[3] = {0, 0, 0};
+    bool valid = false;
+};
+
+}  // namespace
+
+struct GvomHandle {
+    GvomParams p;
+    Geom g;
+    int B = 0;
+    cudaStream_t own = nullptr, st = nullptr;
+    std::mutex mu;
+    std::vector<Slot> slots;
+    long long buffer_index = 0, last_buffer_index = 0;
+    double ego[3] = {0, 0, 0};
+    // combined map, double buffered (current / previous)
+    int *cidx[2] = {nullptr, nullptr};
+    VoxelRec *crec[2] = {nullptr, nullptr};
+    double cod[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    int cur = 0;
+    bool have_comb = false;
+    // per-scan scratch
+    std::vector<unsigned long long *> cnt;  // one dense count array per concurrent scan
+    float4 *prec = nullptr, *sorted = nullptr;
+    int *prank = nullptr;
+    long long pcap = 0;
+    void *dpts = nullptr;
+    size_t dpts_bytes = 0;
+    ScanCounters *d_ctr = nullptr;  // kMaxBatch
+    int *d_slotC = nullptr;         // per ring slot occupied count
+    int *d_combC = nullptr;         // 2 (per combined buffer)
+    int last_ctr = -1;              // counters of the last processed scan
+    // 2-D maps
+    double *height = nullptr, *inferred = nullptr, *slope_x = nullptr, *slope_y = nullptr, *rough = nullptr,
+           *guess = nullptr;
+    int *pos_density = nullptr, *pos = nullptr, *neg = nullptr, *vis = nullptr;
+    bool have_maps = false;
+    // debug
+    int *d_dbg = nullptr;
+    long long bytes = 0;
+    int pageable_access = 0;
+};
+
+namespace {
+
+int dalloc(GvomHandle *h, void **p, size_t bytes) {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(GVOM_ERR_OOM, std::string("device allocation of ") + std::to_string(bytes) +
+                                      " bytes failed: " + cudaGetErrorString(e));
+    }
+    h->bytes += (long long)bytes;
+    return GVOM_OK;
+}
+
+template <typename T>
+int dalloc_t(GvomHandle *h, T **p, size_t n) {
+    return dalloc(h, reinterpret_cast<void **>(p), n * sizeof(T));
+}
+
+void dfree(GvomHandle *h, void *p, size_t bytes) {
+    if (p) {
+        cudaFree(p);
+        h->bytes -= (long long)bytes;
+    }
+}
+
+long long ext_cells(const Geom &g) { return (long long)g.Xe * g.Xe * g.Ze; }
+
+int check_params(const GvomParams *p) {
+    if (!p) return fail(GVOM_ERR_ARG, "params is NULL");
+    if (p->xy_size <= 0 || p->z_size <= 0 || p->buffer_size <= 0)
+        return fail(GVOM_ERR_ARG, "xy_size, z_size and buffer_size must be positive");
+    if (p->buffer_size > kMaxSources - 1)
+        return fail(GVOM_ERR_ARG, "buffer_size above " + std::to_string(kMaxSources - 1) + " is not supported");
+    if (!(p->xy_resolution > 0) || !(p->z_resolution > 0))
+        return fail(GVOM_ERR_ARG, "resolutions must be positive");
+    if (p->xy_eigen_dist < 0 || p->z_eigen_dist < 0 || p->xy_eigen_dist > 8 || p->z_eigen_dist > 8)
+        return fail(GVOM_ERR_ARG, "eigen distances must be in [0, 8]");
+    const long long V = (long long)p->xy_size * p->xy_size * p->z_size;
+    if (V >= (1LL << 31) - 1) return fail(GVOM_ERR_ARG, "grid too large (voxel count must fit int32)");
+    return GVOM_OK;
+}
+
+// grow the point scratch so that `n` points fit
+int ensure_points(GvomHandle *h, long long n) {
+    if (n <= h->pcap) return GVOM_OK;
+    long long cap = std::max<long long>(n, h->pcap * 2);
+    cap = std::max<long long>(cap, 4096);
+    if (cap >= (1LL << 31)) return fail(GVOM_ERR_ARG, "too many points");
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    dfree(h, h->prec, h->pcap * sizeof(float4));
+    dfree(h, h->sorted, h->pcap * sizeof(float4));
+    dfree(h, h->prank, h->pcap * sizeof(int));
+    h->prec = h->sorted = nullptr;
+    h->prank = nullptr;
+    h->pcap = 0;
+    int rc;
+    if ((rc = dalloc_t(h, &h->prec, cap)) || (rc = dalloc_t(h, &h->sorted, cap)) || (rc = dalloc_t(h, &h->prank, cap)))
+        return rc;
+    h->pcap = cap;
+    return GVOM_OK;
+}
+
+int ensure_dpts(GvomHandle *h, size_t bytes) {
+    if (bytes <= h->dpts_bytes) return GVOM_OK;
+    size_t cap = std::max(bytes, h->dpts_bytes * 2);
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    dfree(h, h->dpts, h->dpts_bytes);
+    h->dpts = nullptr;
+    h->dpts_bytes = 0;
+    int rc = dalloc(h, &h->dpts, cap);
+    if (rc) return rc;
+    h->dpts_bytes = cap;
+    return GVOM_OK;
+}
+
+int ensure_cnt(GvomHandle *h, int nscans) {
+    while ((int)h->cnt.size() < nscans) {
+        unsigned long long *c = nullptr;
+        const long long ve = ext_cells(h->g);
+        int rc = dalloc_t(h, &c, (size_t)ve);
+        if (rc) return rc;
+        CUDA_TRY(cudaMemsetAsync(c, 0, (size_t)ve * 8, h->st));
+        h->cnt.push_back(c);
+    }
+    return GVOM_OK;
+}
+
+int ensure_slot(GvomHandle *h, int s, long long need) {
+    Slot &sl = h->slots[s];
+    need = std::min<long long>(need, h->g.V);
+    need = std::max<long long>(need, 1);
+    if (sl.cap >= need) return GVOM_OK;
+    long long cap = std::min<long long>(h->g.V, std::max<long long>(need, sl.cap * 2));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    dfree(h, sl.rec, sl.cap * sizeof(VoxelRec));
+    sl.rec = nullptr;
+    sl.cap = 0;
+    int rc = dalloc_t(h, &sl.rec, (size_t)cap);
+    if (rc) return rc;
+    sl.cap = cap;
+    return GVOM_OK;
+}
+
+void ray_origin(const GvomHandle *h, const double ego[3], double od[3]) {
+    // scripts/gvom.py:138-141
+    od[0] = std::floor((ego[0] / h->p.xy_resolution) - (double)h->g.X / 2.0);
+    od[1] = std::floor((ego[1] / h->p.xy_resolution) - (double)h->g.X / 2.0);
+    od[2] = std::floor((ego[2] / h->p.z_resolution) - (double)h->g.Z / 2.0);
+}
+
+int bytes_of(int dtype) { return dtype == GVOM_F64 ? 8 : 4; }
+
+struct ScanIn {
+    const void *dev_pts;
+    int dtype, tdtype;
+    long long n, stride;
+    double ego[3];
+    double T[16];
+};
+
+// Enqueue the per-scan pipeline for `k` scans whose points are in device memory.
+int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
+    const int k = (int)scans.size();
+    if (k == 0) return GVOM_OK;
+    int rc;
+    if ((rc = ensure_cnt(h, k))) return rc;
+    long long total_pts = 0, max_n = 0;
+    for (auto &s : scans) {
+        total_pts += s.n;
+        max_n = std::max(max_n, s.n);
+    }
+    if ((rc = ensure_points(h, std::max<long long>(total_pts, 1)))) return rc;
+    ProcessConst pc;
+    pc.g = h->g;
+    pc.xy_res = h->p.xy_resolution;
+    pc.z_res = h->p.z_resolution;
+    pc.md2 = h->p.min_distance * h->p.min_distance;
+    pc.step_cap = 2 * std::max(h->g.X, h->g.Z) + 8;
+    pc.nscans = k;
+    ScanDesc table[kMaxBatch];
+    std::memset(table, 0, sizeof(table));
+    int block = 0;
+    long long base = 0;
+    std::vector<int> slot_of(k);
+    for (int i = 0; i < k; i++) {
+        const ScanIn &s = scans[i];
+        const int slot = (int)((h->buffer_index + i) % h->B);
+        slot_of[i] = slot;
+        if ((rc = ensure_slot(h, slot, s.n))) return rc;
+        ScanDesc &d = table[i];
+        d.pts = s.dev_pts;
+        d.n = s.n;
+        d.stride = s.stride;
+        d.tmode = s.tdtype == GVOM_NONE ? 0 : (s.tdtype == GVOM_F32 ? 1 : 2);
+        for (int r = 0; r < 12; r++) d.T[r] = s.T[r];
+        ray_origin(h, s.ego, d.od);
+        bool fast = true;
+        for (int a = 0; a < 3; a++) {
+            d.oi[a] = (int)d.od[a];
+            if (std::fabs(d.od[a]) >= 16777216.0) fast = false;
+        }
+        d.fast_floor = fast ? 1 : 0;
+        d.pt0[0] = (float)(s.ego[0] / h->p.xy_resolution);
+        d.pt0[1] = (float)(s.ego[1] / h->p.xy_resolution);
+        d.pt0[2] = (float)(s.ego[2] / h->p.z_resolution);
+        d.slot = slot;
+        d.block_begin = block;
+        d.nblocks = (int)((s.n + 255) / 256);
+        block += d.nblocks;
+        d.pt_base = base;
+        base += s.n;
+        d.cnt = h->cnt[i];
+        d.idx = h->slots[slot].idx;
+        d.rec = h->slots[slot].rec;
+        d.rec_cap = h->slots[slot].cap;
+        d.ctr = h->d_ctr + i;
+    }
+    CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * k, h->st));
+    CUDA_TRY(launch_process(pc, table, k, block, (int)std::min<long long>(max_n, h->g.V), scans[0].dtype, h->prec,
+                            h->prank, h->sorted, h->st));
+    for (int i = 0; i < k; i++) {
+        CUDA_TRY(cudaMemcpyAsync(h->d_slotC + slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+        Slot &sl = h->slots[slot_of[i]];
+        for (int a = 0; a < 3; a++) sl.od[a] = table[i].od[a];
+        sl.valid = true;
+    }
+    // ring bookkeeping (scripts/gvom.py:198-216) and the latest ego (:110-112)
+    for (int a = 0; a < 3; a++) h->ego[a] = scans[k - 1].ego[a];
+    h->last_buffer_index = slot_of[k - 1];
+    h->buffer_index = (slot_of[k - 1] + 1) % h->B;
+    h->last_ctr = k - 1;
+    return GVOM_OK;
+}
+
+int fill_scan(GvomHandle *h, ScanIn &s, int dtype, long long n, long long stride, const double ego[3],
+              const void *T, int tdtype) {
+    if (dtype != GVOM_F32 && dtype != GVOM_F64) return fail(GVOM_ERR_ARG, "points dtype must be float32 or float64");
+    if (n < 0) return fail(GVOM_ERR_ARG, "negative point count");
+    if (stride < 3) return fail(GVOM_ERR_ARG, "row_stride must be >= 3");
+    if (!ego) return fail(GVOM_ERR_ARG, "ego position is NULL");
+    if (T && tdtype != GVOM_F32 && tdtype != GVOM_F64) return fail(GVOM_ERR_ARG, "transform dtype must be float32 or float64");
+    s.dtype = dtype;
+    s.n = n;
+    s.stride = stride;
+    for (int a = 0; a < 3; a++) s.ego[a] = ego[a];
+    s.tdtype = T ? tdtype : GVOM_NONE;
+    for (int r = 0; r < 16; r++) s.T[r] = 0.0;
+    if (T) {
+        for (int r = 0; r < 16; r++)
+            s.T[r] = tdtype == GVOM_F64 ? static_cast<const double *>(T)[r] : (double)static_cast<const float *>(T)[r];
+    }
+    (void)h;
+    return GVOM_OK;
+}
+
+bool is_pinned_host(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *gvom_last_error(void) { return g_err.c_str(); }
+
+const char *gvom_version(void) { return "gvom_gb300 0.1 (sm_103a)"; }
+
+int gvom_create(const GvomParams *params, GvomHandle **out) {
+    if (!out) return fail(GVOM_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int rc = check_params(params);
+    if (rc) return rc;
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    GvomHandle *h = new GvomHandle();
+    h->p = *params;
+    Geom &g = h->g;
+    g.X = params->xy_size;
+    g.Z = params->z_size;
+    g.exy = params->xy_eigen_dist;
+    g.ez = params->z_eigen_dist;
+    g.Xe = g.X + 2 * g.exy;
+    g.Ze = g.Z + 2 * g.ez;
+    g.V = (long long)g.X * g.X * g.Z;
+    g.Vext = ext_cells(g);
+    h->B = params->buffer_size;
+    h->slots.resize(h->B);
+    cudaDeviceGetAttribute(&h->pageable_access, cudaDevAttrPageableMemoryAccess, dev);
+    // admission: the resident footprint must fit in free device memory with margin
+    const long long X2 = (long long)g.X * g.X;
+    const long long need = (long long)h->B * g.V * 4 + 2 * g.V * (4 + (long long)sizeof(VoxelRec)) + g.Vext * 8 +
+                           X2 * (6 * 8 + 4 * 4) + (64LL << 20);
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        delete h;
+        return fail(GVOM_ERR_CUDA, "cudaMemGetInfo failed");
+    }
+    if ((long long)fr < need) {
+        delete h;
+        return fail(GVOM_ERR_OOM, "admission refused: instance needs " + std::to_string(need) + " bytes, " +
+                                      std::to_string((long long)fr) + " free");
+    }
+    if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        delete h;
+        return fail(GVOM_ERR_CUDA, "stream creation failed");
+    }
+    h->st = h->own;
+    auto bail = [&](int code) {
+        gvom_destroy(h);
+        return code;
+    };
+    for (int s = 0; s < h->B; s++) {
+        if ((rc = dalloc_t(h, &h->slots[s].idx, (size_t)g.V))) return bail(rc);
+    }
+    for (int b = 0; b < 2; b++) {
+        if ((rc = dalloc_t(h, &h->cidx[b], (size_t)g.V))) return bail(rc);
+        if ((rc = dalloc_t(h, &h->crec[b], (size_t)g.V))) return bail(rc);
+    }
+    // counters + scan table
+    if ((rc = dalloc(h, reinterpret_cast<void **>(&h->d_ctr), sizeof(ScanCounters) * kMaxBatch)))
+        return bail(rc);
+    if ((rc = dalloc_t(h, &h->d_slotC, (size_t)h->B))) return bail(rc);
+    if ((rc = dalloc_t(h, &h->d_combC, 2))) return bail(rc);
+    double **maps[6] = {&h->height, &h->inferred, &h->slope_x, &h->slope_y, &h->rough, &h->guess};
+    for (auto m : maps)
+        if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
+    int **imaps[4] = {&h->pos_density, &h->pos, &h->neg, &h->vis};
+    for (auto m : imaps)
+        if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
+    if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->B, h->st) != cudaSuccess ||
+        cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 2, h->st) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(GVOM_ERR_CUDA, "memset failed"));
+    }
+    if ((rc = ensure_cnt(h, 1))) return bail(rc);
+    if (cudaStreamSynchronize(h->st) != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(GVOM_ERR_CUDA, "initialisation failed"));
+    }
+    *out = h;
+    return GVOM_OK;
+}
+
+int gvom_destroy(GvomHandle *h) {
+    if (!h) return GVOM_OK;
+    if (h->st) cudaStreamSynchronize(h->st);
+    if (h->own) cudaStreamSynchronize(h->own);
+    for (auto &s : h->slots) {
+        cudaFree(s.idx);
+        cudaFree(s.rec);
+    }
+    for (int b = 0; b < 2; b++) {
+        cudaFree(h->cidx[b]);
+        cudaFree(h->crec[b]);
+    }
+    for (auto c : h->cnt) cudaFree(c);
+    cudaFree(h->prec);
+    cudaFree(h->sorted);
+    cudaFree(h->prank);
+    cudaFree(h->dpts);
+    cudaFree(h->d_ctr);
+    cudaFree(h->d_slotC);
+    cudaFree(h->d_combC);
+    cudaFree(h->height);
+    cudaFree(h->inferred);
+    cudaFree(h->slope_x);
+    cudaFree(h->slope_y);
+    cudaFree(h->rough);
+    cudaFree(h->guess);
+    cudaFree(h->pos_density);
+    cudaFree(h->pos);
+    cudaFree(h->neg);
+    cudaFree(h->vis);
+    cudaFree(h->d_dbg);
+    if (h->own) cudaStreamDestroy(h->own);
+    delete h;
+    return GVOM_OK;
+}
+
+int gvom_process(GvomHandle *h, const void *points, int32_t dtype, int64_t n, int64_t row_stride,
+                 const double ego[3], const void *transform, int32_t transform_dtype) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    if (n > 0 && !points) return fail(GVOM_ERR_ARG, "points is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    ScanIn s;
+    int rc = fill_scan(h, s, dtype, n, row_stride, ego, transform, transform_dtype);
+    if (rc) return rc;
+    const size_t bytes = (size_t)n * (size_t)row_stride * (size_t)bytes_of(dtype);
+    if ((rc = ensure_dpts(h, bytes))) return rc;
+    if (bytes) {
+        CUDA_TRY(cudaMemcpyAsync(h->dpts, points, bytes, cudaMemcpyHostToDevice, h->st));
+    }
+    s.dev_pts = h->dpts;
+    std::vector<ScanIn> v{s};
+    if ((rc = enqueue_scans(h, v))) return rc;
+    if (bytes && is_pinned_host(points)) CUDA_TRY(cudaStreamSynchronize(h->st));  // caller may reuse its buffer
+    return GVOM_OK;
+}
+
+int gvom_process_device(GvomHandle *h, const void *d_points, int32_t dtype, int64_t n, int64_t row_stride,
+                        const double ego[3], const void *transform, int32_t transform_dtype) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    if (n > 0 && !d_points) return fail(GVOM_ERR_ARG, "points is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    ScanIn s;
+    int rc = fill_scan(h, s, dtype, n, row_stride, ego, transform, transform_dtype);
+    if (rc) return rc;
+    s.dev_pts = d_points;
+    std::vector<ScanIn> v{s};
+    return enqueue_scans(h, v);
+}
+
+int gvom_process_batch(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    if (n_scans < 0 || (n_scans > 0 && !scans)) return fail(GVOM_ERR_ARG, "bad scan list");
+    if (n_scans == 0) return GVOM_OK;
+    std::lock_guard<std::mutex> lk(h->mu);
+    // scans that a later scan of the same batch overwrites (ring wrap) only update the ego
+    const int first = std::max(0, n_scans - std::min(h->B, kMaxBatch));
+    const int dt = scans[first].dtype;
+    std::vector<ScanIn> v;
+    size_t total_bytes = 0;
+    for (int i = first; i < n_scans; i++) {
+        ScanIn s;
+        int rc = fill_scan(h, s, scans[i].dtype, scans[i].n, scans[i].row_stride, scans[i].ego, scans[i].transform,
+                           scans[i].transform_dtype);
+        if (rc) return rc;
+        if (s.dtype != dt) return fail(GVOM_ERR_ARG, "all scans of a batch must share one points dtype");
+        if (s.n > 0 && !scans[i].points) return fail(GVOM_ERR_ARG, "points is NULL");
+        total_bytes += (size_t)s.n * (size_t)s.stride * (size_t)bytes_of(s.dtype);
+        total_bytes = (total_bytes + 255) & ~(size_t)255;
+        v.push_back(s);
+    }
+    int rc;
+    if (!points_on_device) {
+        if ((rc = ensure_dpts(h, total_bytes))) return rc;
+        size_t off = 0;
+        bool pinned = false;
+        for (size_t j = 0; j < v.size(); j++) {
+            const GvomScan &sc = scans[first + (int)j];
+            const size_t b = (size_t)v[j].n * (size_t)v[j].stride * (size_t)bytes_of(v[j].dtype);
+            if (b) {
+                CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h->dpts) + off, sc.points, b, cudaMemcpyHostToDevice, h->st));
+                pinned = pinned || is_pinned_host(sc.points);
+            }
+            v[j].dev_pts = static_cast<char *>(h->dpts) + off;
+            off = (off + b + 255) & ~(size_t)255;
+        }
+        if ((rc = enqueue_scans(h, v))) return rc;
+        if (pinned) CUDA_TRY(cudaStreamSynchronize(h->st));
+    } else {
+        for (size_t j = 0; j < v.size(); j++) v[j].dev_pts = scans[first + (int)j].points;
+        if ((rc = enqueue_scans(h, v))) return rc;
+    }
+    for (int a = 0; a < 3; a++) h->ego[a] = scans[n_scans - 1].ego[a];
+    return GVOM_OK;
+}
+
+static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, double *rough, int32_t *vis,
+                        bool to_host) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    const Slot &ls = h->slots[h->last_buffer_index];
+    if (!ls.valid) return fail(GVOM_NO_DATA, "ERROR: No data in buffer");
+    const int nb = h->have_comb ? 1 - h->cur : 0;  // buffer receiving the new combined map
+    MergeParams mp;
+    std::memset(&mp, 0, sizeof(mp));
+    mp.g = h->g;
+    for (int a = 0; a < 3; a++) mp.co[a] = ls.od[a];
+    int ns = 0;
+    for (int i = 0; i < h->B; i++) {
+        const Slot &s = h->slots[i];
+        if (!s.valid) continue;
+        MergeSrc &m = mp.src[ns++];
+        m.idx = s.idx;
+        m.rec = s.rec;
+        m.dx = (int)(mp.co[0] - s.od[0]);
+        m.dy = (int)(mp.co[1] - s.od[1]);
+        m.dz = (int)(mp.co[2] - s.od[2]);
+        m.is_last = 0;
+    }
+    if (h->have_comb) {
+        MergeSrc &m = mp.src[ns++];
+        m.idx = h->cidx[h->cur];
+        m.rec = h->crec[h->cur];
+        m.dx = (int)(mp.co[0] - h->cod[h->cur][0]);
+        m.dy = (int)(mp.co[1] - h->cod[h->cur][1]);
+        m.dz = (int)(mp.co[2] - h->cod[h->cur][2]);
+        m.is_last = 1;
+    }
+    mp.nsrc = ns;
+    mp.out_idx = h->cidx[nb];
+    mp.out_rec = h->crec[nb];
+    mp.out_count = h->d_combC + nb;
+    mp.xy_res = h->p.xy_resolution;
+    mp.z_res = h->p.z_resolution;
+    for (int a = 0; a < 3; a++) mp.ego[a] = h->ego[a];
+    mp.robot_r2 = h->p.robot_radius * h->p.robot_radius;
+    mp.disc_h = h->ego[2] - h->p.ground_to_lidar_height;
+    mp.pos_thr = h->p.positive_obstacle_threshold;
+    mp.robot_h = h->p.robot_height;
+    mp.height = h->height;
+    mp.inferred = h->inferred;
+    mp.pos_density = h->pos_density;
+    Maps2DParams m2;
+    m2.X = h->g.X;
+    m2.xy_res = h->p.xy_resolution;
+    m2.slope_thr = h->p.slope_obstacle_threshold;
+    m2.neg_thr = h->p.negative_obstacle_threshold;
+    m2.height = h->height;
+    m2.inferred = h->inferred;
+    m2.pos_density = h->pos_density;
+    m2.slope_x = h->slope_x;
+    m2.slope_y = h->slope_y;
+    m2.rough = h->rough;
+    m2.guess = h->guess;
+    m2.pos = h->pos;
+    m2.neg = h->neg;
+    m2.vis = h->vis;
+    CUDA_TRY(cudaMemsetAsync(mp.out_count, 0, sizeof(int), h->st));
+    CUDA_TRY(launch_combine(mp, m2, h->st));
+    for (int a = 0; a < 3; a++) h->cod[nb][a] = mp.co[a];
+    h->cur = nb;
+    h->have_comb = true;
+    h->have_maps = true;
+    if (origin) {
+        // scripts/gvom.py:385-388
+        origin[0] = mp.co[0] * h->p.xy_resolution;
+        origin[1] = mp.co[1] * h->p.xy_resolution;
+        origin[2] = mp.co[2] * h->p.z_resolution;
+    }
+    const size_t X2 = (size_t)h->g.X * h->g.X;
+    const cudaMemcpyKind kind = to_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (pos) CUDA_TRY(cudaMemcpyAsync(pos, h->pos, X2 * 4, kind, h->st));
+    if (neg) CUDA_TRY(cudaMemcpyAsync(neg, h->neg, X2 * 4, kind, h->st));
+    if (rough) CUDA_TRY(cudaMemcpyAsync(rough, h->rough, X2 * 8, kind, h->st));
+    if (vis) CUDA_TRY(cudaMemcpyAsync(vis, h->vis, X2 * 4, kind, h->st));
+    if (to_host) CUDA_TRY(cudaStreamSynchronize(h->st));
+    return GVOM_OK;
+}
+
+int gvom_combine(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, double *roughness, int32_t *visibility) {
+    return combine_impl(h, origin, pos, neg, roughness, visibility, true);
+}
+
+int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t *d_neg, double *d_roughness,
+                        int32_t *d_visibility) {
+    return combine_impl(h, origin, d_pos, d_neg, d_roughness, d_visibility, false);
+}
+
+int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64_t *rows) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->have_comb) return fail(GVOM_NO_DATA, "No data");
+    const long long V = h->g.V;
+    const int chunk = debug_chunk();
+    const int nblocks = (int)((V + chunk - 1) / chunk);
+    if (!h->d_dbg) {
+        int rc = dalloc_t(h, &h->d_dbg, (size_t)nblocks + 1);
+        if (rc) return rc;
+    }
+    CUDA_TRY(launch_debug_count(h->cidx[h->cur], V, h->d_dbg, nblocks, h->st));
+    std::vector<int> counts(nblocks);
+    CUDA_TRY(cudaMemcpyAsync(counts.data(), h->d_dbg, sizeof(int) * nblocks, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    long long tot = 0;
+    for (int b = 0; b < nblocks; b++) {
+        const int c = counts[b];
+        counts[b] = (int)tot;
+        tot += c;
+    }
+    if (rows) *rows = tot;
+    if (!out || tot == 0) return GVOM_OK;
+    CUDA_TRY(cudaMemcpyAsync(h->d_dbg, counts.data(), sizeof(int) * nblocks, cudaMemcpyHostToDevice, h->st));
+    float *dout = nullptr;
+    const long long nrow = std::min<long long>(tot, capacity_rows);
+    int rc = dalloc_t(h, &dout, (size_t)std::max<long long>(nrow, 1) * 8);
+    if (rc) return rc;
+    DebugVoxParams p;
+    p.idx = h->cidx[h->cur];
+    p.rec = h->crec[h->cur];
+    p.block_off = h->d_dbg;
+    p.V = V;
+    p.X = h->g.X;
+    for (int a = 0; a < 3; a++) p.co[a] = h->cod[h->cur][a];
+    p.xy_res = h->p.xy_resolution;
+    p.z_res = h->p.z_resolution;
+    p.out = dout;
+    p.cap = nrow;
+    cudaError_t e = launch_debug_voxels(p, nblocks, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, (size_t)nrow * 8 * sizeof(float), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    dfree(h, dout, (size_t)std::max<long long>(nrow, 1) * 8 * sizeof(float));
+    if (e != cudaSuccess) return fail(GVOM_ERR_CUDA, std::string("debug voxel export: ") + cudaGetErrorString(e));
+    return GVOM_OK;
+}
+
+static int debug_maps(GvomHandle *h, float *out_h, float *out_i) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->have_maps) return fail(GVOM_NO_DATA, "No data");
+    if (!out_h && !out_i) return fail(GVOM_ERR_ARG, "output is NULL");
+    const size_t X2 = (size_t)h->g.X * h->g.X;
+    const size_t cols = out_h ? 7 : 3;
+    float *dout = nullptr;
+    int rc = dalloc_t(h, &dout, X2 * cols);
+    if (rc) return rc;
+    DebugMapParams p;
+    p.X = h->g.X;
+    for (int a = 0; a < 3; a++) p.co[a] = h->cod[h->cur][a];
+    p.xy_res = h->p.xy_resolution;
+    p.z_res = h->p.z_resolution;
+    p.height = h->height;
+    p.rough = h->rough;
+    p.slope_x = h->slope_x;
+    p.slope_y = h->slope_y;
+    p.guess = h->guess;
+    p.out_h = out_h ? dout : nullptr;
+    p.out_i = out_h ? nullptr : dout;
+    cudaError_t e = launch_debug_maps(p, h->st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(out_h ? (void *)out_h : (void *)out_i, dout, X2 * cols * sizeof(float),
+                            cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    dfree(h, dout, X2 * cols * sizeof(float));
+    if (e != cudaSuccess) return fail(GVOM_ERR_CUDA, std::string("debug map export: ") + cudaGetErrorString(e));
+    return GVOM_OK;
+}
+
+int gvom_debug_height_map(GvomHandle *h, float *out) { return debug_maps(h, out, nullptr); }
+
+int gvom_debug_inferred_height_map(GvomHandle *h, float *out) { return debug_maps(h, nullptr, out); }
+
+int gvom_ring_state(GvomHandle *h, int64_t *buffer_index, int64_t *last_buffer_index) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (buffer_index) *buffer_index = h->buffer_index;
+    if (last_buffer_index) *last_buffer_index = h->last_buffer_index;
+    return GVOM_OK;
+}
+
+static int read_int(GvomHandle *h, const int *d, int *v) {
+    CUDA_TRY(cudaMemcpyAsync(v, d, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    return GVOM_OK;
+}
+
+int gvom_slot_count(GvomHandle *h, int32_t slot, int64_t *count) {
+    if (!h || !count) return fail(GVOM_ERR_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (slot < 0 || slot >= h->B) return fail(GVOM_ERR_ARG, "slot out of range");
+    if (!h->slots[slot].valid) {
+        *count = -1;
+        return GVOM_OK;
+    }
+    int c = 0;
+    int rc = read_int(h, h->d_slotC + slot, &c);
+    if (rc) return rc;
+    *count = c;
+    return GVOM_OK;
+}
+
+// unpack records into the reference's per-array layout
+static int copy_records(GvomHandle *h, const VoxelRec *d_rec, long long C, int32_t *hit, int32_t *total, float *min_h,
+                        float *metrics, float *eigen) {
+    if (C <= 0) return GVOM_OK;
+    if (!hit && !total && !min_h && !metrics && !eigen) return GVOM_OK;
+    std::vector<VoxelRec> r((size_t)C);
+    CUDA_TRY(cudaMemcpyAsync(r.data(), d_rec, sizeof(VoxelRec) * C, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    for (long long c = 0; c < C; c++) {
+        const VoxelRec &v = r[c];
+        if (hit) hit[c] = v.hit;
+        if (total) total[c] = v.total;
+        if (min_h) min_h[c] = v.min_h;
+        if (metrics) {
+            float *m = metrics + c * 10;
+            m[0] = v.mean[0];
+            m[1] = v.mean[1];
+            m[2] = v.mean[2];
+            for (int t = 0; t < 6; t++) m[3 + t] = v.cov[t];
+            m[9] = v.count;
+        }
+        if (eigen) {
+            eigen[c * 3 + 0] = v.aux[0];
+            eigen[c * 3 + 1] = v.aux[1];
+            eigen[c * 3 + 2] = v.aux[2];
+        }
+    }
+    return GVOM_OK;
+}
+
+int gvom_get_slot(GvomHandle *h, int32_t slot, int32_t *index, int32_t *hit, int32_t *total, float *min_height,
+                  float *metrics, double origin[3]) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (slot < 0 || slot >= h->B) return fail(GVOM_ERR_ARG, "slot out of range");
+    const Slot &s = h->slots[slot];
+    if (!s.valid) return fail(GVOM_NO_DATA, "slot is empty");
+    int C = 0;
+    int rc = read_int(h, h->d_slotC + slot, &C);
+    if (rc) return rc;
+    if (index) {
+        CUDA_TRY(cudaMemcpyAsync(index, s.idx, sizeof(int) * h->g.V, cudaMemcpyDeviceToHost, h->st));
+        CUDA_TRY(cudaStreamSynchronize(h->st));
+    }
+    if ((rc = copy_records(h, s.rec, C, hit, total, min_height, metrics, nullptr))) return rc;
+    if (origin)
+        for (int a = 0; a < 3; a++) origin[a] = s.od[a];
+    return GVOM_OK;
+}
+
+int gvom_combined_count(GvomHandle *h, int64_t *count) {
+    if (!h || !count) return fail(GVOM_ERR_ARG, "NULL argument");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->have_comb) {
+        *count = -1;
+        return GVOM_OK;
+    }
+    int c = 0;
+    int rc = read_int(h, h->d_combC + h->cur, &c);
+    if (rc) return rc;
+    *count = c;
+    return GVOM_OK;
+}
+
+int gvom_get_combined(GvomHandle *h, int32_t *index, int32_t *hit, int32_t *total, float *min_height, float *metrics,
+                      float *eigen, double origin[3]) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->have_comb) return fail(GVOM_NO_DATA, "No data");
+    int C = 0;
+    int rc = read_int(h, h->d_combC + h->cur, &C);
+    if (rc) return rc;
+    if (index) {
+        CUDA_TRY(cudaMemcpyAsync(index, h->cidx[h->cur], sizeof(int) * h->g.V, cudaMemcpyDeviceToHost, h->st));
+        CUDA_TRY(cudaStreamSynchronize(h->st));
+    }
+    if ((rc = copy_records(h, h->crec[h->cur], C, hit, total, min_height, metrics, eigen))) return rc;
+    if (origin)
+        for (int a = 0; a < 3; a++) origin[a] = h->cod[h->cur][a];
+    return GVOM_OK;
+}
+
+int gvom_get_maps(GvomHandle *h, double *height, double *inferred, double *slope_x, double *slope_y, double *roughness,
+                  double *guess) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->have_maps) return fail(GVOM_NO_DATA, "No data");
+    const size_t b = (size_t)h->g.X * h->g.X * 8;
+    double *dst[6] = {height, inferred, slope_x, slope_y, roughness, guess};
+    const double *src[6] = {h->height, h->inferred, h->slope_x, h->slope_y, h->rough, h->guess};
+    for (int i = 0; i < 6; i++)
+        if (dst[i]) CUDA_TRY(cudaMemcpyAsync(dst[i], src[i], b, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    return GVOM_OK;
+}
+
+int gvom_set_stream(GvomHandle *h, void *stream) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    cudaStream_t ns = stream ? static_cast<cudaStream_t>(stream) : h->own;
+    if (ns != h->st) {
+        // order the new stream after everything queued so far
+        cudaEvent_t ev;
+        CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        cudaError_t e = cudaEventRecord(ev, h->st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ns, ev, 0);
+        cudaEventDestroy(ev);
+        if (e != cudaSuccess) return fail(GVOM_ERR_CUDA, std::string("set_stream: ") + cudaGetErrorString(e));
+        h->st = ns;
+    }
+    return GVOM_OK;
+}
+
+int gvom_synchronize(GvomHandle *h) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    CUDA_TRY(cudaGetLastError());
+    return GVOM_OK;
+}
+
+int gvom_last_process_stats(GvomHandle *h, int64_t *valid_points, int64_t *hits, int64_t *ray_steps) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (h->last_ctr < 0) return fail(GVOM_NO_DATA, "no scan processed yet");
+    ScanCounters c;
+    CUDA_TRY(cudaMemcpyAsync(&c, h->d_ctr + h->last_ctr, sizeof(c), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    if (c.overflow) return fail(GVOM_ERR_STATE, "record capacity overflow in the last scan");
+    if (valid_points) *valid_points = (int64_t)c.valid;
+    if (hits) *hits = (int64_t)c.hits;
+    if (ray_steps) *ray_steps = (int64_t)c.steps;
+    return GVOM_OK;
+}
+
+int gvom_device_bytes(GvomHandle *h, int64_t *bytes) {
+    if (!h || !bytes) return fail(GVOM_ERR_ARG, "NULL argument");
+    *bytes = h->bytes;
+    return GVOM_OK;
+}
+
+}  // extern "C"

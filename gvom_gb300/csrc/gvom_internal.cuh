@@ -1,0 +1,203 @@
+// Internal types and device helpers of the GB300 G-VOM path.
+//
+// Data layout in device memory (one map instance):
+//   per ring slot   idx  int32[V]        voxel id -> compact index (>=0), -1 unknown,
+//                                        <= -2 free with -(v+1) pass-throughs
+//                   rec  VoxelRec[cap]   per occupied voxel statistics (64 B)
+//   combined (x2)   cidx int32[V], crec VoxelRec[V] (double-buffered: current / previous)
+//   per scan scratch cnt  u64[Vext]      dense (hit << 32 | total) over the grid plus the
+//                                        eigen-neighbourhood halo; zero between scans
+//                   prec float4[N]       per point: voxel fraction xyz + extended cell id
+//                   prank int32[N]       per point: rank inside its cell
+//                   sorted float4[N]     points grouped by cell
+//   2-D maps        height/inferred/slope/roughness/guess f64[X*X], pos/neg/vis int32[X*X]
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gvom {
+
+constexpr int kMaxBatch = 16;         // scans per batched launch
+constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
+
+// Per-voxel record.  Ring slots store aux[0] = voxel id (int bits); the
+// combined map stores the three eigenvalues (descending) in aux.
+struct __align__(16) VoxelRec {
+    float mean[3];   // mean of the neighbourhood points, voxel units, relative to the voxel corner
+    float cov[6];    // xx xy xz yy yz zz
+    float count;     // points in the neighbourhood
+    int hit;
+    int total;
+    float min_h;     // lowest point height inside the voxel, fraction of a voxel
+    float aux[3];
+};
+static_assert(sizeof(VoxelRec) == 64, "VoxelRec must be 64 bytes");
+
+struct Geom {
+    int X, Z;      // grid
+    int exy, ez;   // neighbourhood half-widths (xy_eigen_dist, z_eigen_dist)
+    int Xe, Ze;    // extended grid X + 2 exy, Z + 2 ez
+    long long V, Vext;
+};
+
+struct ScanCounters {
+    int C;                      // occupied voxels allocated
+    int pts;                    // points placed into cell groups
+    int overflow;               // capacity exceeded (should never happen)
+    int pad;
+    unsigned long long valid;   // points passing the finite / min-distance filter
+    unsigned long long hits;    // in-grid hits
+    unsigned long long steps;   // ray-march increments
+};
+
+struct ScanDesc {
+    const void *pts;       // device points
+    long long n, stride;   // rows, elements per row
+    int tmode;             // 0 none, 1 float32 transform, 2 float64 transform
+    int fast_floor;        // origin small enough for the float32 voxel-index path
+    double T[12];          // transform rows 0..2 (a float32 transform is stored exactly)
+    double od[3];          // voxel origin (integer-valued doubles)
+    int oi[3];
+    float pt0[3];          // ray start: (float)(ego / resolution)
+    int slot;
+    int block_begin;       // first block of this scan in point-parallel launches
+    int nblocks;
+    long long pt_base;     // offset of this scan in prec / prank / sorted
+    unsigned long long *cnt;
+    int *idx;              // slot index map
+    VoxelRec *rec;         // slot records
+    long long rec_cap;
+    ScanCounters *ctr;
+};
+
+template <int NS>
+struct ScanTable {
+    ScanDesc s[NS];
+};
+
+struct ProcessConst {
+    Geom g;
+    double xy_res, z_res;
+    double md2;            // min_distance^2
+    int step_cap;          // upper bound on ray steps inside the grid
+    int nscans;
+};
+
+struct MergeSrc {
+    const int *idx;
+    const VoxelRec *rec;
+    int dx, dy, dz;        // combined origin - source origin (voxels)
+    int is_last;           // previous combined map: clearing rule (scripts/gvom.py:1058)
+};
+
+struct MergeParams {
+    Geom g;
+    MergeSrc src[kMaxSources];
+    int nsrc;
+    int *out_idx;
+    VoxelRec *out_rec;
+    int *out_count;
+    double co[3];          // combined origin (voxels)
+    double xy_res, z_res;
+    double ego[3];
+    double robot_r2;       // robot_radius^2
+    double disc_h;         // ego z - ground_to_lidar_height
+    double pos_thr, robot_h;
+    double *height, *inferred;
+    int *pos_density;
+};
+
+struct Maps2DParams {
+    int X;
+    double xy_res;
+    double slope_thr, neg_thr;
+    const double *height, *inferred;
+    const int *pos_density;
+    double *slope_x, *slope_y, *rough, *guess;
+    int *pos, *neg, *vis;
+};
+
+struct DebugVoxParams {
+    const int *idx;
+    const VoxelRec *rec;
+    const int *block_off;
+    long long V;
+    int X;
+    double co[3];
+    double xy_res, z_res;
+    float *out;
+    long long cap;
+};
+
+struct DebugMapParams {
+    int X;
+    double co[3];
+    double xy_res, z_res;
+    const double *height, *rough, *slope_x, *slope_y, *guess;
+    float *out_h;   // (X*X, 7) or NULL
+    float *out_i;   // (X*X, 3) or NULL
+};
+
+// host launchers (k_process.cu, k_combine.cu)
+cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
+                           int dtype, float4 *prec, int *prank, float4 *sorted, cudaStream_t st);
+cudaError_t launch_combine(const MergeParams &mp, const Maps2DParams &m2, cudaStream_t st);
+cudaError_t launch_debug_count(const int *idx, long long V, int *counts, int nblocks, cudaStream_t st);
+cudaError_t launch_debug_voxels(const DebugVoxParams &p, int nblocks, cudaStream_t st);
+cudaError_t launch_debug_maps(const DebugMapParams &p, cudaStream_t st);
+int debug_chunk();
+
+// ---------------------------------------------------------------------------
+// exact arithmetic helpers
+// ---------------------------------------------------------------------------
+
+// floor((double)p - od) for an integer-valued od, as the reference computes a
+// ray voxel index (scripts/gvom.py:1215-1223).  For |od| < 2^24 the float32
+// path floor(p) - oi is exact except for p in (-1, 0), where rounding of the
+// double subtraction may reach the integer above; those take the double path.
+// Returns INT_MIN for values far outside any grid (and NaN).
+__device__ __forceinline__ int ray_index(float p, int oi, double od, int fast) {
+    if (!(fabsf(p) < 1073741824.0f)) return INT32_MIN;
+    if (fast && !(p > -1.0f && p < 0.0f)) return __float2int_rd(p) - oi;
+    double t = __dsub_rn((double)p, od);
+    double f = floor(t);
+    if (!(fabs(f) < 1.0e9)) return INT32_MIN;
+    return (int)f;
+}
+
+// Number of iterations of `while (length < R) { ...; length += inc; }` with
+// a float64 accumulator starting at 0 (scripts/gvom.py:1206-1231), capped.
+// The accumulated rounding error of length stays below k * 2^-41 for the
+// lengths that occur (< 2^11 voxels), so when R / inc is farther than 1e-6
+// from an integer the count is ceil(R / inc); otherwise the loop is replayed.
+__device__ __forceinline__ int ray_step_count(double R, double inc, int cap) {
+    if (!(R > 0.0)) return 0;
+    double est = __ddiv_rn(R, inc);
+    if (!(est < (double)cap)) return cap;
+    double kc = ceil(est);
+    if (kc - est > 1e-6 && est - (kc - 1.0) > 1e-6) return (int)kc;
+    double L = 0.0;
+    int K = 0;
+    while (L < R && K < cap) {
+        K++;
+        L = __dadd_rn(L, inc);
+    }
+    return K;
+}
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// Kahan-compensated float32 accumulator.
+struct KSum {
+    float s, c;
+    __device__ __forceinline__ void init() { s = 0.f; c = 0.f; }
+    __device__ __forceinline__ void add(float v) {
+        float y = __fsub_rn(v, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+};
+
+}  // namespace gvom

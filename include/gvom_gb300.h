@@ -1,0 +1,173 @@
+/*
+ * gvom_gb300.h - C ABI of the GB300-native G-VOM scan->map hot path.
+ *
+ * One handle = one map instance (the reference's `Gvom` object): a ring of
+ * `buffer_size` per-scan voxel maps plus the previous combined map, all held
+ * in device memory.  Every entry point returns a status code (GVOM_OK = 0);
+ * gvom_last_error() gives the message of the calling thread's last failure.
+ * Calls on one handle are serialised by the library, so process and combine
+ * may be issued from different threads as the reference allows
+ * (README.md:49, scripts/gvom.py:198-208, 243-292, 333-336).
+ *
+ * Arrays:
+ *   points     (n, row_stride) row-major, dtype GVOM_F32 or GVOM_F64; columns 0-2 are x, y, z
+ *   transform  4x4 row-major, GVOM_F32 or GVOM_F64, or NULL (no transform)
+ *   2-D maps   (xy_size, xy_size) row-major [x][y] (y fastest), like the reference's outputs
+ *   voxel id   x + y*xy_size + z*xy_size*xy_size (scripts/gvom.py:1167)
+ */
+#ifndef GVOM_GB300_H
+#define GVOM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GVOM_OK 0
+#define GVOM_NO_DATA 1     /* combine/debug on an empty ring (scripts/gvom.py:225-227, 396-431) */
+#define GVOM_ERR_ARG 2     /* bad argument (shape, dtype, null pointer, size limit) */
+#define GVOM_ERR_OOM 3     /* device allocation failed or refused by the free-memory admission check */
+#define GVOM_ERR_CUDA 4    /* CUDA runtime error (message in gvom_last_error) */
+#define GVOM_ERR_TIMEOUT 5 /* a bounded wait ran out */
+#define GVOM_ERR_STATE 6   /* call not valid in the handle's current state */
+
+#define GVOM_NONE (-1)
+#define GVOM_F32 0
+#define GVOM_F64 1
+
+/* Constructor parameters, in the order of Gvom.__init__ (scripts/gvom.py:21-22). */
+typedef struct GvomParams {
+    double xy_resolution;
+    double z_resolution;
+    int32_t xy_size;
+    int32_t z_size;
+    int32_t buffer_size;
+    double min_distance;
+    double positive_obstacle_threshold;
+    double negative_obstacle_threshold;
+    double slope_obstacle_threshold;
+    double robot_height;
+    double robot_radius;
+    double ground_to_lidar_height;
+    int32_t xy_eigen_dist;
+    int32_t z_eigen_dist;
+} GvomParams;
+
+typedef struct GvomHandle GvomHandle;
+
+/* One scan of a batch (see gvom_process_batch). */
+typedef struct GvomScan {
+    const void *points;      /* host or device pointer, per `points_on_device` of the call */
+    int32_t dtype;           /* GVOM_F32 / GVOM_F64 */
+    int32_t transform_dtype; /* GVOM_NONE / GVOM_F32 / GVOM_F64 */
+    int64_t n;
+    int64_t row_stride;      /* elements per row, >= 3 */
+    double ego[3];
+    const void *transform;   /* host pointer, 16 elements, or NULL */
+} GvomScan;
+
+/* Replaces Gvom.__init__ (scripts/gvom.py:21-101).  Allocates the instance's
+ * device state; refuses (GVOM_ERR_OOM) when free device memory is short. */
+int gvom_create(const GvomParams *params, GvomHandle **out);
+
+/* Releases every device buffer of the instance. */
+int gvom_destroy(GvomHandle *h);
+
+/* Replaces Gvom.Process_pointcloud (scripts/gvom.py:105-217): voxelises one
+ * scan (optional 4x4 transform, hit counts, ray-traced pass-through counts,
+ * per-voxel statistics) into ring slot `buffer_index` and advances the ring.
+ * `points` is a host pointer; it may be reused when the call returns. */
+int gvom_process(GvomHandle *h, const void *points, int32_t dtype, int64_t n, int64_t row_stride,
+                 const double ego[3], const void *transform, int32_t transform_dtype);
+
+/* Same as gvom_process with `points` already in device memory (stream-ordered
+ * on the instance stream; the buffer must stay valid until the work is done). */
+int gvom_process_device(GvomHandle *h, const void *d_points, int32_t dtype, int64_t n,
+                        int64_t row_stride, const double ego[3], const void *transform,
+                        int32_t transform_dtype);
+
+/* Several scans, equivalent to calling gvom_process on each in order, run as
+ * one set of launches over all scans.  No reference counterpart; it serves
+ * multi-sensor callers of Process_pointcloud (README.md:49). */
+int gvom_process_batch(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device);
+
+/* Replaces Gvom.combine_maps (scripts/gvom.py:222-393).  Writes the world
+ * origin of the map (3 doubles) and the positive-obstacle, negative-obstacle,
+ * roughness and visibility maps into host buffers.  GVOM_NO_DATA when the
+ * last written slot is empty. */
+int gvom_combine(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, double *roughness,
+                 int32_t *visibility);
+
+/* Same as gvom_combine with the four maps written to device memory,
+ * stream-ordered on the instance stream (no host synchronisation). */
+int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t *d_neg,
+                        double *d_roughness, int32_t *d_visibility);
+
+/* Replaces Gvom.make_debug_voxel_map (scripts/gvom.py:395-410, 481-503):
+ * rows [x, y, z, hit/total, hit, l0-l1, l1-l2, l2] of every occupied voxel of
+ * the combined map, in ascending voxel-id order.  *rows = number of rows; at
+ * most `capacity_rows` are written (call with out = NULL to size). */
+int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64_t *rows);
+
+/* Replace make_debug_height_map / make_debug_inferred_height_map
+ * (scripts/gvom.py:412-442, 455-479): (xy_size^2, 7) and (xy_size^2, 3) float32. */
+int gvom_debug_height_map(GvomHandle *h, float *out);
+int gvom_debug_inferred_height_map(GvomHandle *h, float *out);
+
+/* ---- state access for parity checks (host copies) ---------------------- */
+
+/* Ring position: next slot to write and last slot written
+ * (Gvom.buffer_index / last_buffer_index, scripts/gvom.py:72-73, 211-216). */
+int gvom_ring_state(GvomHandle *h, int64_t *buffer_index, int64_t *last_buffer_index);
+
+/* Occupied-voxel count of ring slot `slot` (-1 if the slot is empty). */
+int gvom_slot_count(GvomHandle *h, int32_t slot, int64_t *count);
+
+/* Copies slot `slot`: index map (V int32), per occupied voxel hit, total,
+ * min height and 10 statistics (mean xyz, cov xx xy xz yy yz zz, count),
+ * and its voxel origin.  Any pointer may be NULL. */
+int gvom_get_slot(GvomHandle *h, int32_t slot, int32_t *index, int32_t *hit, int32_t *total,
+                  float *min_height, float *metrics, double origin[3]);
+
+/* Occupied-voxel count of the current combined map (-1 before the first combine). */
+int gvom_combined_count(GvomHandle *h, int64_t *count);
+
+/* Copies the current combined map (scripts/gvom.py:259-318 state): index map,
+ * hit, total, min height, 10 statistics and 3 eigenvalues per occupied voxel,
+ * and its voxel origin.  Any pointer may be NULL. */
+int gvom_get_combined(GvomHandle *h, int32_t *index, int32_t *hit, int32_t *total, float *min_height,
+                      float *metrics, float *eigen, double origin[3]);
+
+/* Copies the 2-D intermediate maps of the last combine (height, inferred
+ * height, x/y slope, roughness, guessed height delta), each xy_size^2 float64. */
+int gvom_get_maps(GvomHandle *h, double *height, double *inferred, double *slope_x, double *slope_y,
+                  double *roughness, double *guess);
+
+/* ---- streams and timing -------------------------------------------------- */
+
+/* Use `stream` (a cudaStream_t) for all further work of this handle; NULL
+ * restores the handle's own stream. */
+int gvom_set_stream(GvomHandle *h, void *stream);
+
+/* Blocks until all queued work of the handle is complete. */
+int gvom_synchronize(GvomHandle *h);
+
+/* Device-side counts of the last processed scan: valid points, in-grid hits,
+ * ray steps (pass-through increments). */
+int gvom_last_process_stats(GvomHandle *h, int64_t *valid_points, int64_t *hits, int64_t *ray_steps);
+
+/* Bytes of device memory held by the handle. */
+int gvom_device_bytes(GvomHandle *h, int64_t *bytes);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *gvom_last_error(void);
+
+/* Library version string. */
+const char *gvom_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GVOM_GB300_H */

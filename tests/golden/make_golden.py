@@ -1,0 +1,231 @@
+"""Generate the golden fixtures in tests/golden/ by running the REFERENCE mapper.
+
+Runs the reference's own scripts/gvom.py, unchanged, from the reference
+checkout (default /root/reference, or $GVOM_REFERENCE) on the host through
+the sequential numba stand-in in oracle/numba_shim, for a set of small scenes,
+and writes each scene's inputs and the reference's outputs and internal state
+(in canonical voxel order) to tests/golden/<scene>.npz.
+
+The fixtures pin the C oracle: tests/test_oracle_golden.py checks that the
+oracle reproduces every array here.  This script needs the reference checkout,
+so it runs only in the build container; its outputs are committed.
+
+    python tests/golden/make_golden.py [scene ...]
+"""
+from __future__ import annotations
+
+import importlib.util
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle", "numba_shim"))
+sys.path.insert(1, REPO)
+
+import numba  # noqa: E402  (the stand-in)
+from numba import cuda as shim_cuda  # noqa: E402
+
+from oracle.canonical import canonical_map  # noqa: E402
+
+REF = os.environ.get("GVOM_REFERENCE", "/root/reference")
+
+
+def load_reference():
+    path = os.path.join(REF, "scripts", "gvom.py")
+    spec = importlib.util.spec_from_file_location("gvom_reference", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    mod.math = numba.math_proxy  # compiled-Numba typing of math.sqrt / math.floor
+    return mod
+
+
+# ---------------------------------------------------------------------------
+# scenes: (params, ops); ops = [("P", points, ego, T or None), ("C",), ...]
+# ---------------------------------------------------------------------------
+
+def kat_params(X=16, Z=8, B=2, res=1.0, robot_radius=0.5, min_distance=0.5):
+    return (res, res, X, Z, B, min_distance, 0.5, 0.5, 0.3, 2.0, robot_radius, 1.0, 1, 1)
+
+
+def P(points, ego, T=None, dtype=np.float32):
+    return ("P", np.asarray(points, dtype=dtype).reshape(-1, 3), tuple(float(v) for v in ego), T)
+
+
+def scene_kat_rays():
+    """Axis-aligned rays in 6 directions, a diagonal with a 3-way tie, a ray leaving the grid."""
+    ego = (0.5, 0.5, 0.5)
+    pts = [(5.5, 0.5, 0.5), (-4.5, 0.5, 0.5), (0.5, 5.5, 0.5), (0.5, -4.5, 0.5), (0.5, 0.5, 3.25),
+           (0.5, 0.5, -2.5), (3.5, 3.5, 3.5), (30.5, 0.5, 0.5), (0.75, 0.6, 0.5),
+           (0.3, 0.2, 0.1)]
+    return kat_params(), [P(pts, ego), ("C",)]
+
+
+def scene_kat_clear(n_pass):
+    """Occupied voxel then `n_pass` rays through it in the next scan (clearing rule, gvom.py:1058)."""
+    ego = (0.5, 0.5, 0.5)
+    s1 = [(3.5, 0.5, 0.5)] * 3
+    s2 = [(6.5, 0.5, 0.5)] * n_pass
+    return kat_params(B=1), [P(s1, ego), ("C",), P(s2, ego), ("C",), ("C",)]
+
+
+def scene_kat_shift():
+    """Two slots whose origins differ by one voxel in every axis, then a third overwriting slot 0."""
+    rng = np.random.default_rng(11)
+    pts1 = rng.uniform(-6, 7, (200, 3)) * [1, 1, 0.5]
+    pts2 = rng.uniform(-6, 7, (200, 3)) * [1, 1, 0.5] + 1.0
+    pts3 = rng.uniform(-6, 7, (200, 3)) * [1, 1, 0.5] - 1.0
+    return kat_params(B=2), [P(pts1, (0.5, 0.5, 0.5)), P(pts2, (1.5, 1.5, 1.5)), ("C",),
+                             P(pts3, (-0.5, -0.5, -0.5)), ("C",)]
+
+
+def scene_kat_planes():
+    """A flat and a tilted ground patch plus a wall: slope, roughness, positive obstacles."""
+    pts = []
+    for x in np.arange(-7.25, 7.5, 0.5):
+        for y in np.arange(-7.25, 7.5, 0.5):
+            if x < 0:
+                z = -1.5 + 0.05  # flat
+            else:
+                z = -1.5 + 0.05 + 0.15 * x  # tilted
+            pts.append((x, y, z))
+    for k in range(14):  # a dense wall column at (4.3, -5.7), many hits per voxel
+        for rep in range(12):
+            pts.append((4.3 + 0.01 * rep, -5.7, -1.4 + 0.25 * k))
+    ego = (0.25, 0.25, 0.75)
+    return kat_params(robot_radius=1.0), [P(pts, ego), ("C",)]
+
+
+def scene_kat_guess():
+    """Known heights with holes seen only as free space (guess_height, gvom.py:592-714)."""
+    pts = []
+    rng = np.random.default_rng(5)
+    for x in np.arange(-7.5, 7.5, 1.0):
+        for y in np.arange(-7.5, 7.5, 1.0):
+            if (abs(x - 2.0) < 2.1 and abs(y + 1.0) < 1.6) or (x < -4 and y > 3):
+                continue  # hole: rays pass over it, no return
+            pts.append((x + rng.uniform(-0.3, 0.3), y + rng.uniform(-0.3, 0.3), -2.5 + rng.uniform(0, 0.4)))
+    # rays that pass low over the holes and end far away
+    for t in np.linspace(-3.0, 3.0, 25):
+        pts.append((40.0, 40.0 * t / 3.0 - 10.0, -12.0))
+        pts.append((-40.0, 40.0 * t / 3.0 + 10.0, -12.0))
+    ego = (0.5, 0.5, 0.5)
+    return kat_params(X=16, Z=8, robot_radius=0.5), [P(pts, ego), ("C",)]
+
+
+def scene_synthetic(name, X=32, Z=16, res=0.5, B=3, beams=16, columns=256, n_scans=6,
+                    combine_after=(1, 2, 4, 5), tdtype=np.float32, pdtype=np.float32,
+                    veg=0.0, dropout=0.0, eig=(1, 1)):
+    from gvom_gb300.synthetic import Lidar, Terrain, Vegetation, make_scan, make_trajectory
+    terrain = Terrain.make(0, extent=X * res, path_len=n_scans * 0.4)
+    vegetation = None
+    if veg > 0:
+        ext = X * res
+        vegetation = Vegetation.make(terrain, (-ext, ext + n_scans), (-ext, ext), density=veg)
+    lidar = Lidar(beams=beams, columns=columns)
+    poses = make_trajectory(n_scans)
+    params = (res, res, X, Z, B, 1.0, 0.5, 0.5, 0.3, 2.0, 2.0, 1.0, eig[0], eig[1])
+    ops = []
+    for i, pose in enumerate(poses):
+        s = make_scan(terrain, lidar, pose, i, vegetation=vegetation, footprint=X * res,
+                      dropout=dropout, transform_dtype=tdtype)
+        ops.append(("P", s.points.astype(pdtype), s.ego, s.transform))
+        if i in combine_after:
+            ops.append(("C",))
+    return params, ops
+
+
+def scene_small_32x512():
+    """One 32x512 scan, 0.2 m voxels, 128x128x32, buffer 2: process then combine."""
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["small_32x512"]
+    s = make_workload_scans(w, 1)[0]
+    return w.gvom_args(), [("P", s.points, s.ego, s.transform), ("C",)]
+
+
+SCENES = {
+    "kat_rays": scene_kat_rays,
+    "kat_clear10": lambda: scene_kat_clear(10),
+    "kat_clear11": lambda: scene_kat_clear(11),
+    "kat_shift": scene_kat_shift,
+    "kat_planes": scene_kat_planes,
+    "kat_guess": scene_kat_guess,
+    "synth_f32": lambda: scene_synthetic("synth_f32"),
+    "synth_f64T_veg": lambda: scene_synthetic("synth_f64T_veg", tdtype=np.float64, veg=2.0, n_scans=5,
+                                              combine_after=(0, 2, 4)),
+    "synth_f64pts_eig20": lambda: scene_synthetic("synth_f64pts_eig20", pdtype=np.float64, eig=(2, 0),
+                                                  n_scans=4, combine_after=(1, 3), B=2, dropout=0.3),
+    "small_32x512": scene_small_32x512,
+}
+
+
+def run_reference(mod, params, ops):
+    g = mod.Gvom(*params)
+    out = {"params": np.array(params, dtype=np.float64)}
+    kinds = []
+    pi = ci = 0
+    for op in ops:
+        if op[0] == "P":
+            _, pts, ego, T = op
+            kinds.append("P")
+            out[f"p{pi}_points"] = pts
+            out[f"p{pi}_ego"] = np.array(ego, dtype=np.float64)
+            if T is not None:
+                out[f"p{pi}_T"] = np.asarray(T)
+            g.Process_pointcloud(pts.copy(), tuple(ego), None if T is None else np.asarray(T).copy())
+            s = g.last_buffer_index
+            can = canonical_map(g.index_buffer[s].copy_to_host(),
+                                hit=g.hit_count_buffer[s].copy_to_host(),
+                                total=g.total_count_buffer[s].copy_to_host(),
+                                min_h=g.min_height_buffer[s].copy_to_host()[: len(g.hit_count_buffer[s])],
+                                metrics=g.metrics_buffer[s].copy_to_host())
+            for k, v in can.items():
+                out[f"p{pi}_slot_{k}"] = v
+            out[f"p{pi}_slot_origin"] = g.origin_buffer[s].copy_to_host()
+            pi += 1
+        else:
+            kinds.append("C")
+            res = g.combine_maps()
+            origin, pos, neg, rough, vis = res
+            out[f"c{ci}_origin"] = origin
+            out[f"c{ci}_pos"] = pos
+            out[f"c{ci}_neg"] = neg
+            out[f"c{ci}_rough"] = rough
+            out[f"c{ci}_vis"] = vis
+            can = canonical_map(g.combined_index_map.copy_to_host(),
+                                hit=g.combined_hit_count.copy_to_host(),
+                                total=g.combined_total_count.copy_to_host(),
+                                min_h=g.combined_min_height.copy_to_host(),
+                                metrics=g.combined_metrics.copy_to_host(),
+                                eigen=g.voxels_eigenvalues.copy_to_host())
+            for k, v in can.items():
+                out[f"c{ci}_comb_{k}"] = v
+            for k, arr in (("height", g.height_map), ("inferred", g.inferred_height_map),
+                           ("slope_x", g.x_slope_map), ("slope_y", g.y_slope_map),
+                           ("guess", g.guessed_height_delta)):
+                out[f"c{ci}_{k}"] = arr.copy_to_host()
+            out[f"c{ci}_debug_voxels"] = g.make_debug_voxel_map()
+            out[f"c{ci}_debug_height"] = g.make_debug_height_map()
+            out[f"c{ci}_debug_inferred"] = g.make_debug_inferred_height_map()
+            ci += 1
+    out["ops"] = np.array("".join(kinds))
+    return out
+
+
+def main(argv):
+    names = argv or list(SCENES)
+    mod = load_reference()
+    for name in names:
+        t = time.time()
+        params, ops = SCENES[name]()
+        out = run_reference(mod, params, ops)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"{name}: {time.time() - t:.1f} s, {os.path.getsize(path) / 1024:.0f} KiB", flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,203 @@
+"""GPU parity: libgvom_gb300.so (through the C ABI) against the golden fixtures
+and the CPU oracle.
+
+Integer outputs (occupied set in canonical voxel order, hit / pass-through
+counts, compact-record hit/total, min height bits, obstacle and visibility
+maps) must be bit-exact; float maps within 1e-4 m (heights) or 1e-3 relative
+(roughness, slope); statistics within replay.STAT_ATOL.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_files
+from oracle.canonical import canonical_state
+from oracle.oracle import OracleGvom
+from replay import compare_combine, compare_slot, load, params_of, replay_and_compare
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def Gvom(gpu_lib):
+    from gvom_gb300 import Gvom as G
+    return G
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_golden_replay(Gvom, name):
+    fx = load(os.path.join(GOLDEN, name))
+    g = Gvom(*params_of(fx))
+    replay_and_compare(g, fx)
+
+
+def _run_both(Gvom, params, scans, combine_every=1):
+    g = Gvom(*params)
+    o = OracleGvom(*params)
+    for i, s in enumerate(scans):
+        g.Process_pointcloud(s.points, s.ego, s.transform)
+        o.Process_pointcloud(s.points, s.ego, s.transform)
+        _, last = g.ring_state()
+        assert g.ring_state() == o.ring_state()
+        compare_slot(canonical_state(g.slot_state(last)), canonical_state(o.slot_state(last)), f"scan {i}")
+        gs, os_ = g.last_process_stats(), o.last_process_stats()
+        assert gs == os_, (gs, os_)
+        if (i + 1) % combine_every == 0:
+            out = g.combine_maps()
+            ref = o.combine_maps()
+            refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
+            compare_combine(out, refd, g.maps_state(), params, f"combine after scan {i}")
+            compare_slot(canonical_state(g.combined_state()), canonical_state(o.combined_state()), "combined")
+    return g, o
+
+
+def test_small_32x512_vs_oracle(Gvom):
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["small_32x512"]
+    scans = make_workload_scans(w, 3)
+    _run_both(Gvom, w.gvom_args(), scans)
+
+
+def test_os1_64_vegetation_trajectory_vs_oracle(Gvom):
+    """256x256x64 @ 0.15 m, buffer 4, OS1-64 + vegetation, f32 transforms, 6 scans."""
+    import torch
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["os1_64_veg"]
+    scans = make_workload_scans(w, 6, device="cuda" if torch.cuda.is_available() else "cpu")
+    _run_both(Gvom, w.gvom_args(), scans, combine_every=2)
+
+
+def test_float64_ros_style_inputs(Gvom):
+    """float64 transform (ROS tf) and float64 points; strided (N,4) rows."""
+    from gvom_gb300.synthetic import Lidar, Terrain, make_scan, make_trajectory
+    t = Terrain.make(0, extent=19.2, path_len=2.0)
+    lid = Lidar(beams=32, columns=256)
+    params = (0.15, 0.15, 128, 32, 3, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    g = Gvom(*params)
+    o = OracleGvom(*params)
+    for i, p in enumerate(make_trajectory(4)):
+        s = make_scan(t, lid, p, i, transform_dtype=np.float64)
+        pts = s.points.astype(np.float64) if i % 2 else s.points
+        xyzi = np.concatenate([pts, np.ones((pts.shape[0], 1), pts.dtype)], 1)
+        g.Process_pointcloud(xyzi, s.ego, s.transform)
+        o.Process_pointcloud(xyzi, s.ego, s.transform)
+        _, last = g.ring_state()
+        compare_slot(canonical_state(g.slot_state(last)), canonical_state(o.slot_state(last)), f"scan {i}")
+    out, ref = g.combine_maps(), o.combine_maps()
+    refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
+    compare_combine(out, refd, g.maps_state(), params, "combine")
+
+
+def test_eigen_distances_and_far_world_offset(Gvom):
+    """eigen distances (2, 0) and a 1e4 m world offset (precision stress)."""
+    from gvom_gb300.synthetic import Lidar, Terrain, make_scan, make_trajectory
+    t = Terrain.make(0, extent=25.6, path_len=2.0, offset=(1.0e4, 0.0, 0.0))
+    lid = Lidar(beams=32, columns=512)
+    params = (0.1, 0.1, 256, 48, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 2, 0)
+    scans = [make_scan(t, lid, p, i) for i, p in enumerate(make_trajectory(3))]
+    _run_both(Gvom, params, scans)
+
+
+def test_empty_and_out_of_grid_scans(Gvom):
+    params = (0.2, 0.2, 64, 16, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    g = Gvom(*params)
+    o = OracleGvom(*params)
+    assert g.combine_maps() is None
+    empty = np.zeros((0, 3), np.float32)
+    far = np.array([[500.0, 0.0, 0.0], [0.0, -400.0, 3.0]], np.float32)  # no hit inside the grid
+    for pts in (empty, far, empty):
+        g.Process_pointcloud(pts, (0.1, 0.2, 1.0))
+        o.Process_pointcloud(pts, (0.1, 0.2, 1.0))
+        _, last = g.ring_state()
+        compare_slot(canonical_state(g.slot_state(last)), canonical_state(o.slot_state(last)), "scan")
+        out, ref = g.combine_maps(), o.combine_maps()
+        for a, b in zip(out, ref):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_nonfinite_points_dropped_like_oracle(Gvom):
+    params = (0.2, 0.2, 64, 16, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    rng = np.random.default_rng(3)
+    pts = rng.uniform(-6, 6, (2000, 3)).astype(np.float32)
+    pts[::97, 1] = np.nan
+    pts[::89, 2] = np.inf
+    g, o = Gvom(*params), OracleGvom(*params)
+    g.Process_pointcloud(pts, (0.0, 0.0, 0.0))
+    o.Process_pointcloud(pts, (0.0, 0.0, 0.0))
+    assert g.last_process_stats() == o.last_process_stats()
+    compare_slot(canonical_state(g.slot_state(0)), canonical_state(o.slot_state(0)), "scan")
+
+
+def test_batch_equals_sequential(Gvom):
+    """process_batch over uneven scans (dropout) == Process_pointcloud one by one."""
+    from gvom_gb300.synthetic import WORKLOADS, Lidar, make_scan, make_trajectory, scene_for
+    w = WORKLOADS["small_32x512"]
+    t, _ = scene_for(w)
+    scans = []
+    for i, p in enumerate(make_trajectory(5)):
+        lid = Lidar(beams=(16, 32, 64)[i % 3], columns=512)
+        scans.append(make_scan(t, lid, p, i, dropout=0.3 * (i % 2)))
+    params = w.gvom_args()[:4] + (8,) + w.gvom_args()[5:]
+    a, b = Gvom(*params), Gvom(*params)
+    for s in scans:
+        a.Process_pointcloud(s.points, s.ego, s.transform)
+    b.process_batch([(s.points, s.ego, s.transform) for s in scans])
+    assert a.ring_state() == b.ring_state()
+    for slot in range(5):
+        compare_slot(canonical_state(a.slot_state(slot)), canonical_state(b.slot_state(slot)), f"slot {slot}")
+    ra, rb = a.combine_maps(), b.combine_maps()
+    for x, y in zip(ra, rb):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_torch_device_input_and_device_outputs(Gvom):
+    import torch
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["small_32x512"]
+    s = make_workload_scans(w, 1)[0]
+    a, b = Gvom(*w.gvom_args()), Gvom(*w.gvom_args())
+    a.Process_pointcloud(s.points, s.ego, s.transform)
+    b.Process_pointcloud(torch.from_numpy(s.points).cuda(), s.ego, torch.from_numpy(s.transform))
+    ra = a.combine_maps()
+    X = w.xy_size
+    dev = [torch.empty((X, X), dtype=d, device="cuda") for d in (torch.int32, torch.int32, torch.float64, torch.int32)]
+    origin = b.combine_maps_device(*dev)
+    b.synchronize()
+    np.testing.assert_array_equal(origin, ra[0])
+    for x, y in zip(ra[1:], dev):
+        np.testing.assert_array_equal(x, y.cpu().numpy())
+
+
+def test_debug_exports_vs_oracle(Gvom):
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    from oracle.canonical import sort_debug_voxels
+    from replay import assert_exact, assert_stats
+    w = WORKLOADS["small_32x512"]
+    s = make_workload_scans(w, 1)[0]
+    g, o = Gvom(*w.gvom_args()), OracleGvom(*w.gvom_args())
+    assert g.make_debug_voxel_map() is None
+    for m in (g, o):
+        m.Process_pointcloud(s.points, s.ego, s.transform)
+        m.combine_maps()
+    dv = g.make_debug_voxel_map()
+    rv = sort_debug_voxels(o.make_debug_voxel_map())
+    assert_exact(dv[:, :5], rv[:, :5], "debug voxel rows")
+    assert np.all(np.diff(dv[:, 2]) >= 0), "rows not in voxel-id order"
+    assert_stats(dv[:, 5:], rv[:, 5:], "eigen gaps")
+
+
+def test_repeated_combines_accumulate_like_reference(Gvom):
+    """combine_maps called repeatedly without new scans re-adds the ring (scripts/gvom.py:242-298)."""
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["small_32x512"]
+    scans = make_workload_scans(w, 2)
+    g, o = Gvom(*w.gvom_args()), OracleGvom(*w.gvom_args())
+    for m in (g, o):
+        for s in scans:
+            m.Process_pointcloud(s.points, s.ego, s.transform)
+    for k in range(4):
+        out, ref = g.combine_maps(), o.combine_maps()
+        refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
+        compare_combine(out, refd, g.maps_state(), w.gvom_args(), f"combine {k}")
+        compare_slot(canonical_state(g.combined_state()), canonical_state(o.combined_state()), f"combined {k}")
