@@ -29,8 +29,9 @@ EXPORTS = (
     "gvom_debug_inferred_height_map", "gvom_ring_state", "gvom_slot_count", "gvom_get_slot",
     "gvom_combined_count", "gvom_get_combined", "gvom_get_maps", "gvom_set_stream",
     "gvom_synchronize", "gvom_last_process_stats", "gvom_device_bytes", "gvom_last_error",
-    "gvom_version",
+    "gvom_version", "gvom_set_stage_timing", "gvom_stage_times", "gvom_stage_name",
 )
+GVOM_STAGES = 7
 
 
 class GvomParams(C.Structure):
@@ -96,6 +97,9 @@ def load(path: str | None = None):
         "gvom_last_process_stats": ([P, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "gvom_device_bytes": ([P, C.POINTER(i64)], C.c_int),
         "gvom_last_error": ([], C.c_char_p),
+        "gvom_set_stage_timing": ([P, i32], C.c_int),
+        "gvom_stage_times": ([P, C.POINTER(C.c_double), C.POINTER(i64), i32], C.c_int),
+        "gvom_stage_name": ([i32], C.c_char_p),
         "gvom_version": ([], C.c_char_p),
     }
     for name, (args, res) in sig.items():

@@ -33,6 +33,75 @@ int fail(int code, const std::string &msg) {
             return fail(GVOM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e__));   \
     } while (0)
 
+constexpr int kStages = kProcessKernels + kCombineKernels;
+const char *kStageNames[kStages] = {"k_voxelize_trace", "k_assign", "k_scatter", "k_voxel_stats",
+                                    "k_cleanup", "k_merge", "k_maps2d"};
+
+// CUDA events around each kernel launch, harvested when the host waits.
+struct StageTimer {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    struct Pending {
+        int first, nk;
+        cudaEvent_t ev[kProcessKernels + 1];
+    };
+    std::vector<Pending> pending;
+    double ms[kStages] = {0};
+    long long n[kStages] = {0};
+
+    cudaEvent_t get() {
+        if (pool.empty()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            return e;
+        }
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    // returns an event array for `nk` kernels starting at stage `first`, or nullptr when off
+    cudaEvent_t *begin(int first, int nk) {
+        if (!on) return nullptr;
+        if (pending.size() >= 512) harvest();
+        Pending p;
+        p.first = first;
+        p.nk = nk;
+        for (int i = 0; i <= nk; i++) {
+            p.ev[i] = get();
+            if (!p.ev[i]) return nullptr;
+        }
+        pending.push_back(p);
+        return pending.back().ev;
+    }
+    void harvest() {
+        for (auto &p : pending) {
+            cudaEventSynchronize(p.ev[p.nk]);
+            for (int i = 0; i < p.nk; i++) {
+                float t = 0.f;
+                if (cudaEventElapsedTime(&t, p.ev[i], p.ev[i + 1]) == cudaSuccess) {
+                    ms[p.first + i] += t;
+                    n[p.first + i] += 1;
+                }
+            }
+            for (int i = 0; i <= p.nk; i++) pool.push_back(p.ev[i]);
+        }
+        pending.clear();
+        cudaGetLastError();
+    }
+    void reset() {
+        harvest();
+        for (int i = 0; i < kStages; i++) {
+            ms[i] = 0;
+            n[i] = 0;
+        }
+    }
+    ~StageTimer() {
+        for (auto &p : pending)
+            for (int i = 0; i <= p.nk; i++) cudaEventDestroy(p.ev[i]);
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+
 struct Slot {
     int *idx = nullptr;
     VoxelRec *rec = nullptr;
@@ -78,6 +147,7 @@ struct GvomHandle {
     int *d_dbg = nullptr;
     long long bytes = 0;
     int pageable_access = 0;
+    StageTimer timer;
 };
 
 namespace {
@@ -261,7 +331,7 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
     }
     CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * k, h->st));
     CUDA_TRY(launch_process(pc, table, k, block, (int)std::min<long long>(max_n, h->g.V), scans[0].dtype, h->prec,
-                            h->prank, h->sorted, h->st));
+                            h->prank, h->sorted, h->st, h->timer.begin(0, kProcessKernels)));
     for (int i = 0; i < k; i++) {
         CUDA_TRY(cudaMemcpyAsync(h->d_slotC + slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
         Slot &sl = h->slots[slot_of[i]];
@@ -572,7 +642,7 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     m2.neg = h->neg;
     m2.vis = h->vis;
     CUDA_TRY(cudaMemsetAsync(mp.out_count, 0, sizeof(int), h->st));
-    CUDA_TRY(launch_combine(mp, m2, h->st));
+    CUDA_TRY(launch_combine(mp, m2, h->st, h->timer.begin(kProcessKernels, kCombineKernels)));
     for (int a = 0; a < 3; a++) h->cod[nb][a] = mp.co[a];
     h->cur = nb;
     h->have_comb = true;
@@ -847,6 +917,29 @@ int gvom_last_process_stats(GvomHandle *h, int64_t *valid_points, int64_t *hits,
     if (hits) *hits = (int64_t)c.hits;
     if (ray_steps) *ray_steps = (int64_t)c.steps;
     return GVOM_OK;
+}
+
+int gvom_set_stage_timing(GvomHandle *h, int32_t on) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->timer.reset();
+    h->timer.on = on != 0;
+    return GVOM_OK;
+}
+
+int gvom_stage_times(GvomHandle *h, double *total_ms, int64_t *launches, int32_t n_stages) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->timer.harvest();
+    for (int i = 0; i < n_stages && i < kStages; i++) {
+        if (total_ms) total_ms[i] = h->timer.ms[i];
+        if (launches) launches[i] = h->timer.n[i];
+    }
+    return GVOM_OK;
+}
+
+const char *gvom_stage_name(int32_t stage) {
+    return (stage >= 0 && stage < kStages) ? kStageNames[stage] : "";
 }
 
 int gvom_device_bytes(GvomHandle *h, int64_t *bytes) {

@@ -140,9 +140,14 @@ struct DebugMapParams {
 };
 
 // host launchers (k_process.cu, k_combine.cu)
+// `ev` (nullable): kProcessKernels + 1 (resp. kCombineKernels + 1) events,
+// recorded before the first kernel and after each kernel.
+constexpr int kProcessKernels = 5;  // voxelize_trace, assign, scatter, voxel_stats, cleanup
+constexpr int kCombineKernels = 2;  // merge, maps2d
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
-                           int dtype, float4 *prec, int *prank, float4 *sorted, cudaStream_t st);
-cudaError_t launch_combine(const MergeParams &mp, const Maps2DParams &m2, cudaStream_t st);
+                           int dtype, float4 *prec, int *prank, float4 *sorted, cudaStream_t st,
+                           cudaEvent_t *ev = nullptr);
+cudaError_t launch_combine(const MergeParams &mp, const Maps2DParams &m2, cudaStream_t st, cudaEvent_t *ev = nullptr);
 cudaError_t launch_debug_count(const int *idx, long long V, int *counts, int nblocks, cudaStream_t st);
 cudaError_t launch_debug_voxels(const DebugVoxParams &p, int nblocks, cudaStream_t st);
 cudaError_t launch_debug_maps(const DebugMapParams &p, cudaStream_t st);

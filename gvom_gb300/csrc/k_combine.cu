@@ -58,37 +58,51 @@ __device__ void eigen_f64(float xx, float xy, float xz, float yy, float yz, floa
     e[1] = __double2float_rn(__dsub_rn(__dsub_rn(__dmul_rn(3.0, q), (double)e[0]), (double)e[2]));
 }
 
-// float32 evaluation of the same closed form; near-degenerate voxels
-// (smallest / largest eigenvalue below 1e-6 in magnitude) are re-solved in
-// float64 by eigen_f64.
+// One Jacobi rotation zeroing a_pq of a symmetric 3x3 matrix (eigenvalues
+// only); r is the remaining index.
+__device__ __forceinline__ void jacobi_rot(float &app, float &aqq, float &apq, float &arp, float &arq) {
+    if (apq == 0.0f) return;
+    const float theta = (aqq - app) / (2.0f * apq);
+    float t;
+    if (fabsf(theta) > 1.0e18f) t = 0.5f / theta;
+    else t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+    const float c = 1.0f / sqrtf(t * t + 1.0f);
+    const float s = t * c;
+    const float tau = s / (1.0f + c);
+    app -= t * apq;
+    aqq += t * apq;
+    apq = 0.0f;
+    const float rp = arp, rq = arq;
+    arp = rp - s * (rq + tau * rp);
+    arq = rq + s * (rp - tau * rq);
+}
+
+// Eigenvalues (descending) of the symmetric 3x3 covariance.  Cyclic Jacobi in
+// float32: backward stable, so each eigenvalue (and the gaps between nearly
+// equal ones, which the closed form loses) is within ~1e-7 |A|.  Voxels whose
+// smallest / largest eigenvalue ratio is below 1e-6 are re-solved in float64
+// with the reference's closed form (eigen_f64).
 __device__ void eigen_solve(float xx, float xy, float xz, float yy, float yz, float zz, float e[3]) {
-    const float p1 = __fadd_rn(__fadd_rn(__fmul_rn(xy, xy), __fmul_rn(xz, xz)), __fmul_rn(yz, yz));
-    const float q = __fdiv_rn(__fadd_rn(__fadd_rn(xx, yy), zz), 3.0f);
-    if (p1 == 0.0f) {
-        eigen_f64(xx, xy, xz, yy, yz, zz, e);  // diagonal: exact either way, cheap
-        return;
+    float a00 = xx, a01 = xy, a02 = xz, a11 = yy, a12 = yz, a22 = zz;
+    const float scale = fabsf(a00) + fabsf(a11) + fabsf(a22) + fabsf(a01) + fabsf(a02) + fabsf(a12);
+#pragma unroll 1
+    for (int sweep = 0; sweep < 8; sweep++) {
+        if (fabsf(a01) + fabsf(a02) + fabsf(a12) <= 1.0e-9f * scale) break;
+        jacobi_rot(a00, a11, a01, a02, a12);
+        jacobi_rot(a00, a22, a02, a01, a12);
+        jacobi_rot(a11, a22, a12, a01, a02);
     }
-    const float dxx = xx - q, dyy = yy - q, dzz = zz - q;
-    const float p2 = dxx * dxx + dyy * dyy + dzz * dzz + 2.0f * p1;
-    const float p = sqrtf(p2 / 6.0f);
-    const float ip = 1.0f / p;
-    const float B0 = dxx * ip, B1 = xy * ip, B2 = xz * ip, B3 = dyy * ip, B4 = yz * ip, B5 = dzz * ip;
-    float r = B0 * (B3 * B5 - B4 * B4) - B1 * (B1 * B5 - B4 * B2) + B2 * (B1 * B4 - B3 * B2);
-    r = 0.5f * r;
-    float phi;
-    if (r <= -1.0f) phi = (float)(M_PI / 3.0);
-    else if (r >= 1.0f) phi = 0.0f;
-    else phi = acosf(r) / 3.0f;
-    const float e0 = q + 2.0f * p * cosf(phi);
-    const float e2 = q + 2.0f * p * cosf(phi + (float)(2.0 * M_PI / 3.0));
-    const float e1 = 3.0f * q - e0 - e2;
-    if (!(fabsf(e2) >= 1e-6f * fabsf(e0))) {
+    float l0 = a00, l1 = a11, l2 = a22, t;
+    if (l0 < l1) { t = l0; l0 = l1; l1 = t; }
+    if (l1 < l2) { t = l1; l1 = l2; l2 = t; }
+    if (l0 < l1) { t = l0; l0 = l1; l1 = t; }
+    if (!(fabsf(l2) >= 1e-6f * fabsf(l0))) {
         eigen_f64(xx, xy, xz, yy, yz, zz, e);
         return;
     }
-    e[0] = e0;
-    e[1] = e1;
-    e[2] = e2;
+    e[0] = l0;
+    e[1] = l1;
+    e[2] = l2;
 }
 
 // ---------------------------------------------------------------------------
@@ -487,12 +501,15 @@ __global__ void k_debug_maps(DebugMapParams p) {
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_combine(const MergeParams &mp, const Maps2DParams &m2, cudaStream_t st) {
+cudaError_t launch_combine(const MergeParams &mp, const Maps2DParams &m2, cudaStream_t st, cudaEvent_t *ev) {
     const int X = mp.g.X;
+    if (ev) cudaEventRecord(ev[0], st);
     dim3 gm((X + 31) / 32, (X + 7) / 8);
     k_merge<<<gm, dim3(32, 8), 0, st>>>(mp);
+    if (ev) cudaEventRecord(ev[1], st);
     dim3 g2((X + kTY - 1) / kTY, (X + kTX - 1) / kTX);
     k_maps2d<<<g2, dim3(kTY, kTX), 0, st>>>(m2);
+    if (ev) cudaEventRecord(ev[2], st);
     return cudaGetLastError();
 }
 

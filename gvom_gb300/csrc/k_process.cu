@@ -384,28 +384,37 @@ __global__ void __launch_bounds__(256) k_cleanup(const ProcessConst pc, const __
 // ---------------------------------------------------------------------------
 template <int NS>
 static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int total_blocks, int max_n, int dtype,
-                             float4 *prec, int *prank, float4 *sorted, cudaStream_t st) {
+                             float4 *prec, int *prank, float4 *sorted, cudaStream_t st, cudaEvent_t *ev) {
     ScanTable<NS> tab;
     for (int i = 0; i < NS; i++) tab.s[i] = i < pc.nscans ? table[i] : table[0];
     if (total_blocks < 1) total_blocks = 1;
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecord(ev[i], st);
+    };
+    mark(0);
     if (dtype == 1)
         k_voxelize_trace<double, NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
     else
         k_voxelize_trace<float, NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
+    mark(1);
     dim3 ga((unsigned)((pc.g.Vext + 255) / 256), pc.nscans);
     k_assign<NS><<<ga, 256, 0, st>>>(pc, tab);
+    mark(2);
     k_scatter<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank, sorted);
+    mark(3);
     dim3 gs((unsigned)((max_n + 127) / 128 > 0 ? (max_n + 127) / 128 : 1), pc.nscans);
     k_voxel_stats<NS><<<gs, 128, 0, st>>>(pc, tab, sorted);
+    mark(4);
     k_cleanup<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
+    mark(5);
     return cudaGetLastError();
 }
 
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
-                           int dtype, float4 *prec, int *prank, float4 *sorted, cudaStream_t st) {
-    if (nscans == 1) return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st);
-    if (nscans <= 4) return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st);
-    return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st);
+                           int dtype, float4 *prec, int *prank, float4 *sorted, cudaStream_t st, cudaEvent_t *ev) {
+    if (nscans == 1) return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st, ev);
+    if (nscans <= 4) return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st, ev);
+    return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st, ev);
 }
 
 }  // namespace gvom

@@ -245,6 +245,18 @@ class Gvom:
     def set_stream(self, stream_ptr: int | None):
         check(self._l.gvom_set_stream(self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
 
+    def set_stage_timing(self, on: bool):
+        """Record CUDA events around every kernel launch (resets the totals)."""
+        check(self._l.gvom_set_stage_timing(self._h, 1 if on else 0))
+
+    def stage_times(self):
+        """{kernel name: (total ms, launches)} since stage timing was enabled."""
+        n = _lib.GVOM_STAGES
+        ms = (C.c_double * n)()
+        cnt = (C.c_int64 * n)()
+        check(self._l.gvom_stage_times(self._h, ms, cnt, n))
+        return {self._l.gvom_stage_name(i).decode(): (ms[i], cnt[i]) for i in range(n)}
+
     def device_bytes(self) -> int:
         b = C.c_int64()
         check(self._l.gvom_device_bytes(self._h, C.byref(b)))

@@ -195,12 +195,17 @@ def _pose_matrix(pose: Pose, z: float, offset) -> np.ndarray:
 
 def cast_rays(terrain: Terrain, origin: np.ndarray, dirs: np.ndarray, max_range: float,
               device="cpu", coarse: float = 0.2, refine_iters: int = 14,
-              chunk: int = 16384) -> np.ndarray:
-    """First intersection range of each ray with the surface (max_range if none)."""
-    o = torch.tensor(origin, dtype=torch.float64, device=device)
-    d_all = torch.as_tensor(dirs, dtype=torch.float64, device=device)
-    ts = torch.arange(coarse, max_range + 1e-9, coarse, dtype=torch.float64, device=device)
-    out = torch.full((d_all.shape[0],), max_range, dtype=torch.float64, device=device)
+              chunk: int = 16384, dtype=None) -> np.ndarray:
+    """First intersection range of each ray with the surface (max_range if none).
+
+    Runs in float64 on CPU; on a GPU it defaults to float32 (coordinates are
+    local, offset-free, so float32 resolves ~1e-5 m)."""
+    if dtype is None:
+        dtype = torch.float64 if str(device) == "cpu" else torch.float32
+    o = torch.tensor(origin, dtype=dtype, device=device)
+    d_all = torch.as_tensor(dirs, dtype=dtype, device=device)
+    ts = torch.arange(coarse, max_range + 1e-9, coarse, dtype=dtype, device=device)
+    out = torch.full((d_all.shape[0],), max_range, dtype=dtype, device=device)
     for s in range(0, d_all.shape[0], chunk):
         d = d_all[s:s + chunk]
         p = o[None, None, :] + ts[None, :, None] * d[:, None, :]
@@ -217,7 +222,7 @@ def cast_rays(terrain: Terrain, origin: np.ndarray, dirs: np.ndarray, max_range:
             lo = torch.where(b, lo, mid)
         r = torch.where(hit_any, hi, torch.full_like(hi, max_range))
         out[s:s + chunk] = r
-    return out.cpu().numpy()
+    return out.cpu().double().numpy()
 
 
 def make_scan(terrain: Terrain, lidar: Lidar, pose: Pose, scan_index: int = 0,

@@ -153,6 +153,15 @@ int gvom_set_stream(GvomHandle *h, void *stream);
 /* Blocks until all queued work of the handle is complete. */
 int gvom_synchronize(GvomHandle *h);
 
+/* Per-kernel device time: when enabled, CUDA events are recorded around each
+ * kernel launch of process / combine; gvom_stage_times waits for the queued
+ * work and returns, for stages 0..n-1, the summed milliseconds and launch
+ * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
+#define GVOM_STAGES 7
+int gvom_set_stage_timing(GvomHandle *h, int32_t on);
+int gvom_stage_times(GvomHandle *h, double *total_ms, int64_t *launches, int32_t n_stages);
+const char *gvom_stage_name(int32_t stage);
+
 /* Device-side counts of the last processed scan: valid points, in-grid hits,
  * ray steps (pass-through increments). */
 int gvom_last_process_stats(GvomHandle *h, int64_t *valid_points, int64_t *hits, int64_t *ray_steps);

@@ -21,9 +21,15 @@ from oracle.canonical import canonical_map, canonical_state
 
 HEIGHT_ATOL = 1e-4
 REL_TOL = 1e-3
-# mean/cov are in voxel units (|mean| < 2, cov < 1); eigenvalues likewise.
-STAT_ATOL = 2e-4
-STAT_RTOL = 1e-3
+# mean/cov are in voxel units (|mean| < 2, cov < 1).
+STAT_ATOL = 1e-5
+STAT_RTOL = 1e-4
+# Eigenvalues: the reference's closed form (scripts/gvom.py:1446-1487) takes
+# float32 covariances and forms p1 in float32; near a repeated eigenvalue
+# (r -> +-1) its result carries noise of order p*sqrt(eps32) ~ 3e-4 * |l_max|,
+# so two correct solvers agree only to that scale.
+EIG_RTOL = 1e-3
+EIG_ATOL = 1e-6
 
 
 def load(path):
@@ -86,6 +92,20 @@ def assert_stats(a, b, what):
         raise AssertionError(f"{what}: {bad.size} mismatches (max abs err "
                              f"{np.abs(a - b).max():.3g}), first at {bad[:5]}: "
                              f"{a.reshape(-1)[bad[:5]]} vs {b.reshape(-1)[bad[:5]]}")
+
+
+def assert_eigen(a, b, what, scale=None):
+    """Eigenvalue rows (n, 3) (or the debug export's gap columns) within
+    EIG_RTOL of the row's largest eigenvalue magnitude."""
+    a = np.asarray(a, np.float64).reshape(len(a), -1)
+    b = np.asarray(b, np.float64).reshape(len(b), -1)
+    if scale is None:
+        scale = np.abs(b).max(axis=1, keepdims=True)
+    ok = np.abs(a - b) <= EIG_ATOL + EIG_RTOL * scale
+    if not ok.all():
+        bad = np.flatnonzero(~ok.reshape(-1))
+        raise AssertionError(f"{what}: {bad.size} mismatches (max abs err {np.abs(a - b).max():.3g}), "
+                             f"first at {bad[:5]}: {a.reshape(-1)[bad[:5]]} vs {b.reshape(-1)[bad[:5]]}")
 
 
 def compare_slot(got: dict, ref: dict, what: str, stats=True):
@@ -153,7 +173,7 @@ def replay_and_compare(mapper, fx, stats=True, debug=True):
             rc = {k[len("comb_"):]: v for k, v in ref.items() if k.startswith("comb_")}
             compare_slot(cst, rc, f"combine {ci} combined map", stats=stats)
             if stats:
-                assert_stats(cst["eigen"], rc["eigen"], f"combine {ci} eigenvalues")
+                assert_eigen(cst["eigen"], rc["eigen"], f"combine {ci} eigenvalues")
             compare_combine(out, ref, mapper.maps_state(), params, f"combine {ci}")
             if debug:
                 dv = mapper.make_debug_voxel_map()
@@ -163,7 +183,9 @@ def replay_and_compare(mapper, fx, stats=True, debug=True):
                 rv = sort_debug_voxels(rv)
                 assert_exact(dv[:, :5], rv[:, :5], f"combine {ci} debug voxel rows")
                 if stats:
-                    assert_stats(dv[:, 5:], rv[:, 5:], f"combine {ci} debug voxel eigen gaps")
+                    lmax = np.abs(rv[:, 5:6] + rv[:, 6:7] + rv[:, 7:8])  # l0 = gaps + l2
+                    assert_eigen(dv[:, 5:], rv[:, 5:], f"combine {ci} debug voxel eigen gaps",
+                                 scale=np.maximum(lmax, np.abs(rv[:, 5:]).max(axis=1, keepdims=True)))
                 dh = mapper.make_debug_height_map()
                 rh = ref["debug_height"]
                 assert_exact(dh[:, :2], rh[:, :2], f"combine {ci} debug height xy")
