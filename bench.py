@@ -56,12 +56,16 @@ def stage_bytes(name, n, V, Vext, X2, C_slot, C_sum, Cc, Cc_last, nsrc):
         return 8 * Vext + 4 * V + 12 * C_slot
     if name == "k_scatter":
         return 20 * n + 16 * n
+    if name == "k_cell_moments":
+        return 20 * n + 16 * n + 48 * C_slot
     if name == "k_voxel_stats":
-        return 16 * n + 52 * C_slot
+        return 52 * C_slot + 27 * 56 * C_slot
     if name == "k_cleanup":
         return 20 * n
     if name == "k_merge":
-        return 4 * V * nsrc + 4 * V + 52 * (C_sum + Cc_last) + 52 * Cc + 20 * X2
+        return 4 * V * nsrc + 4 * V + 52 * (C_sum + Cc_last) + 52 * Cc + 8 * X2 * ((V // X2 + 7) // 8)
+    if name == "k_columns":
+        return 8 * X2 * ((V // X2 + 7) // 8) + 28 * X2
     if name == "k_maps2d":
         return 20 * X2 + 20 * X2 + 24 * X2
     return 0
@@ -378,7 +382,7 @@ def run_gpu(args, w):
                            "e2e_p50": 1e3 * float(np.percentile(e2e_times, 50)),
                            "e2e_p99": 1e3 * float(np.percentile(e2e_times, 99))},
             "e2e": {"value": e2e_pts / e2e_t, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": 7 * args.steps,
+            "gpu_launches": 9 * args.steps,
             "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                          "peak_source": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                          "alg_bytes_per_launch": int(alg), "ms_per_launch": per_launch_ms,

@@ -31,7 +31,7 @@ EXPORTS = (
     "gvom_synchronize", "gvom_last_process_stats", "gvom_device_bytes", "gvom_last_error",
     "gvom_version", "gvom_set_stage_timing", "gvom_stage_times", "gvom_stage_name",
 )
-GVOM_STAGES = 7
+GVOM_STAGES = 9
 
 
 class GvomParams(C.Structure):

@@ -34,8 +34,8 @@ int fail(int code, const std::string &msg) {
     } while (0)
 
 constexpr int kStages = kProcessKernels + kCombineKernels;
-const char *kStageNames[kStages] = {"k_voxelize_trace", "k_assign", "k_scatter", "k_voxel_stats",
-                                    "k_cleanup", "k_merge", "k_maps2d"};
+const char *kStageNames[kStages] = {"k_voxelize_trace", "k_assign", "k_scatter", "k_cell_moments", "k_voxel_stats",
+                                    "k_cleanup", "k_merge", "k_columns", "k_maps2d"};
 
 // CUDA events around each kernel launch, harvested when the host waits.
 struct StageTimer {
@@ -131,17 +131,21 @@ struct GvomHandle {
     std::vector<unsigned long long *> cnt;  // one dense count array per concurrent scan
     float4 *prec = nullptr, *sorted = nullptr;
     int *prank = nullptr;
+    char *moments = nullptr;  // per point slot, kCellMomBytes each
     long long pcap = 0;
     void *dpts = nullptr;
     size_t dpts_bytes = 0;
     ScanCounters *d_ctr = nullptr;  // kMaxBatch
     int *d_slotC = nullptr;         // per ring slot occupied count
-    int *d_combC = nullptr;         // 2 (per combined buffer)
+    int *d_combC = nullptr;         // [0..1] occupied count per combined buffer, [2] float64 eigen refinements
     int last_ctr = -1;              // counters of the last processed scan
     // 2-D maps
     double *height = nullptr, *inferred = nullptr, *slope_x = nullptr, *slope_y = nullptr, *rough = nullptr,
            *guess = nullptr;
     int *pos_density = nullptr, *pos = nullptr, *neg = nullptr, *vis = nullptr;
+    int *zlow = nullptr;
+    float *mlow = nullptr;
+    int2 *colinfo = nullptr;  // (Z / 8 chunks) x X x X
     bool have_maps = false;
     // debug
     int *d_dbg = nullptr;
@@ -190,7 +194,10 @@ int check_params(const GvomParams *p) {
     if (p->xy_eigen_dist < 0 || p->z_eigen_dist < 0 || p->xy_eigen_dist > 8 || p->z_eigen_dist > 8)
         return fail(GVOM_ERR_ARG, "eigen distances must be in [0, 8]");
     const long long V = (long long)p->xy_size * p->xy_size * p->z_size;
-    if (V >= (1LL << 31) - 1) return fail(GVOM_ERR_ARG, "grid too large (voxel count must fit int32)");
+    const long long Vext = (long long)(p->xy_size + 2 * p->xy_eigen_dist) * (p->xy_size + 2 * p->xy_eigen_dist) *
+                           (p->z_size + 2 * p->z_eigen_dist);
+    if (V >= (1LL << 31) - 1 || Vext >= (1LL << 31) - 1)
+        return fail(GVOM_ERR_ARG, "grid too large (voxel count must fit int32)");
     return GVOM_OK;
 }
 
@@ -204,11 +211,14 @@ int ensure_points(GvomHandle *h, long long n) {
     dfree(h, h->prec, h->pcap * sizeof(float4));
     dfree(h, h->sorted, h->pcap * sizeof(float4));
     dfree(h, h->prank, h->pcap * sizeof(int));
+    dfree(h, h->moments, h->pcap * kCellMomBytes);
     h->prec = h->sorted = nullptr;
     h->prank = nullptr;
+    h->moments = nullptr;
     h->pcap = 0;
     int rc;
-    if ((rc = dalloc_t(h, &h->prec, cap)) || (rc = dalloc_t(h, &h->sorted, cap)) || (rc = dalloc_t(h, &h->prank, cap)))
+    if ((rc = dalloc_t(h, &h->prec, cap)) || (rc = dalloc_t(h, &h->sorted, cap)) || (rc = dalloc_t(h, &h->prank, cap)) ||
+        (rc = dalloc(h, reinterpret_cast<void **>(&h->moments), (size_t)cap * kCellMomBytes)))
         return rc;
     h->pcap = cap;
     return GVOM_OK;
@@ -264,6 +274,21 @@ void ray_origin(const GvomHandle *h, const double ego[3], double od[3]) {
 
 int bytes_of(int dtype) { return dtype == GVOM_F64 ? 8 : 4; }
 
+// Constants for the exact integer division by a voxel size r > 0:
+// r = mr 2^er (53-bit mr), W = floor(2^116 / mr) (gvom_exact.cuh).
+ExactRes exact_res(double r) {
+    int e;
+    const double f = std::frexp(r, &e);
+    ExactRes R;
+    R.mr = (unsigned long long)std::ldexp(f, 53);
+    R.er = e - 53;
+    unsigned __int128 w = ((unsigned __int128)1 << 116) / R.mr;
+    if (w >> 64) w = ~0ull;
+    R.W = (unsigned long long)w;
+    R.pad = 0;
+    return R;
+}
+
 struct ScanIn {
     const void *dev_pts;
     int dtype, tdtype;
@@ -289,6 +314,15 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
     pc.xy_res = h->p.xy_resolution;
     pc.z_res = h->p.z_resolution;
     pc.md2 = h->p.min_distance * h->p.min_distance;
+    {
+        // smallest float32 whose value is >= md2
+        float f = (float)pc.md2;
+        if ((double)f < pc.md2) f = std::nextafter(f, INFINITY);
+        while ((double)std::nextafter(f, -INFINITY) >= pc.md2) f = std::nextafter(f, -INFINITY);
+        pc.md2_f32 = f;
+        pc.rxy = exact_res(h->p.xy_resolution);
+        pc.rz = exact_res(h->p.z_resolution);
+    }
     pc.step_cap = 2 * std::max(h->g.X, h->g.Z) + 8;
     pc.nscans = k;
     ScanDesc table[kMaxBatch];
@@ -331,7 +365,7 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
     }
     CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * k, h->st));
     CUDA_TRY(launch_process(pc, table, k, block, (int)std::min<long long>(max_n, h->g.V), scans[0].dtype, h->prec,
-                            h->prank, h->sorted, h->st, h->timer.begin(0, kProcessKernels)));
+                            h->prank, h->sorted, h->moments, h->st, h->timer.begin(0, kProcessKernels)));
     for (int i = 0; i < k; i++) {
         CUDA_TRY(cudaMemcpyAsync(h->d_slotC + slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
         Slot &sl = h->slots[slot_of[i]];
@@ -444,15 +478,17 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     if ((rc = dalloc(h, reinterpret_cast<void **>(&h->d_ctr), sizeof(ScanCounters) * kMaxBatch)))
         return bail(rc);
     if ((rc = dalloc_t(h, &h->d_slotC, (size_t)h->B))) return bail(rc);
-    if ((rc = dalloc_t(h, &h->d_combC, 2))) return bail(rc);
+    if ((rc = dalloc_t(h, &h->d_combC, 4))) return bail(rc);
     double **maps[6] = {&h->height, &h->inferred, &h->slope_x, &h->slope_y, &h->rough, &h->guess};
     for (auto m : maps)
         if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
-    int **imaps[4] = {&h->pos_density, &h->pos, &h->neg, &h->vis};
+    int **imaps[5] = {&h->pos_density, &h->pos, &h->neg, &h->vis, &h->zlow};
     for (auto m : imaps)
         if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
+    if ((rc = dalloc_t(h, &h->mlow, (size_t)X2))) return bail(rc);
+    if ((rc = dalloc_t(h, &h->colinfo, (size_t)X2 * ((g.Z + 7) / 8)))) return bail(rc);
     if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->B, h->st) != cudaSuccess ||
-        cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 2, h->st) != cudaSuccess) {
+        cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 4, h->st) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(GVOM_ERR_CUDA, "memset failed"));
     }
@@ -481,6 +517,7 @@ int gvom_destroy(GvomHandle *h) {
     cudaFree(h->prec);
     cudaFree(h->sorted);
     cudaFree(h->prank);
+    cudaFree(h->moments);
     cudaFree(h->dpts);
     cudaFree(h->d_ctr);
     cudaFree(h->d_slotC);
@@ -495,6 +532,9 @@ int gvom_destroy(GvomHandle *h) {
     cudaFree(h->pos);
     cudaFree(h->neg);
     cudaFree(h->vis);
+    cudaFree(h->zlow);
+    cudaFree(h->mlow);
+    cudaFree(h->colinfo);
     cudaFree(h->d_dbg);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
@@ -616,24 +656,47 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     mp.out_idx = h->cidx[nb];
     mp.out_rec = h->crec[nb];
     mp.out_count = h->d_combC + nb;
-    mp.xy_res = h->p.xy_resolution;
-    mp.z_res = h->p.z_resolution;
-    for (int a = 0; a < 3; a++) mp.ego[a] = h->ego[a];
-    mp.robot_r2 = h->p.robot_radius * h->p.robot_radius;
-    mp.disc_h = h->ego[2] - h->p.ground_to_lidar_height;
-    mp.pos_thr = h->p.positive_obstacle_threshold;
-    mp.robot_h = h->p.robot_height;
-    mp.height = h->height;
-    mp.inferred = h->inferred;
-    mp.pos_density = h->pos_density;
+    mp.colinfo = h->colinfo;
+    ColumnParams cp;
+    std::memset(&cp, 0, sizeof(cp));
+    cp.X = h->g.X;
+    cp.Z = h->g.Z;
+    cp.idx = mp.out_idx;
+    cp.rec = mp.out_rec;
+    cp.colinfo = h->colinfo;
+    for (int a = 0; a < 3; a++) {
+        cp.co[a] = mp.co[a];
+        cp.ego[a] = h->ego[a];
+    }
+    cp.xy_res = h->p.xy_resolution;
+    cp.z_res = h->p.z_resolution;
+    cp.robot_r2 = h->p.robot_radius * h->p.robot_radius;
+    cp.disc_h = h->ego[2] - h->p.ground_to_lidar_height;
+    cp.pos_thr = h->p.positive_obstacle_threshold;
+    cp.robot_h = h->p.robot_height;
+    cp.pthr_v = (float)(h->p.positive_obstacle_threshold / h->p.z_resolution);
+    cp.robh_v = (float)(h->p.robot_height / h->p.z_resolution);
+    cp.base_xf = (float)(mp.co[0] * h->p.xy_resolution - h->ego[0]);
+    cp.base_yf = (float)(mp.co[1] * h->p.xy_resolution - h->ego[1]);
+    cp.res_f = (float)h->p.xy_resolution;
+    cp.r2_f = (float)cp.robot_r2;
+    cp.height = h->height;
+    cp.inferred = h->inferred;
+    cp.pos_density = h->pos_density;
+    cp.zlow = h->zlow;
+    cp.mlow = h->mlow;
     Maps2DParams m2;
     m2.X = h->g.X;
     m2.xy_res = h->p.xy_resolution;
+    m2.z_res = h->p.z_resolution;
     m2.slope_thr = h->p.slope_obstacle_threshold;
+    m2.slope_thr_f = (float)h->p.slope_obstacle_threshold;
     m2.neg_thr = h->p.negative_obstacle_threshold;
     m2.height = h->height;
     m2.inferred = h->inferred;
     m2.pos_density = h->pos_density;
+    m2.zlow = h->zlow;
+    m2.mlow = h->mlow;
     m2.slope_x = h->slope_x;
     m2.slope_y = h->slope_y;
     m2.rough = h->rough;
@@ -642,7 +705,7 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     m2.neg = h->neg;
     m2.vis = h->vis;
     CUDA_TRY(cudaMemsetAsync(mp.out_count, 0, sizeof(int), h->st));
-    CUDA_TRY(launch_combine(mp, m2, h->st, h->timer.begin(kProcessKernels, kCombineKernels)));
+    CUDA_TRY(launch_combine(mp, cp, m2, h->st, h->timer.begin(kProcessKernels, kCombineKernels)));
     for (int a = 0; a < 3; a++) h->cod[nb][a] = mp.co[a];
     h->cur = nb;
     h->have_comb = true;
@@ -853,14 +916,38 @@ int gvom_get_combined(GvomHandle *h, int32_t *index, int32_t *hit, int32_t *tota
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
     if (!h->have_comb) return fail(GVOM_NO_DATA, "No data");
-    int C = 0;
-    int rc = read_int(h, h->d_combC + h->cur, &C);
-    if (rc) return rc;
-    if (index) {
-        CUDA_TRY(cudaMemcpyAsync(index, h->cidx[h->cur], sizeof(int) * h->g.V, cudaMemcpyDeviceToHost, h->st));
-        CUDA_TRY(cudaStreamSynchronize(h->st));
+    // the device map addresses records by voxel id; export them compacted in
+    // ascending voxel-id order, with the index map renumbered to match
+    std::vector<int32_t> idx((size_t)h->g.V);
+    CUDA_TRY(cudaMemcpyAsync(idx.data(), h->cidx[h->cur], sizeof(int) * h->g.V, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    std::vector<int32_t> vids;
+    for (long long v = 0; v < h->g.V; v++)
+        if (idx[v] >= 0) {
+            idx[v] = (int32_t)vids.size();
+            vids.push_back((int32_t)v);
+        }
+    if (index) std::memcpy(index, idx.data(), sizeof(int) * h->g.V);
+    const int C = (int)vids.size();
+    if (C > 0 && (hit || total || min_height || metrics || eigen)) {
+        int *d_vids = nullptr;
+        VoxelRec *d_out = nullptr;
+        int rc = dalloc_t(h, &d_vids, (size_t)C);
+        if (rc) return rc;
+        rc = dalloc_t(h, &d_out, (size_t)C);
+        if (rc) {
+            dfree(h, d_vids, sizeof(int) * C);
+            return rc;
+        }
+        cudaError_t e = cudaMemcpyAsync(d_vids, vids.data(), sizeof(int) * C, cudaMemcpyHostToDevice, h->st);
+        if (e == cudaSuccess) e = launch_gather_records(h->crec[h->cur], d_vids, C, d_out, h->st);
+        int rc2 = GVOM_OK;
+        if (e == cudaSuccess) rc2 = copy_records(h, d_out, C, hit, total, min_height, metrics, eigen);
+        else rc2 = fail(GVOM_ERR_CUDA, std::string("gather: ") + cudaGetErrorString(e));
+        dfree(h, d_vids, sizeof(int) * C);
+        dfree(h, d_out, sizeof(VoxelRec) * C);
+        if (rc2) return rc2;
     }
-    if ((rc = copy_records(h, h->crec[h->cur], C, hit, total, min_height, metrics, eigen))) return rc;
     if (origin)
         for (int a = 0; a < 3; a++) origin[a] = h->cod[h->cur][a];
     return GVOM_OK;

@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "gvom_exact.cuh"
+
 namespace gvom {
 
 constexpr int kMaxBatch = 16;         // scans per batched launch
@@ -80,6 +82,8 @@ struct ProcessConst {
     Geom g;
     double xy_res, z_res;
     double md2;            // min_distance^2
+    float md2_f32;         // smallest float32 >= md2 (float32 points compare in float32)
+    ExactRes rxy, rz;      // exact-division constants of xy_res / z_res
     int step_cap;          // upper bound on ray steps inside the grid
     int nscans;
 };
@@ -96,24 +100,40 @@ struct MergeParams {
     MergeSrc src[kMaxSources];
     int nsrc;
     int *out_idx;
-    VoxelRec *out_rec;
-    int *out_count;
+    VoxelRec *out_rec;     // indexed by voxel id
+    int *out_count;        // occupied voxels
+    int2 *colinfo;         // per (z chunk, y, x): lowest occupied z, lowest known-free z (Z if none)
+    double co[3];          // combined origin (voxels)
+};
+
+struct ColumnParams {
+    int X, Z;
+    const int *idx;        // combined index map
+    const VoxelRec *rec;   // combined records (by voxel id)
+    const int2 *colinfo;
     double co[3];          // combined origin (voxels)
     double xy_res, z_res;
     double ego[3];
     double robot_r2;       // robot_radius^2
     double disc_h;         // ego z - ground_to_lidar_height
     double pos_thr, robot_h;
+    float pthr_v, robh_v;  // pos_thr / z_res, robot_height / z_res
+    float base_xf, base_yf, res_f, r2_f;  // robot disc in float32: x_world - ego = base + x * res
     double *height, *inferred;
     int *pos_density;
+    int *zlow;             // lowest occupied z per column (-1 if none)
+    float *mlow;           // its in-voxel minimum height fraction
 };
 
 struct Maps2DParams {
     int X;
-    double xy_res;
+    double xy_res, z_res;
     double slope_thr, neg_thr;
+    float slope_thr_f;
     const double *height, *inferred;
     const int *pos_density;
+    const int *zlow;
+    const float *mlow;
     double *slope_x, *slope_y, *rough, *guess;
     int *pos, *neg, *vis;
 };
@@ -142,12 +162,15 @@ struct DebugMapParams {
 // host launchers (k_process.cu, k_combine.cu)
 // `ev` (nullable): kProcessKernels + 1 (resp. kCombineKernels + 1) events,
 // recorded before the first kernel and after each kernel.
-constexpr int kProcessKernels = 5;  // voxelize_trace, assign, scatter, voxel_stats, cleanup
-constexpr int kCombineKernels = 2;  // merge, maps2d
+constexpr int kProcessKernels = 6;  // voxelize_trace, assign, scatter, cell_moments, voxel_stats, cleanup
+constexpr int kCombineKernels = 3;  // merge, columns, maps2d
+constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
-                           int dtype, float4 *prec, int *prank, float4 *sorted, cudaStream_t st,
+                           int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
                            cudaEvent_t *ev = nullptr);
-cudaError_t launch_combine(const MergeParams &mp, const Maps2DParams &m2, cudaStream_t st, cudaEvent_t *ev = nullptr);
+cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
+cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
+                           cudaEvent_t *ev = nullptr);
 cudaError_t launch_debug_count(const int *idx, long long V, int *counts, int nblocks, cudaStream_t st);
 cudaError_t launch_debug_voxels(const DebugVoxParams &p, int nblocks, cudaStream_t st);
 cudaError_t launch_debug_maps(const DebugMapParams &p, cudaStream_t st);
@@ -161,8 +184,12 @@ int debug_chunk();
 // ray voxel index (scripts/gvom.py:1215-1223).  For |od| < 2^24 the float32
 // path floor(p) - oi is exact except for p in (-1, 0), where rounding of the
 // double subtraction may reach the integer above; those take the double path.
+// floor(p) for |p| < 2^22 is read off the bits of p + 1.5 * 2^23 rounded
+// down (the sum lies in [2^23, 2^24], where float32 spacing is 1).
 // Returns INT_MIN for values far outside any grid (and NaN).
 __device__ __forceinline__ int ray_index(float p, int oi, double od, int fast) {
+    if (fast && fabsf(p) < 4194304.0f && !(p > -1.0f && p < 0.0f))
+        return __float_as_int(__fadd_rd(p, 12582912.0f)) - 0x4B400000 - oi;
     if (!(fabsf(p) < 1073741824.0f)) return INT32_MIN;
     if (fast && !(p > -1.0f && p < 0.0f)) return __float2int_rd(p) - oi;
     double t = __dsub_rn((double)p, od);
@@ -172,16 +199,25 @@ __device__ __forceinline__ int ray_index(float p, int oi, double od, int fast) {
 }
 
 // Number of iterations of `while (length < R) { ...; length += inc; }` with
-// a float64 accumulator starting at 0 (scripts/gvom.py:1206-1231), capped.
+// a float64 accumulator starting at 0, R = (double)rl - 1 and
+// inc = |1.0 / (double)sk| (scripts/gvom.py:1206-1231), capped at `cap`.
 // The accumulated rounding error of length stays below k * 2^-41 for the
-// lengths that occur (< 2^11 voxels), so when R / inc is farther than 1e-6
-// from an integer the count is ceil(R / inc); otherwise the loop is replayed.
-__device__ __forceinline__ int ray_step_count(double R, double inc, int cap) {
-    if (!(R > 0.0)) return 0;
-    double est = __ddiv_rn(R, inc);
-    if (!(est < (double)cap)) return cap;
-    double kc = ceil(est);
-    if (kc - est > 1e-6 && est - (kc - 1.0) > 1e-6) return (int)kc;
+// lengths that occur (< 2^11 voxels), so when R / inc is clear of an integer
+// the count is ceil(R / inc).  R / inc = R |sk| (1 + O(2^-53)); R = rl - 1 is
+// exact in float32 for 1 < rl < 2^23 and the float32 product adds at most
+// 2^-24 relative error, so a 2^-18 relative margin decides it; otherwise the
+// float64 loop is replayed exactly.
+__device__ __forceinline__ int ray_step_count(float rl, float sk, int cap) {
+    if (!(rl > 1.0f)) return 0;  // R <= 0 (or NaN)
+    if (rl < 8388608.0f) {
+        const float est = __fmul_rn(__fsub_rn(rl, 1.0f), fabsf(sk));
+        if (!(est < (float)cap)) return cap;
+        const float fl = floorf(est);
+        const float margin = 3.8147e-6f * fmaxf(est, 1.0f);  // 2^-18
+        if (est - fl > margin && fl + 1.0f - est > margin) return (int)fl + 1;
+    }
+    const double R = __dsub_rn((double)rl, 1.0);
+    const double inc = fabs(__ddiv_rn(1.0, (double)sk));
     double L = 0.0;
     int K = 0;
     while (L < R && K < cap) {

@@ -1,74 +1,73 @@
 // Map-combine kernels: Gvom.combine_maps (scripts/gvom.py:222-393).
 //
-//   k_merge    one thread per (x, y) column, walking z: merges every ring slot
+//   k_merge    one thread per (x, y, 8-plane z chunk): merges every ring slot
 //              (slot order) and the previous combined map with their ego
-//              shifts and the clearing rule (scripts/gvom.py:1009-1063),
-//              allocates compact indices, Chan-merges the statistics
-//              (scripts/gvom.py:888-980), solves the 3x3 eigenvalues
-//              (scripts/gvom.py:1423-1487), and in the same walk reduces the
-//              column to its height, inferred height and positive-obstacle
-//              band density (scripts/gvom.py:515-590)
+//              shifts and the clearing rule (scripts/gvom.py:1009-1063) and
+//              Chan-merges the statistics of occupied voxels
+//              (scripts/gvom.py:888-980) and solves their eigenvalues
+//              (scripts/gvom.py:1423-1487).  The combined map addresses its
+//              records by voxel id, so nothing is allocated; each thread
+//              leaves the lowest occupied / known-free z of its chunk.
+//   k_columns  one thread per column: height (lowest occupied voxel or the
+//              robot disc), inferred height (lowest known-free voxel) and the
+//              positive-obstacle band density (scripts/gvom.py:515-590)
 //   k_maps2d   one thread per cell on a shared-memory tile with a 15-cell
 //              halo: slope / roughness, guessed height delta, positive,
 //              negative and visibility maps (scripts/gvom.py:444-805)
 //   debug      make_debug_voxel_map / height / inferred exporters
 //              (scripts/gvom.py:395-503)
+//
+// GB300's float64 rate is a small fraction of its float32 rate, so integer
+// and threshold decisions are taken in float32 wherever an error bound shows
+// the float64 result cannot differ, and fall back to the reference's float64
+// sequence only near a boundary.
 #include "gvom_internal.cuh"
 
 namespace gvom {
 
 constexpr int kOcc = 0x7fffffff;
 constexpr int kOutside = INT32_MIN;
+constexpr int kZC = 8;  // z planes per k_merge thread
 
 // ---------------------------------------------------------------------------
-// eigenvalues of a symmetric 3x3 matrix, trigonometric closed form
-// (scripts/gvom.py:1423-1487)
+// k_merge
 // ---------------------------------------------------------------------------
-// float64 restatement in the reference's operand types (inputs float32).
-__device__ void eigen_f64(float xx, float xy, float xz, float yy, float yz, float zz, float e[3]) {
-    const float p1 = __fadd_rn(__fadd_rn(__fmul_rn(xy, xy), __fmul_rn(xz, xz)), __fmul_rn(yz, yz));
-    const float tr = __fadd_rn(__fadd_rn(xx, yy), zz);
-    const double q = __ddiv_rn((double)tr, 3.0);
-    if (p1 == 0.0f) {
-        const float m12 = yy > zz ? yy : zz;
-        e[0] = xx > m12 ? xx : m12;
-        const float n12 = yy < zz ? yy : zz;
-        e[2] = xx < n12 ? xx : n12;
-        e[1] = __double2float_rn(__dsub_rn(__dsub_rn(__dmul_rn(3.0, q), (double)e[0]), (double)e[2]));
-        return;
+template <int NSRC>
+struct SrcVals {
+    int v[NSRC];
+};
+
+template <int NSRC>
+__device__ __forceinline__ void merge_load_plane(const MergeParams &mp, int x, int y, int z, bool col, int (&v)[NSRC]) {
+    const int X = mp.g.X, Z = mp.g.Z;
+#pragma unroll
+    for (int s = 0; s < NSRC; s++) {
+        v[s] = kOutside;
+        if (s < mp.nsrc && col && z < Z) {
+            const int xs = x + mp.src[s].dx, ys = y + mp.src[s].dy, zs = z + mp.src[s].dz;
+            if ((unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X && (unsigned)zs < (unsigned)Z)
+                v[s] = __ldg(&mp.src[s].idx[xs + ys * X + zs * X * X]);
+        }
     }
-    const double dxx = __dsub_rn((double)xx, q), dyy = __dsub_rn((double)yy, q), dzz = __dsub_rn((double)zz, q);
-    double p2 = __dadd_rn(__dmul_rn(dxx, dxx), __dmul_rn(dyy, dyy));
-    p2 = __dadd_rn(p2, __dmul_rn(dzz, dzz));
-    p2 = __dadd_rn(p2, __dmul_rn(2.0, (double)p1));
-    const double p = sqrt(__ddiv_rn(p2, 6.0));
-    const double B0 = __ddiv_rn(dxx, p), B1 = __ddiv_rn((double)xy, p), B2 = __ddiv_rn((double)xz, p);
-    const double B3 = __ddiv_rn(dyy, p), B4 = __ddiv_rn((double)yz, p), B5 = __ddiv_rn(dzz, p);
-    double r = __dsub_rn(__dmul_rn(B0, __dsub_rn(__dmul_rn(B3, B5), __dmul_rn(B4, B4))),
-                         __dmul_rn(B1, __dsub_rn(__dmul_rn(B1, B5), __dmul_rn(B4, B2))));
-    r = __dadd_rn(r, __dmul_rn(B2, __dsub_rn(__dmul_rn(B1, B4), __dmul_rn(B3, B2))));
-    r = __ddiv_rn(r, 2.0);
-    double phi;
-    if (r <= -1.0) phi = __ddiv_rn(M_PI, 3.0);
-    else if (r >= 1.0) phi = 0.0;
-    else phi = __ddiv_rn(acos(r), 3.0);
-    const double tp = __dmul_rn(2.0, p);
-    e[0] = __double2float_rn(__dadd_rn(q, __dmul_rn(tp, cos(phi))));
-    e[2] = __double2float_rn(__dadd_rn(q, __dmul_rn(tp, cos(__dadd_rn(phi, __ddiv_rn(2.0 * M_PI, 3.0))))));
-    e[1] = __double2float_rn(__dsub_rn(__dsub_rn(__dmul_rn(3.0, q), (double)e[0]), (double)e[2]));
 }
 
-// One Jacobi rotation zeroing a_pq of a symmetric 3x3 matrix (eigenvalues
-// only); r is the remaining index.
+// ---------------------------------------------------------------------------
+// eigenvalues (scripts/gvom.py:1423-1487): cyclic Jacobi in float32, which is
+// backward stable -- every eigenvalue, and the gap between nearly equal ones
+// (which the closed form loses), is within a few ulp of |A|.  Near-degenerate
+// voxels (smallest / largest eigenvalue below 1e-6) with a well-separated
+// middle eigenvalue get the smallest one in float64 from the determinant:
+// l2 = det(A) / (l0 l1).
+// ---------------------------------------------------------------------------
 __device__ __forceinline__ void jacobi_rot(float &app, float &aqq, float &apq, float &arp, float &arq) {
     if (apq == 0.0f) return;
-    const float theta = (aqq - app) / (2.0f * apq);
+    const float theta = __fdividef(aqq - app, 2.0f * apq);
     float t;
-    if (fabsf(theta) > 1.0e18f) t = 0.5f / theta;
+    if (fabsf(theta) > 1.0e18f) t = __fdividef(0.5f, theta);
     else t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
-    const float c = 1.0f / sqrtf(t * t + 1.0f);
+    const float c = rsqrtf(t * t + 1.0f);
     const float s = t * c;
-    const float tau = s / (1.0f + c);
+    const float tau = __fdividef(s, 1.0f + c);
     app -= t * apq;
     aqq += t * apq;
     apq = 0.0f;
@@ -77,17 +76,13 @@ __device__ __forceinline__ void jacobi_rot(float &app, float &aqq, float &apq, f
     arq = rq + s * (rp - tau * rq);
 }
 
-// Eigenvalues (descending) of the symmetric 3x3 covariance.  Cyclic Jacobi in
-// float32: backward stable, so each eigenvalue (and the gaps between nearly
-// equal ones, which the closed form loses) is within ~1e-7 |A|.  Voxels whose
-// smallest / largest eigenvalue ratio is below 1e-6 are re-solved in float64
-// with the reference's closed form (eigen_f64).
-__device__ void eigen_solve(float xx, float xy, float xz, float yy, float yz, float zz, float e[3]) {
-    float a00 = xx, a01 = xy, a02 = xz, a11 = yy, a12 = yz, a22 = zz;
+__device__ __forceinline__ void eigen3(const float C[6], float e[3]) {
+    float a00 = C[0], a01 = C[1], a02 = C[2], a11 = C[3], a12 = C[4], a22 = C[5];
     const float scale = fabsf(a00) + fabsf(a11) + fabsf(a22) + fabsf(a01) + fabsf(a02) + fabsf(a12);
+    const float tol = 2.0e-7f * scale;
 #pragma unroll 1
     for (int sweep = 0; sweep < 8; sweep++) {
-        if (fabsf(a01) + fabsf(a02) + fabsf(a12) <= 1.0e-9f * scale) break;
+        if (fabsf(a01) + fabsf(a02) + fabsf(a12) <= tol) break;
         jacobi_rot(a00, a11, a01, a02, a12);
         jacobi_rot(a00, a22, a02, a01, a12);
         jacobi_rot(a11, a22, a12, a01, a02);
@@ -96,247 +91,439 @@ __device__ void eigen_solve(float xx, float xy, float xz, float yy, float yz, fl
     if (l0 < l1) { t = l0; l0 = l1; l1 = t; }
     if (l1 < l2) { t = l1; l1 = l2; l2 = t; }
     if (l0 < l1) { t = l0; l0 = l1; l1 = t; }
-    if (!(fabsf(l2) >= 1e-6f * fabsf(l0))) {
-        eigen_f64(xx, xy, xz, yy, yz, zz, e);
-        return;
+    if (!(fabsf(l2) >= 1e-6f * fabsf(l0)) && fabsf(l1) >= 1e-6f * fabsf(l0)) {
+        const double b00 = C[0], b01 = C[1], b02 = C[2], b11 = C[3], b12 = C[4], b22 = C[5];
+        const double det = b00 * (b11 * b22 - b12 * b12) - b01 * (b01 * b22 - b12 * b02) + b02 * (b01 * b12 - b11 * b02);
+        l2 = (float)(det / ((double)l0 * (double)l1));
     }
     e[0] = l0;
     e[1] = l1;
     e[2] = l2;
 }
 
-// ---------------------------------------------------------------------------
-// k_merge
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void load_rec(const VoxelRec *r, float4 &a, float4 &b, float4 &c, float4 &d) {
-    const float4 *p = reinterpret_cast<const float4 *>(r);
-    a = __ldg(p);
-    b = __ldg(p + 1);
-    c = __ldg(p + 2);
-    d = __ldg(p + 3);
+// Chan merge of every occupied source voxel, in source order, into the
+// combined record at `vid` (scripts/gvom.py:926-980), float32, then its
+// eigenvalues.
+template <int NSRC>
+__device__ __forceinline__ void merge_voxel(const MergeParams &mp, int vid) {
+    const int X = mp.g.X, Z = mp.g.Z;
+    const int x = vid % X, y = (vid / X) % X, z = vid / (X * X);
+    float n = 0.f, m0 = 0.f, m1 = 0.f, m2 = 0.f;
+    float C[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    int hit = 0, total = 0;
+    float minh = 1.0f;
+    for (int s = 0; s < mp.nsrc; s++) {
+        const int xs = x + mp.src[s].dx, ys = y + mp.src[s].dy, zs = z + mp.src[s].dz;
+        if (!((unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X && (unsigned)zs < (unsigned)Z)) continue;
+        const int o = mp.src[s].idx[xs + ys * X + zs * X * X];
+        if (o < 0) continue;
+        const float4 *p = reinterpret_cast<const float4 *>(&mp.src[s].rec[o]);
+        const float4 a = __ldg(p), b = __ldg(p + 1), cc = __ldg(p + 2), d = __ldg(p + 3);
+        // a = mean0 mean1 mean2 xx | b = xy xz yy yz | cc = zz count hit total | d = minh aux
+        const float n2 = cc.y;
+        const float o_m[3] = {a.x, a.y, a.z};
+        const float o_c[6] = {a.w, b.x, b.y, b.z, b.w, cc.x};
+        const float den = __fadd_rn(n, n2);
+        const float nm0 = __fdiv_rn(__fadd_rn(__fmul_rn(m0, n), __fmul_rn(o_m[0], n2)), den);
+        const float nm1 = __fdiv_rn(__fadd_rn(__fmul_rn(m1, n), __fmul_rn(o_m[1], n2)), den);
+        const float nm2 = __fdiv_rn(__fadd_rn(__fmul_rn(m2, n), __fmul_rn(o_m[2], n2)), den);
+        const float cm[3] = {m0, m1, m2};
+        const float mn[3] = {nm0, nm1, nm2};
+        const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+        for (int t = 0; t < 6; t++) {
+            const float t1 = __fmul_rn(n, C[t]);
+            const float t2 = __fmul_rn(n2, o_c[t]);
+            const float t3 = __fmul_rn(__fmul_rn(n, __fsub_rn(cm[pa[t]], mn[pa[t]])), __fsub_rn(cm[pb[t]], mn[pb[t]]));
+            const float t4 = __fmul_rn(__fmul_rn(n2, __fsub_rn(o_m[pa[t]], mn[pa[t]])), __fsub_rn(o_m[pb[t]], mn[pb[t]]));
+            C[t] = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), t4), den);
+        }
+        m0 = nm0;
+        m1 = nm1;
+        m2 = nm2;
+        n = den;
+        hit += __float_as_int(cc.z);
+        total += __float_as_int(cc.w);
+        minh = fminf(minh, d.x);
+    }
+    float e[3];
+    eigen3(C, e);
+    float4 *o = reinterpret_cast<float4 *>(&mp.out_rec[vid]);
+    o[0] = make_float4(m0, m1, m2, C[0]);
+    o[1] = make_float4(C[1], C[2], C[3], C[4]);
+    o[2] = make_float4(C[5], n, __int_as_float(hit), __int_as_float(total));
+    o[3] = make_float4(minh, e[0], e[1], e[2]);
 }
 
-__global__ void __launch_bounds__(256) k_merge(MergeParams mp) {
-    const Geom g = mp.g;
-    const int X = g.X, Z = g.Z;
+// Phase 1: every thread decides its kZC voxels (index merge), writes the
+// combined index map and queues occupied voxels in shared memory.  Phase 2:
+// the block merges the queued voxels' statistics with full warps (occupied
+// voxels are sparse, so merging in place would run one lane per warp).
+template <int NSRC>
+__global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergeParams mp) {
+    __shared__ int queue[256 * kZC];
+    __shared__ int qn;
+    const int X = mp.g.X, Z = mp.g.Z;
     const int x = blockIdx.x * 32 + threadIdx.x;
     const int y = blockIdx.y * 8 + threadIdx.y;
+    const int z0 = blockIdx.z * kZC;
+    const int tid = threadIdx.y * 32 + threadIdx.x;
     const bool col = x < X && y < X;
-    const long long plane = (long long)X * X;
-    const unsigned lane = (threadIdx.y * 32 + threadIdx.x) & 31u;  // blockDim.x == 32: lane == threadIdx.x
-    (void)lane;
-
-    double h = -1000.0;
-    if (col) {
-        // height disc around the ego (scripts/gvom.py:566-570)
-        const double xp = __dsub_rn(__dmul_rn(__dadd_rn(mp.co[0], (double)x), mp.xy_res), mp.ego[0]);
-        const double yp = __dsub_rn(__dmul_rn(__dadd_rn(mp.co[1], (double)y), mp.xy_res), mp.ego[1]);
-        if (__dadd_rn(__dmul_rn(xp, xp), __dmul_rn(yp, yp)) <= mp.robot_r2) h = mp.disc_h;
-    }
-    bool hset = false, iset = false, band = false;
-    double ih = -1000.0;
-    long long zmin = 0, zmax = -1;
-    double dens = 0.0, nn = 0.0;
-
-    for (int z = 0; z < Z; z++) {
-        int v[kMaxSources];
+    const int plane = X * X;
+    if (tid == 0) qn = 0;
+    int v[kZC][NSRC];
 #pragma unroll
-        for (int s = 0; s < kMaxSources; s++) {
-            v[s] = kOutside;
-            if (s < mp.nsrc && col) {
-                const int xs = x + mp.src[s].dx, ys = y + mp.src[s].dy, zs = z + mp.src[s].dz;
-                if (xs >= 0 && xs < X && ys >= 0 && ys < X && zs >= 0 && zs < Z)
-                    v[s] = __ldg(&mp.src[s].idx[(long long)xs + (long long)ys * X + (long long)zs * plane]);
-            }
-        }
+    for (int k = 0; k < kZC; k++) merge_load_plane<NSRC>(mp, x, y, z0 + k, col, v[k]);
+    __syncthreads();
+    int occ_z = Z, free_z = Z;
+#pragma unroll
+    for (int k = 0; k < kZC; k++) {
+        const int z = z0 + k;
         int comb = -1;
 #pragma unroll
-        for (int s = 0; s < kMaxSources; s++) {
-            if (s < mp.nsrc && v[s] != kOutside) {
-                const int o = v[s];
+        for (int s = 0; s < NSRC; s++) {
+            if (s < mp.nsrc && v[k][s] != kOutside) {
+                const int o = v[k][s];
                 const bool alloc = mp.src[s].is_last ? (o >= 0 && comb <= -1 && comb >= -11) : (o >= 0 && comb <= -1);
                 if (alloc) comb = kOcc;
                 else if (o < -1 && comb <= -1) comb += o + 1;
             }
         }
-        const bool occ = comb == kOcc;
-        const unsigned om = __ballot_sync(0xffffffffu, occ);
-        int base = 0;
-        if (om) {
-            const int leader = __ffs(om) - 1;
-            if ((int)threadIdx.x == leader) base = atomicAdd(mp.out_count, __popc(om));
-            base = __shfl_sync(0xffffffffu, base, leader);
+        const bool occ = col && z < Z && comb == kOcc;
+        const unsigned m = __ballot_sync(0xffffffffu, occ);
+        if (m) {
+            int base = 0;
+            if (threadIdx.x == 0) base = atomicAdd(&qn, __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (occ) queue[base + __popc(m & ((1u << threadIdx.x) - 1u))] = x + y * X + z * plane;
         }
-        int hit = 0, total = 0;
-        float minh = 1.0f;
-        if (occ) {
-            const int c = base + __popc(om & ((1u << threadIdx.x) - 1u));
-            float n = 0.f, m0 = 0.f, m1 = 0.f, m2 = 0.f;
-            float C[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-            for (int s = 0; s < kMaxSources; s++) {
-                if (s < mp.nsrc && v[s] >= 0 && v[s] != kOutside) {
-                    float4 a, b, cc, d;
-                    load_rec(&mp.src[s].rec[v[s]], a, b, cc, d);
-                    // a = mean0 mean1 mean2 xx | b = xy xz yy yz | cc = zz count hit total | d = minh aux
-                    const float n2 = cc.y;
-                    const float o_m[3] = {a.x, a.y, a.z};
-                    const float o_c[6] = {a.w, b.x, b.y, b.z, b.w, cc.x};
-                    const float den = __fadd_rn(n, n2);
-                    const float nm0 = __fdiv_rn(__fadd_rn(__fmul_rn(m0, n), __fmul_rn(o_m[0], n2)), den);
-                    const float nm1 = __fdiv_rn(__fadd_rn(__fmul_rn(m1, n), __fmul_rn(o_m[1], n2)), den);
-                    const float nm2 = __fdiv_rn(__fadd_rn(__fmul_rn(m2, n), __fmul_rn(o_m[2], n2)), den);
-                    const float cm[3] = {m0, m1, m2};
-                    const float mn[3] = {nm0, nm1, nm2};
-                    const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
-#pragma unroll
-                    for (int t = 0; t < 6; t++) {
-                        const float t1 = __fmul_rn(n, C[t]);
-                        const float t2 = __fmul_rn(n2, o_c[t]);
-                        const float t3 = __fmul_rn(__fmul_rn(n, __fsub_rn(cm[pa[t]], mn[pa[t]])), __fsub_rn(cm[pb[t]], mn[pb[t]]));
-                        const float t4 = __fmul_rn(__fmul_rn(n2, __fsub_rn(o_m[pa[t]], mn[pa[t]])), __fsub_rn(o_m[pb[t]], mn[pb[t]]));
-                        C[t] = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), t4), den);
-                    }
-                    m0 = nm0;
-                    m1 = nm1;
-                    m2 = nm2;
-                    n = den;
-                    hit += __float_as_int(cc.z);
-                    total += __float_as_int(cc.w);
-                    minh = fminf(minh, d.x);
-                }
+        if (col && z < Z) {
+            const int vid = x + y * X + z * plane;
+            if (occ) {
+                comb = vid;
+                if (occ_z == Z) occ_z = z;
+            } else if (comb < -1 && free_z == Z) {
+                free_z = z;
             }
-            float e[3];
-            eigen_solve(C[0], C[1], C[2], C[3], C[4], C[5], e);
-            float4 *o = reinterpret_cast<float4 *>(&mp.out_rec[c]);
-            o[0] = make_float4(m0, m1, m2, C[0]);
-            o[1] = make_float4(C[1], C[2], C[3], C[4]);
-            o[2] = make_float4(C[5], n, __int_as_float(hit), __int_as_float(total));
-            o[3] = make_float4(minh, e[0], e[1], e[2]);
-            comb = c;
-        }
-        if (col) {
-            mp.out_idx[(long long)x + (long long)y * X + (long long)z * plane] = comb;
-            if (comb >= 0 && !hset) {
-                // lowest occupied voxel -> height (scripts/gvom.py:572-576)
-                h = __dmul_rn(__dadd_rn(__dadd_rn((double)minh, (double)z), mp.co[2]), mp.z_res);
-                hset = true;
-                // positive-obstacle band above it (scripts/gvom.py:529-539)
-                const double mino = __dadd_rn(h, mp.pos_thr), maxo = __dadd_rn(h, mp.robot_h);
-                zmin = (long long)floor(__dsub_rn(__ddiv_rn(mino, mp.z_res), mp.co[2])) + 1;
-                zmax = (long long)floor(__dsub_rn(__ddiv_rn(maxo, mp.z_res), mp.co[2]));
-                band = zmin >= 0 && zmin < Z && zmax >= 0 && zmax < Z;
-            }
-            if (comb < -1 && !iset) {
-                // lowest known-free voxel -> inferred height (scripts/gvom.py:585-590)
-                ih = __dmul_rn(__dadd_rn((double)z, mp.co[2]), mp.z_res);
-                iset = true;
-            }
-            if (band && z >= zmin && z <= zmax && comb >= 0 && hit > 10) {
-                // scripts/gvom.py:541-549
-                nn = __dadd_rn(nn, (double)total);
-                dens = __dadd_rn(dens, (double)hit);
-            }
+            mp.out_idx[vid] = comb;
         }
     }
-    if (col) {
-        int pd = 0;
-        if (band) {
-            if (nn > 0.0) dens = __ddiv_rn(dens, nn);
-            pd = (int)__dmul_rn(dens, 100.0);
-        }
-        const long long m2d = (long long)x * X + y;
-        mp.height[m2d] = h;
-        mp.inferred[m2d] = ih;
-        mp.pos_density[m2d] = pd;
-    }
+    if (col) mp.colinfo[blockIdx.z * plane + y * X + x] = make_int2(occ_z, free_z);
+    __syncthreads();
+    const int n_q = qn;
+    for (int i = tid; i < n_q; i += 256) merge_voxel<NSRC>(mp, queue[i]);
+    if (tid == 0 && n_q) atomicAdd(mp.out_count, n_q);
 }
 
 // ---------------------------------------------------------------------------
-// k_maps2d: tile of 8 (x) by 32 (y) cells plus a 15-cell halo of heights.
+// k_columns
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool near_integer(float w, float margin) {
+    const float f = floorf(w);
+    return !(w - f > margin && f + 1.0f - w > margin);
+}
+
+__global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnParams cp) {
+    const int X = cp.X, Z = cp.Z;
+    const int x = blockIdx.x * 32 + threadIdx.x;
+    const int y = blockIdx.y * 8 + threadIdx.y;
+    if (x >= X || y >= X) return;
+    const int plane = X * X;
+    int occ_z = Z, free_z = Z;
+    for (int ch = 0; ch * kZC < Z; ch++) {
+        const int2 ci = cp.colinfo[ch * plane + y * X + x];
+        if (occ_z == Z) occ_z = ci.x;
+        if (free_z == Z) free_z = ci.y;
+    }
+    double h = -1000.0;
+    int zl = -1;
+    float ml = 0.f;
+    int pd = 0;
+    if (occ_z < Z) {
+        // lowest occupied voxel -> height (scripts/gvom.py:572-576)
+        const float minh = cp.rec[x + y * X + occ_z * plane].min_h;
+        h = __dmul_rn(__dadd_rn(__dadd_rn((double)minh, (double)occ_z), cp.co[2]), cp.z_res);
+        zl = occ_z;
+        ml = minh;
+        // positive-obstacle band (scripts/gvom.py:529-555):
+        // zmin = floor((h + pos_thr) / z_res - oz) + 1, zmax = floor((h + robot_h) / z_res - oz);
+        // in exact arithmetic these are occ_z + floor(minh + thr / z_res) (+1)
+        int zmin, zmax;
+        const float wmin = minh + cp.pthr_v, wmax = minh + cp.robh_v;
+        if (!near_integer(wmin, 1e-4f) && !near_integer(wmax, 1e-4f)) {
+            zmin = occ_z + (int)floorf(wmin) + 1;
+            zmax = occ_z + (int)floorf(wmax);
+        } else {
+            const double mino = __dadd_rn(h, cp.pos_thr), maxo = __dadd_rn(h, cp.robot_h);
+            const double fmin = floor(__dsub_rn(__ddiv_rn(mino, cp.z_res), cp.co[2]));
+            const double fmax = floor(__dsub_rn(__ddiv_rn(maxo, cp.z_res), cp.co[2]));
+            zmin = (fabs(fmin) < 1e9) ? (int)fmin + 1 : -1;
+            zmax = (fabs(fmax) < 1e9) ? (int)fmax : -1;
+        }
+        if (zmin >= 0 && zmin < Z && zmax >= 0 && zmax < Z) {
+            long long nn = 0, dens = 0;
+            for (int z = zmin; z <= zmax; z++) {
+                const int idx = cp.idx[x + y * X + z * plane];
+                if (idx >= 0) {
+                    const float2 ht = reinterpret_cast<const float2 *>(&cp.rec[idx])[5];  // hit, total
+                    const int hit = __float_as_int(ht.x);
+                    if (hit > 10) {
+                        nn += __float_as_int(ht.y);
+                        dens += hit;
+                    }
+                }
+            }
+            // integer-valued float64 sums are exact, so only the final density needs float64
+            if (nn > 0) pd = (int)__dmul_rn(__ddiv_rn((double)dens, (double)nn), 100.0);
+        }
+    } else {
+        // robot disc (scripts/gvom.py:566-570): decided in float32 unless near the rim
+        const float xp = cp.base_xf + (float)x * cp.res_f, yp = cp.base_yf + (float)y * cp.res_f;
+        const float s = xp * xp + yp * yp;
+        bool in;
+        if (fabsf(s - cp.r2_f) > 1e-3f * cp.r2_f + 1e-4f) {
+            in = s <= cp.r2_f;
+        } else {
+            const double xd = __dsub_rn(__dmul_rn(__dadd_rn(cp.co[0], (double)x), cp.xy_res), cp.ego[0]);
+            const double yd = __dsub_rn(__dmul_rn(__dadd_rn(cp.co[1], (double)y), cp.xy_res), cp.ego[1]);
+            in = __dadd_rn(__dmul_rn(xd, xd), __dmul_rn(yd, yd)) <= cp.robot_r2;
+        }
+        if (in) h = cp.disc_h;
+    }
+    const double ih = free_z < Z ? __dmul_rn(__dadd_rn((double)free_z, cp.co[2]), cp.z_res) : -1000.0;
+    const int m2d = x * X + y;
+    cp.height[m2d] = h;
+    cp.inferred[m2d] = ih;
+    cp.pos_density[m2d] = pd;
+    cp.zlow[m2d] = zl;
+    cp.mlow[m2d] = ml;
+}
+
+// gathers occupied combined records in ascending voxel-id order (state export)
+__global__ void k_gather_records(const VoxelRec *__restrict__ rec, const int *__restrict__ vids, int n,
+                                 VoxelRec *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = rec[vids[i]];
+}
+
+// ---------------------------------------------------------------------------
+// k_maps2d: tile of 8 (x) by 32 (y) cells plus a 15-cell halo in shared
+// memory: heights, lowest occupied z / in-voxel height of each column,
+// known-height flags and, per column / row, the next known cell (so each
+// ring segment of the guess search is one lookup).
 // ---------------------------------------------------------------------------
 constexpr int kTX = 8, kTY = 32, kHalo = 15;
 constexpr int kSX = kTX + 2 * kHalo, kSY = kTY + 2 * kHalo;
 
-__global__ void __launch_bounds__(256) k_maps2d(Maps2DParams mp) {
+// h > -1000.0 on the bit pattern (no float64 compare)
+__device__ __forceinline__ bool height_known(double h) {
+    const long long b = __double_as_longlong(h);
+    return b >= 0 || (b & 0x7fffffffffffffffLL) < 0x408F400000000000LL;  // |h| < 1000
+}
+
+// __calculate_slope (scripts/gvom.py:717-805) in the reference's float64
+// operation order.
+__device__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY], int x0t, int y0t, int x0, int y0,
+                          int X, double res, double &rough, double &slx, double &sly) {
+#define H(gx, gy) sh[(gx) - x0t + kHalo][(gy) - y0t + kHalo]
+#define K(gx, gy) kn[(gx) - x0t + kHalo][(gy) - y0t + kHalo]
+    const int xl = max(0, x0 - 1), xh = min(X, x0 + 2), yl = max(0, y0 - 1), yh = min(X, y0 + 2);
+    double px[9], py[9], pz[9];
+    int i = 0;
+    double mx = 0.0, my = 0.0, mz = 0.0;
+    for (int xx = xl; xx < xh; xx++)
+        for (int yy = yl; yy < yh; yy++)
+            if (K(xx, yy)) {
+                px[i] = __dmul_rn((double)xx, res);
+                py[i] = __dmul_rn((double)yy, res);
+                pz[i] = H(xx, yy);
+                mx = __dadd_rn(mx, px[i]);
+                my = __dadd_rn(my, py[i]);
+                mz = __dadd_rn(mz, pz[i]);
+                i++;
+            }
+#undef H
+#undef K
+    const int n_good = i;
+    mx = __ddiv_rn(mx, (double)i);
+    my = __ddiv_rn(my, (double)i);
+    mz = __ddiv_rn(mz, (double)i);
+    double sxx = 0.0, sxy = 0.0, sxz = 0.0, syy = 0.0, syz = 0.0;
+    for (int j = 0; j < n_good; j++) {
+        const double dx = __dsub_rn(px[j], mx), dy = __dsub_rn(py[j], my), dz = __dsub_rn(pz[j], mz);
+        sxx = __dadd_rn(sxx, __dmul_rn(dx, dx));
+        sxy = __dadd_rn(sxy, __dmul_rn(dx, dy));
+        sxz = __dadd_rn(sxz, __dmul_rn(dx, dz));
+        syy = __dadd_rn(syy, __dmul_rn(dy, dy));
+        syz = __dadd_rn(syz, __dmul_rn(dy, dz));
+    }
+    const double det = __dsub_rn(__dmul_rn(sxx, syy), __dmul_rn(sxy, sxy));
+    if (det == 0.0) return;
+    double a0 = __ddiv_rn(__dsub_rn(__dmul_rn(syy, sxz), __dmul_rn(sxy, syz)), det);
+    double a1 = __ddiv_rn(__dsub_rn(__dmul_rn(sxx, syz), __dmul_rn(sxy, sxz)), det);
+    const double m = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(a0, a0), __dmul_rn(a1, a1)), 1.0));
+    a0 = __ddiv_rn(a0, m);
+    a1 = __ddiv_rn(a1, m);
+    double err = 0.0;
+    for (int j = 0; j < n_good; j++) {
+        const double e = __dsub_rn(__dsub_rn(pz[j], mz),
+                                   __dadd_rn(__dmul_rn(a0, __dsub_rn(px[j], mx)), __dmul_rn(a1, __dsub_rn(py[j], my))));
+        err = __dadd_rn(err, __dmul_rn(e, e));
+    }
+    err = __ddiv_rn(err, (double)n_good);
+    if (err > 0.0) err = log(err);
+    rough = err;
+    const double im = __ddiv_rn(1.0, m);
+    slx = atan2(a0, im);
+    sly = atan2(a1, im);
+}
+
+__global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DParams mp) {
     __shared__ double sh[kSX][kSY];
+    __shared__ int szl[kSX][kSY];
+    __shared__ float sml[kSX][kSY];
+    __shared__ unsigned char kn[kSX][kSY];
+    __shared__ unsigned char nky[kSX][kSY + 2];  // next known y index (in tile coords) at or after sy, kSY if none
+    __shared__ unsigned char nkx[kSY][kSX + 2];  // next known x index at or after sx
     const int X = mp.X;
     const int x0t = blockIdx.y * kTX, y0t = blockIdx.x * kTY;
     const int tid = threadIdx.y * kTY + threadIdx.x;
     for (int k = tid; k < kSX * kSY; k += kTX * kTY) {
         const int sx = k / kSY, sy = k % kSY;
         const int gx = x0t + sx - kHalo, gy = y0t + sy - kHalo;
-        sh[sx][sy] = (gx >= 0 && gx < X && gy >= 0 && gy < X) ? mp.height[(long long)gx * X + gy] : -1000.0;
+        const bool in = gx >= 0 && gx < X && gy >= 0 && gy < X;
+        const int c = gx * X + gy;
+        const double hv = in ? mp.height[c] : -1000.0;
+        sh[sx][sy] = hv;
+        kn[sx][sy] = (in && height_known(hv)) ? 1 : 0;
+        szl[sx][sy] = in ? mp.zlow[c] : -1;
+        sml[sx][sy] = in ? mp.mlow[c] : 0.f;
+    }
+    __syncthreads();
+    for (int k = tid; k < kSX + kSY; k += kTX * kTY) {
+        if (k < kSX) {
+            unsigned char nxt = kSY;
+            for (int sy = kSY - 1; sy >= 0; sy--) {
+                if (kn[k][sy]) nxt = (unsigned char)sy;
+                nky[k][sy] = nxt;
+            }
+        } else {
+            const int sy = k - kSX;
+            unsigned char nxt = kSX;
+            for (int sx = kSX - 1; sx >= 0; sx--) {
+                if (kn[sx][sy]) nxt = (unsigned char)sx;
+                nkx[sy][sx] = nxt;
+            }
+        }
     }
     __syncthreads();
     const int x0 = x0t + threadIdx.y, y0 = y0t + threadIdx.x;
     if (x0 >= X || y0 >= X) return;
-#define H(gx, gy) sh[(gx) - x0t + kHalo][(gy) - y0t + kHalo]
-    const long long cell = (long long)x0 * X + y0;
-    const double hc = H(x0, y0);
+    const int tx = threadIdx.y + kHalo, ty = threadIdx.x + kHalo;  // this cell in tile coords
+    const int cell = x0 * X + y0;
+    const bool known = kn[tx][ty];
 
-    // __calculate_slope (scripts/gvom.py:717-805)
+    // slope / roughness: float32 plane fit where every neighbour height comes
+    // from an occupied voxel (height differences are then exact sums of a
+    // voxel count and an in-voxel fraction); the reference's float64 sequence
+    // where a neighbour is a robot-disc height or the float32 fit is near a
+    // cancellation (singular normal matrix, residual far below the height
+    // spread, log near 0, a slope component near 0)
     double rough = -1.0, slx = 0.0, sly = 0.0;
     {
         const int xl = max(0, x0 - 1), xh = min(X, x0 + 2), yl = max(0, y0 - 1), yh = min(X, y0 + 2);
-        int n_good = 0;
+        int n_good = 0, sxi = 0, syi = 0;
+        bool all_vox = true;
+        int zr = 0;
+        float mr = 0.f;
         for (int xx = xl; xx < xh; xx++)
-            for (int yy = yl; yy < yh; yy++)
-                if (H(xx, yy) > -1000.0) n_good++;
-        if (n_good >= 3) {
-            double px[9], py[9], pz[9];
-            int i = 0;
-            double mx = 0.0, my = 0.0, mz = 0.0;
-            for (int xx = xl; xx < xh; xx++)
-                for (int yy = yl; yy < yh; yy++)
-                    if (H(xx, yy) > -1000.0) {
-                        px[i] = __dmul_rn((double)xx, mp.xy_res);
-                        py[i] = __dmul_rn((double)yy, mp.xy_res);
-                        pz[i] = H(xx, yy);
-                        mx = __dadd_rn(mx, px[i]);
-                        my = __dadd_rn(my, py[i]);
-                        mz = __dadd_rn(mz, pz[i]);
-                        i++;
+            for (int yy = yl; yy < yh; yy++) {
+                const int sx = xx - x0t + kHalo, sy = yy - y0t + kHalo;
+                if (kn[sx][sy]) {
+                    if (n_good == 0) {
+                        zr = szl[sx][sy];
+                        mr = sml[sx][sy];
                     }
-            mx = __ddiv_rn(mx, (double)i);
-            my = __ddiv_rn(my, (double)i);
-            mz = __ddiv_rn(mz, (double)i);
-            double sxx = 0.0, sxy = 0.0, sxz = 0.0, syy = 0.0, syz = 0.0;
-            for (int j = 0; j < n_good; j++) {
-                const double dx = __dsub_rn(px[j], mx), dy = __dsub_rn(py[j], my), dz = __dsub_rn(pz[j], mz);
-                sxx = __dadd_rn(sxx, __dmul_rn(dx, dx));
-                sxy = __dadd_rn(sxy, __dmul_rn(dx, dy));
-                sxz = __dadd_rn(sxz, __dmul_rn(dx, dz));
-                syy = __dadd_rn(syy, __dmul_rn(dy, dy));
-                syz = __dadd_rn(syz, __dmul_rn(dy, dz));
-            }
-            const double det = __dsub_rn(__dmul_rn(sxx, syy), __dmul_rn(sxy, sxy));
-            if (det != 0.0) {
-                double a0 = __ddiv_rn(__dsub_rn(__dmul_rn(syy, sxz), __dmul_rn(sxy, syz)), det);
-                double a1 = __ddiv_rn(__dsub_rn(__dmul_rn(sxx, syz), __dmul_rn(sxy, sxz)), det);
-                const double m = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(a0, a0), __dmul_rn(a1, a1)), 1.0));
-                a0 = __ddiv_rn(a0, m);
-                a1 = __ddiv_rn(a1, m);
-                double err = 0.0;
-                for (int j = 0; j < n_good; j++) {
-                    const double e = __dsub_rn(__dsub_rn(pz[j], mz),
-                                               __dadd_rn(__dmul_rn(a0, __dsub_rn(px[j], mx)),
-                                                         __dmul_rn(a1, __dsub_rn(py[j], my))));
-                    err = __dadd_rn(err, __dmul_rn(e, e));
+                    all_vox = all_vox && szl[sx][sy] >= 0;
+                    n_good++;
+                    sxi += xx - x0;
+                    syi += yy - y0;
                 }
-                err = __ddiv_rn(err, (double)n_good);
-                if (err > 0.0) err = log(err);
-                rough = err;
-                const double im = __ddiv_rn(1.0, m);
-                slx = atan2(a0, im);
-                sly = atan2(a1, im);
+            }
+        if (n_good >= 3) {
+            bool exact = !all_vox;
+            float a0 = 0.f, a1 = 0.f, m = 1.f, err = 0.f, szz = 0.f;
+            const float nf = (float)n_good;
+            if (!exact) {
+                const float res = (float)mp.xy_res, zres = (float)mp.z_res;
+                const float cx = (float)sxi / nf, cy = (float)syi / nf;
+                float dxs[9], dys[9], dzs[9];
+                float zsum = 0.f;
+                int i = 0;
+                for (int xx = xl; xx < xh; xx++)
+                    for (int yy = yl; yy < yh; yy++) {
+                        const int sx = xx - x0t + kHalo, sy = yy - y0t + kHalo;
+                        if (kn[sx][sy]) {
+                            dxs[i] = ((float)(xx - x0) - cx) * res;
+                            dys[i] = ((float)(yy - y0) - cy) * res;
+                            dzs[i] = ((sml[sx][sy] - mr) + (float)(szl[sx][sy] - zr)) * zres;
+                            zsum += dzs[i];
+                            i++;
+                        }
+                    }
+                const float zm = zsum / nf;
+                float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f;
+                for (int j = 0; j < i; j++) {
+                    const float dz = dzs[j] - zm;
+                    dzs[j] = dz;
+                    sxx += dxs[j] * dxs[j];
+                    sxy += dxs[j] * dys[j];
+                    sxz += dxs[j] * dz;
+                    syy += dys[j] * dys[j];
+                    syz += dys[j] * dz;
+                    szz += dz * dz;
+                }
+                const float det = sxx * syy - sxy * sxy;
+                exact = !(fabsf(det) > 1e-3f * sxx * syy);
+                if (!exact) {
+                    a0 = (syy * sxz - sxy * syz) / det;
+                    a1 = (sxx * syz - sxy * sxz) / det;
+                    m = sqrtf(a0 * a0 + a1 * a1 + 1.0f);
+                    a0 /= m;
+                    a1 /= m;
+                    for (int j = 0; j < i; j++) {
+                        const float e = dzs[j] - (a0 * dxs[j] + a1 * dys[j]);
+                        err += e * e;
+                    }
+                    err /= nf;
+                }
+            }
+            float rf = 0.f, sxf = 0.f, syf = 0.f;
+            if (!exact) {
+                rf = logf(err);
+                const float im = 1.0f / m;
+                sxf = atan2f(a0, im);
+                syf = atan2f(a1, im);
+                // a slope component much smaller than the other is ill-conditioned in any
+                // precision: take the reference's float64 sequence for it
+                const float big = fmaxf(fabsf(sxf), fabsf(syf)), small = fminf(fabsf(sxf), fabsf(syf));
+                exact = !(err > 1e-4f * (szz / nf)) || fabsf(rf) < 1.0f || small < 5e-3f * big || big < 2e-3f;
+            }
+            if (exact) {
+                slope_f64(sh, kn, x0t, y0t, x0, y0, X, mp.xy_res, rough, slx, sly);
+            } else {
+                rough = (double)rf;
+                slx = (double)sxf;
+                sly = (double)syf;
             }
         }
     }
 
-    // __guess_height (scripts/gvom.py:592-714), loop-condition and y_nh quirks included
+    // __guess_height (scripts/gvom.py:592-714), loop-condition and y_nh quirks
+    // included; each ring segment is scanned in increasing order, so its first
+    // known cell is one lookup in the next-known tables
     double guess = 0.0;
-    if (!(hc > -1000.0) && !(mp.inferred[cell] == -1000.0)) {
+    if (!known && !(mp.inferred[cell] == -1000.0)) {
         bool xpd = false, xnd = false, ypd = false, ynd = false;
         int xp = x0, xn = x0, yp = y0, yn = y0;
         double xph = -1000.0, xnh = -1000.0, yph = -1000.0, ynh = -1000.0;
@@ -346,33 +533,41 @@ __global__ void __launch_bounds__(256) k_maps2d(Maps2DParams mp) {
             i += 1;
             if (!xpd) {
                 if (xp < X) {
-                    for (int dy = -i; dy < i; dy++) {
-                        if (y0 + dy >= X || y0 + dy < 0) continue;
-                        if (H(xp, y0 + dy) > -1000.0) { xph = H(xp, y0 + dy); xpd = true; break; }
+                    const int lo = max(y0 - i, 0), hi = min(y0 + i, X);  // dy in [-i, i)
+                    if (lo < hi) {
+                        const int sx = xp - x0t + kHalo;
+                        const int f = nky[sx][lo - y0t + kHalo];
+                        if (f < hi - y0t + kHalo) { xph = sh[sx][f]; xpd = true; }
                     }
                 } else xpd = true;
             }
             if (!xnd) {
                 if (xn >= 0) {
-                    for (int dy = -i + 1; dy < i + 1; dy++) {
-                        if (y0 + dy >= X || y0 + dy < 0) continue;
-                        if (H(xn, y0 + dy) > -1000.0) { xnh = H(xn, y0 + dy); xnd = true; break; }
+                    const int lo = max(y0 - i + 1, 0), hi = min(y0 + i + 1, X);  // dy in [-i+1, i+1)
+                    if (lo < hi) {
+                        const int sx = xn - x0t + kHalo;
+                        const int f = nky[sx][lo - y0t + kHalo];
+                        if (f < hi - y0t + kHalo) { xnh = sh[sx][f]; xnd = true; }
                     }
                 } else xnd = true;
             }
             if (!ypd) {
                 if (yp < X) {
-                    for (int dx = -i + 1; dx < i + 1; dx++) {
-                        if (x0 + dx >= X || x0 + dx < 0) continue;
-                        if (H(x0 + dx, yp) > -1000.0) { yph = H(x0 + dx, yp); ypd = true; break; }
+                    const int lo = max(x0 - i + 1, 0), hi = min(x0 + i + 1, X);  // dx in [-i+1, i+1)
+                    if (lo < hi) {
+                        const int sy = yp - y0t + kHalo;
+                        const int f = nkx[sy][lo - x0t + kHalo];
+                        if (f < hi - x0t + kHalo) { yph = sh[f][sy]; ypd = true; }
                     }
                 } else ypd = true;
             }
             if (!ynd) {
                 if (yn >= 0) {
-                    for (int dx = -i; dx < i; dx++) {
-                        if (x0 + dx >= X || x0 + dx < 0) continue;
-                        if (H(x0 + dx, yn) > -1000.0) { ynh = H(x0 + dx, yn); ynd = true; break; }
+                    const int lo = max(x0 - i, 0), hi = min(x0 + i, X);  // dx in [-i, i)
+                    if (lo < hi) {
+                        const int sy = yn - y0t + kHalo;
+                        const int f = nkx[sy][lo - x0t + kHalo];
+                        if (f < hi - x0t + kHalo) { ynh = sh[f][sy]; ynd = true; }
                     }
                 } else ynd = true;
             }
@@ -385,12 +580,17 @@ __global__ void __launch_bounds__(256) k_maps2d(Maps2DParams mp) {
         const double dh = __dsub_rn(mx, mn);
         if (dh > 0.0) guess = dh;
     }
-#undef H
-    // __make_positive_obstacle_map slope gate (scripts/gvom.py:524-526)
-    const double sn = sqrt(__dadd_rn(__dmul_rn(slx, slx), __dmul_rn(sly, sly)));
-    mp.pos[cell] = sn >= mp.slope_thr ? 100 : mp.pos_density[cell];
-    mp.neg[cell] = guess > mp.neg_thr ? 100 : 0;            // scripts/gvom.py:505-512
-    mp.vis[cell] = hc > -1000.0 ? 1 : 0;                    // scripts/gvom.py:444-452
+    // __make_positive_obstacle_map slope gate (scripts/gvom.py:524-526): in
+    // float32 unless |slope| is near the threshold
+    bool steep;
+    {
+        const float sn = sqrtf((float)slx * (float)slx + (float)sly * (float)sly);
+        if (fabsf(sn - mp.slope_thr_f) > 1e-5f * mp.slope_thr_f + 1e-6f) steep = sn >= mp.slope_thr_f;
+        else steep = sqrt(__dadd_rn(__dmul_rn(slx, slx), __dmul_rn(sly, sly))) >= mp.slope_thr;
+    }
+    mp.pos[cell] = steep ? 100 : mp.pos_density[cell];
+    mp.neg[cell] = guess > mp.neg_thr ? 100 : 0;  // scripts/gvom.py:505-512
+    mp.vis[cell] = known ? 1 : 0;                 // scripts/gvom.py:444-452
     mp.rough[cell] = rough;
     mp.slope_x[cell] = slx;
     mp.slope_y[cell] = sly;
@@ -501,15 +701,28 @@ __global__ void k_debug_maps(DebugMapParams p) {
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_combine(const MergeParams &mp, const Maps2DParams &m2, cudaStream_t st, cudaEvent_t *ev) {
-    const int X = mp.g.X;
+template <int NSRC>
+static void launch_merge(const MergeParams &mp, dim3 g, cudaStream_t st) {
+    k_merge<NSRC><<<g, dim3(32, 8), 0, st>>>(mp);
+}
+
+cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
+                           cudaEvent_t *ev) {
+    const int X = mp.g.X, Z = mp.g.Z;
     if (ev) cudaEventRecord(ev[0], st);
-    dim3 gm((X + 31) / 32, (X + 7) / 8);
-    k_merge<<<gm, dim3(32, 8), 0, st>>>(mp);
+    dim3 gm((X + 31) / 32, (X + 7) / 8, (Z + kZC - 1) / kZC);
+    if (mp.nsrc <= 2) launch_merge<2>(mp, gm, st);
+    else if (mp.nsrc <= 3) launch_merge<3>(mp, gm, st);
+    else if (mp.nsrc <= 5) launch_merge<5>(mp, gm, st);
+    else if (mp.nsrc <= 9) launch_merge<9>(mp, gm, st);
+    else launch_merge<kMaxSources>(mp, gm, st);
     if (ev) cudaEventRecord(ev[1], st);
+    dim3 gc((X + 31) / 32, (X + 7) / 8);
+    k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);
+    if (ev) cudaEventRecord(ev[2], st);
     dim3 g2((X + kTY - 1) / kTY, (X + kTX - 1) / kTX);
     k_maps2d<<<g2, dim3(kTY, kTX), 0, st>>>(m2);
-    if (ev) cudaEventRecord(ev[2], st);
+    if (ev) cudaEventRecord(ev[3], st);
     return cudaGetLastError();
 }
 
@@ -530,5 +743,10 @@ cudaError_t launch_debug_maps(const DebugMapParams &p, cudaStream_t st) {
 }
 
 int debug_chunk() { return kDbgChunk; }
+
+cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st) {
+    if (n > 0) k_gather_records<<<(n + 255) / 256, 256, 0, st>>>(rec, vids, n, out);
+    return cudaGetLastError();
+}
 
 }  // namespace gvom

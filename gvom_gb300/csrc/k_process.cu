@@ -12,6 +12,8 @@
 //
 // All float arithmetic that decides an integer result uses the IEEE-rounded
 // intrinsics in the reference's operand types, without contraction.
+#include <algorithm>
+
 #include "gvom_internal.cuh"
 
 namespace gvom {
@@ -79,14 +81,18 @@ __device__ __forceinline__ void transform_point<double>(const ScanDesc &sd, doub
     z = o[2];
 }
 
-// d2 = x*x + y*y + z*z in the point dtype (scripts/gvom.py:1145-1148).
-__device__ __forceinline__ double point_d2(float x, float y, float z) {
+// d2 = x*x + y*y + z*z in the point dtype, compared with min_distance^2 in
+// float64 (scripts/gvom.py:1145-1148).  For float32 points the comparison
+// (double)d2 < md2 equals d2 < md2_f32, the smallest float32 whose value is
+// >= md2 (computed on the host), so it needs no float64 operation.
+__device__ __forceinline__ bool below_min_distance(float x, float y, float z, const ProcessConst &pc) {
     float s = __fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y));
-    return (double)__fadd_rn(s, __fmul_rn(z, z));
+    s = __fadd_rn(s, __fmul_rn(z, z));
+    return s < pc.md2_f32;
 }
-__device__ __forceinline__ double point_d2(double x, double y, double z) {
+__device__ __forceinline__ bool below_min_distance(double x, double y, double z, const ProcessConst &pc) {
     double s = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
-    return __dadd_rn(s, __dmul_rn(z, z));
+    return __dadd_rn(s, __dmul_rn(z, z)) < pc.md2;
 }
 
 __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned long long v) {
@@ -97,16 +103,34 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned l
 
 // ---------------------------------------------------------------------------
 // k_voxelize_trace: one thread per point.
+//
+// Every ray starts at the ego, so the cells around it receive an increment
+// from almost every ray.  Steps that land inside a kCube^3 block of cells
+// centred on the ego voxel are counted in shared memory and flushed once per
+// block (one global atomic per touched cell); all other steps add straight
+// into the dense count words.
 // ---------------------------------------------------------------------------
+constexpr int kCube = 16;
+constexpr int kCubeCells = kCube * kCube * kCube;
+
 template <typename PT, int NS>
 __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
                                                        float4 *__restrict__ prec, int *__restrict__ prank) {
+    __shared__ unsigned cube[kCubeCells];
     const int s = find_scan(tab, pc.nscans, blockIdx.x);
     const ScanDesc &sd = tab.s[s];
     const Geom g = pc.g;
+    const int ffloor = sd.fast_floor;
+    // cube origin: ego voxel - kCube/2 in each axis
+    const int cx0 = ray_index(sd.pt0[0], sd.oi[0], sd.od[0], ffloor) - kCube / 2;
+    const int cy0 = ray_index(sd.pt0[1], sd.oi[1], sd.od[1], ffloor) - kCube / 2;
+    const int cz0 = ray_index(sd.pt0[2], sd.oi[2], sd.od[2], ffloor) - kCube / 2;
+    for (int k = threadIdx.x; k < kCubeCells; k += blockDim.x) cube[k] = 0u;
+    __syncthreads();
     const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
     const bool active = i < sd.n;
     unsigned long long n_valid = 0, n_hit = 0, n_steps = 0;
+    const int Xe = g.Xe, XeXe = g.Xe * g.Xe;
     if (active) {
         const long long gi = sd.pt_base + i;
         float4 rec = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
@@ -114,33 +138,62 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
         PT x, y, z;
         load_point<PT>(sd, i, x, y, z);
         if (sd.tmode) transform_point<PT>(sd, x, y, z);
-        bool ok = isfinite((double)x) && isfinite((double)y) && isfinite((double)z);
-        if (ok && point_d2(x, y, z) < pc.md2) ok = false;
+        bool ok = isfinite(x) && isfinite(y) && isfinite(z);
+        if (ok && below_min_distance(x, y, z, pc)) ok = false;
         if (ok) {
             n_valid = 1;
-            // hit voxel in float64 (scripts/gvom.py:1153-1171)
-            const double q0 = __ddiv_rn((double)x, pc.xy_res);
-            const double q1 = __ddiv_rn((double)y, pc.xy_res);
-            const double q2 = __ddiv_rn((double)z, pc.z_res);
-            const double t0 = __dsub_rn(q0, sd.od[0]), t1 = __dsub_rn(q1, sd.od[1]), t2 = __dsub_rn(q2, sd.od[2]);
-            const double f0 = floor(t0), f1 = floor(t1), f2 = floor(t2);
-            // extended cell (grid + neighbourhood halo)
-            if (f0 >= -(double)g.exy && f0 < (double)(g.X + g.exy) && f1 >= -(double)g.exy &&
-                f1 < (double)(g.X + g.exy) && f2 >= -(double)g.ez && f2 < (double)(g.Z + g.ez)) {
-                const int bx = (int)f0, by = (int)f1, bz = (int)f2;
+            // hit voxel, fractions and ray end (scripts/gvom.py:1153-1171, 1182-1184):
+            // the float64 results, computed exactly with integer arithmetic
+            // (gvom_exact.cuh); float64 only for inputs it declines
+            float e0, e1, e2, fr0, fr1, fr2;
+            int bx = 0, by = 0, bz = 0;
+            bool fast = false, rng_ok = true;
+            if (sizeof(PT) == 4 && sd.fast_floor) {
+                long long b0, b1, b2;
+                bool r0, r1, r2;
+                fast = gx_coord((float)x, pc.rxy, sd.oi[0], e0, b0, fr0, r0) &&
+                       gx_coord((float)y, pc.rxy, sd.oi[1], e1, b1, fr1, r1) &&
+                       gx_coord((float)z, pc.rz, sd.oi[2], e2, b2, fr2, r2);
+                rng_ok = r0 && r1 && r2;
+                bx = (int)b0;
+                by = (int)b1;
+                bz = (int)b2;
+            }
+            bool in_ext;
+            if (!fast) {
+                const double q0 = __ddiv_rn((double)x, pc.xy_res);
+                const double q1 = __ddiv_rn((double)y, pc.xy_res);
+                const double q2 = __ddiv_rn((double)z, pc.z_res);
+                const double t0 = __dsub_rn(q0, sd.od[0]), t1 = __dsub_rn(q1, sd.od[1]), t2 = __dsub_rn(q2, sd.od[2]);
+                const double f0 = floor(t0), f1 = floor(t1), f2 = floor(t2);
+                in_ext = f0 >= -(double)g.exy && f0 < (double)(g.X + g.exy) && f1 >= -(double)g.exy &&
+                         f1 < (double)(g.X + g.exy) && f2 >= -(double)g.ez && f2 < (double)(g.Z + g.ez);
+                if (in_ext) {
+                    bx = (int)f0;
+                    by = (int)f1;
+                    bz = (int)f2;
+                    fr0 = __double2float_rn(__dsub_rn(t0, f0));
+                    fr1 = __double2float_rn(__dsub_rn(t1, f1));
+                    fr2 = __double2float_rn(__dsub_rn(t2, f2));
+                }
+                e0 = __double2float_rn(q0);
+                e1 = __double2float_rn(q1);
+                e2 = __double2float_rn(q2);
+            } else {
+                in_ext = rng_ok && bx >= -g.exy && bx < g.X + g.exy && by >= -g.exy && by < g.X + g.exy &&
+                         bz >= -g.ez && bz < g.Z + g.ez;
+            }
+            if (in_ext) {
                 const bool in_grid = bx >= 0 && bx < g.X && by >= 0 && by < g.X && bz >= 0 && bz < g.Z;
-                const long long cell =
-                    (long long)(bx + g.exy) + (long long)(by + g.exy) * g.Xe + (long long)(bz + g.ez) * g.Xe * g.Xe;
+                const int cell = (bx + g.exy) + (by + g.exy) * Xe + (bz + g.ez) * XeXe;
                 const unsigned long long inc = in_grid ? ((1ull << 32) | 1ull) : (1ull << 32);
                 const unsigned long long old = atomicAdd(&sd.cnt[cell], inc);
                 rank = (int)(old >> 32);
-                rec = make_float4(__double2float_rn(__dsub_rn(t0, f0)), __double2float_rn(__dsub_rn(t1, f1)),
-                                  __double2float_rn(__dsub_rn(t2, f2)), __int_as_float((int)cell));
+                rec = make_float4(fr0, fr1, fr2, __int_as_float(cell));
                 n_hit = in_grid;
             }
             // ray march (scripts/gvom.py:1174-1231), float32 state
             float px = sd.pt0[0], py = sd.pt0[1], pz = sd.pt0[2];
-            const float e0 = __double2float_rn(q0), e1 = __double2float_rn(q1), e2 = __double2float_rn(q2);
             float s0 = __fsub_rn(e0, px), s1 = __fsub_rn(e1, py), s2 = __fsub_rn(e2, pz);
             float ss = __fadd_rn(__fmul_rn(s0, s0), __fmul_rn(s1, s1));
             ss = __fadd_rn(ss, __fmul_rn(s2, s2));
@@ -159,23 +212,26 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
             const float ix = k == 0 ? __fdiv_rn(sk, ak) : __fdiv_rn(s0, ak);
             const float iy = k == 1 ? __fdiv_rn(sk, ak) : __fdiv_rn(s1, ak);
             const float iz = k == 2 ? __fdiv_rn(sk, ak) : __fdiv_rn(s2, ak);
-            const double R = __dsub_rn((double)rl, 1.0);
-            const double linc = fabs(__ddiv_rn(1.0, (double)sk));
-            const int K = ray_step_count(R, linc, pc.step_cap);
-            const int fast = sd.fast_floor;
-            unsigned long long* __restrict__ cnt = sd.cnt;
+            const int K = ray_step_count(rl, sk, pc.step_cap);
+            unsigned long long *__restrict__ cnt = sd.cnt;
             int st = 0;
             for (; st < K; st++) {
                 px = __fadd_rn(px, ix);
                 py = __fadd_rn(py, iy);
                 pz = __fadd_rn(pz, iz);
-                const int vx = ray_index(px, sd.oi[0], sd.od[0], fast);
-                const int vy = ray_index(py, sd.oi[1], sd.od[1], fast);
-                const int vz = ray_index(pz, sd.oi[2], sd.od[2], fast);
+                const int vx = ray_index(px, sd.oi[0], sd.od[0], ffloor);
+                const int vy = ray_index(py, sd.oi[1], sd.od[1], ffloor);
+                const int vz = ray_index(pz, sd.oi[2], sd.od[2], ffloor);
                 if ((unsigned)vx >= (unsigned)g.X || (unsigned)vy >= (unsigned)g.X || (unsigned)vz >= (unsigned)g.Z) break;
-                const long long cell =
-                    (long long)(vx + g.exy) + (long long)(vy + g.exy) * g.Xe + (long long)(vz + g.ez) * g.Xe * g.Xe;
-                atomicAdd(&cnt[cell], 1ull);
+                const unsigned ux = (unsigned)(vx - cx0), uy = (unsigned)(vy - cy0), uz = (unsigned)(vz - cz0);
+                if (ux < (unsigned)kCube && uy < (unsigned)kCube && uz < (unsigned)kCube) {
+                    atomicAdd(&cube[ux + kCube * (uy + kCube * uz)], 1u);
+                } else {
+                    // neighbouring rays of a warp often step into the same cell: one atomic per distinct cell
+                    const int cell = (vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe;
+                    const unsigned grp = __match_any_sync(__activemask(), cell);
+                    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&cnt[cell], (unsigned long long)__popc(grp));
+                }
             }
             n_steps = st;
         }
@@ -185,82 +241,153 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
     warp_add_u64(&sd.ctr->valid, n_valid);
     warp_add_u64(&sd.ctr->hits, n_hit);
     warp_add_u64(&sd.ctr->steps, n_steps);
+    __syncthreads();
+    for (int k = threadIdx.x; k < kCubeCells; k += blockDim.x) {
+        const unsigned c = cube[k];
+        if (c) {
+            const int vx = cx0 + (k % kCube), vy = cy0 + ((k / kCube) % kCube), vz = cz0 + k / (kCube * kCube);
+            atomicAdd(&sd.cnt[(vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe], (unsigned long long)c);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
-// k_assign: one thread per extended cell, blockIdx.y = scan.
-// In-grid cells: hit > 0 -> compact index (warp-aggregated counter) and the
-// record's hit/total/voxel id; else -(total)-1 (scripts/gvom.py:1233-1247).
-// Cells holding points (occupied or halo) get a point-group offset; the count
-// word is rewritten to (offset << 32 | points) for k_scatter / k_voxel_stats.
-// Free cells are cleared here; point cells are cleared by k_cleanup.
+// block-wide exclusive scan of two counters (256 threads); returns this
+// thread's exclusive prefixes and the block totals
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void block_scan2(int a, int b, int &ea, int &eb, int &ta, int &tb) {
+    __shared__ int wa[8], wb[8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int ia = a, ib = b;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int na = __shfl_up_sync(0xffffffffu, ia, o), nb = __shfl_up_sync(0xffffffffu, ib, o);
+        if (lane >= o) {
+            ia += na;
+            ib += nb;
+        }
+    }
+    if (lane == 31) {
+        wa[w] = ia;
+        wb[w] = ib;
+    }
+    __syncthreads();
+    int pa = 0, pb = 0, sa = 0, sb = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        if (k < w) {
+            pa += wa[k];
+            pb += wb[k];
+        }
+        sa += wa[k];
+        sb += wb[k];
+    }
+    ea = pa + ia - a;
+    eb = pb + ib - b;
+    ta = sa;
+    tb = sb;
+}
+
+// ---------------------------------------------------------------------------
+// k_assign: a tile of kAssignTile extended cells per block (256 threads x
+// kAssignPer cells, strided so every load and store is coalesced),
+// blockIdx.y = scan.  In-grid cells: hit > 0 -> compact index and the
+// record's hit/total/voxel id; else -(total)-1 (scripts/gvom.py:1233-1247).
+// Cells holding points (occupied or halo) get a point-group offset; their
+// count word becomes (offset << 32 | points) for k_scatter / k_voxel_stats.
+// Free cells are cleared here, point cells by k_cleanup.  One counter
+// atomic per block.
+// ---------------------------------------------------------------------------
+constexpr int kAssignPer = 16;
+constexpr int kAssignTile = 256 * kAssignPer;
+
+struct CellWalk {  // extended-grid coordinates of e, e + 256, e + 512, ...
+    int ex, ey, ez;
+    __device__ __forceinline__ void init(int e, int Xe) {
+        ex = e % Xe;
+        const int t = e / Xe;
+        ey = t % Xe;
+        ez = t / Xe;
+    }
+    __device__ __forceinline__ void next(int Xe) {
+        ex += 256;
+        while (ex >= Xe) {
+            ex -= Xe;
+            if (++ey == Xe) {
+                ey = 0;
+                ez++;
+            }
+        }
+    }
+};
+
 template <int NS>
 __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab) {
     const ScanDesc &sd = tab.s[blockIdx.y];
     const Geom g = pc.g;
-    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned long long v = 0;
-    int ex = 0, ey = 0, ez = 0;
-    bool inr = e < g.Vext;
-    if (inr) {
-        v = sd.cnt[e];
-        long long t = e;
-        ex = (int)(t % g.Xe);
-        t /= g.Xe;
-        ey = (int)(t % g.Xe);
-        ez = (int)(t / g.Xe);
-    }
-    const int hit = (int)(v >> 32);
-    const int total = (int)(v & 0xffffffffull);
-    const int gx = ex - g.exy, gy = ey - g.exy, gz = ez - g.ez;
-    const bool in_grid = inr && gx >= 0 && gx < g.X && gy >= 0 && gy < g.X && gz >= 0 && gz < g.Z;
-    const bool occ = in_grid && hit > 0;
-    const bool grp = inr && hit > 0;  // cell holds points
-    const unsigned lane = lane_id();
-    const unsigned lt = (1u << lane) - 1u;
-    // compact index
-    const unsigned om = __ballot_sync(0xffffffffu, occ);
-    int cbase = 0;
-    if (om) {
-        const int leader = __ffs(om) - 1;
-        if ((int)lane == leader) cbase = atomicAdd(&sd.ctr->C, __popc(om));
-        cbase = __shfl_sync(0xffffffffu, cbase, leader);
-    }
-    const int c = cbase + __popc(om & lt);
-    // point-group offset: warp exclusive scan of hit counts
-    int incl = grp ? hit : 0;
+    const int Vext = (int)g.Vext;
+    const int base = blockIdx.x * kAssignTile + threadIdx.x;
+    unsigned long long v[kAssignPer];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int n = __shfl_up_sync(0xffffffffu, incl, o);
-        if ((int)lane >= o) incl += n;
+    for (int k = 0; k < kAssignPer; k++) {
+        const int e = base + k * 256;
+        v[k] = e < Vext ? sd.cnt[e] : 0ull;
     }
-    const int wsum = __shfl_sync(0xffffffffu, incl, 31);
-    int pbase = 0;
-    if (wsum) {
-        if (lane == 31) pbase = atomicAdd(&sd.ctr->pts, wsum);
-        pbase = __shfl_sync(0xffffffffu, pbase, 31);
+    int n_occ = 0, n_pts = 0;
+    CellWalk cw;
+    cw.init(base, g.Xe);
+#pragma unroll
+    for (int k = 0; k < kAssignPer; k++) {
+        const int hit = (int)(v[k] >> 32);
+        const bool in_grid = (unsigned)(cw.ex - g.exy) < (unsigned)g.X && (unsigned)(cw.ey - g.exy) < (unsigned)g.X &&
+                             (unsigned)(cw.ez - g.ez) < (unsigned)g.Z;
+        if (in_grid && hit > 0) n_occ++;
+        n_pts += hit;
+        cw.next(g.Xe);
     }
-    const int off = pbase + incl - (grp ? hit : 0);
-    if (!inr) return;
-    if (in_grid) {
-        const long long gid = (long long)gx + (long long)gy * g.X + (long long)gz * g.X * g.X;
-        if (occ) {
-            if (c < sd.rec_cap) {
-                VoxelRec *r = &sd.rec[c];
-                r->hit = hit;
-                r->total = total;
-                r->aux[0] = __int_as_float((int)gid);
-            } else {
-                atomicOr(&sd.ctr->overflow, 1);
+    int eo, ep, to, tp;
+    block_scan2(n_occ, n_pts, eo, ep, to, tp);
+    __shared__ int bases[2];
+    if (threadIdx.x == 0) {
+        bases[0] = to ? atomicAdd(&sd.ctr->C, to) : 0;
+        bases[1] = tp ? atomicAdd(&sd.ctr->pts, tp) : 0;
+    }
+    __syncthreads();
+    int c = bases[0] + eo, off = bases[1] + ep;
+    cw.init(base, g.Xe);
+#pragma unroll
+    for (int k = 0; k < kAssignPer; k++) {
+        const int e = base + k * 256;
+        if (e < Vext) {
+            const int hit = (int)(v[k] >> 32);
+            const int total = (int)(v[k] & 0xffffffffull);
+            const int gx = cw.ex - g.exy, gy = cw.ey - g.exy, gz = cw.ez - g.ez;
+            const bool in_grid = (unsigned)gx < (unsigned)g.X && (unsigned)gy < (unsigned)g.X && (unsigned)gz < (unsigned)g.Z;
+            if (in_grid) {
+                const int gid = gx + gy * g.X + gz * g.X * g.X;
+                if (hit > 0) {
+                    if (c < sd.rec_cap) {
+                        VoxelRec *r = &sd.rec[c];
+                        r->hit = hit;
+                        r->total = total;
+                        r->aux[0] = __int_as_float(gid);
+                    } else {
+                        atomicOr(&sd.ctr->overflow, 1);
+                    }
+                    sd.idx[gid] = c;
+                    c++;
+                } else {
+                    sd.idx[gid] = -total - 1;
+                    if (total) sd.cnt[e] = 0ull;
+                }
             }
-            sd.idx[gid] = c;
-        } else {
-            sd.idx[gid] = -total - 1;
-            if (total) sd.cnt[e] = 0ull;
+            if (hit > 0) {
+                sd.cnt[e] = ((unsigned long long)(unsigned)off << 32) | (unsigned)hit;
+                off += hit;
+            }
         }
+        cw.next(g.Xe);
     }
-    if (grp) sd.cnt[e] = ((unsigned long long)(unsigned)off << 32) | (unsigned)hit;
 }
 
 // ---------------------------------------------------------------------------
@@ -285,82 +412,120 @@ __global__ void __launch_bounds__(256) k_scatter(const ProcessConst pc, const __
 }
 
 // ---------------------------------------------------------------------------
-// k_voxel_stats: one thread per occupied voxel, blockIdx.y = scan.
-// Two-pass mean / covariance over the points of the (2exy+1)^2 (2ez+1)
-// neighbourhood (scripts/gvom.py:1249-1387), float32 on coordinates centred
-// on the voxel centre with Kahan-compensated sums; minimum height over the
-// voxel's own points (scripts/gvom.py:1389-1421), exact.
+// Neighbourhood statistics (scripts/gvom.py:1249-1421) in two steps.
+//
+// k_cell_moments: one thread per cell that holds points (the thread of the
+// cell's rank-0 point).  Over the cell's points, in ascending point order:
+// count, mean of the in-cell fraction and the second moments about that mean
+// (float32, Kahan-compensated, coordinates centred on the cell centre), and
+// the minimum height fraction (exact).  Stored at the cell's group offset.
+//
+// k_voxel_stats: one thread per occupied voxel.  Combines the moments of
+// the (2exy+1)^2 (2ez+1) neighbour cells, each shifted by its offset from the
+// voxel, with the pairwise (Chan) update in a fixed cell order; the result
+// is the neighbourhood mean (relative to the voxel corner), covariance and
+// count the reference accumulates point by point.
 // ---------------------------------------------------------------------------
+struct __align__(16) CellMom {
+    float m[3];     // mean fraction - 0.5
+    float n;        // points
+    float c[6];     // second moments about the mean: xx xy xz yy yz zz
+    float min_h;    // lowest height fraction
+    float pad;
+};
+
 template <int NS>
-__global__ void __launch_bounds__(128) k_voxel_stats(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
-                                                    const float4 *__restrict__ sorted) {
-    const ScanDesc &sd = tab.s[blockIdx.y];
-    const Geom g = pc.g;
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    const int C = *(volatile int *)&sd.ctr->C;
-    if (c >= C || c >= sd.rec_cap) return;
-    VoxelRec *r = &sd.rec[c];
-    const int gid = __float_as_int(r->aux[0]);
-    const int x = gid % g.X, y = (gid / g.X) % g.X, z = gid / (g.X * g.X);
-    const long long e0 = (long long)(x + g.exy) + (long long)(y + g.exy) * g.Xe + (long long)(z + g.ez) * g.Xe * g.Xe;
-    const float4 *__restrict__ P = sorted + sd.pt_base;
-    // own cell: min height
-    float mh = 1.0f;
-    {
-        const unsigned long long v = sd.cnt[e0];
-        const int off = (int)(v >> 32), n = (int)(v & 0xffffffffull);
-        for (int j = 0; j < n; j++) mh = fminf(mh, P[off + j].z);
-    }
+__global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
+                                                     const float4 *__restrict__ prec, const int *__restrict__ prank,
+                                                     const float4 *__restrict__ sorted, CellMom *__restrict__ mom) {
+    const int s = find_scan(tab, pc.nscans, blockIdx.x);
+    const ScanDesc &sd = tab.s[s];
+    const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
+    if (i >= sd.n) return;
+    const long long gi = sd.pt_base + i;
+    const int cell = __float_as_int(prec[gi].w);
+    if (cell < 0 || prank[gi] != 0) return;
+    const unsigned long long v = sd.cnt[cell];
+    const int off = (int)(v >> 32), n = (int)(v & 0xffffffffull);
+    const float4 *__restrict__ P = sorted + sd.pt_base + off;
     KSum sx, sy, sz;
     sx.init(); sy.init(); sz.init();
-    int n_all = 0;
-    for (int dz = -g.ez; dz <= g.ez; dz++)
-        for (int dy = -g.exy; dy <= g.exy; dy++)
-            for (int dx = -g.exy; dx <= g.exy; dx++) {
-                const long long e = e0 + dx + (long long)dy * g.Xe + (long long)dz * g.Xe * g.Xe;
-                const unsigned long long v = sd.cnt[e];
-                const int n = (int)(v & 0xffffffffull);
-                if (!n) continue;
-                const int off = (int)(v >> 32);
-                // centred coordinate of a neighbour point: frac + offset - 0.5
-                const float ox = (float)dx - 0.5f, oy = (float)dy - 0.5f, oz = (float)dz - 0.5f;
-                for (int j = 0; j < n; j++) {
-                    const float4 p = P[off + j];
-                    sx.add(__fadd_rn(p.x, ox));
-                    sy.add(__fadd_rn(p.y, oy));
-                    sz.add(__fadd_rn(p.z, oz));
-                }
-                n_all += n;
-            }
-    const float nf = (float)n_all;
-    const float mx = __fdiv_rn(sx.s, nf), my = __fdiv_rn(sy.s, nf), mz = __fdiv_rn(sz.s, nf);
+    float mh = 1.0f;
+    for (int j = 0; j < n; j++) {
+        const float4 p = P[j];
+        sx.add(__fsub_rn(p.x, 0.5f));
+        sy.add(__fsub_rn(p.y, 0.5f));
+        sz.add(__fsub_rn(p.z, 0.5f));
+        mh = fminf(mh, p.z);
+    }
+    const float nf = (float)n;
+    const float mx = __fdiv_rn(__fsub_rn(sx.s, sx.c), nf), my = __fdiv_rn(__fsub_rn(sy.s, sy.c), nf);
+    const float mz = __fdiv_rn(__fsub_rn(sz.s, sz.c), nf);
     KSum cxx, cxy, cxz, cyy, cyz, czz;
     cxx.init(); cxy.init(); cxz.init(); cyy.init(); cyz.init(); czz.init();
-    for (int dz = -g.ez; dz <= g.ez; dz++)
-        for (int dy = -g.exy; dy <= g.exy; dy++)
-            for (int dx = -g.exy; dx <= g.exy; dx++) {
-                const long long e = e0 + dx + (long long)dy * g.Xe + (long long)dz * g.Xe * g.Xe;
-                const unsigned long long v = sd.cnt[e];
-                const int n = (int)(v & 0xffffffffull);
-                if (!n) continue;
-                const int off = (int)(v >> 32);
-                const float ox = (float)dx - 0.5f - mx, oy = (float)dy - 0.5f - my, oz = (float)dz - 0.5f - mz;
-                for (int j = 0; j < n; j++) {
-                    const float4 p = P[off + j];
-                    const float ux = __fadd_rn(p.x, ox), uy = __fadd_rn(p.y, oy), uz = __fadd_rn(p.z, oz);
-                    cxx.add(__fmul_rn(ux, ux));
-                    cxy.add(__fmul_rn(ux, uy));
-                    cxz.add(__fmul_rn(ux, uz));
-                    cyy.add(__fmul_rn(uy, uy));
-                    cyz.add(__fmul_rn(uy, uz));
-                    czz.add(__fmul_rn(uz, uz));
+    for (int j = 0; j < n; j++) {
+        const float4 p = P[j];
+        const float ux = __fsub_rn(__fsub_rn(p.x, 0.5f), mx), uy = __fsub_rn(__fsub_rn(p.y, 0.5f), my);
+        const float uz = __fsub_rn(__fsub_rn(p.z, 0.5f), mz);
+        cxx.add(__fmul_rn(ux, ux));
+        cxy.add(__fmul_rn(ux, uy));
+        cxz.add(__fmul_rn(ux, uz));
+        cyy.add(__fmul_rn(uy, uy));
+        cyz.add(__fmul_rn(uy, uz));
+        czz.add(__fmul_rn(uz, uz));
+    }
+    float4 *o = reinterpret_cast<float4 *>(&mom[sd.pt_base + off]);
+    o[0] = make_float4(mx, my, mz, nf);
+    o[1] = make_float4(__fsub_rn(cxx.s, cxx.c), __fsub_rn(cxy.s, cxy.c), __fsub_rn(cxz.s, cxz.c), __fsub_rn(cyy.s, cyy.c));
+    o[2] = make_float4(__fsub_rn(cyz.s, cyz.c), __fsub_rn(czz.s, czz.c), mh, 0.f);
+}
+
+template <int NS>
+__global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
+                                                    const CellMom *__restrict__ mom) {
+    const ScanDesc &sd = tab.s[blockIdx.y];
+    const Geom g = pc.g;
+    const int C = min(*(volatile int *)&sd.ctr->C, (int)sd.rec_cap);
+    const CellMom *__restrict__ M = mom + sd.pt_base;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+        VoxelRec *r = &sd.rec[c];
+        const int gid = __float_as_int(r->aux[0]);
+        const int x = gid % g.X, y = (gid / g.X) % g.X, z = gid / (g.X * g.X);
+        const int e0 = (x + g.exy) + (y + g.exy) * g.Xe + (z + g.ez) * g.Xe * g.Xe;
+        float n = 0.f, m0 = 0.f, m1 = 0.f, m2 = 0.f;
+        float C0 = 0.f, C1 = 0.f, C2 = 0.f, C3 = 0.f, C4 = 0.f, C5 = 0.f;
+        float mh = 1.0f;
+        for (int dz = -g.ez; dz <= g.ez; dz++)
+            for (int dy = -g.exy; dy <= g.exy; dy++)
+                for (int dx = -g.exy; dx <= g.exy; dx++) {
+                    const unsigned long long v = sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe];
+                    if (!(v & 0xffffffffull)) continue;
+                    const CellMom cm = M[(int)(v >> 32)];
+                    if (dx == 0 && dy == 0 && dz == 0) mh = cm.min_h;
+                    // cell mean in this voxel's frame, centred on the voxel centre
+                    const float b0 = __fadd_rn(cm.m[0], (float)dx), b1 = __fadd_rn(cm.m[1], (float)dy);
+                    const float b2 = __fadd_rn(cm.m[2], (float)dz);
+                    const float nb = cm.n, nn = __fadd_rn(n, nb);
+                    const float d0 = __fsub_rn(b0, m0), d1 = __fsub_rn(b1, m1), d2 = __fsub_rn(b2, m2);
+                    const float wb = __fdiv_rn(nb, nn);
+                    const float f = __fmul_rn(n, wb);  // n * nb / (n + nb)
+                    m0 = __fadd_rn(m0, __fmul_rn(d0, wb));
+                    m1 = __fadd_rn(m1, __fmul_rn(d1, wb));
+                    m2 = __fadd_rn(m2, __fmul_rn(d2, wb));
+                    C0 = __fadd_rn(__fadd_rn(C0, cm.c[0]), __fmul_rn(__fmul_rn(d0, d0), f));
+                    C1 = __fadd_rn(__fadd_rn(C1, cm.c[1]), __fmul_rn(__fmul_rn(d0, d1), f));
+                    C2 = __fadd_rn(__fadd_rn(C2, cm.c[2]), __fmul_rn(__fmul_rn(d0, d2), f));
+                    C3 = __fadd_rn(__fadd_rn(C3, cm.c[3]), __fmul_rn(__fmul_rn(d1, d1), f));
+                    C4 = __fadd_rn(__fadd_rn(C4, cm.c[4]), __fmul_rn(__fmul_rn(d1, d2), f));
+                    C5 = __fadd_rn(__fadd_rn(C5, cm.c[5]), __fmul_rn(__fmul_rn(d2, d2), f));
+                    n = nn;
                 }
-            }
-    float4 *o = reinterpret_cast<float4 *>(r);
-    o[0] = make_float4(mx + 0.5f, my + 0.5f, mz + 0.5f, __fdiv_rn(cxx.s, nf));
-    o[1] = make_float4(__fdiv_rn(cxy.s, nf), __fdiv_rn(cxz.s, nf), __fdiv_rn(cyy.s, nf), __fdiv_rn(cyz.s, nf));
-    reinterpret_cast<float2 *>(r)[4] = make_float2(__fdiv_rn(czz.s, nf), nf);
-    r->min_h = mh;
+        float4 *o = reinterpret_cast<float4 *>(r);
+        o[0] = make_float4(__fadd_rn(m0, 0.5f), __fadd_rn(m1, 0.5f), __fadd_rn(m2, 0.5f), __fdiv_rn(C0, n));
+        o[1] = make_float4(__fdiv_rn(C1, n), __fdiv_rn(C2, n), __fdiv_rn(C3, n), __fdiv_rn(C4, n));
+        reinterpret_cast<float2 *>(r)[4] = make_float2(__fdiv_rn(C5, n), n);
+        r->min_h = mh;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -384,7 +549,7 @@ __global__ void __launch_bounds__(256) k_cleanup(const ProcessConst pc, const __
 // ---------------------------------------------------------------------------
 template <int NS>
 static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int total_blocks, int max_n, int dtype,
-                             float4 *prec, int *prank, float4 *sorted, cudaStream_t st, cudaEvent_t *ev) {
+                             float4 *prec, int *prank, float4 *sorted, CellMom *mom, cudaStream_t st, cudaEvent_t *ev) {
     ScanTable<NS> tab;
     for (int i = 0; i < NS; i++) tab.s[i] = i < pc.nscans ? table[i] : table[0];
     if (total_blocks < 1) total_blocks = 1;
@@ -397,24 +562,29 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
     else
         k_voxelize_trace<float, NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
     mark(1);
-    dim3 ga((unsigned)((pc.g.Vext + 255) / 256), pc.nscans);
+    dim3 ga((unsigned)((pc.g.Vext + kAssignTile - 1) / kAssignTile), pc.nscans);
     k_assign<NS><<<ga, 256, 0, st>>>(pc, tab);
     mark(2);
     k_scatter<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank, sorted);
     mark(3);
-    dim3 gs((unsigned)((max_n + 127) / 128 > 0 ? (max_n + 127) / 128 : 1), pc.nscans);
-    k_voxel_stats<NS><<<gs, 128, 0, st>>>(pc, tab, sorted);
+    k_cell_moments<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank, sorted, mom);
     mark(4);
-    k_cleanup<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
+    const int want = (max_n + 255) / 256;
+    dim3 gs((unsigned)std::max(1, std::min(want, 152 * 8)), pc.nscans);
+    k_voxel_stats<NS><<<gs, 256, 0, st>>>(pc, tab, mom);
     mark(5);
+    k_cleanup<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
+    mark(6);
     return cudaGetLastError();
 }
 
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
-                           int dtype, float4 *prec, int *prank, float4 *sorted, cudaStream_t st, cudaEvent_t *ev) {
-    if (nscans == 1) return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st, ev);
-    if (nscans <= 4) return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st, ev);
-    return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, st, ev);
+                           int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
+                           cudaEvent_t *ev) {
+    CellMom *mom = static_cast<CellMom *>(moments);
+    if (nscans == 1) return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev);
+    if (nscans <= 4) return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev);
+    return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev);
 }
 
 }  // namespace gvom

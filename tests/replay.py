@@ -21,6 +21,7 @@ from oracle.canonical import canonical_map, canonical_state
 
 HEIGHT_ATOL = 1e-4
 REL_TOL = 1e-3
+SLOPE_ATOL = 1e-9
 # mean/cov are in voxel units (|mean| < 2, cov < 1).
 STAT_ATOL = 1e-5
 STAT_RTOL = 1e-4
@@ -137,7 +138,7 @@ def compare_combine(got_out, ref: dict, got_maps: dict, params, what: str):
             raise AssertionError(f"{what} {k}: max err {d.max()}")
     assert_exact(vis, ref["vis"], f"{what} visibility")
     for k in ("slope_x", "slope_y"):
-        assert_rel(got_maps[k], ref[k], f"{what} {k}", atol=1e-9)
+        assert_rel(got_maps[k], ref[k], f"{what} {k}", atol=SLOPE_ATOL)
     assert_rel(got_maps["guess"], ref["guess"], f"{what} guessed height delta", atol=HEIGHT_ATOL)
     assert_rel(rough, ref["rough"], f"{what} roughness", atol=1e-9)
     slope_thr = params[8]
