@@ -181,17 +181,19 @@ int debug_chunk();
 // ---------------------------------------------------------------------------
 
 // floor((double)p - od) for an integer-valued od, as the reference computes a
-// ray voxel index (scripts/gvom.py:1215-1223).  For |od| < 2^24 the float32
-// path floor(p) - oi is exact except for p in (-1, 0), where rounding of the
-// double subtraction may reach the integer above; those take the double path.
-// floor(p) for |p| < 2^22 is read off the bits of p + 1.5 * 2^23 rounded
-// down (the sum lies in [2^23, 2^24], where float32 spacing is 1).
+// ray voxel index (scripts/gvom.py:1215-1223).  For |od| < 2^24 this equals
+// floor(p) - oi, except for p in (-2^-20, 0): there p - od may round to the
+// integer -od itself (the float64 spacing near |od| < 2^24 is at most 2^-29,
+// so for p <= -2^-20 the rounded difference stays below -od and the float32
+// answer holds); that sliver takes the double path.  floor(p) for |p| < 2^22
+// is read off the bits of p + 1.5 * 2^23 rounded down (the sum lies in
+// [2^23, 2^24], where float32 spacing is 1).
 // Returns INT_MIN for values far outside any grid (and NaN).
 __device__ __forceinline__ int ray_index(float p, int oi, double od, int fast) {
-    if (fast && fabsf(p) < 4194304.0f && !(p > -1.0f && p < 0.0f))
+    if (fast && fabsf(p) < 4194304.0f && !(p > -9.5367431640625e-07f && p < 0.0f))
         return __float_as_int(__fadd_rd(p, 12582912.0f)) - 0x4B400000 - oi;
     if (!(fabsf(p) < 1073741824.0f)) return INT32_MIN;
-    if (fast && !(p > -1.0f && p < 0.0f)) return __float2int_rd(p) - oi;
+    if (fast && !(p > -9.5367431640625e-07f && p < 0.0f)) return __float2int_rd(p) - oi;
     double t = __dsub_rn((double)p, od);
     double f = floor(t);
     if (!(fabs(f) < 1.0e9)) return INT32_MIN;

@@ -71,6 +71,13 @@ __global__ void check(double res, ExactRes R, int mode, unsigned long long seed,
             const int vi = ray_index(pt, (int)od, od, fast);
             const double tr = floor(__dsub_rn((double)pt, od));
             if (fabs(tr) < 1e9 && vi != (int)tr) ri_bad++;
+            // small negative positions (ray near the world origin plane) with origins up to 2^24
+            const float pn = -ldexpf((float)u + 1e-3f, -(int)(u2 * 40.0));
+            const double on = floor((u2 - 0.5) * (mode == 1 ? 3.3e7 : 600.0));
+            const int fn = fabs(on) < 16777216.0 ? 1 : 0;
+            const int vn = ray_index(pn, (int)on, on, fn);
+            const double tn = floor(__dsub_rn((double)pn, on));
+            if (fabs(tn) < 1e9 && vn != (int)tn) ri_bad++;
         }
     }
     atomicAdd(&out->trials, (unsigned long long)per_thread);
