@@ -342,15 +342,34 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
         d.tmode = s.tdtype == GVOM_NONE ? 0 : (s.tdtype == GVOM_F32 ? 1 : 2);
         for (int r = 0; r < 12; r++) d.T[r] = s.T[r];
         ray_origin(h, s.ego, d.od);
-        bool fast = true;
+        // ray positions stay within one step of the grid, so for
+        // |origin| + grid + 2 < 2^22 every position the march visits is below
+        // 2^22 in magnitude (the float32 floor of ray_index applies)
+        bool fast = true, exact = true;
+        const double lim = 4194304.0 - (double)std::max(h->g.X, h->g.Z) - 2.0;
         for (int a = 0; a < 3; a++) {
-            d.oi[a] = (int)d.od[a];
-            if (std::fabs(d.od[a]) >= 16777216.0) fast = false;
+            if (!(std::fabs(d.od[a]) < 2147483648.0)) exact = false;
+            if (!(std::fabs(d.od[a]) < lim)) fast = false;
         }
+        for (int a = 0; a < 3; a++) d.oi[a] = exact ? (int)d.od[a] : 0;
         d.fast_floor = fast ? 1 : 0;
+        d.exact_ok = exact ? 1 : 0;
         d.pt0[0] = (float)(s.ego[0] / h->p.xy_resolution);
         d.pt0[1] = (float)(s.ego[1] / h->p.xy_resolution);
         d.pt0[2] = (float)(s.ego[2] / h->p.z_resolution);
+        // shared-memory cube of ray-step counts around the ego voxel, clamped
+        // into the grid (any placement is valid; near the ego is where every
+        // ray passes)
+        d.cube_on = (fast && h->g.X >= kCube && h->g.Z >= kCube) ? 1 : 0;
+        for (int a = 0; a < 3; a++) {
+            const int dim = a < 2 ? h->g.X : h->g.Z;
+            int c = 0;
+            if (d.cube_on) {
+                const double ev = std::floor((double)d.pt0[a] - d.od[a]);
+                c = (int)std::min(std::max(ev - kCube / 2, 0.0), (double)(dim - kCube));
+            }
+            d.cube0[a] = c;
+        }
         d.slot = slot;
         d.block_begin = block;
         d.nblocks = (int)((s.n + 255) / 256);

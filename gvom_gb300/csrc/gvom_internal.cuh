@@ -21,6 +21,8 @@
 namespace gvom {
 
 constexpr int kMaxBatch = 16;         // scans per batched launch
+constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
+constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
 
 // Per-voxel record.  Ring slots store aux[0] = voxel id (int bits); the
@@ -57,11 +59,14 @@ struct ScanDesc {
     const void *pts;       // device points
     long long n, stride;   // rows, elements per row
     int tmode;             // 0 none, 1 float32 transform, 2 float64 transform
-    int fast_floor;        // origin small enough for the float32 voxel-index path
+    int fast_floor;        // |origin| + grid < 2^22: float32 ray voxel indices (see ray_index)
+    int exact_ok;          // |origin| < 2^31: integer hit-voxel arithmetic (gx_coord)
     double T[12];          // transform rows 0..2 (a float32 transform is stored exactly)
     double od[3];          // voxel origin (integer-valued doubles)
-    int oi[3];
+    int oi[3];             // the same as int (valid when exact_ok)
     float pt0[3];          // ray start: (float)(ego / resolution)
+    int cube0[3];          // grid voxel of the shared-memory cube's low corner
+    int cube_on;           // the cube lies inside the grid (grid >= kCube per axis)
     int slot;
     int block_begin;       // first block of this scan in point-parallel launches
     int nblocks;
@@ -198,6 +203,13 @@ __device__ __forceinline__ int ray_index(float p, int oi, double od, int fast) {
     double f = floor(t);
     if (!(fabs(f) < 1.0e9)) return INT32_MIN;
     return (int)f;
+}
+
+// p in (-2^-20, 0): the one range where floor(p) - origin can differ from the
+// reference's floor((double)p - origin) (see ray_index).  -0.0 is excluded:
+// both formulas give -origin there.
+__device__ __forceinline__ bool in_sliver(float p) {
+    return (unsigned)__float_as_int(p) - 0x80000001u < 0x357FFFFFu;
 }
 
 // Number of iterations of `while (length < R) { ...; length += inc; }` with

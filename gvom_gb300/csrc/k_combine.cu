@@ -321,8 +321,16 @@ __device__ __forceinline__ bool height_known(double h) {
     return b >= 0 || (b & 0x7fffffffffffffffLL) < 0x408F400000000000LL;  // |h| < 1000
 }
 
+// atan2(a, im) with im = RN(1/m), m = sqrt(a0^2 + a1^2 + 1) >= 1: atan2f of
+// the rounded arguments (relative error a few 1e-7); for |a| below the
+// float32 normal range the angle is a * m to within (a m)^2 / 3 relative.
+__device__ __forceinline__ double slope_angle(double a, double m, double im) {
+    if (fabs(a) < 1e-30) return __dmul_rn(a, m);
+    return (double)atan2f((float)a, (float)im);
+}
+
 // __calculate_slope (scripts/gvom.py:717-805) in the reference's float64
-// operation order.
+// operation order up to the final log / atan2.
 __device__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY], int x0t, int y0t, int x0, int y0,
                           int X, double res, double &rough, double &slx, double &sly) {
 #define H(gx, gy) sh[(gx) - x0t + kHalo][(gy) - y0t + kHalo]
@@ -371,23 +379,38 @@ __device__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY
         err = __dadd_rn(err, __dmul_rn(e, e));
     }
     err = __ddiv_rn(err, (double)n_good);
-    if (err > 0.0) err = log(err);
+    // log and atan2 of these exact float64 values in float32: the results are
+    // compared at 1e-3 relative, and the float32 functions stay within a few
+    // 1e-7 relative here.  log(err) near err = 1 goes through log1p of the
+    // exact err - 1; values outside the float32 range keep float64.
+    if (err > 0.0) {
+        if (err >= 0.5 && err <= 2.0) err = (double)log1pf((float)__dsub_rn(err, 1.0));
+        else if (err > 1e-30 && err < 1e30) err = (double)logf((float)err);
+        else err = log(err);
+    }
     rough = err;
     const double im = __ddiv_rn(1.0, m);
-    slx = atan2(a0, im);
-    sly = atan2(a1, im);
+    slx = slope_angle(a0, m, im);
+    sly = slope_angle(a1, m, im);
 }
 
 __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DParams mp) {
     __shared__ double sh[kSX][kSY];
-    __shared__ int szl[kSX][kSY];
-    __shared__ float sml[kSX][kSY];
+    // lowest occupied z and in-voxel height per column for the float32 plane
+    // fit; afterwards reused for the results of the float64 queue
+    __shared__ __align__(16) unsigned char fit_buf[kSX * kSY * 8];
+    int (*szl)[kSY] = reinterpret_cast<int (*)[kSY]>(fit_buf);
+    float (*sml)[kSY] = reinterpret_cast<float (*)[kSY]>(fit_buf + kSX * kSY * 4);
+    double (*qres)[3] = reinterpret_cast<double (*)[3]>(fit_buf);
+    __shared__ int qcell[kTX * kTY];
+    __shared__ int qn;
     __shared__ unsigned char kn[kSX][kSY];
     __shared__ unsigned char nky[kSX][kSY + 2];  // next known y index (in tile coords) at or after sy, kSY if none
     __shared__ unsigned char nkx[kSY][kSX + 2];  // next known x index at or after sx
     const int X = mp.X;
     const int x0t = blockIdx.y * kTX, y0t = blockIdx.x * kTY;
     const int tid = threadIdx.y * kTY + threadIdx.x;
+    if (tid == 0) qn = 0;
     for (int k = tid; k < kSX * kSY; k += kTX * kTY) {
         const int sx = k / kSY, sy = k % kSY;
         const int gx = x0t + sx - kHalo, gy = y0t + sy - kHalo;
@@ -418,7 +441,7 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
     }
     __syncthreads();
     const int x0 = x0t + threadIdx.y, y0 = y0t + threadIdx.x;
-    if (x0 >= X || y0 >= X) return;
+    const bool valid = x0 < X && y0 < X;
     const int tx = threadIdx.y + kHalo, ty = threadIdx.x + kHalo;  // this cell in tile coords
     const int cell = x0 * X + y0;
     const bool known = kn[tx][ty];
@@ -430,6 +453,7 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
     // cancellation (singular normal matrix, residual far below the height
     // spread, log near 0, a slope component near 0)
     double rough = -1.0, slx = 0.0, sly = 0.0;
+    bool need_exact = false;
     {
         const int xl = max(0, x0 - 1), xh = min(X, x0 + 2), yl = max(0, y0 - 1), yh = min(X, y0 + 2);
         int n_good = 0, sxi = 0, syi = 0;
@@ -450,7 +474,7 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
                     syi += yy - y0;
                 }
             }
-        if (n_good >= 3) {
+        if (valid && n_good >= 3) {
             bool exact = !all_vox;
             float a0 = 0.f, a1 = 0.f, m = 1.f, err = 0.f, szz = 0.f;
             const float nf = (float)n_good;
@@ -510,13 +534,35 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
                 exact = !(err > 1e-4f * (szz / nf)) || fabsf(rf) < 1.0f || small < 5e-3f * big || big < 2e-3f;
             }
             if (exact) {
-                slope_f64(sh, kn, x0t, y0t, x0, y0, X, mp.xy_res, rough, slx, sly);
+                need_exact = true;
+                qcell[atomicAdd(&qn, 1)] = tid;
             } else {
                 rough = (double)rf;
                 slx = (double)sxf;
                 sly = (double)syf;
             }
         }
+    }
+    // cells that need the float64 sequence are compacted into a queue so that
+    // whole warps run it, instead of one lane in every warp that has one
+    __syncthreads();  // queue complete; szl / sml no longer read
+    {
+        const int nq = qn;
+        for (int q = tid; q < nq; q += kTX * kTY) {
+            const int t = qcell[q];
+            double r = -1.0, a = 0.0, b = 0.0;
+            slope_f64(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, X, mp.xy_res, r, a, b);
+            qres[t][0] = r;
+            qres[t][1] = a;
+            qres[t][2] = b;
+        }
+    }
+    __syncthreads();
+    if (!valid) return;
+    if (need_exact) {
+        rough = qres[tid][0];
+        slx = qres[tid][1];
+        sly = qres[tid][2];
     }
 
     // __guess_height (scripts/gvom.py:592-714), loop-condition and y_nh quirks

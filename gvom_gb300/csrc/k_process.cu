@@ -105,13 +105,12 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned l
 // k_voxelize_trace: one thread per point.
 //
 // Every ray starts at the ego, so the cells around it receive an increment
-// from almost every ray.  Steps that land inside a kCube^3 block of cells
-// centred on the ego voxel are counted in shared memory and flushed once per
-// block (one global atomic per touched cell); all other steps add straight
-// into the dense count words.
+// from almost every ray.  A ray's first steps, while they stay inside a
+// kCube^3 block of cells around the ego voxel (sd.cube0, inside the grid),
+// are counted in shared memory and flushed once per block (one global atomic
+// per touched cell); the remaining steps add straight into the dense count
+// words, one atomic per distinct cell of the warp.
 // ---------------------------------------------------------------------------
-constexpr int kCube = 16;
-constexpr int kCubeCells = kCube * kCube * kCube;
 
 template <typename PT, int NS>
 __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
@@ -121,11 +120,8 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
     const ScanDesc &sd = tab.s[s];
     const Geom g = pc.g;
     const int ffloor = sd.fast_floor;
-    // cube origin: ego voxel - kCube/2 in each axis
-    const int cx0 = ray_index(sd.pt0[0], sd.oi[0], sd.od[0], ffloor) - kCube / 2;
-    const int cy0 = ray_index(sd.pt0[1], sd.oi[1], sd.od[1], ffloor) - kCube / 2;
-    const int cz0 = ray_index(sd.pt0[2], sd.oi[2], sd.od[2], ffloor) - kCube / 2;
-    for (int k = threadIdx.x; k < kCubeCells; k += blockDim.x) cube[k] = 0u;
+    if (sd.cube_on)
+        for (int k = threadIdx.x; k < kCubeCells; k += blockDim.x) cube[k] = 0u;
     __syncthreads();
     const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
     const bool active = i < sd.n;
@@ -148,7 +144,7 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
             float e0, e1, e2, fr0, fr1, fr2;
             int bx = 0, by = 0, bz = 0;
             bool fast = false, rng_ok = true;
-            if (sizeof(PT) == 4 && sd.fast_floor) {
+            if (sizeof(PT) == 4 && sd.exact_ok) {
                 long long b0, b1, b2;
                 bool r0, r1, r2;
                 fast = gx_coord((float)x, pc.rxy, sd.oi[0], e0, b0, fr0, r0) &&
@@ -215,22 +211,61 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
             const int K = ray_step_count(rl, sk, pc.step_cap);
             unsigned long long *__restrict__ cnt = sd.cnt;
             int st = 0;
-            for (; st < K; st++) {
-                px = __fadd_rn(px, ix);
-                py = __fadd_rn(py, iy);
-                pz = __fadd_rn(pz, iz);
-                const int vx = ray_index(px, sd.oi[0], sd.od[0], ffloor);
-                const int vy = ray_index(py, sd.oi[1], sd.od[1], ffloor);
-                const int vz = ray_index(pz, sd.oi[2], sd.od[2], ffloor);
-                if ((unsigned)vx >= (unsigned)g.X || (unsigned)vy >= (unsigned)g.X || (unsigned)vz >= (unsigned)g.Z) break;
-                const unsigned ux = (unsigned)(vx - cx0), uy = (unsigned)(vy - cy0), uz = (unsigned)(vz - cz0);
-                if (ux < (unsigned)kCube && uy < (unsigned)kCube && uz < (unsigned)kCube) {
-                    atomicAdd(&cube[ux + kCube * (uy + kCube * uz)], 1u);
-                } else {
-                    // neighbouring rays of a warp often step into the same cell: one atomic per distinct cell
+            if (ffloor) {
+                // float32 voxel indices: floor(p) from the bits of p + 1.5 * 2^23 rounded
+                // down, offset by the origin (ray_index); positions in the sliver
+                // (-2^-20, 0) take the float64 formula
+                const int kx = 0x4B400000 + sd.oi[0], ky = 0x4B400000 + sd.oi[1], kz = 0x4B400000 + sd.oi[2];
+                if (sd.cube_on) {
+                    // phase 1: steps inside the cube around the ego.  Each axis index is
+                    // monotone along the ray, so the first step outside the cube ends
+                    // this phase for good; the cube lies inside the grid.
+                    const int cx = kx + sd.cube0[0], cy = ky + sd.cube0[1], cz = kz + sd.cube0[2];
+                    for (; st < K; st++) {
+                        const float nx = __fadd_rn(px, ix), ny = __fadd_rn(py, iy), nz = __fadd_rn(pz, iz);
+                        const unsigned ux = (unsigned)(__float_as_int(__fadd_rd(nx, 12582912.0f)) - cx);
+                        const unsigned uy = (unsigned)(__float_as_int(__fadd_rd(ny, 12582912.0f)) - cy);
+                        const unsigned uz = (unsigned)(__float_as_int(__fadd_rd(nz, 12582912.0f)) - cz);
+                        if (((ux | uy | uz) >= (unsigned)kCube) | in_sliver(nx) | in_sliver(ny) | in_sliver(nz)) break;
+                        px = nx;
+                        py = ny;
+                        pz = nz;
+                        atomicAdd(&cube[ux + kCube * (uy + kCube * uz)], 1u);
+                    }
+                }
+                // phase 2: everywhere else in the grid, one global atomic per step and
+                // per distinct cell of the warp; the ray ends at its first step outside
+                // the grid (scripts/gvom.py:1216-1225)
+                for (; st < K; st++) {
+                    px = __fadd_rn(px, ix);
+                    py = __fadd_rn(py, iy);
+                    pz = __fadd_rn(pz, iz);
+                    int vx = __float_as_int(__fadd_rd(px, 12582912.0f)) - kx;
+                    int vy = __float_as_int(__fadd_rd(py, 12582912.0f)) - ky;
+                    int vz = __float_as_int(__fadd_rd(pz, 12582912.0f)) - kz;
+                    if (in_sliver(px) | in_sliver(py) | in_sliver(pz)) {
+                        vx = ray_index(px, sd.oi[0], sd.od[0], 1);
+                        vy = ray_index(py, sd.oi[1], sd.od[1], 1);
+                        vz = ray_index(pz, sd.oi[2], sd.od[2], 1);
+                    }
+                    if ((unsigned)vx >= (unsigned)g.X || (unsigned)vy >= (unsigned)g.X || (unsigned)vz >= (unsigned)g.Z)
+                        break;
                     const int cell = (vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe;
                     const unsigned grp = __match_any_sync(__activemask(), cell);
                     if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&cnt[cell], (unsigned long long)__popc(grp));
+                }
+            } else {
+                // origin far from the world origin: float64 voxel indices
+                for (; st < K; st++) {
+                    px = __fadd_rn(px, ix);
+                    py = __fadd_rn(py, iy);
+                    pz = __fadd_rn(pz, iz);
+                    const int vx = ray_index(px, sd.oi[0], sd.od[0], 0);
+                    const int vy = ray_index(py, sd.oi[1], sd.od[1], 0);
+                    const int vz = ray_index(pz, sd.oi[2], sd.od[2], 0);
+                    if ((unsigned)vx >= (unsigned)g.X || (unsigned)vy >= (unsigned)g.X || (unsigned)vz >= (unsigned)g.Z)
+                        break;
+                    atomicAdd(&cnt[(vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe], 1ull);
                 }
             }
             n_steps = st;
@@ -242,10 +277,12 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
     warp_add_u64(&sd.ctr->hits, n_hit);
     warp_add_u64(&sd.ctr->steps, n_steps);
     __syncthreads();
+    if (!sd.cube_on) return;
     for (int k = threadIdx.x; k < kCubeCells; k += blockDim.x) {
         const unsigned c = cube[k];
         if (c) {
-            const int vx = cx0 + (k % kCube), vy = cy0 + ((k / kCube) % kCube), vz = cz0 + k / (kCube * kCube);
+            const int vx = sd.cube0[0] + (k % kCube), vy = sd.cube0[1] + ((k / kCube) % kCube),
+                      vz = sd.cube0[2] + k / (kCube * kCube);
             atomicAdd(&sd.cnt[(vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe], (unsigned long long)c);
         }
     }
