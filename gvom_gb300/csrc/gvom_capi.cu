@@ -833,6 +833,66 @@ static int debug_maps(GvomHandle *h, float *out_h, float *out_i) {
     return GVOM_OK;
 }
 
+namespace {
+
+// Address of the allocation-free export's scratch array, looked up once per
+// device (with that device current) and cached; the lock also serialises the
+// calls that share the array.
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu[kMaxDevices];
+int *g_static_ptr[kMaxDevices] = {};
+
+}  // namespace
+
+int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_rows, int64_t *rows) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    if (capacity_rows < 0) return fail(GVOM_ERR_ARG, "capacity_rows is negative");
+    std::lock_guard<std::mutex> lk(h->mu);
+    const long long V = h->g.V;
+    const int chunk = debug_chunk();
+    const long long nblocks = (V + chunk - 1) / chunk;
+    if (nblocks > kStaticDebugBlocks)
+        return fail(GVOM_ERR_ARG, "grid of " + std::to_string(V) + " voxels is above the " +
+                                      std::to_string((long long)kStaticDebugBlocks * chunk) +
+                                      " voxels the allocation-free export supports; use gvom_debug_voxel_map");
+    if (!h->have_comb) return fail(GVOM_NO_DATA, "No data");
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(GVOM_ERR_ARG, "device index out of range");
+    std::lock_guard<std::mutex> dl(g_static_mu[dev]);
+    if (!g_static_ptr[dev]) {
+        int *p = nullptr;
+        const cudaError_t e = debug_static_scratch(&p);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return fail(GVOM_ERR_CUDA, std::string("scratch address lookup: ") + cudaGetErrorString(e));
+        }
+        g_static_ptr[dev] = p;
+    }
+    int *scratch = g_static_ptr[dev];
+    CUDA_TRY(launch_debug_count(h->cidx[h->cur], V, scratch, (int)nblocks, h->st));
+    CUDA_TRY(launch_debug_offsets(scratch, (int)nblocks, h->st));
+    if (d_out && capacity_rows > 0) {
+        DebugVoxParams p;
+        p.idx = h->cidx[h->cur];
+        p.rec = h->crec[h->cur];
+        p.block_off = scratch;
+        p.V = V;
+        p.X = h->g.X;
+        for (int a = 0; a < 3; a++) p.co[a] = h->cod[h->cur][a];
+        p.xy_res = h->p.xy_resolution;
+        p.z_res = h->p.z_resolution;
+        p.out = d_out;
+        p.cap = capacity_rows;
+        CUDA_TRY(launch_debug_voxels(p, (int)nblocks, h->st));
+    }
+    int total = 0;
+    CUDA_TRY(cudaMemcpyAsync(&total, scratch + nblocks, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    if (rows) *rows = total;
+    return GVOM_OK;
+}
+
 int gvom_debug_height_map(GvomHandle *h, float *out) { return debug_maps(h, out, nullptr); }
 
 int gvom_debug_inferred_height_map(GvomHandle *h, float *out) { return debug_maps(h, nullptr, out); }

@@ -181,6 +181,12 @@ cudaError_t launch_debug_voxels(const DebugVoxParams &p, int nblocks, cudaStream
 cudaError_t launch_debug_maps(const DebugMapParams &p, cudaStream_t st);
 int debug_chunk();
 
+// allocation-free debug voxel export (k_debug_static.cu): per-block scratch of
+// kStaticDebugBlocks + 1 words in a fixed device array
+constexpr int kStaticDebugBlocks = 32768;
+cudaError_t debug_static_scratch(int **ptr);
+cudaError_t launch_debug_offsets(int *words, int n, cudaStream_t st);
+
 // ---------------------------------------------------------------------------
 // exact arithmetic helpers
 // ---------------------------------------------------------------------------

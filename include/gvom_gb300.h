@@ -110,6 +110,21 @@ int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t
  * most `capacity_rows` are written (call with out = NULL to size). */
 int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64_t *rows);
 
+/* Allocation-free form of gvom_debug_voxel_map; no counterpart in the
+ * reference.  For callers that must not allocate or free device memory: a
+ * debug publisher sharing the GPU with a latency-bound mapping loop (cudaFree
+ * synchronises the device and stalls every other instance's work), or a
+ * process whose device footprint must stay fixed after start-up.  The same
+ * rows, in the same order, go to `d_out`, a DEVICE buffer of capacity_rows x 8
+ * floats owned by the caller (NULL or capacity 0: only size).  The only
+ * scratch is a fixed 128 KB device array; grids above 32M voxels
+ * (xy_size^2 * z_size > 33,554,432) are refused with GVOM_ERR_ARG.  The first
+ * call on a device looks up that array's address; make it before any stream
+ * capture.  The array is shared by all instances on a device: calls are
+ * serialised by a process-wide lock held until their device work is done.
+ * Returns after the rows are written (host waits on the instance stream). */
+int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_rows, int64_t *rows);
+
 /* Replace make_debug_height_map / make_debug_inferred_height_map
  * (scripts/gvom.py:412-442, 455-479): (xy_size^2, 7) and (xy_size^2, 3) float32. */
 int gvom_debug_height_map(GvomHandle *h, float *out);
