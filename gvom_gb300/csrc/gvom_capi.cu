@@ -151,6 +151,7 @@ struct GvomHandle {
     int *d_dbg = nullptr;
     long long bytes = 0;
     int pageable_access = 0;
+    int num_sms = 1;
     StageTimer timer;
 };
 
@@ -240,7 +241,8 @@ int ensure_dpts(GvomHandle *h, size_t bytes) {
 int ensure_cnt(GvomHandle *h, int nscans) {
     while ((int)h->cnt.size() < nscans) {
         unsigned long long *c = nullptr;
-        const long long ve = ext_cells(h->g);
+        // padded to whole k_assign blocks of cells; the padding stays zero
+        const long long ve = (ext_cells(h->g) + kAssignBlockCells - 1) / kAssignBlockCells * kAssignBlockCells;
         int rc = dalloc_t(h, &c, (size_t)ve);
         if (rc) return rc;
         CUDA_TRY(cudaMemsetAsync(c, 0, (size_t)ve * 8, h->st));
@@ -324,6 +326,8 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
         pc.rz = exact_res(h->p.z_resolution);
     }
     pc.step_cap = 2 * std::max(h->g.X, h->g.Z) + 8;
+    pc.num_sms = h->num_sms;
+    pc.xe_magic = ~0ull / (unsigned long long)h->g.Xe + 1ull;
     pc.nscans = k;
     ScanDesc table[kMaxBatch];
     std::memset(table, 0, sizeof(table));
@@ -461,6 +465,8 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     h->B = params->buffer_size;
     h->slots.resize(h->B);
     cudaDeviceGetAttribute(&h->pageable_access, cudaDevAttrPageableMemoryAccess, dev);
+    if (cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || h->num_sms < 1)
+        h->num_sms = 1;
     // admission: the resident footprint must fit in free device memory with margin
     const long long X2 = (long long)g.X * g.X;
     const long long need = (long long)h->B * g.V * 4 + 2 * g.V * (4 + (long long)sizeof(VoxelRec)) + g.Vext * 8 +

@@ -21,6 +21,8 @@
 namespace gvom {
 
 constexpr int kMaxBatch = 16;         // scans per batched launch
+constexpr int kAssignPer = 8;         // consecutive count words per k_assign thread
+constexpr int kAssignBlockCells = 256 * kAssignPer;
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
 constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
@@ -91,6 +93,8 @@ struct ProcessConst {
     ExactRes rxy, rz;      // exact-division constants of xy_res / z_res
     int step_cap;          // upper bound on ray steps inside the grid
     int nscans;
+    int num_sms;           // multiprocessors of the device (persistent grids)
+    unsigned long long xe_magic;  // floor((2^64 - 1) / Xe) + 1 (divisions by the extended row length)
 };
 
 struct MergeSrc {

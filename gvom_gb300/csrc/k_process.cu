@@ -326,61 +326,47 @@ __device__ __forceinline__ void block_scan2(int a, int b, int &ea, int &eb, int 
 }
 
 // ---------------------------------------------------------------------------
-// k_assign: a tile of kAssignTile extended cells per block (256 threads x
-// kAssignPer cells, strided so every load and store is coalesced),
-// blockIdx.y = scan.  In-grid cells: hit > 0 -> compact index and the
-// record's hit/total/voxel id; else -(total)-1 (scripts/gvom.py:1233-1247).
-// Cells holding points (occupied or halo) get a point-group offset; their
-// count word becomes (offset << 32 | points) for k_scatter / k_voxel_stats.
-// Free cells are cleared here, point cells by k_cleanup.  One counter
-// atomic per block.
+// k_assign: one pass over the dense count words; a block covers
+// kAssignBlockCells consecutive extended cells, thread i the cells i, i + 256,
+// ... (every load and store of a warp is contiguous), blockIdx.y = scan.
+// In-grid cells: hit > 0 -> compact index and the record's hit/total/voxel
+// id; else -(total)-1 (scripts/gvom.py:1233-1247).  Cells holding points
+// (occupied or halo) get a point-group offset; their count word becomes
+// (offset << 32 | points) for k_scatter / k_voxel_stats.  Free cells are
+// cleared here, point cells by k_cleanup.  One counter atomic per block.
+// The count arrays are padded to whole blocks of cells (zero cells).
 // ---------------------------------------------------------------------------
-constexpr int kAssignPer = 16;
-constexpr int kAssignTile = 256 * kAssignPer;
 
-struct CellWalk {  // extended-grid coordinates of e, e + 256, e + 512, ...
-    int ex, ey, ez;
-    __device__ __forceinline__ void init(int e, int Xe) {
-        ex = e % Xe;
-        const int t = e / Xe;
-        ey = t % Xe;
-        ez = t / Xe;
-    }
-    __device__ __forceinline__ void next(int Xe) {
-        ex += 256;
-        while (ex >= Xe) {
-            ex -= Xe;
-            if (++ey == Xe) {
-                ey = 0;
-                ez++;
-            }
-        }
-    }
-};
+// (x, y, z) of extended cell e: e = x + Xe (y + Xe z), divisions by Xe as a
+// multiply-high by xe_magic = floor((2^64 - 1) / Xe) + 1, exact for e < 2^32
+// (xe_magic wraps to 0 for Xe = 1, where the quotient is e itself)
+__device__ __forceinline__ bool cell_in_grid(unsigned e, const Geom &g, unsigned long long magic, int &gid) {
+    const unsigned row = magic ? (unsigned)__umul64hi((unsigned long long)e, magic) : e;
+    const unsigned ez = magic ? (unsigned)__umul64hi((unsigned long long)row, magic) : row;
+    const int ex = (int)(e - row * (unsigned)g.Xe), ey = (int)(row - ez * (unsigned)g.Xe);
+    const int gx = ex - g.exy, gy = ey - g.exy, gz = (int)ez - g.ez;
+    gid = gx + g.X * (gy + g.X * gz);
+    return (unsigned)gx < (unsigned)g.X && (unsigned)gy < (unsigned)g.X && (unsigned)gz < (unsigned)g.Z;
+}
 
 template <int NS>
 __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab) {
     const ScanDesc &sd = tab.s[blockIdx.y];
     const Geom g = pc.g;
     const int Vext = (int)g.Vext;
-    const int base = blockIdx.x * kAssignTile + threadIdx.x;
+    const int base = blockIdx.x * kAssignBlockCells + threadIdx.x;
     unsigned long long v[kAssignPer];
 #pragma unroll
-    for (int k = 0; k < kAssignPer; k++) {
-        const int e = base + k * 256;
-        v[k] = e < Vext ? sd.cnt[e] : 0ull;
-    }
+    for (int k = 0; k < kAssignPer; k++) v[k] = sd.cnt[base + k * 256];  // padded: always in bounds
     int n_occ = 0, n_pts = 0;
-    CellWalk cw;
-    cw.init(base, g.Xe);
 #pragma unroll
     for (int k = 0; k < kAssignPer; k++) {
         const int hit = (int)(v[k] >> 32);
-        const bool in_grid = (unsigned)(cw.ex - g.exy) < (unsigned)g.X && (unsigned)(cw.ey - g.exy) < (unsigned)g.X &&
-                             (unsigned)(cw.ez - g.ez) < (unsigned)g.Z;
-        if (in_grid && hit > 0) n_occ++;
-        n_pts += hit;
-        cw.next(g.Xe);
+        if (hit > 0) {
+            int gid;
+            n_pts += hit;
+            if (cell_in_grid((unsigned)(base + k * 256), g, pc.xe_magic, gid)) n_occ++;
+        }
     }
     int eo, ep, to, tp;
     block_scan2(n_occ, n_pts, eo, ep, to, tp);
@@ -391,39 +377,34 @@ __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __g
     }
     __syncthreads();
     int c = bases[0] + eo, off = bases[1] + ep;
-    cw.init(base, g.Xe);
 #pragma unroll
     for (int k = 0; k < kAssignPer; k++) {
         const int e = base + k * 256;
-        if (e < Vext) {
-            const int hit = (int)(v[k] >> 32);
-            const int total = (int)(v[k] & 0xffffffffull);
-            const int gx = cw.ex - g.exy, gy = cw.ey - g.exy, gz = cw.ez - g.ez;
-            const bool in_grid = (unsigned)gx < (unsigned)g.X && (unsigned)gy < (unsigned)g.X && (unsigned)gz < (unsigned)g.Z;
-            if (in_grid) {
-                const int gid = gx + gy * g.X + gz * g.X * g.X;
-                if (hit > 0) {
-                    if (c < sd.rec_cap) {
-                        VoxelRec *r = &sd.rec[c];
-                        r->hit = hit;
-                        r->total = total;
-                        r->aux[0] = __int_as_float(gid);
-                    } else {
-                        atomicOr(&sd.ctr->overflow, 1);
-                    }
-                    sd.idx[gid] = c;
-                    c++;
-                } else {
-                    sd.idx[gid] = -total - 1;
-                    if (total) sd.cnt[e] = 0ull;
-                }
-            }
+        if (e >= Vext) break;
+        const int hit = (int)(v[k] >> 32);
+        const int total = (int)(v[k] & 0xffffffffull);
+        int gid;
+        if (cell_in_grid((unsigned)e, g, pc.xe_magic, gid)) {
             if (hit > 0) {
-                sd.cnt[e] = ((unsigned long long)(unsigned)off << 32) | (unsigned)hit;
-                off += hit;
+                if (c < sd.rec_cap) {
+                    VoxelRec *r = &sd.rec[c];
+                    r->hit = hit;
+                    r->total = total;
+                    r->aux[0] = __int_as_float(gid);
+                } else {
+                    atomicOr(&sd.ctr->overflow, 1);
+                }
+                sd.idx[gid] = c;
+                c++;
+            } else {
+                sd.idx[gid] = -total - 1;
+                if (total) sd.cnt[e] = 0ull;
             }
         }
-        cw.next(g.Xe);
+        if (hit > 0) {
+            sd.cnt[e] = ((unsigned long long)(unsigned)off << 32) | (unsigned)hit;
+            off += hit;
+        }
     }
 }
 
@@ -599,7 +580,7 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
     else
         k_voxelize_trace<float, NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
     mark(1);
-    dim3 ga((unsigned)((pc.g.Vext + kAssignTile - 1) / kAssignTile), pc.nscans);
+    dim3 ga((unsigned)((pc.g.Vext + kAssignBlockCells - 1) / kAssignBlockCells), pc.nscans);
     k_assign<NS><<<ga, 256, 0, st>>>(pc, tab);
     mark(2);
     k_scatter<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank, sorted);
