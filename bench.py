@@ -63,7 +63,9 @@ def stage_bytes(name, n, V, Vext, X2, C_slot, C_sum, Cc, Cc_last, nsrc):
     if name == "k_cleanup":
         return 20 * n
     if name == "k_merge":
-        return 4 * V * nsrc + 4 * V + 52 * (C_sum + Cc_last) + 52 * Cc + 8 * X2 * ((V // X2 + 7) // 8)
+        return 4 * V * nsrc + 4 * V + 4 * Cc + 8 * X2 * ((V // X2 + 7) // 8)
+    if name == "k_merge_stats":
+        return 4 * Cc + 4 * nsrc * Cc + 64 * (C_sum + Cc_last) + 64 * Cc
     if name == "k_columns":
         return 8 * X2 * ((V // X2 + 7) // 8) + 28 * X2
     if name == "k_maps2d":

@@ -32,7 +32,7 @@ EXPORTS = (
     "gvom_version", "gvom_set_stage_timing", "gvom_stage_times", "gvom_stage_name",
     "gvom_debug_voxel_map_noalloc",
 )
-GVOM_STAGES = 9
+GVOM_STAGES = 10
 
 
 class GvomParams(C.Structure):

@@ -35,7 +35,7 @@ int fail(int code, const std::string &msg) {
 
 constexpr int kStages = kProcessKernels + kCombineKernels;
 const char *kStageNames[kStages] = {"k_voxelize_trace", "k_assign", "k_scatter", "k_cell_moments", "k_voxel_stats",
-                                    "k_cleanup", "k_merge", "k_columns", "k_maps2d"};
+                                    "k_cleanup", "k_merge", "k_merge_stats", "k_columns", "k_maps2d"};
 
 // CUDA events around each kernel launch, harvested when the host waits.
 struct StageTimer {
@@ -146,6 +146,7 @@ struct GvomHandle {
     int *zlow = nullptr;
     float *mlow = nullptr;
     int2 *colinfo = nullptr;  // (Z / 8 chunks) x X x X
+    int *occ_list = nullptr;  // occupied voxel ids of the combined map being built (V)
     bool have_maps = false;
     // debug
     int *d_dbg = nullptr;
@@ -469,7 +470,8 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         h->num_sms = 1;
     // admission: the resident footprint must fit in free device memory with margin
     const long long X2 = (long long)g.X * g.X;
-    const long long need = (long long)h->B * g.V * 4 + 2 * g.V * (4 + (long long)sizeof(VoxelRec)) + g.Vext * 8 +
+    const long long need = (long long)h->B * g.V * 4 + 2 * g.V * (4 + (long long)sizeof(VoxelRec)) + g.V * 4 +
+                           g.Vext * 8 +
                            X2 * (6 * 8 + 4 * 4) + (64LL << 20);
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
@@ -512,6 +514,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
     if ((rc = dalloc_t(h, &h->mlow, (size_t)X2))) return bail(rc);
     if ((rc = dalloc_t(h, &h->colinfo, (size_t)X2 * ((g.Z + 7) / 8)))) return bail(rc);
+    if ((rc = dalloc_t(h, &h->occ_list, (size_t)g.V))) return bail(rc);
     if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->B, h->st) != cudaSuccess ||
         cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 4, h->st) != cudaSuccess) {
         cudaGetLastError();
@@ -560,6 +563,7 @@ int gvom_destroy(GvomHandle *h) {
     cudaFree(h->zlow);
     cudaFree(h->mlow);
     cudaFree(h->colinfo);
+    cudaFree(h->occ_list);
     cudaFree(h->d_dbg);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
@@ -681,6 +685,8 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     mp.out_idx = h->cidx[nb];
     mp.out_rec = h->crec[nb];
     mp.out_count = h->d_combC + nb;
+    mp.list = h->occ_list;
+    mp.num_sms = h->num_sms;
     mp.colinfo = h->colinfo;
     ColumnParams cp;
     std::memset(&cp, 0, sizeof(cp));

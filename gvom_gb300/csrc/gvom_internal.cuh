@@ -111,6 +111,8 @@ struct MergeParams {
     int *out_idx;
     VoxelRec *out_rec;     // indexed by voxel id
     int *out_count;        // occupied voxels
+    int *list;             // voxel ids of the occupied voxels (capacity V)
+    int num_sms;
     int2 *colinfo;         // per (z chunk, y, x): lowest occupied z, lowest known-free z (Z if none)
     double co[3];          // combined origin (voxels)
 };
@@ -172,7 +174,7 @@ struct DebugMapParams {
 // `ev` (nullable): kProcessKernels + 1 (resp. kCombineKernels + 1) events,
 // recorded before the first kernel and after each kernel.
 constexpr int kProcessKernels = 6;  // voxelize_trace, assign, scatter, cell_moments, voxel_stats, cleanup
-constexpr int kCombineKernels = 3;  // merge, columns, maps2d
+constexpr int kCombineKernels = 4;  // merge, merge_stats, columns, maps2d
 constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,

@@ -8,6 +8,8 @@
 //              (scripts/gvom.py:1423-1487).  The combined map addresses its
 //              records by voxel id, so nothing is allocated; each thread
 //              leaves the lowest occupied / known-free z of its chunk.
+//   k_merge_stats  one thread per listed occupied voxel: statistics merge
+//              and eigenvalues
 //   k_columns  one thread per column: height (lowest occupied voxel or the
 //              robot disc), inferred height (lowest known-free voxel) and the
 //              positive-obstacle band density (scripts/gvom.py:515-590)
@@ -103,62 +105,92 @@ __device__ __forceinline__ void eigen3(const float C[6], float e[3]) {
 
 // Chan merge of every occupied source voxel, in source order, into the
 // combined record at `vid` (scripts/gvom.py:926-980), float32, then its
-// eigenvalues.
+// eigenvalues.  The sources' compact indices are gathered first and the
+// records loaded kMergeChunk at a time, so the loads of a chunk overlap.
+constexpr int kMergeChunk = 4;
+
 template <int NSRC>
 __device__ __forceinline__ void merge_voxel(const MergeParams &mp, int vid) {
     const int X = mp.g.X, Z = mp.g.Z;
     const int x = vid % X, y = (vid / X) % X, z = vid / (X * X);
+    int o[NSRC];
+#pragma unroll
+    for (int s = 0; s < NSRC; s++) {
+        o[s] = -1;
+        if (s < mp.nsrc) {
+            const int xs = x + mp.src[s].dx, ys = y + mp.src[s].dy, zs = z + mp.src[s].dz;
+            if ((unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X && (unsigned)zs < (unsigned)Z)
+                o[s] = __ldg(&mp.src[s].idx[xs + ys * X + zs * X * X]);
+        }
+    }
     float n = 0.f, m0 = 0.f, m1 = 0.f, m2 = 0.f;
     float C[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int hit = 0, total = 0;
     float minh = 1.0f;
-    for (int s = 0; s < mp.nsrc; s++) {
-        const int xs = x + mp.src[s].dx, ys = y + mp.src[s].dy, zs = z + mp.src[s].dz;
-        if (!((unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X && (unsigned)zs < (unsigned)Z)) continue;
-        const int o = mp.src[s].idx[xs + ys * X + zs * X * X];
-        if (o < 0) continue;
-        const float4 *p = reinterpret_cast<const float4 *>(&mp.src[s].rec[o]);
-        const float4 a = __ldg(p), b = __ldg(p + 1), cc = __ldg(p + 2), d = __ldg(p + 3);
-        // a = mean0 mean1 mean2 xx | b = xy xz yy yz | cc = zz count hit total | d = minh aux
-        const float n2 = cc.y;
-        const float o_m[3] = {a.x, a.y, a.z};
-        const float o_c[6] = {a.w, b.x, b.y, b.z, b.w, cc.x};
-        const float den = __fadd_rn(n, n2);
-        const float nm0 = __fdiv_rn(__fadd_rn(__fmul_rn(m0, n), __fmul_rn(o_m[0], n2)), den);
-        const float nm1 = __fdiv_rn(__fadd_rn(__fmul_rn(m1, n), __fmul_rn(o_m[1], n2)), den);
-        const float nm2 = __fdiv_rn(__fadd_rn(__fmul_rn(m2, n), __fmul_rn(o_m[2], n2)), den);
-        const float cm[3] = {m0, m1, m2};
-        const float mn[3] = {nm0, nm1, nm2};
-        const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
 #pragma unroll
-        for (int t = 0; t < 6; t++) {
-            const float t1 = __fmul_rn(n, C[t]);
-            const float t2 = __fmul_rn(n2, o_c[t]);
-            const float t3 = __fmul_rn(__fmul_rn(n, __fsub_rn(cm[pa[t]], mn[pa[t]])), __fsub_rn(cm[pb[t]], mn[pb[t]]));
-            const float t4 = __fmul_rn(__fmul_rn(n2, __fsub_rn(o_m[pa[t]], mn[pa[t]])), __fsub_rn(o_m[pb[t]], mn[pb[t]]));
-            C[t] = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), t4), den);
+    for (int s0 = 0; s0 < NSRC; s0 += kMergeChunk) {
+        float4 ra[kMergeChunk], rb[kMergeChunk], rc[kMergeChunk], rd[kMergeChunk];
+#pragma unroll
+        for (int j = 0; j < kMergeChunk; j++) {
+            const int s = s0 + j;
+            if (s < NSRC && o[s] >= 0) {
+                const float4 *p = reinterpret_cast<const float4 *>(&mp.src[s].rec[o[s]]);
+                ra[j] = __ldg(p);
+                rb[j] = __ldg(p + 1);
+                rc[j] = __ldg(p + 2);
+                rd[j] = __ldg(p + 3);
+            }
         }
-        m0 = nm0;
-        m1 = nm1;
-        m2 = nm2;
-        n = den;
-        hit += __float_as_int(cc.z);
-        total += __float_as_int(cc.w);
-        minh = fminf(minh, d.x);
+#pragma unroll
+        for (int j = 0; j < kMergeChunk; j++) {
+            const int s = s0 + j;
+            if (!(s < NSRC && o[s] >= 0)) continue;
+            // ra = mean0 mean1 mean2 xx | rb = xy xz yy yz | rc = zz count hit total | rd = minh aux
+            const float4 a = ra[j], bq = rb[j], cc = rc[j], d = rd[j];
+            const float n2 = cc.y;
+            const float o_m[3] = {a.x, a.y, a.z};
+            const float o_c[6] = {a.w, bq.x, bq.y, bq.z, bq.w, cc.x};
+            const float den = __fadd_rn(n, n2);
+            const float nm0 = __fdiv_rn(__fadd_rn(__fmul_rn(m0, n), __fmul_rn(o_m[0], n2)), den);
+            const float nm1 = __fdiv_rn(__fadd_rn(__fmul_rn(m1, n), __fmul_rn(o_m[1], n2)), den);
+            const float nm2 = __fdiv_rn(__fadd_rn(__fmul_rn(m2, n), __fmul_rn(o_m[2], n2)), den);
+            const float cm[3] = {m0, m1, m2};
+            const float mn[3] = {nm0, nm1, nm2};
+            const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
+            for (int t = 0; t < 6; t++) {
+                const float t1 = __fmul_rn(n, C[t]);
+                const float t2 = __fmul_rn(n2, o_c[t]);
+                const float t3 =
+                    __fmul_rn(__fmul_rn(n, __fsub_rn(cm[pa[t]], mn[pa[t]])), __fsub_rn(cm[pb[t]], mn[pb[t]]));
+                const float t4 =
+                    __fmul_rn(__fmul_rn(n2, __fsub_rn(o_m[pa[t]], mn[pa[t]])), __fsub_rn(o_m[pb[t]], mn[pb[t]]));
+                C[t] = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), t4), den);
+            }
+            m0 = nm0;
+            m1 = nm1;
+            m2 = nm2;
+            n = den;
+            hit += __float_as_int(cc.z);
+            total += __float_as_int(cc.w);
+            minh = fminf(minh, d.x);
+        }
     }
     float e[3];
     eigen3(C, e);
-    float4 *o = reinterpret_cast<float4 *>(&mp.out_rec[vid]);
-    o[0] = make_float4(m0, m1, m2, C[0]);
-    o[1] = make_float4(C[1], C[2], C[3], C[4]);
-    o[2] = make_float4(C[5], n, __int_as_float(hit), __int_as_float(total));
-    o[3] = make_float4(minh, e[0], e[1], e[2]);
+    float4 *out = reinterpret_cast<float4 *>(&mp.out_rec[vid]);
+    out[0] = make_float4(m0, m1, m2, C[0]);
+    out[1] = make_float4(C[1], C[2], C[3], C[4]);
+    out[2] = make_float4(C[5], n, __int_as_float(hit), __int_as_float(total));
+    out[3] = make_float4(minh, e[0], e[1], e[2]);
 }
 
-// Phase 1: every thread decides its kZC voxels (index merge), writes the
-// combined index map and queues occupied voxels in shared memory.  Phase 2:
-// the block merges the queued voxels' statistics with full warps (occupied
-// voxels are sparse, so merging in place would run one lane per warp).
+// k_merge: every thread decides its kZC voxels (index merge), writes the
+// combined index map and queues occupied voxels in shared memory; the block
+// appends its queue to the global list of occupied voxels (one atomic).
+// k_merge_stats then merges the listed voxels' statistics with full warps
+// (occupied voxels are sparse: merging in place would run one lane per warp
+// and hold the whole block on that lane's dependent loads).
 template <int NSRC>
 __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergeParams mp) {
     __shared__ int queue[256 * kZC];
@@ -171,24 +203,41 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
     const bool col = x < X && y < X;
     const int plane = X * X;
     if (tid == 0) qn = 0;
-    int v[kZC][NSRC];
+    // index merge, source by source in source order (scripts/gvom.py:242-298):
+    // a source's kZC loads are independent, and the state per plane is one int
+    int cmb[kZC];
 #pragma unroll
-    for (int k = 0; k < kZC; k++) merge_load_plane<NSRC>(mp, x, y, z0 + k, col, v[k]);
+    for (int k = 0; k < kZC; k++) cmb[k] = -1;
+#pragma unroll
+    for (int s = 0; s < NSRC; s++) {
+        if (s >= mp.nsrc) break;
+        const MergeSrc &src = mp.src[s];
+        const int xs = x + src.dx, ys = y + src.dy;
+        if (!(col && (unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X)) continue;
+        const int *col_s = src.idx + xs + ys * X;
+        int vs[kZC];
+#pragma unroll
+        for (int k = 0; k < kZC; k++) {
+            const int zs = z0 + k + src.dz;
+            vs[k] = (z0 + k < Z && (unsigned)zs < (unsigned)Z) ? __ldg(col_s + zs * plane) : kOutside;
+        }
+#pragma unroll
+        for (int k = 0; k < kZC; k++) {
+            const int o = vs[k];
+            if (o == kOutside) continue;
+            int comb = cmb[k];
+            const bool alloc = src.is_last ? (o >= 0 && comb <= -1 && comb >= -11) : (o >= 0 && comb <= -1);
+            if (alloc) comb = kOcc;
+            else if (o < -1 && comb <= -1) comb += o + 1;
+            cmb[k] = comb;
+        }
+    }
     __syncthreads();
     int occ_z = Z, free_z = Z;
 #pragma unroll
     for (int k = 0; k < kZC; k++) {
         const int z = z0 + k;
-        int comb = -1;
-#pragma unroll
-        for (int s = 0; s < NSRC; s++) {
-            if (s < mp.nsrc && v[k][s] != kOutside) {
-                const int o = v[k][s];
-                const bool alloc = mp.src[s].is_last ? (o >= 0 && comb <= -1 && comb >= -11) : (o >= 0 && comb <= -1);
-                if (alloc) comb = kOcc;
-                else if (o < -1 && comb <= -1) comb += o + 1;
-            }
-        }
+        int comb = cmb[k];
         const bool occ = col && z < Z && comb == kOcc;
         const unsigned m = __ballot_sync(0xffffffffu, occ);
         if (m) {
@@ -211,8 +260,17 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
     if (col) mp.colinfo[blockIdx.z * plane + y * X + x] = make_int2(occ_z, free_z);
     __syncthreads();
     const int n_q = qn;
-    for (int i = tid; i < n_q; i += 256) merge_voxel<NSRC>(mp, queue[i]);
-    if (tid == 0 && n_q) atomicAdd(mp.out_count, n_q);
+    __shared__ int lbase;
+    if (tid == 0) lbase = n_q ? atomicAdd(mp.out_count, n_q) : 0;
+    __syncthreads();
+    for (int i = tid; i < n_q; i += 256) mp.list[lbase + i] = queue[i];
+}
+
+template <int NSRC>
+__global__ void __launch_bounds__(256) k_merge_stats(const __grid_constant__ MergeParams mp) {
+    const int n = *mp.out_count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        merge_voxel<NSRC>(mp, mp.list[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -748,8 +806,10 @@ __global__ void k_debug_maps(DebugMapParams p) {
 // launchers
 // ---------------------------------------------------------------------------
 template <int NSRC>
-static void launch_merge(const MergeParams &mp, dim3 g, cudaStream_t st) {
+static void launch_merge(const MergeParams &mp, dim3 g, cudaStream_t st, cudaEvent_t *ev) {
     k_merge<NSRC><<<g, dim3(32, 8), 0, st>>>(mp);
+    if (ev) cudaEventRecord(ev[1], st);
+    k_merge_stats<NSRC><<<mp.num_sms * 4, 256, 0, st>>>(mp);
 }
 
 cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
@@ -757,18 +817,18 @@ cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const 
     const int X = mp.g.X, Z = mp.g.Z;
     if (ev) cudaEventRecord(ev[0], st);
     dim3 gm((X + 31) / 32, (X + 7) / 8, (Z + kZC - 1) / kZC);
-    if (mp.nsrc <= 2) launch_merge<2>(mp, gm, st);
-    else if (mp.nsrc <= 3) launch_merge<3>(mp, gm, st);
-    else if (mp.nsrc <= 5) launch_merge<5>(mp, gm, st);
-    else if (mp.nsrc <= 9) launch_merge<9>(mp, gm, st);
-    else launch_merge<kMaxSources>(mp, gm, st);
-    if (ev) cudaEventRecord(ev[1], st);
+    if (mp.nsrc <= 2) launch_merge<2>(mp, gm, st, ev);
+    else if (mp.nsrc <= 3) launch_merge<3>(mp, gm, st, ev);
+    else if (mp.nsrc <= 5) launch_merge<5>(mp, gm, st, ev);
+    else if (mp.nsrc <= 9) launch_merge<9>(mp, gm, st, ev);
+    else launch_merge<kMaxSources>(mp, gm, st, ev);
+    if (ev) cudaEventRecord(ev[2], st);
     dim3 gc((X + 31) / 32, (X + 7) / 8);
     k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);
-    if (ev) cudaEventRecord(ev[2], st);
+    if (ev) cudaEventRecord(ev[3], st);
     dim3 g2((X + kTY - 1) / kTY, (X + kTX - 1) / kTX);
     k_maps2d<<<g2, dim3(kTY, kTX), 0, st>>>(m2);
-    if (ev) cudaEventRecord(ev[3], st);
+    if (ev) cudaEventRecord(ev[4], st);
     return cudaGetLastError();
 }
 

@@ -172,7 +172,7 @@ int gvom_synchronize(GvomHandle *h);
  * kernel launch of process / combine; gvom_stage_times waits for the queued
  * work and returns, for stages 0..n-1, the summed milliseconds and launch
  * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
-#define GVOM_STAGES 9
+#define GVOM_STAGES 10
 int gvom_set_stage_timing(GvomHandle *h, int32_t on);
 int gvom_stage_times(GvomHandle *h, double *total_ms, int64_t *launches, int32_t n_stages);
 const char *gvom_stage_name(int32_t stage);
