@@ -109,7 +109,8 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned l
 // kCube^3 block of cells around the ego voxel (sd.cube0, inside the grid),
 // are counted in shared memory and flushed once per block (one global atomic
 // per touched cell); the remaining steps add straight into the dense count
-// words, one atomic per distinct cell of the warp.
+// words (fire-and-forget reductions; aggregating equal cells across a warp
+// with match.any measured slower than the extra reductions it saves).
 // ---------------------------------------------------------------------------
 
 template <typename PT, int NS>
@@ -233,9 +234,9 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
                         atomicAdd(&cube[ux + kCube * (uy + kCube * uz)], 1u);
                     }
                 }
-                // phase 2: everywhere else in the grid, one global atomic per step and
-                // per distinct cell of the warp; the ray ends at its first step outside
-                // the grid (scripts/gvom.py:1216-1225)
+                // phase 2: everywhere else in the grid, one global reduction per step;
+                // the ray ends at its first step outside the grid
+                // (scripts/gvom.py:1216-1225)
                 for (; st < K; st++) {
                     px = __fadd_rn(px, ix);
                     py = __fadd_rn(py, iy);
@@ -250,9 +251,7 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
                     }
                     if ((unsigned)vx >= (unsigned)g.X || (unsigned)vy >= (unsigned)g.X || (unsigned)vz >= (unsigned)g.Z)
                         break;
-                    const int cell = (vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe;
-                    const unsigned grp = __match_any_sync(__activemask(), cell);
-                    if ((int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&cnt[cell], (unsigned long long)__popc(grp));
+                    atomicAdd(&cnt[(vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe], 1ull);
                 }
             } else {
                 // origin far from the world origin: float64 voxel indices

@@ -122,6 +122,11 @@ class Lidar:
     max_range: float = 60.0
     noise_sigma: float = 0.02
     mount_height: float = 1.0
+    # mounting on the vehicle: offset in the vehicle frame (m), yaw and pitch (deg)
+    mount_x: float = 0.0
+    mount_y: float = 0.0
+    mount_yaw_deg: float = 0.0
+    mount_pitch_deg: float = 0.0
 
     @property
     def n_points(self) -> int:
@@ -185,11 +190,17 @@ class Scan:
     meta: dict = field(default_factory=dict)
 
 
-def _pose_matrix(pose: Pose, z: float, offset) -> np.ndarray:
+def _pose_matrix(pose: Pose, z: float, offset, lidar: "Lidar | None" = None) -> np.ndarray:
     c, s = math.cos(pose.yaw), math.sin(pose.yaw)
     T = np.eye(4)
     T[:3, :3] = [[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]]
     T[:3, 3] = [pose.x + offset[0], pose.y + offset[1], z + offset[2]]
+    if lidar is not None and (lidar.mount_x or lidar.mount_y or lidar.mount_yaw_deg or lidar.mount_pitch_deg):
+        my, mp = math.radians(lidar.mount_yaw_deg), math.radians(lidar.mount_pitch_deg)
+        Rz = np.array([[math.cos(my), -math.sin(my), 0.0], [math.sin(my), math.cos(my), 0.0], [0.0, 0.0, 1.0]])
+        Ry = np.array([[math.cos(mp), 0.0, math.sin(mp)], [0.0, 1.0, 0.0], [-math.sin(mp), 0.0, math.cos(mp)]])
+        T[:3, 3] += T[:3, :3] @ np.array([lidar.mount_x, lidar.mount_y, 0.0])
+        T[:3, :3] = T[:3, :3] @ Rz @ Ry
     return T
 
 
@@ -234,7 +245,7 @@ def make_scan(terrain: Terrain, lidar: Lidar, pose: Pose, scan_index: int = 0,
     g = float(terrain.height(torch.tensor([pose.x], dtype=torch.float64),
                              torch.tensor([pose.y], dtype=torch.float64))[0])
     z_sensor = g + lidar.mount_height
-    T = _pose_matrix(pose, z_sensor, off)
+    T = _pose_matrix(pose, z_sensor, off, lidar)
     R = T[:3, :3]
     d_s = lidar.directions()
     keep = np.ones(d_s.shape[0], dtype=bool)
@@ -245,6 +256,8 @@ def make_scan(terrain: Terrain, lidar: Lidar, pose: Pose, scan_index: int = 0,
     d_s = d_s[keep]
     d_w = d_s @ R.T
     origin_local = np.array([pose.x, pose.y, z_sensor])
+    if lidar.mount_x or lidar.mount_y:
+        origin_local = T[:3, 3] - np.asarray(off, dtype=np.float64)
     r = cast_rays(terrain, origin_local, d_w, lidar.max_range, device=device)
     rng_n = np.random.default_rng([noise_seed, scan_index])
     r = r + rng_n.normal(0.0, lidar.noise_sigma, r.shape)
@@ -333,3 +346,70 @@ def make_workload_scans(w: Workload, n: int | None = None, device="cpu", dropout
     return [make_scan(terrain, lidar, p, i, vegetation=veg, footprint=w.xy_size * w.res,
                       dropout=dropout, transform_dtype=w.transform_dtype, device=device)
             for i, p in enumerate(poses)]
+
+
+# ---------------------------------------------------------------------------
+# Batched form: several sensors per vehicle, every step's scans in one launch
+# ---------------------------------------------------------------------------
+
+# four mountings: front, rear, left, right (offset m, yaw deg, pitch deg)
+MOUNTS = ((0.6, 0.0, 0.0, -5.0), (-0.6, 0.0, 180.0, -5.0), (0.0, 0.4, 90.0, -10.0), (0.0, -0.4, -90.0, -10.0))
+
+
+@dataclass
+class Sensor:
+    beams: int
+    columns: int
+    dropout: float  # probability that a whole beam is missing in a scan
+    mount: int      # index into MOUNTS
+
+
+@dataclass
+class BatchedWorkload:
+    name: str
+    res: float
+    xy_size: int
+    z_size: int
+    buffer_size: int
+    sensors: tuple
+    n_steps: int = 24
+    transform_dtype: type = np.float32
+
+    def gvom_args(self):
+        return Workload(self.name, self.res, self.xy_size, self.z_size, self.buffer_size, 0, 0).gvom_args()
+
+    @property
+    def voxels(self) -> int:
+        return self.xy_size * self.xy_size * self.z_size
+
+    def lidar(self, k: int) -> Lidar:
+        sn = self.sensors[k]
+        mx, my, yaw, pitch = MOUNTS[sn.mount]
+        return Lidar(beams=sn.beams, columns=sn.columns, mount_x=mx, mount_y=my, mount_yaw_deg=yaw,
+                     mount_pitch_deg=pitch)
+
+
+BATCHED = {
+    # 8 sensors of 16,384-262,144 points (before 0-60 % beam dropout) on 4 mountings;
+    # 0.15 m voxels, 256 x 256 x 64, buffer 16 (two steps of 8 scans)
+    "batched_8": BatchedWorkload("batched_8", 0.15, 256, 64, 16, (
+        Sensor(32, 512, 0.0, 0), Sensor(64, 512, 0.1, 1), Sensor(64, 1024, 0.2, 2), Sensor(128, 1024, 0.3, 3),
+        Sensor(64, 2048, 0.4, 0), Sensor(128, 2048, 0.6, 1), Sensor(32, 1024, 0.5, 2), Sensor(128, 512, 0.15, 3))),
+}
+
+
+def make_batched_steps(w: BatchedWorkload, n_steps: int | None = None, device="cpu") -> list:
+    """`n_steps` steps along the seeded trajectory, each a list of one scan per
+    sensor (sensor k's beam dropout re-drawn per step from seed 3)."""
+    n_steps = w.n_steps if n_steps is None else n_steps
+    extent = w.xy_size * w.res
+    terrain = Terrain.make(SEED_TERRAIN, extent=extent, path_len=max(1, n_steps) * 0.4)
+    poses = make_trajectory(n_steps)
+    steps = []
+    for i, p in enumerate(poses):
+        scans = []
+        for k, sn in enumerate(w.sensors):
+            scans.append(make_scan(terrain, w.lidar(k), p, i * len(w.sensors) + k, dropout=sn.dropout,
+                                   transform_dtype=w.transform_dtype, device=device))
+        steps.append(scans)
+    return steps
