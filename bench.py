@@ -287,7 +287,7 @@ def _reduce_max_sum(torch, dist, t_val, pts):
     return float(tm[0]), float(ts[1])
 
 
-def measure_form(form, args, torch, dist, lrank, flush, headline):
+def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
     import ctypes as C
 
     from gvom_gb300 import Gvom
@@ -302,6 +302,8 @@ def measure_form(form, args, torch, dist, lrank, flush, headline):
     g = Gvom(*w.gvom_args())
     g.set_stream(stream.cuda_stream)
     lib = g._l
+    # per-kernel stage times need direct launches; the timed steps replay CUDA graphs when `graphs`
+    timing_pass = graphs
     outs = [torch.empty((X, X), dtype=d, device="cuda") for d in (torch.int32, torch.int32, torch.float64, torch.int32)]
     out_ptrs = [C.c_void_p(t.data_ptr()) for t in outs]
     origin = np.zeros(3)
@@ -332,33 +334,48 @@ def measure_form(form, args, torch, dist, lrank, flush, headline):
         step_device(i)
     torch.cuda.synchronize()
 
-    # ---- timed region (device-resident inputs) ----
+    # ---- timed regions (device-resident inputs) ----
     n_steps = args.steps if headline else max(10, min(args.steps, args.form_steps))
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(n_steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(n_steps)]
-    g.set_stage_timing(True)
-    clocks = Clocks(lrank, "" if headline else "_" + form.name)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    clocks.start()
-    t_wall0 = time.perf_counter()
-    pts_total = 0
-    for k in range(n_steps):
-        flush.zero_()
-        starts[k].record(stream)
-        step_device(args.warmup + k)
-        ends[k].record(stream)
-        pts_total += form.points[(args.warmup + k) % len(form)]
-    torch.cuda.synchronize()
-    t_wall1 = time.perf_counter()
-    if dist:
-        dist.barrier()
-    clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    stages = g.stage_times()
-    g.set_stage_timing(False)
-    t_dev_max, pts_all = _reduce_max_sum(torch, dist, sum(step_ms) / 1e3, pts_total)
+
+    def timed(n, use_graphs, stage_timing, clk_tag=None):
+        g.set_graphs(use_graphs)
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+        for i in range(3):  # warm the graph executables / the timing events
+            step_device(i)
+        g.set_stage_timing(stage_timing)
+        clocks = Clocks(lrank, clk_tag) if clk_tag is not None else None
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        t0 = time.perf_counter()
+        pts = 0
+        for k in range(n):
+            flush.zero_()
+            starts[k].record(stream)
+            step_device(args.warmup + k)
+            ends[k].record(stream)
+            pts += form.points[(args.warmup + k) % len(form)]
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        if dist:
+            dist.barrier()
+        clk = clocks.stop() if clocks else None
+        ms = [x.elapsed_time(y) for x, y in zip(starts, ends)]
+        st = g.stage_times() if stage_timing else None
+        g.set_stage_timing(False)
+        t, p = _reduce_max_sum(torch, dist, sum(ms) / 1e3, pts)
+        return ms, t, p, wall, clk, st
+
+    # the headline: CUDA-graph replay (or direct launches with graphs=False)
+    step_ms, t_dev_max, pts_all, wall_timed, clk, _ = timed(n_steps, graphs, False,
+                                                            "" if headline else "_" + form.name)
+    # direct launches, for comparison, and a pass with per-kernel CUDA events
+    n_aux = max(10, min(n_steps, 300))
+    ms_direct, t_direct, pts_direct, _, _, _ = timed(n_aux, False, False)
+    _, _, _, _, _, stages = timed(n_aux, False, True)
 
     # state sizes for the roofline accounting (last step)
     C_sum = 0
@@ -393,6 +410,7 @@ def measure_form(form, args, torch, dist, lrank, flush, headline):
     # ---- e2e through the public API with host buffers ----
     e2e_times = []
     g.set_stream(None)
+    g.set_graphs(graphs)
     torch.cuda.synchronize()
 
     def step_e2e(i):
@@ -422,7 +440,8 @@ def measure_form(form, args, torch, dist, lrank, flush, headline):
     g.close()
     return {
         "value": pts_all / t_dev_max, "ms_per_step": 1e3 * t_dev_max / n_steps, "steps": n_steps,
-        "config": form.config(),
+        "config": dict(form.config(), launch="cuda graphs" if graphs else "direct"),
+        "direct_launches": {"value": pts_direct / t_direct, "ms_per_step": 1e3 * t_direct / n_aux, "steps": n_aux},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "e2e_p50": 1e3 * float(np.percentile(e2e_times, 50)),
                        "e2e_p99": 1e3 * float(np.percentile(e2e_times, 99))},
@@ -434,7 +453,7 @@ def measure_form(form, args, torch, dist, lrank, flush, headline):
                      "traffic": profiled_traffic(dom_name, form.name)},
         "stages": stage_tab,
         "ray_last_scan": ray,
-        "wall_s_timed": t_wall1 - t_wall0,
+        "wall_s_timed": wall_timed,
         "clocks": clk,
     }
 
@@ -473,6 +492,7 @@ def run_gpu(args):
                            parallelism=f"replicas x{world}"),
             "latency_ms": res["latency_ms"], "e2e": res["e2e"], "gpu_launches": res["gpu_launches"],
             "roofline": res["roofline"], "stages": res["stages"], "ray_last_scan": res["ray_last_scan"],
+            "direct_launches": res["direct_launches"],
             "wall_s_timed": res["wall_s_timed"], "clocks": res["clocks"], "cpu_baseline": cpu,
             "forms": forms,
         }

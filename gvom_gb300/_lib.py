@@ -30,7 +30,7 @@ EXPORTS = (
     "gvom_combined_count", "gvom_get_combined", "gvom_get_maps", "gvom_set_stream",
     "gvom_synchronize", "gvom_last_process_stats", "gvom_device_bytes", "gvom_last_error",
     "gvom_version", "gvom_set_stage_timing", "gvom_stage_times", "gvom_stage_name",
-    "gvom_debug_voxel_map_noalloc",
+    "gvom_debug_voxel_map_noalloc", "gvom_set_graphs",
 )
 GVOM_STAGES = 10
 
@@ -86,6 +86,7 @@ def load(path: str | None = None):
         "gvom_combine_device": ([P, P, P, P, P, P], C.c_int),
         "gvom_debug_voxel_map": ([P, P, i64, C.POINTER(i64)], C.c_int),
         "gvom_debug_voxel_map_noalloc": ([P, P, i64, C.POINTER(i64)], C.c_int),
+        "gvom_set_graphs": ([P, i32], C.c_int),
         "gvom_debug_height_map": ([P, P], C.c_int),
         "gvom_debug_inferred_height_map": ([P, P], C.c_int),
         "gvom_ring_state": ([P, C.POINTER(i64), C.POINTER(i64)], C.c_int),

@@ -154,6 +154,10 @@ struct GvomHandle {
     int pageable_access = 0;
     int num_sms = 1;
     StageTimer timer;
+    // CUDA graphs: each process / combine launch sequence is captured and
+    // replayed through an executable graph updated in place
+    bool graphs = false;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // [0] process, [1] combine
 };
 
 namespace {
@@ -184,6 +188,42 @@ void dfree(GvomHandle *h, void *p, size_t bytes) {
 }
 
 long long ext_cells(const Geom &g) { return (long long)g.Xe * g.Xe * g.Ze; }
+
+// Runs `enqueue` (stream-ordered work on h->st only, no allocation and no
+// host synchronisation) directly, or in graph mode captures it and launches
+// the executable graph `which`, updated in place when the captured topology
+// matches the previous one and re-instantiated otherwise.
+template <class F>
+int run_graphed(GvomHandle *h, int which, F &&enqueue) {
+    if (!h->graphs) return enqueue();
+    CUDA_TRY(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue();
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    if (rc || e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : fail(GVOM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
+    cudaGraphExec_t &x = h->gexec[which];
+    if (x) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(x, g, &info) != cudaSuccess) {
+            cudaGetLastError();
+            cudaGraphExecDestroy(x);
+            x = nullptr;
+        }
+    }
+    cudaError_t ei = cudaSuccess;
+    if (!x) ei = cudaGraphInstantiate(&x, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+        x = nullptr;
+        return fail(GVOM_ERR_CUDA, std::string("graph instantiation: ") + cudaGetErrorString(ei));
+    }
+    CUDA_TRY(cudaGraphLaunch(x, h->st));
+    return GVOM_OK;
+}
 
 int check_params(const GvomParams *p) {
     if (!p) return fail(GVOM_ERR_ARG, "params is NULL");
@@ -387,11 +427,18 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
         d.rec_cap = h->slots[slot].cap;
         d.ctr = h->d_ctr + i;
     }
-    CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * k, h->st));
-    CUDA_TRY(launch_process(pc, table, k, block, (int)std::min<long long>(max_n, h->g.V), scans[0].dtype, h->prec,
-                            h->prank, h->sorted, h->moments, h->st, h->timer.begin(0, kProcessKernels)));
+    rc = run_graphed(h, 0, [&]() -> int {
+        CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * k, h->st));
+        CUDA_TRY(launch_process(pc, table, k, block, (int)std::min<long long>(max_n, h->g.V), scans[0].dtype,
+                                h->prec, h->prank, h->sorted, h->moments, h->st,
+                                h->graphs ? nullptr : h->timer.begin(0, kProcessKernels)));
+        for (int i = 0; i < k; i++)
+            CUDA_TRY(cudaMemcpyAsync(h->d_slotC + slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
+                                     h->st));
+        return GVOM_OK;
+    });
+    if (rc) return rc;
     for (int i = 0; i < k; i++) {
-        CUDA_TRY(cudaMemcpyAsync(h->d_slotC + slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice, h->st));
         Slot &sl = h->slots[slot_of[i]];
         for (int a = 0; a < 3; a++) sl.od[a] = table[i].od[a];
         sl.valid = true;
@@ -533,6 +580,8 @@ int gvom_destroy(GvomHandle *h) {
     if (!h) return GVOM_OK;
     if (h->st) cudaStreamSynchronize(h->st);
     if (h->own) cudaStreamSynchronize(h->own);
+    for (auto &x : h->gexec)
+        if (x) cudaGraphExecDestroy(x);
     for (auto &s : h->slots) {
         cudaFree(s.idx);
         cudaFree(s.rec);
@@ -735,8 +784,12 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     m2.pos = h->pos;
     m2.neg = h->neg;
     m2.vis = h->vis;
-    CUDA_TRY(cudaMemsetAsync(mp.out_count, 0, sizeof(int), h->st));
-    CUDA_TRY(launch_combine(mp, cp, m2, h->st, h->timer.begin(kProcessKernels, kCombineKernels)));
+    const int rcg = run_graphed(h, 1, [&]() -> int {
+        CUDA_TRY(cudaMemsetAsync(mp.out_count, 0, sizeof(int), h->st));
+        CUDA_TRY(launch_combine(mp, cp, m2, h->st, h->graphs ? nullptr : h->timer.begin(kProcessKernels, kCombineKernels)));
+        return GVOM_OK;
+    });
+    if (rcg) return rcg;
     for (int a = 0; a < 3; a++) h->cod[nb][a] = mp.co[a];
     h->cur = nb;
     h->have_comb = true;
@@ -1094,6 +1147,13 @@ int gvom_last_process_stats(GvomHandle *h, int64_t *valid_points, int64_t *hits,
     if (valid_points) *valid_points = (int64_t)c.valid;
     if (hits) *hits = (int64_t)c.hits;
     if (ray_steps) *ray_steps = (int64_t)c.steps;
+    return GVOM_OK;
+}
+
+int gvom_set_graphs(GvomHandle *h, int32_t on) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->graphs = on != 0;
     return GVOM_OK;
 }
 

@@ -245,6 +245,11 @@ class Gvom:
     def set_stream(self, stream_ptr: int | None):
         check(self._l.gvom_set_stream(self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
 
+    def set_graphs(self, on: bool):
+        """Capture each process / combine launch sequence into a CUDA graph and
+        replay it (updated in place while its shape holds)."""
+        check(self._l.gvom_set_graphs(self._h, 1 if on else 0))
+
     def set_stage_timing(self, on: bool):
         """Record CUDA events around every kernel launch (resets the totals)."""
         check(self._l.gvom_set_stage_timing(self._h, 1 if on else 0))

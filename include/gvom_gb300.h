@@ -172,6 +172,13 @@ int gvom_synchronize(GvomHandle *h);
  * kernel launch of process / combine; gvom_stage_times waits for the queued
  * work and returns, for stages 0..n-1, the summed milliseconds and launch
  * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
+/* CUDA-graph mode (off by default); no counterpart in the reference.  When on,
+ * each process / combine call captures its launch sequence and replays it
+ * through an executable graph that is updated in place while the sequence
+ * keeps its shape (the same batch-size class and source count), which removes
+ * per-kernel launch gaps.  Stage timing records nothing while it is on. */
+int gvom_set_graphs(GvomHandle *h, int32_t on);
+
 #define GVOM_STAGES 10
 int gvom_set_stage_timing(GvomHandle *h, int32_t on);
 int gvom_stage_times(GvomHandle *h, double *total_ms, int64_t *launches, int32_t n_stages);

@@ -202,3 +202,27 @@ def test_repeated_combines_accumulate_like_reference(Gvom):
         refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
         compare_combine(out, refd, g.maps_state(), w.gvom_args(), f"combine {k}")
         compare_slot(canonical_state(g.combined_state()), canonical_state(o.combined_state()), f"combined {k}")
+
+
+def test_graph_mode_equals_direct_launches(Gvom):
+    """CUDA-graph replay (captured, updated in place, re-instantiated when the
+    batch-size class or the source count changes) == direct launches."""
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["small_32x512"]
+    scans = make_workload_scans(w, 7)
+    params = w.gvom_args()[:4] + (4,) + w.gvom_args()[5:]
+    a, b = Gvom(*params), Gvom(*params)
+    b.set_graphs(True)
+    plan = [[0], [1], [2, 3], [4], [5, 6], [0]]  # one scan, then a batch, as the ring fills up
+    for k, idx in enumerate(plan):
+        batch = [(scans[i].points, scans[i].ego, scans[i].transform) for i in idx]
+        for m in (a, b):
+            if len(batch) == 1:
+                m.Process_pointcloud(*batch[0])
+            else:
+                m.process_batch(batch)
+        ra, rb = a.combine_maps(), b.combine_maps()
+        for x, y in zip(ra, rb):
+            np.testing.assert_array_equal(x, y)
+        assert a.ring_state() == b.ring_state()
+        compare_slot(canonical_state(a.combined_state()), canonical_state(b.combined_state()), f"combined {k}")
