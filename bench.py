@@ -458,6 +458,81 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
     }
 
 
+def measure_served(args, torch):
+    """Served form: two device-resident map instances behind the request loop
+    of gvom_gb300.serve -- 16 OS1-64 sensors at 10 Hz (Poisson arrivals) on a
+    256 x 256 x 64 / 0.15 m map and 4 OS1-128x2048 sensors at 10 Hz on a
+    512 x 512 x 96 / 0.1 m map.  Reports p50/p99 scan->map latency (submission
+    to combine_maps outputs on the host) at that load, and the points/sec the
+    loop sustains when every request of the window is queued at once."""
+    from gvom_gb300 import serve
+    from gvom_gb300 import synthetic as S
+
+    duration = args.served_seconds
+    specs = [  # (params, sensors, (beams, columns), rate)
+        (S.WORKLOADS["os1_64_veg"].gvom_args()[:4] + (16,) + S.WORKLOADS["os1_64_veg"].gvom_args()[5:], 16, (64, 1024), 10.0),
+        (S.WORKLOADS["os1_128_far"].gvom_args()[:4] + (8,) + S.WORKLOADS["os1_128_far"].gvom_args()[5:], 4, (128, 2048), 10.0),
+    ]
+    pools = []  # per instance, per sensor: a cycle of scans along the trajectory
+    for params, n_sensors, (beams, cols), _ in specs:
+        res, X = params[0], params[2]
+        terrain = S.Terrain.make(S.SEED_TERRAIN, extent=X * res, path_len=4.0)
+        poses = S.make_trajectory(4)
+        per_sensor = []
+        for k in range(n_sensors):
+            mx, my, yaw, pitch = S.MOUNTS[k % 4]
+            lid = S.Lidar(beams=beams, columns=cols, mount_x=mx, mount_y=my, mount_yaw_deg=yaw + 7.0 * (k // 4),
+                          mount_pitch_deg=pitch)
+            per_sensor.append([S.make_scan(terrain, lid, p, 1000 * k + i, device="cuda") for i, p in enumerate(poses)])
+        pools.append(per_sensor)
+    torch.cuda.synchronize()
+
+    def run(events, tag):
+        srv = serve.MapServer([sp[0] for sp in specs])
+        nxt = [[0] * len(p) for p in pools]
+        reqs = []
+        t0 = time.perf_counter()
+        for t, (inst, k) in events:
+            now = time.perf_counter() - t0
+            if t > now:
+                time.sleep(t - now)
+            s = pools[inst][k][nxt[inst][k] % len(pools[inst][k])]
+            nxt[inst][k] += 1
+            reqs.append(srv.submit(inst, s.points, s.ego, s.transform))
+        for r in reqs:
+            r.done.wait(120)
+        t_end = max(r.t_done for r in reqs)
+        span = t_end - t0
+        srv.close()
+        out = {"requests": len(reqs), "span_s": span, "point_budget": srv.point_budget,
+               "points_per_s": sum(r.points.shape[0] for r in reqs) / span, "instances": []}
+        for i, sp in enumerate(specs):
+            lat = [1e3 * r.latency for r in reqs if r.instance == i]
+            nb = [len(seqs) for inst, seqs in srv.batches if inst == i]
+            out["instances"].append({"grid": [sp[0][2], sp[0][2], sp[0][3]], "voxel_m": sp[0][0],
+                                     "sensors": sp[1], "rate_hz": sp[3],
+                                     "points_per_scan": pools[i][0][0].points.shape[0],
+                                     "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                                     "max_ms": float(np.max(lat)), "batches": len(nb),
+                                     "mean_batch": float(np.mean(nb))})
+        errors = [r.result for r in reqs if isinstance(r.result, Exception)]
+        if errors:
+            raise RuntimeError(f"served {tag}: {errors[0]}")
+        return out
+
+    rates = []
+    for i, sp in enumerate(specs):
+        rates += [(i, k, sp[3]) for k in range(sp[1])]
+    arr = serve.poisson_arrivals([r for _, _, r in rates], duration, seed=S.SEED_ARRIVALS)
+    events = [(t, (rates[j][0], rates[j][1])) for t, j in arr]
+    run(events[: max(1, len(events) // 8)], "warm-up")
+    at_load = run(events, "at load")
+    saturated = run([(0.0, e[1]) for e in events], "saturated")
+    return {"at_load": at_load, "saturated": saturated,
+            "note": "latency = submission to combine_maps outputs on the host; the saturated run queues every "
+                    "request of the window at once and reports the points/sec the loop sustains"}
+
+
 def run_gpu(args):
     import torch
 
@@ -475,6 +550,10 @@ def run_gpu(args):
     res = measure_form(head, args, torch, dist, lrank, flush, headline=True)
     forms = {}
     for name in [f for f in args.forms.split(",") if f and f != args.workload]:
+        if name == "served":
+            if world == 1:
+                forms[name] = measure_served(args, torch)
+            continue
         fm = Form(name, "cuda", None)
         forms[name] = measure_form(fm, args, torch, dist, lrank, flush, headline=False)
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -509,7 +588,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gvom", choices=["gvom", "reference"])
     ap.add_argument("--workload", default="os1_64_veg", help="headline form")
-    ap.add_argument("--forms", default="batched_8", help="comma-separated other forms measured in the same run")
+    ap.add_argument("--forms", default="batched_8,served", help="comma-separated other forms measured in the same run")
+    ap.add_argument("--served-seconds", type=float, default=3.0, help="arrival window of the served form")
     ap.add_argument("--form-steps", type=int, default=300, help="timed steps of each other form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
