@@ -385,7 +385,10 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
         d.n = s.n;
         d.stride = s.stride;
         d.tmode = s.tdtype == GVOM_NONE ? 0 : (s.tdtype == GVOM_F32 ? 1 : 2);
-        for (int r = 0; r < 12; r++) d.T[r] = s.T[r];
+        for (int r = 0; r < 12; r++) {
+            d.T[r] = s.T[r];
+            d.Tf[r] = (float)s.T[r];
+        }
         ray_origin(h, s.ego, d.od);
         // ray positions stay within one step of the grid, so for
         // |origin| + grid + 2 < 2^22 every position the march visits is below

@@ -64,6 +64,7 @@ struct ScanDesc {
     int fast_floor;        // |origin| + grid < 2^22: float32 ray voxel indices (see ray_index)
     int exact_ok;          // |origin| < 2^31: integer hit-voxel arithmetic (gx_coord)
     double T[12];          // transform rows 0..2 (a float32 transform is stored exactly)
+    float Tf[12];          // the same rows as float32 (exact for a float32 transform)
     double od[3];          // voxel origin (integer-valued doubles)
     int oi[3];             // the same as int (valid when exact_ok)
     float pt0[3];          // ray start: (float)(ego / resolution)

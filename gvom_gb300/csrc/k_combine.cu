@@ -204,7 +204,10 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
     const int plane = X * X;
     if (tid == 0) qn = 0;
     // index merge, source by source in source order (scripts/gvom.py:242-298):
-    // a source's kZC loads are independent, and the state per plane is one int
+    // a source's kZC loads are independent, and the state per plane is one int.
+    // Entries outside a shifted source read as -1, which changes nothing: only
+    // an occupied entry (>= 0) or a free one (<= -2) acts, and only on a
+    // combined value that is not occupied yet (<= -1).
     int cmb[kZC];
 #pragma unroll
     for (int k = 0; k < kZC; k++) cmb[k] = -1;
@@ -214,22 +217,27 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
         const MergeSrc &src = mp.src[s];
         const int xs = x + src.dx, ys = y + src.dy;
         if (!(col && (unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X)) continue;
-        const int *col_s = src.idx + xs + ys * X;
+        // planes k with 0 <= z0 + k + dz < Z (and z0 + k < Z)
+        const int klo = max(0, -(z0 + src.dz)), khi = min(min(kZC, Z - z0), Z - z0 - src.dz);
+        const int *colp = src.idx + xs + ys * X;
         int vs[kZC];
 #pragma unroll
-        for (int k = 0; k < kZC; k++) {
-            const int zs = z0 + k + src.dz;
-            vs[k] = (z0 + k < Z && (unsigned)zs < (unsigned)Z) ? __ldg(col_s + zs * plane) : kOutside;
-        }
+        for (int k = 0; k < kZC; k++)
+            vs[k] = (k >= klo && k < khi) ? __ldg(colp + (z0 + k + src.dz) * plane) : -1;
+        if (src.is_last) {
+            // previous combined map: an occupied voxel comes back only if at most
+            // 10 new rays passed through it (scripts/gvom.py:1058)
 #pragma unroll
-        for (int k = 0; k < kZC; k++) {
-            const int o = vs[k];
-            if (o == kOutside) continue;
-            int comb = cmb[k];
-            const bool alloc = src.is_last ? (o >= 0 && comb <= -1 && comb >= -11) : (o >= 0 && comb <= -1);
-            if (alloc) comb = kOcc;
-            else if (o < -1 && comb <= -1) comb += o + 1;
-            cmb[k] = comb;
+            for (int k = 0; k < kZC; k++) {
+                const int o = vs[k], c = cmb[k];
+                if (c <= -1) cmb[k] = (o >= 0) ? (c >= -11 ? kOcc : c) : (o < -1 ? c + o + 1 : c);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kZC; k++) {
+                const int o = vs[k], c = cmb[k];
+                if (c <= -1) cmb[k] = (o >= 0) ? kOcc : (o < -1 ? c + o + 1 : c);
+            }
         }
     }
     __syncthreads();

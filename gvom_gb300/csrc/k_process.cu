@@ -47,8 +47,8 @@ __device__ __forceinline__ void transform_point<float>(const ScanDesc &sd, float
     if (sd.tmode == 1) {
 #pragma unroll
         for (int r = 0; r < 3; r++) {
-            float t0 = (float)sd.T[r * 4 + 0], t1 = (float)sd.T[r * 4 + 1];
-            float t2 = (float)sd.T[r * 4 + 2], t3 = (float)sd.T[r * 4 + 3];
+            const float t0 = sd.Tf[r * 4 + 0], t1 = sd.Tf[r * 4 + 1];
+            const float t2 = sd.Tf[r * 4 + 2], t3 = sd.Tf[r * 4 + 3];
             float s = __fadd_rn(__fmul_rn(x, t0), __fmul_rn(y, t1));
             s = __fadd_rn(s, __fmul_rn(z, t2));
             o[r] = __fadd_rn(s, t3);
@@ -108,21 +108,38 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned l
 // from almost every ray.  A ray's first steps, while they stay inside a
 // kCube^3 block of cells around the ego voxel (sd.cube0, inside the grid),
 // are counted in shared memory and flushed once per block (one global atomic
-// per touched cell); the remaining steps add straight into the dense count
-// words (fire-and-forget reductions; aggregating equal cells across a warp
-// with match.any measured slower than the extra reductions it saves).
+// per touched cell).  The remaining steps go through a per-block shared hash
+// table of (cell, count): neighbouring rays of a block cross many of the
+// same cells, and a shared atomic is several times cheaper than a scattered
+// global reduction; a step whose slot holds another cell adds straight into
+// the dense count words.
 // ---------------------------------------------------------------------------
+
+// per-block shared hash table for the ray steps outside the cube
+// (GVOM_TRACE_HASH_BITS = log2 slots; 0 = every such step adds globally)
+#ifndef GVOM_TRACE_HASH_BITS
+#define GVOM_TRACE_HASH_BITS 11
+#endif
+constexpr int kHashBits = GVOM_TRACE_HASH_BITS > 0 ? GVOM_TRACE_HASH_BITS : 1;
+constexpr bool kHash = GVOM_TRACE_HASH_BITS > 0;
+constexpr unsigned kHashEmpty = 0xffffffffu;
 
 template <typename PT, int NS>
 __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
                                                        float4 *__restrict__ prec, int *__restrict__ prank) {
     __shared__ unsigned cube[kCubeCells];
+    __shared__ unsigned htag[1 << kHashBits], hcnt[1 << kHashBits];
     const int s = find_scan(tab, pc.nscans, blockIdx.x);
     const ScanDesc &sd = tab.s[s];
     const Geom g = pc.g;
     const int ffloor = sd.fast_floor;
     if (sd.cube_on)
         for (int k = threadIdx.x; k < kCubeCells; k += blockDim.x) cube[k] = 0u;
+    if (kHash)
+        for (int k = threadIdx.x; k < (1 << kHashBits); k += blockDim.x) {
+            htag[k] = kHashEmpty;
+            hcnt[k] = 0u;
+        }
     __syncthreads();
     const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
     const bool active = i < sd.n;
@@ -234,9 +251,10 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
                         atomicAdd(&cube[ux + kCube * (uy + kCube * uz)], 1u);
                     }
                 }
-                // phase 2: everywhere else in the grid, one global reduction per step;
-                // the ray ends at its first step outside the grid
-                // (scripts/gvom.py:1216-1225)
+                // phase 2: everywhere else in the grid; the ray ends at its first step
+                // outside the grid (scripts/gvom.py:1216-1225).  Steps are counted in
+                // the block's shared hash table of (cell, count) when the cell owns or
+                // claims its slot, else by a global reduction.
                 for (; st < K; st++) {
                     px = __fadd_rn(px, ix);
                     py = __fadd_rn(py, iy);
@@ -251,7 +269,19 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
                     }
                     if ((unsigned)vx >= (unsigned)g.X || (unsigned)vy >= (unsigned)g.X || (unsigned)vz >= (unsigned)g.Z)
                         break;
-                    atomicAdd(&cnt[(vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe], 1ull);
+                    const unsigned cell = (unsigned)((vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe);
+                    if (kHash) {
+                        const unsigned h = (cell * 2654435761u) >> (32 - kHashBits);
+                        unsigned tag = htag[h];
+                        if (tag == kHashEmpty) {
+                            tag = atomicCAS(&htag[h], kHashEmpty, cell);
+                            if (tag == kHashEmpty) tag = cell;
+                        }
+                        if (tag == cell) atomicAdd(&hcnt[h], 1u);
+                        else atomicAdd(&cnt[cell], 1ull);
+                    } else {
+                        atomicAdd(&cnt[cell], 1ull);
+                    }
                 }
             } else {
                 // origin far from the world origin: float64 voxel indices
@@ -276,6 +306,11 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
     warp_add_u64(&sd.ctr->hits, n_hit);
     warp_add_u64(&sd.ctr->steps, n_steps);
     __syncthreads();
+    if (kHash)
+        for (int k = threadIdx.x; k < (1 << kHashBits); k += blockDim.x) {
+            const unsigned t = htag[k];
+            if (t != kHashEmpty) atomicAdd(&sd.cnt[t], (unsigned long long)hcnt[k]);
+        }
     if (!sd.cube_on) return;
     for (int k = threadIdx.x; k < kCubeCells; k += blockDim.x) {
         const unsigned c = cube[k];
