@@ -325,6 +325,11 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
             arr[j].transform = T.ctypes.data_as(C.c_void_p)
         calls.append(arr)
 
+    # launch shapes for this workload (gvom_gb300.autotune, on a private mapper)
+    from gvom_gb300.autotune import autotune
+    tune_steps = [[(s.points, s.ego, s.transform) for s in st] for st in form.steps[:4]]
+    tuning = autotune(g, tune_steps, reps=8, use_cache=False, save=False) if args.autotune else g.get_tuning()
+
     def step_device(i):
         arr = calls[i % len(calls)]
         check(lib.gvom_process_batch(g._h, arr, len(arr), 1))
@@ -440,7 +445,7 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
     g.close()
     return {
         "value": pts_all / t_dev_max, "ms_per_step": 1e3 * t_dev_max / n_steps, "steps": n_steps,
-        "config": dict(form.config(), launch="cuda graphs" if graphs else "direct"),
+        "config": dict(form.config(), launch="cuda graphs" if graphs else "direct", tuning=tuning),
         "direct_launches": {"value": pts_direct / t_direct, "ms_per_step": 1e3 * t_direct / n_aux, "steps": n_aux},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "e2e_p50": 1e3 * float(np.percentile(e2e_times, 50)),
@@ -592,6 +597,8 @@ def main():
     ap.add_argument("--served-seconds", type=float, default=3.0, help="arrival window of the served form")
     ap.add_argument("--form-steps", type=int, default=300, help="timed steps of each other form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="default launch shapes instead of tuning them on the workload first")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -30,7 +30,7 @@ EXPORTS = (
     "gvom_combined_count", "gvom_get_combined", "gvom_get_maps", "gvom_set_stream",
     "gvom_synchronize", "gvom_last_process_stats", "gvom_device_bytes", "gvom_last_error",
     "gvom_version", "gvom_set_stage_timing", "gvom_stage_times", "gvom_stage_name",
-    "gvom_debug_voxel_map_noalloc", "gvom_set_graphs",
+    "gvom_debug_voxel_map_noalloc", "gvom_set_graphs", "gvom_set_tuning", "gvom_get_tuning",
 )
 GVOM_STAGES = 10
 
@@ -53,6 +53,11 @@ class GvomScan(C.Structure):
         ("n", C.c_int64), ("row_stride", C.c_int64), ("ego", C.c_double * 3),
         ("transform", C.c_void_p),
     ]
+
+
+class GvomTuning(C.Structure):
+    _fields_ = [("points_per_block", C.c_int32), ("assign_words_per_thread", C.c_int32),
+                ("merge_planes_per_thread", C.c_int32), ("stats_blocks_per_sm", C.c_int32)]
 
 
 class GvomError(RuntimeError):
@@ -87,6 +92,8 @@ def load(path: str | None = None):
         "gvom_debug_voxel_map": ([P, P, i64, C.POINTER(i64)], C.c_int),
         "gvom_debug_voxel_map_noalloc": ([P, P, i64, C.POINTER(i64)], C.c_int),
         "gvom_set_graphs": ([P, i32], C.c_int),
+        "gvom_set_tuning": ([P, C.POINTER(GvomTuning)], C.c_int),
+        "gvom_get_tuning": ([P, C.POINTER(GvomTuning)], C.c_int),
         "gvom_debug_height_map": ([P, P], C.c_int),
         "gvom_debug_inferred_height_map": ([P, P], C.c_int),
         "gvom_ring_state": ([P, C.POINTER(i64), C.POINTER(i64)], C.c_int),

@@ -153,6 +153,7 @@ struct GvomHandle {
     long long bytes = 0;
     int pageable_access = 0;
     int num_sms = 1;
+    Tuning tun = kDefaultTuning;
     StageTimer timer;
     // CUDA graphs: each process / combine launch sequence is captured and
     // replayed through an executable graph updated in place
@@ -283,7 +284,7 @@ int ensure_cnt(GvomHandle *h, int nscans) {
     while ((int)h->cnt.size() < nscans) {
         unsigned long long *c = nullptr;
         // padded to whole k_assign blocks of cells; the padding stays zero
-        const long long ve = (ext_cells(h->g) + kAssignBlockCells - 1) / kAssignBlockCells * kAssignBlockCells;
+        const long long ve = (ext_cells(h->g) + kAssignPadCells - 1) / kAssignPadCells * kAssignPadCells;
         int rc = dalloc_t(h, &c, (size_t)ve);
         if (rc) return rc;
         CUDA_TRY(cudaMemsetAsync(c, 0, (size_t)ve * 8, h->st));
@@ -368,6 +369,7 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
     }
     pc.step_cap = 2 * std::max(h->g.X, h->g.Z) + 8;
     pc.num_sms = h->num_sms;
+    pc.assign_per = h->tun.assign_per;
     pc.xe_magic = ~0ull / (unsigned long long)h->g.Xe + 1ull;
     pc.nscans = k;
     ScanDesc table[kMaxBatch];
@@ -420,7 +422,7 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
         }
         d.slot = slot;
         d.block_begin = block;
-        d.nblocks = (int)((s.n + 255) / 256);
+        d.nblocks = (int)((s.n + h->tun.pts_block - 1) / h->tun.pts_block);
         block += d.nblocks;
         d.pt_base = base;
         base += s.n;
@@ -434,7 +436,7 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
         CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * k, h->st));
         CUDA_TRY(launch_process(pc, table, k, block, (int)std::min<long long>(max_n, h->g.V), scans[0].dtype,
                                 h->prec, h->prank, h->sorted, h->moments, h->st,
-                                h->graphs ? nullptr : h->timer.begin(0, kProcessKernels)));
+                                h->graphs ? nullptr : h->timer.begin(0, kProcessKernels), h->tun.pts_block));
         for (int i = 0; i < k; i++)
             CUDA_TRY(cudaMemcpyAsync(h->d_slotC + slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
                                      h->st));
@@ -563,7 +565,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     for (auto m : imaps)
         if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
     if ((rc = dalloc_t(h, &h->mlow, (size_t)X2))) return bail(rc);
-    if ((rc = dalloc_t(h, &h->colinfo, (size_t)X2 * ((g.Z + 7) / 8)))) return bail(rc);
+    if ((rc = dalloc_t(h, &h->colinfo, (size_t)X2 * ((g.Z + 3) / 4)))) return bail(rc);  // chunks of >= 4 planes
     if ((rc = dalloc_t(h, &h->occ_list, (size_t)g.V))) return bail(rc);
     if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->B, h->st) != cudaSuccess ||
         cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 4, h->st) != cudaSuccess) {
@@ -739,11 +741,14 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     mp.out_count = h->d_combC + nb;
     mp.list = h->occ_list;
     mp.num_sms = h->num_sms;
+    mp.planes = h->tun.merge_planes;
+    mp.stats_bpsm = h->tun.stats_bpsm;
     mp.colinfo = h->colinfo;
     ColumnParams cp;
     std::memset(&cp, 0, sizeof(cp));
     cp.X = h->g.X;
     cp.Z = h->g.Z;
+    cp.planes = h->tun.merge_planes;
     cp.idx = mp.out_idx;
     cp.rec = mp.out_rec;
     cp.colinfo = h->colinfo;
@@ -1150,6 +1155,34 @@ int gvom_last_process_stats(GvomHandle *h, int64_t *valid_points, int64_t *hits,
     if (valid_points) *valid_points = (int64_t)c.valid;
     if (hits) *hits = (int64_t)c.hits;
     if (ray_steps) *ray_steps = (int64_t)c.steps;
+    return GVOM_OK;
+}
+
+int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
+    if (!h || !t) return fail(GVOM_ERR_ARG, "handle or tuning is NULL");
+    if (!(t->points_per_block == 128 || t->points_per_block == 256))
+        return fail(GVOM_ERR_ARG, "points_per_block must be 128 or 256");
+    if (!(t->assign_words_per_thread == 4 || t->assign_words_per_thread == 8 || t->assign_words_per_thread == 16))
+        return fail(GVOM_ERR_ARG, "assign_words_per_thread must be 4, 8 or 16");
+    if (!(t->merge_planes_per_thread == 4 || t->merge_planes_per_thread == 8 || t->merge_planes_per_thread == 16))
+        return fail(GVOM_ERR_ARG, "merge_planes_per_thread must be 4, 8 or 16");
+    if (!(t->stats_blocks_per_sm == 2 || t->stats_blocks_per_sm == 4 || t->stats_blocks_per_sm == 8))
+        return fail(GVOM_ERR_ARG, "stats_blocks_per_sm must be 2, 4 or 8");
+    std::lock_guard<std::mutex> lk(h->mu);
+    h->tun.pts_block = t->points_per_block;
+    h->tun.assign_per = t->assign_words_per_thread;
+    h->tun.merge_planes = t->merge_planes_per_thread;
+    h->tun.stats_bpsm = t->stats_blocks_per_sm;
+    return GVOM_OK;
+}
+
+int gvom_get_tuning(GvomHandle *h, GvomTuning *t) {
+    if (!h || !t) return fail(GVOM_ERR_ARG, "handle or tuning is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    t->points_per_block = h->tun.pts_block;
+    t->assign_words_per_thread = h->tun.assign_per;
+    t->merge_planes_per_thread = h->tun.merge_planes;
+    t->stats_blocks_per_sm = h->tun.stats_bpsm;
     return GVOM_OK;
 }
 

@@ -21,8 +21,17 @@
 namespace gvom {
 
 constexpr int kMaxBatch = 16;         // scans per batched launch
-constexpr int kAssignPer = 8;         // consecutive count words per k_assign thread
-constexpr int kAssignBlockCells = 256 * kAssignPer;
+constexpr int kAssignPerMax = 16;     // count words per k_assign thread, at most
+constexpr int kAssignPadCells = 256 * kAssignPerMax;  // count arrays are padded to this many cells
+
+// Launch-shape choices of the autotuner (each affects its own kernels only).
+struct Tuning {
+    int pts_block;      // points per block of the point-parallel kernels: 128 or 256
+    int assign_per;     // count words per k_assign thread: 4, 8 or 16
+    int merge_planes;   // z planes per k_merge thread: 4, 8 or 16
+    int stats_bpsm;     // k_merge_stats blocks per multiprocessor: 2, 4 or 8
+};
+constexpr Tuning kDefaultTuning = {256, 8, 8, 4};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
 constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
@@ -95,6 +104,7 @@ struct ProcessConst {
     int step_cap;          // upper bound on ray steps inside the grid
     int nscans;
     int num_sms;           // multiprocessors of the device (persistent grids)
+    int assign_per;        // Tuning::assign_per
     unsigned long long xe_magic;  // floor((2^64 - 1) / Xe) + 1 (divisions by the extended row length)
 };
 
@@ -114,12 +124,15 @@ struct MergeParams {
     int *out_count;        // occupied voxels
     int *list;             // voxel ids of the occupied voxels (capacity V)
     int num_sms;
+    int planes;            // Tuning::merge_planes (z planes per k_merge thread = colinfo chunk)
+    int stats_bpsm;        // Tuning::stats_bpsm
     int2 *colinfo;         // per (z chunk, y, x): lowest occupied z, lowest known-free z (Z if none)
     double co[3];          // combined origin (voxels)
 };
 
 struct ColumnParams {
     int X, Z;
+    int planes;            // z planes per colinfo chunk
     const int *idx;        // combined index map
     const VoxelRec *rec;   // combined records (by voxel id)
     const int2 *colinfo;
@@ -179,7 +192,7 @@ constexpr int kCombineKernels = 4;  // merge, merge_stats, columns, maps2d
 constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev = nullptr);
+                           cudaEvent_t *ev, int pts_block);
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
 cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
                            cudaEvent_t *ev = nullptr);

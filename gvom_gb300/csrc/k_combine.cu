@@ -29,7 +29,6 @@ namespace gvom {
 
 constexpr int kOcc = 0x7fffffff;
 constexpr int kOutside = INT32_MIN;
-constexpr int kZC = 8;  // z planes per k_merge thread
 
 // ---------------------------------------------------------------------------
 // k_merge
@@ -185,13 +184,13 @@ __device__ __forceinline__ void merge_voxel(const MergeParams &mp, int vid) {
     out[3] = make_float4(minh, e[0], e[1], e[2]);
 }
 
-// k_merge: every thread decides its kZC voxels (index merge), writes the
+// k_merge: every thread decides its ZC voxels (index merge), writes the
 // combined index map and queues occupied voxels in shared memory; the block
 // appends its queue to the global list of occupied voxels (one atomic).
 // k_merge_stats then merges the listed voxels' statistics with full warps
 // (occupied voxels are sparse: merging in place would run one lane per warp
 // and hold the whole block on that lane's dependent loads).
-template <int NSRC>
+template <int NSRC, int kZC>
 __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergeParams mp) {
     __shared__ int queue[256 * kZC];
     __shared__ int qn;
@@ -296,7 +295,7 @@ __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnP
     if (x >= X || y >= X) return;
     const int plane = X * X;
     int occ_z = Z, free_z = Z;
-    for (int ch = 0; ch * kZC < Z; ch++) {
+    for (int ch = 0; ch * cp.planes < Z; ch++) {
         const int2 ci = cp.colinfo[ch * plane + y * X + x];
         if (occ_z == Z) occ_z = ci.x;
         if (free_z == Z) free_z = ci.y;
@@ -814,22 +813,25 @@ __global__ void k_debug_maps(DebugMapParams p) {
 // launchers
 // ---------------------------------------------------------------------------
 template <int NSRC>
-static void launch_merge(const MergeParams &mp, dim3 g, cudaStream_t st, cudaEvent_t *ev) {
-    k_merge<NSRC><<<g, dim3(32, 8), 0, st>>>(mp);
+static void launch_merge(const MergeParams &mp, cudaStream_t st, cudaEvent_t *ev) {
+    const int X = mp.g.X, Z = mp.g.Z, zc = mp.planes;
+    dim3 gm((X + 31) / 32, (X + 7) / 8, (Z + zc - 1) / zc);
+    if (zc == 4) k_merge<NSRC, 4><<<gm, dim3(32, 8), 0, st>>>(mp);
+    else if (zc == 16) k_merge<NSRC, 16><<<gm, dim3(32, 8), 0, st>>>(mp);
+    else k_merge<NSRC, 8><<<gm, dim3(32, 8), 0, st>>>(mp);
     if (ev) cudaEventRecord(ev[1], st);
-    k_merge_stats<NSRC><<<mp.num_sms * 4, 256, 0, st>>>(mp);
+    k_merge_stats<NSRC><<<mp.num_sms * mp.stats_bpsm, 256, 0, st>>>(mp);
 }
 
 cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
                            cudaEvent_t *ev) {
-    const int X = mp.g.X, Z = mp.g.Z;
+    const int X = mp.g.X;
     if (ev) cudaEventRecord(ev[0], st);
-    dim3 gm((X + 31) / 32, (X + 7) / 8, (Z + kZC - 1) / kZC);
-    if (mp.nsrc <= 2) launch_merge<2>(mp, gm, st, ev);
-    else if (mp.nsrc <= 3) launch_merge<3>(mp, gm, st, ev);
-    else if (mp.nsrc <= 5) launch_merge<5>(mp, gm, st, ev);
-    else if (mp.nsrc <= 9) launch_merge<9>(mp, gm, st, ev);
-    else launch_merge<kMaxSources>(mp, gm, st, ev);
+    if (mp.nsrc <= 2) launch_merge<2>(mp, st, ev);
+    else if (mp.nsrc <= 3) launch_merge<3>(mp, st, ev);
+    else if (mp.nsrc <= 5) launch_merge<5>(mp, st, ev);
+    else if (mp.nsrc <= 9) launch_merge<9>(mp, st, ev);
+    else launch_merge<kMaxSources>(mp, st, ev);
     if (ev) cudaEventRecord(ev[2], st);
     dim3 gc((X + 31) / 32, (X + 7) / 8);
     k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);

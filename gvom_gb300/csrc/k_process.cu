@@ -360,8 +360,8 @@ __device__ __forceinline__ void block_scan2(int a, int b, int &ea, int &eb, int 
 }
 
 // ---------------------------------------------------------------------------
-// k_assign: one pass over the dense count words; a block covers
-// kAssignBlockCells consecutive extended cells, thread i the cells i, i + 256,
+// k_assign: one pass over the dense count words; a block covers 256 * PER
+// consecutive extended cells, thread i the cells i, i + 256,
 // ... (every load and store of a warp is contiguous), blockIdx.y = scan.
 // In-grid cells: hit > 0 -> compact index and the record's hit/total/voxel
 // id; else -(total)-1 (scripts/gvom.py:1233-1247).  Cells holding points
@@ -383,18 +383,18 @@ __device__ __forceinline__ bool cell_in_grid(unsigned e, const Geom &g, unsigned
     return (unsigned)gx < (unsigned)g.X && (unsigned)gy < (unsigned)g.X && (unsigned)gz < (unsigned)g.Z;
 }
 
-template <int NS>
+template <int NS, int PER>
 __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab) {
     const ScanDesc &sd = tab.s[blockIdx.y];
     const Geom g = pc.g;
     const int Vext = (int)g.Vext;
-    const int base = blockIdx.x * kAssignBlockCells + threadIdx.x;
-    unsigned long long v[kAssignPer];
+    const int base = blockIdx.x * (256 * PER) + threadIdx.x;
+    unsigned long long v[PER];
 #pragma unroll
-    for (int k = 0; k < kAssignPer; k++) v[k] = sd.cnt[base + k * 256];  // padded: always in bounds
+    for (int k = 0; k < PER; k++) v[k] = sd.cnt[base + k * 256];  // padded: always in bounds
     int n_occ = 0, n_pts = 0;
 #pragma unroll
-    for (int k = 0; k < kAssignPer; k++) {
+    for (int k = 0; k < PER; k++) {
         const int hit = (int)(v[k] >> 32);
         if (hit > 0) {
             int gid;
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __g
     __syncthreads();
     int c = bases[0] + eo, off = bases[1] + ep;
 #pragma unroll
-    for (int k = 0; k < kAssignPer; k++) {
+    for (int k = 0; k < PER; k++) {
         const int e = base + k * 256;
         if (e >= Vext) break;
         const int hit = (int)(v[k] >> 32);
@@ -601,7 +601,8 @@ __global__ void __launch_bounds__(256) k_cleanup(const ProcessConst pc, const __
 // ---------------------------------------------------------------------------
 template <int NS>
 static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int total_blocks, int max_n, int dtype,
-                             float4 *prec, int *prank, float4 *sorted, CellMom *mom, cudaStream_t st, cudaEvent_t *ev) {
+                             float4 *prec, int *prank, float4 *sorted, CellMom *mom, cudaStream_t st, cudaEvent_t *ev,
+                             int bs) {
     ScanTable<NS> tab;
     for (int i = 0; i < NS; i++) tab.s[i] = i < pc.nscans ? table[i] : table[0];
     if (total_blocks < 1) total_blocks = 1;
@@ -610,33 +611,40 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
     };
     mark(0);
     if (dtype == 1)
-        k_voxelize_trace<double, NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
+        k_voxelize_trace<double, NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
     else
-        k_voxelize_trace<float, NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
+        k_voxelize_trace<float, NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
     mark(1);
-    dim3 ga((unsigned)((pc.g.Vext + kAssignBlockCells - 1) / kAssignBlockCells), pc.nscans);
-    k_assign<NS><<<ga, 256, 0, st>>>(pc, tab);
+    {
+        const int per = pc.assign_per;
+        dim3 ga((unsigned)((pc.g.Vext + 256 * per - 1) / (256 * per)), pc.nscans);
+        if (per == 4) k_assign<NS, 4><<<ga, 256, 0, st>>>(pc, tab);
+        else if (per == 16) k_assign<NS, 16><<<ga, 256, 0, st>>>(pc, tab);
+        else k_assign<NS, 8><<<ga, 256, 0, st>>>(pc, tab);
+    }
     mark(2);
-    k_scatter<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank, sorted);
+    k_scatter<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank, sorted);
     mark(3);
-    k_cell_moments<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank, sorted, mom);
+    k_cell_moments<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank, sorted, mom);
     mark(4);
     const int want = (max_n + 255) / 256;
     dim3 gs((unsigned)std::max(1, std::min(want, 152 * 8)), pc.nscans);
     k_voxel_stats<NS><<<gs, 256, 0, st>>>(pc, tab, mom);
     mark(5);
-    k_cleanup<NS><<<total_blocks, 256, 0, st>>>(pc, tab, prec, prank);
+    k_cleanup<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
     mark(6);
     return cudaGetLastError();
 }
 
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev) {
+                           cudaEvent_t *ev, int pts_block) {
     CellMom *mom = static_cast<CellMom *>(moments);
-    if (nscans == 1) return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev);
-    if (nscans <= 4) return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev);
-    return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev);
+    if (nscans == 1)
+        return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block);
+    if (nscans <= 4)
+        return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block);
+    return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block);
 }
 
 }  // namespace gvom

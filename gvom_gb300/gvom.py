@@ -93,6 +93,9 @@ class Gvom:
                  positive_obstacle_threshold, negative_obstacle_threshold, slope_obsacle_threshold,
                  robot_height, robot_radius, ground_to_lidar_height, xy_eigen_dist, z_eigen_dist):
         self._l = _lib.load()
+        self.params = (xy_resolution, z_resolution, xy_size, z_size, buffer_size, min_distance,
+                       positive_obstacle_threshold, negative_obstacle_threshold, slope_obsacle_threshold,
+                       robot_height, robot_radius, ground_to_lidar_height, xy_eigen_dist, z_eigen_dist)
         self.xy_resolution = xy_resolution
         self.z_resolution = z_resolution
         self.xy_size = int(xy_size)
@@ -244,6 +247,18 @@ class Gvom:
 
     def set_stream(self, stream_ptr: int | None):
         check(self._l.gvom_set_stream(self._h, C.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def set_tuning(self, tuning: dict):
+        """Launch shapes (keys of GvomTuning); speed only, never results."""
+        cur = self.get_tuning()
+        cur.update(tuning)
+        t = _lib.GvomTuning(**{k: int(v) for k, v in cur.items()})
+        check(self._l.gvom_set_tuning(self._h, C.byref(t)))
+
+    def get_tuning(self) -> dict:
+        t = _lib.GvomTuning()
+        check(self._l.gvom_get_tuning(self._h, C.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
 
     def set_graphs(self, on: bool):
         """Capture each process / combine launch sequence into a CUDA graph and

@@ -172,6 +172,18 @@ int gvom_synchronize(GvomHandle *h);
  * kernel launch of process / combine; gvom_stage_times waits for the queued
  * work and returns, for stages 0..n-1, the summed milliseconds and launch
  * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
+/* Launch shapes chosen by the autotuner (gvom_gb300/autotune.py); no
+ * counterpart in the reference.  They change speed only, never results.
+ * Defaults: 256, 8, 8, 4. */
+typedef struct GvomTuning {
+    int32_t points_per_block;         /* point-parallel kernels: 128 or 256 */
+    int32_t assign_words_per_thread;  /* index assignment: 4, 8 or 16 */
+    int32_t merge_planes_per_thread;  /* index merge: 4, 8 or 16 z planes */
+    int32_t stats_blocks_per_sm;      /* statistics merge: 2, 4 or 8 */
+} GvomTuning;
+int gvom_set_tuning(GvomHandle *h, const GvomTuning *t);
+int gvom_get_tuning(GvomHandle *h, GvomTuning *t);
+
 /* CUDA-graph mode (off by default); no counterpart in the reference.  When on,
  * each process / combine call captures its launch sequence and replays it
  * through an executable graph that is updated in place while the sequence
