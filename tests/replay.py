@@ -196,3 +196,24 @@ def replay_and_compare(mapper, fx, stats=True, debug=True):
                 ri = ref["debug_inferred"]
                 assert_exact(di[:, :2], ri[:, :2], f"combine {ci} debug inferred xy")
                 assert np.all(np.abs(di[:, 2] - ri[:, 2]) <= HEIGHT_ATOL * 10)
+
+
+def float_errors(got_out, ref: dict, got_maps: dict) -> dict:
+    """Largest deviations of the float outputs from the float64 oracle:
+    absolute for heights, relative (where the oracle value is non-zero) for
+    roughness and slopes."""
+    def rel(a, b):
+        a = np.asarray(a, np.float64)
+        b = np.asarray(b, np.float64)
+        m = np.abs(b) > 0
+        return float(np.max(np.abs(a[m] - b[m]) / np.abs(b[m]))) if m.any() else 0.0
+
+    rough = got_out[3]
+    return {
+        "height_abs": float(np.max(np.abs(got_maps["height"] - ref["height"]))),
+        "inferred_abs": float(np.max(np.abs(got_maps["inferred"] - ref["inferred"]))),
+        "guess_abs": float(np.max(np.abs(got_maps["guess"] - ref["guess"]))),
+        "roughness_rel": rel(rough, ref["rough"]),
+        "slope_x_rel": rel(got_maps["slope_x"], ref["slope_x"]),
+        "slope_y_rel": rel(got_maps["slope_y"], ref["slope_y"]),
+    }

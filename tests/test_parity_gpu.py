@@ -226,3 +226,25 @@ def test_graph_mode_equals_direct_launches(Gvom):
             np.testing.assert_array_equal(x, y)
         assert a.ring_state() == b.ring_state()
         compare_slot(canonical_state(a.combined_state()), canonical_state(b.combined_state()), f"combined {k}")
+
+
+def test_precision_form_os1_128_far_vs_float64_oracle(Gvom):
+    """The precision form at full size: OS1-128x2048 scans (262,144 points),
+    512 x 512 x 96 at 0.1 m, buffer 8, world offset 1e4 m.  Integer outputs
+    bit-exact; the largest float deviations from the float64 oracle are
+    printed and held to the stated tolerances."""
+    import json
+    import torch
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    from replay import float_errors
+    w = WORKLOADS["os1_128_far"]
+    scans = make_workload_scans(w, 2, device="cuda" if torch.cuda.is_available() else "cpu")
+    g, o = _run_both(Gvom, w.gvom_args(), scans)
+    out = g.combine_maps()
+    ref = o.combine_maps()
+    refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
+    compare_combine(out, refd, g.maps_state(), w.gvom_args(), "final combine")
+    errs = float_errors(out, refd, g.maps_state())
+    print("PRECISION os1_128_far " + json.dumps(errs))
+    assert errs["height_abs"] <= 1e-4 and errs["inferred_abs"] <= 1e-4
+    assert errs["roughness_rel"] <= 1e-3 and errs["slope_x_rel"] <= 1e-3 and errs["slope_y_rel"] <= 1e-3
