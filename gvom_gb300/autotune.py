@@ -1,16 +1,19 @@
 """Autotuner for the launch shapes of the GB300 mapper (GvomTuning).
 
-Four choices, each affecting its own kernels only, so they are tuned one at
-a time (coordinate search) on sample steps of the caller's workload:
+Five choices, tuned one at a time (coordinate search) on sample steps of
+the caller's workload:
 
   points_per_block         128 / 256   k_voxelize_trace, k_scatter, k_cell_moments, k_cleanup
   assign_words_per_thread  4 / 8 / 16  k_assign
   merge_planes_per_thread  4 / 8 / 16  k_merge, k_columns
   stats_blocks_per_sm      2 / 4 / 8   k_merge_stats
+  step_overlap             0 / 1       gvom_step: the index merge beside the statistics kernels
 
-Each candidate is timed with the per-kernel CUDA events of the mapper's stage
-timer (direct launches) on a private mapper of the same parameters, so the
-caller's map state is untouched.  Results are cached in a JSON file keyed by
+The first four each affect their own kernels only and are timed with the
+per-kernel CUDA events of the mapper's stage timer (direct launches); the
+overlap changes how kernels share the GPU, so it is timed on whole steps.
+Candidates run on a private mapper of the same parameters, so the caller's
+map state is untouched.  Results are cached in a JSON file keyed by
 GPU name, grid and scans per step ($GVOM_TUNING_CACHE, default
 ~/.cache/gvom_gb300/tuning.json).  Tuning changes speed only: every choice
 gives bit-identical maps.
@@ -25,15 +28,17 @@ CHOICES = {
     "assign_words_per_thread": (4, 8, 16),
     "merge_planes_per_thread": (4, 8, 16),
     "stats_blocks_per_sm": (2, 4, 8),
+    "step_overlap": (0, 1),
 }
 AFFECTS = {
     "points_per_block": ("k_voxelize_trace", "k_scatter", "k_cell_moments", "k_cleanup"),
     "assign_words_per_thread": ("k_assign",),
     "merge_planes_per_thread": ("k_merge", "k_columns"),
     "stats_blocks_per_sm": ("k_merge_stats",),
+    "step_overlap": None,  # whole steps
 }
 DEFAULT = {"points_per_block": 256, "assign_words_per_thread": 8, "merge_planes_per_thread": 8,
-           "stats_blocks_per_sm": 4}
+           "stats_blocks_per_sm": 4, "step_overlap": 1}
 
 
 def cache_path() -> str:
@@ -89,6 +94,20 @@ def time_kernels(mapper, steps, reps: int, kernels, outs=None) -> float:
     return sum(st[k][0] for k in kernels if k in st) / max(1, reps)
 
 
+def time_steps(mapper, steps, reps: int) -> float:
+    """Mean wall time (ms) of gvom_step over `reps` steps, graphs on."""
+    import time
+    mapper.set_graphs(True)
+    for i in range(3):
+        mapper.step(steps[i % len(steps)])
+    mapper.synchronize()
+    t0 = time.perf_counter()
+    for i in range(reps):
+        mapper.step(steps[i % len(steps)])
+    mapper.synchronize()
+    return 1e3 * (time.perf_counter() - t0) / max(1, reps)
+
+
 def search(mapper, steps, reps: int = 10, outs=None, start: dict | None = None) -> tuple[dict, dict]:
     """Coordinate search over CHOICES; returns (best tuning, timings)."""
     best = dict(start or mapper.get_tuning())
@@ -97,7 +116,10 @@ def search(mapper, steps, reps: int = 10, outs=None, start: dict | None = None) 
         t = {}
         for v in values:
             mapper.set_tuning(dict(best, **{knob: v}))
-            t[v] = time_kernels(mapper, steps, reps, AFFECTS[knob], outs)
+            if AFFECTS[knob] is None:
+                t[v] = time_steps(mapper, steps, 3 * reps)
+            else:
+                t[v] = time_kernels(mapper, steps, reps, AFFECTS[knob], outs)
         best[knob] = min(t, key=t.get)
         timings[knob] = {str(k): v for k, v in t.items()}
     mapper.set_tuning(best)

@@ -158,7 +158,10 @@ struct GvomHandle {
     // CUDA graphs: each process / combine launch sequence is captured and
     // replayed through an executable graph updated in place
     bool graphs = false;
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // [0] process, [1] combine
+    cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};  // [0] process, [1] combine, [2] step
+    // a step forks the index merge onto `side` once the index maps are done
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_idx = nullptr, ev_join = nullptr;
 };
 
 namespace {
@@ -216,7 +219,7 @@ int run_graphed(GvomHandle *h, int which, F &&enqueue) {
         }
     }
     cudaError_t ei = cudaSuccess;
-    if (!x) ei = cudaGraphInstantiate(&x, g, 0);
+    if (!x) ei = cudaGraphInstantiate(&x, g, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(g);
     if (ei != cudaSuccess) {
         x = nullptr;
@@ -342,8 +345,19 @@ struct ScanIn {
 };
 
 // Enqueue the per-scan pipeline for `k` scans whose points are in device memory.
-int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
+// A process call in three parts: host preparation (allocation, scan table),
+// the stream-ordered launches, and the host ring bookkeeping.
+struct ProcPlan {
+    ProcessConst pc;
+    ScanDesc table[kMaxBatch];
+    int k = 0, block = 0, max_n = 0, dtype = GVOM_F32;
+    int slot_of[kMaxBatch];
+    double last_ego[3];
+};
+
+int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl) {
     const int k = (int)scans.size();
+    pl.k = k;
     if (k == 0) return GVOM_OK;
     int rc;
     if ((rc = ensure_cnt(h, k))) return rc;
@@ -353,7 +367,7 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
         max_n = std::max(max_n, s.n);
     }
     if ((rc = ensure_points(h, std::max<long long>(total_pts, 1)))) return rc;
-    ProcessConst pc;
+    ProcessConst &pc = pl.pc;
     pc.g = h->g;
     pc.xy_res = h->p.xy_resolution;
     pc.z_res = h->p.z_resolution;
@@ -372,11 +386,11 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
     pc.assign_per = h->tun.assign_per;
     pc.xe_magic = ~0ull / (unsigned long long)h->g.Xe + 1ull;
     pc.nscans = k;
-    ScanDesc table[kMaxBatch];
-    std::memset(table, 0, sizeof(table));
+    ScanDesc *table = pl.table;
+    std::memset(pl.table, 0, sizeof(pl.table));
     int block = 0;
     long long base = 0;
-    std::vector<int> slot_of(k);
+    int *slot_of = pl.slot_of;
     for (int i = 0; i < k; i++) {
         const ScanIn &s = scans[i];
         const int slot = (int)((h->buffer_index + i) % h->B);
@@ -432,27 +446,47 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
         d.rec_cap = h->slots[slot].cap;
         d.ctr = h->d_ctr + i;
     }
-    rc = run_graphed(h, 0, [&]() -> int {
-        CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * k, h->st));
-        CUDA_TRY(launch_process(pc, table, k, block, (int)std::min<long long>(max_n, h->g.V), scans[0].dtype,
-                                h->prec, h->prank, h->sorted, h->moments, h->st,
-                                h->graphs ? nullptr : h->timer.begin(0, kProcessKernels), h->tun.pts_block));
-        for (int i = 0; i < k; i++)
-            CUDA_TRY(cudaMemcpyAsync(h->d_slotC + slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
-                                     h->st));
-        return GVOM_OK;
-    });
-    if (rc) return rc;
-    for (int i = 0; i < k; i++) {
-        Slot &sl = h->slots[slot_of[i]];
-        for (int a = 0; a < 3; a++) sl.od[a] = table[i].od[a];
+    pl.block = block;
+    pl.max_n = (int)std::min<long long>(max_n, h->g.V);
+    pl.dtype = scans[0].dtype;
+    for (int a = 0; a < 3; a++) pl.last_ego[a] = scans[k - 1].ego[a];
+    return GVOM_OK;
+}
+
+// stream-ordered work of a prepared process call on h->st; `after_assign`
+// (nullable) is recorded once the ring slots' index maps are complete
+int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bool timing) {
+    CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * pl.k, h->st));
+    CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec, h->prank, h->sorted,
+                            h->moments, h->st, timing ? h->timer.begin(0, kProcessKernels) : nullptr,
+                            h->tun.pts_block, after_assign));
+    for (int i = 0; i < pl.k; i++)
+        CUDA_TRY(cudaMemcpyAsync(h->d_slotC + pl.slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
+                                 h->st));
+    return GVOM_OK;
+}
+
+// ring bookkeeping (scripts/gvom.py:198-216) and the latest ego (:110-112)
+void commit_scans(GvomHandle *h, const ProcPlan &pl) {
+    for (int i = 0; i < pl.k; i++) {
+        Slot &sl = h->slots[pl.slot_of[i]];
+        for (int a = 0; a < 3; a++) sl.od[a] = pl.table[i].od[a];
         sl.valid = true;
     }
-    // ring bookkeeping (scripts/gvom.py:198-216) and the latest ego (:110-112)
-    for (int a = 0; a < 3; a++) h->ego[a] = scans[k - 1].ego[a];
-    h->last_buffer_index = slot_of[k - 1];
-    h->buffer_index = (slot_of[k - 1] + 1) % h->B;
-    h->last_ctr = k - 1;
+    for (int a = 0; a < 3; a++) h->ego[a] = pl.last_ego[a];
+    h->last_buffer_index = pl.slot_of[pl.k - 1];
+    h->buffer_index = (pl.slot_of[pl.k - 1] + 1) % h->B;
+    h->last_ctr = pl.k - 1;
+}
+
+int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
+    if (scans.empty()) return GVOM_OK;
+    ProcPlan pl;
+    int rc = prepare_scans(h, scans, pl);
+    if (rc) return rc;
+    rc = run_graphed(h, 0, [&]() -> int { return launch_scans(h, pl, nullptr, !h->graphs); });
+    if (rc) return rc;
+    commit_scans(h, pl);
     return GVOM_OK;
 }
 
@@ -536,12 +570,23 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         return fail(GVOM_ERR_OOM, "admission refused: instance needs " + std::to_string(need) + " bytes, " +
                                       std::to_string((long long)fr) + " free");
     }
-    if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess) {
+    // the instance stream at the highest priority, the side stream (index merge
+    // of a step) at the lowest: the step's critical path keeps the SMs it needs
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (cudaStreamCreateWithPriority(&h->own, cudaStreamNonBlocking, prio_greatest) != cudaSuccess) {
         cudaGetLastError();
         delete h;
         return fail(GVOM_ERR_CUDA, "stream creation failed");
     }
     h->st = h->own;
+    if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_idx, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        gvom_destroy(h);
+        return fail(GVOM_ERR_CUDA, "stream / event creation failed");
+    }
     auto bail = [&](int code) {
         gvom_destroy(h);
         return code;
@@ -587,6 +632,12 @@ int gvom_destroy(GvomHandle *h) {
     if (h->own) cudaStreamSynchronize(h->own);
     for (auto &x : h->gexec)
         if (x) cudaGraphExecDestroy(x);
+    if (h->side) {
+        cudaStreamSynchronize(h->side);
+        cudaStreamDestroy(h->side);
+    }
+    if (h->ev_idx) cudaEventDestroy(h->ev_idx);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     for (auto &s : h->slots) {
         cudaFree(s.idx);
         cudaFree(s.rec);
@@ -657,16 +708,16 @@ int gvom_process_device(GvomHandle *h, const void *d_points, int32_t dtype, int6
     return enqueue_scans(h, v);
 }
 
-int gvom_process_batch(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device) {
-    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
-    if (n_scans < 0 || (n_scans > 0 && !scans)) return fail(GVOM_ERR_ARG, "bad scan list");
-    if (n_scans == 0) return GVOM_OK;
-    std::lock_guard<std::mutex> lk(h->mu);
-    // scans that a later scan of the same batch overwrites (ring wrap) only update the ego
+// Validates a scan list and stages host points into the device staging
+// buffer (stream-ordered on h->st).  Scans that a later scan of the same batch
+// overwrites (ring wrap) are dropped; `pinned` tells whether a host buffer
+// was page-locked (the copy must then finish before the call returns).
+static int stage_batch(GvomHandle *h, const GvomScan *scans, int n_scans, int points_on_device,
+                       std::vector<ScanIn> &v, bool &pinned) {
     const int first = std::max(0, n_scans - std::min(h->B, kMaxBatch));
     const int dt = scans[first].dtype;
-    std::vector<ScanIn> v;
     size_t total_bytes = 0;
+    pinned = false;
     for (int i = first; i < n_scans; i++) {
         ScanIn s;
         int rc = fill_scan(h, s, scans[i].dtype, scans[i].n, scans[i].row_stride, scans[i].ego, scans[i].transform,
@@ -678,39 +729,55 @@ int gvom_process_batch(GvomHandle *h, const GvomScan *scans, int32_t n_scans, in
         total_bytes = (total_bytes + 255) & ~(size_t)255;
         v.push_back(s);
     }
-    int rc;
-    if (!points_on_device) {
-        if ((rc = ensure_dpts(h, total_bytes))) return rc;
-        size_t off = 0;
-        bool pinned = false;
-        for (size_t j = 0; j < v.size(); j++) {
-            const GvomScan &sc = scans[first + (int)j];
-            const size_t b = (size_t)v[j].n * (size_t)v[j].stride * (size_t)bytes_of(v[j].dtype);
-            if (b) {
-                CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h->dpts) + off, sc.points, b, cudaMemcpyHostToDevice, h->st));
-                pinned = pinned || is_pinned_host(sc.points);
-            }
-            v[j].dev_pts = static_cast<char *>(h->dpts) + off;
-            off = (off + b + 255) & ~(size_t)255;
-        }
-        if ((rc = enqueue_scans(h, v))) return rc;
-        if (pinned) CUDA_TRY(cudaStreamSynchronize(h->st));
-    } else {
+    if (points_on_device) {
         for (size_t j = 0; j < v.size(); j++) v[j].dev_pts = scans[first + (int)j].points;
-        if ((rc = enqueue_scans(h, v))) return rc;
+        return GVOM_OK;
     }
+    int rc;
+    if ((rc = ensure_dpts(h, total_bytes))) return rc;
+    size_t off = 0;
+    for (size_t j = 0; j < v.size(); j++) {
+        const GvomScan &sc = scans[first + (int)j];
+        const size_t b = (size_t)v[j].n * (size_t)v[j].stride * (size_t)bytes_of(v[j].dtype);
+        if (b) {
+            CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h->dpts) + off, sc.points, b, cudaMemcpyHostToDevice, h->st));
+            pinned = pinned || is_pinned_host(sc.points);
+        }
+        v[j].dev_pts = static_cast<char *>(h->dpts) + off;
+        off = (off + b + 255) & ~(size_t)255;
+    }
+    return GVOM_OK;
+}
+
+int gvom_process_batch(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    if (n_scans < 0 || (n_scans > 0 && !scans)) return fail(GVOM_ERR_ARG, "bad scan list");
+    if (n_scans == 0) return GVOM_OK;
+    std::lock_guard<std::mutex> lk(h->mu);
+    std::vector<ScanIn> v;
+    bool pinned = false;
+    int rc;
+    if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned))) return rc;
+    if ((rc = enqueue_scans(h, v))) return rc;
+    if (pinned) CUDA_TRY(cudaStreamSynchronize(h->st));
     for (int a = 0; a < 3; a++) h->ego[a] = scans[n_scans - 1].ego[a];
     return GVOM_OK;
 }
 
-static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, double *rough, int32_t *vis,
-                        bool to_host) {
-    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
-    std::lock_guard<std::mutex> lk(h->mu);
+// A combine call in three parts, like a process call.
+struct CombPlan {
+    MergeParams mp;
+    ColumnParams cp;
+    Maps2DParams m2;
+    int nb = 0;
+};
+
+int prepare_combine(GvomHandle *h, CombPlan &pl) {
     const Slot &ls = h->slots[h->last_buffer_index];
     if (!ls.valid) return fail(GVOM_NO_DATA, "ERROR: No data in buffer");
     const int nb = h->have_comb ? 1 - h->cur : 0;  // buffer receiving the new combined map
-    MergeParams mp;
+    pl.nb = nb;
+    MergeParams &mp = pl.mp;
     std::memset(&mp, 0, sizeof(mp));
     mp.g = h->g;
     for (int a = 0; a < 3; a++) mp.co[a] = ls.od[a];
@@ -744,7 +811,7 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     mp.planes = h->tun.merge_planes;
     mp.stats_bpsm = h->tun.stats_bpsm;
     mp.colinfo = h->colinfo;
-    ColumnParams cp;
+    ColumnParams &cp = pl.cp;
     std::memset(&cp, 0, sizeof(cp));
     cp.X = h->g.X;
     cp.Z = h->g.Z;
@@ -773,7 +840,8 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     cp.pos_density = h->pos_density;
     cp.zlow = h->zlow;
     cp.mlow = h->mlow;
-    Maps2DParams m2;
+    Maps2DParams &m2 = pl.m2;
+    std::memset(&m2, 0, sizeof(m2));
     m2.X = h->g.X;
     m2.xy_res = h->p.xy_resolution;
     m2.z_res = h->p.z_resolution;
@@ -792,21 +860,44 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     m2.pos = h->pos;
     m2.neg = h->neg;
     m2.vis = h->vis;
-    const int rcg = run_graphed(h, 1, [&]() -> int {
-        CUDA_TRY(cudaMemsetAsync(mp.out_count, 0, sizeof(int), h->st));
-        CUDA_TRY(launch_combine(mp, cp, m2, h->st, h->graphs ? nullptr : h->timer.begin(kProcessKernels, kCombineKernels)));
+    return GVOM_OK;
+}
+
+// stream-ordered work of a prepared combine on h->st.  With `idx_ready`, the
+// index merge runs on the side stream as soon as that event (recorded when
+// the ring's index maps are complete) has fired, overlapping the rest of the
+// process kernels, and joins back before the statistics merge.
+int launch_comb(GvomHandle *h, const CombPlan &pl, cudaEvent_t idx_ready, bool timing) {
+    if (idx_ready) {
+        CUDA_TRY(cudaStreamWaitEvent(h->side, idx_ready, 0));
+        CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->side));
+        CUDA_TRY(launch_merge_index(pl.mp, h->side));
+        CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
+        CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_join, 0));
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr));
         return GVOM_OK;
-    });
-    if (rcg) return rcg;
+    }
+    CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->st));
+    CUDA_TRY(launch_combine(pl.mp, pl.cp, pl.m2, h->st, timing ? h->timer.begin(kProcessKernels, kCombineKernels) : nullptr));
+    return GVOM_OK;
+}
+
+void commit_combine(GvomHandle *h, const CombPlan &pl) {
+    const int nb = pl.nb;
+    const MergeParams &mp = pl.mp;
     for (int a = 0; a < 3; a++) h->cod[nb][a] = mp.co[a];
     h->cur = nb;
     h->have_comb = true;
     h->have_maps = true;
+}
+
+// origin (scripts/gvom.py:385-388) and the four maps to host or device buffers
+int copy_outputs(GvomHandle *h, const CombPlan &pl, double origin[3], int32_t *pos, int32_t *neg, double *rough,
+                 int32_t *vis, bool to_host) {
     if (origin) {
-        // scripts/gvom.py:385-388
-        origin[0] = mp.co[0] * h->p.xy_resolution;
-        origin[1] = mp.co[1] * h->p.xy_resolution;
-        origin[2] = mp.co[2] * h->p.z_resolution;
+        origin[0] = pl.mp.co[0] * h->p.xy_resolution;
+        origin[1] = pl.mp.co[1] * h->p.xy_resolution;
+        origin[2] = pl.mp.co[2] * h->p.z_resolution;
     }
     const size_t X2 = (size_t)h->g.X * h->g.X;
     const cudaMemcpyKind kind = to_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
@@ -818,6 +909,19 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     return GVOM_OK;
 }
 
+static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, double *rough, int32_t *vis,
+                        bool to_host) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    std::lock_guard<std::mutex> lk(h->mu);
+    CombPlan pl;
+    int rc = prepare_combine(h, pl);
+    if (rc) return rc;
+    rc = run_graphed(h, 1, [&]() -> int { return launch_comb(h, pl, nullptr, !h->graphs); });
+    if (rc) return rc;
+    commit_combine(h, pl);
+    return copy_outputs(h, pl, origin, pos, neg, rough, vis, to_host);
+}
+
 int gvom_combine(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, double *roughness, int32_t *visibility) {
     return combine_impl(h, origin, pos, neg, roughness, visibility, true);
 }
@@ -825,6 +929,35 @@ int gvom_combine(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, do
 int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t *d_neg, double *d_roughness,
                         int32_t *d_visibility) {
     return combine_impl(h, origin, d_pos, d_neg, d_roughness, d_visibility, false);
+}
+
+int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device, double origin[3],
+              int32_t *pos, int32_t *neg, double *roughness, int32_t *visibility, int32_t outputs_on_device) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    if (n_scans < 1 || !scans) return fail(GVOM_ERR_ARG, "a step needs at least one scan");
+    std::lock_guard<std::mutex> lk(h->mu);
+    std::vector<ScanIn> v;
+    bool pinned = false;
+    int rc;
+    if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned))) return rc;
+    ProcPlan pp;
+    if ((rc = prepare_scans(h, v, pp))) return rc;
+    commit_scans(h, pp);  // host ring bookkeeping; the combine plan reads the ring after this batch
+    for (int a = 0; a < 3; a++) h->ego[a] = scans[n_scans - 1].ego[a];
+    CombPlan cp;
+    if ((rc = prepare_combine(h, cp))) return rc;
+    const bool timing = !h->graphs && h->timer.on;
+    rc = run_graphed(h, 2, [&]() -> int {
+        // with stage timing the kernels run in sequence so that each interval is one kernel
+        cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
+        if ((rc = launch_scans(h, pp, idx, timing))) return rc;
+        return launch_comb(h, cp, idx, timing);
+    });
+    if (rc) return rc;
+    commit_combine(h, cp);
+    if ((rc = copy_outputs(h, cp, origin, pos, neg, roughness, visibility, !outputs_on_device))) return rc;
+    if (pinned) CUDA_TRY(cudaStreamSynchronize(h->st));
+    return GVOM_OK;
 }
 
 int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64_t *rows) {
@@ -1168,11 +1301,13 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
         return fail(GVOM_ERR_ARG, "merge_planes_per_thread must be 4, 8 or 16");
     if (!(t->stats_blocks_per_sm == 2 || t->stats_blocks_per_sm == 4 || t->stats_blocks_per_sm == 8))
         return fail(GVOM_ERR_ARG, "stats_blocks_per_sm must be 2, 4 or 8");
+    if (!(t->step_overlap == 0 || t->step_overlap == 1)) return fail(GVOM_ERR_ARG, "step_overlap must be 0 or 1");
     std::lock_guard<std::mutex> lk(h->mu);
     h->tun.pts_block = t->points_per_block;
     h->tun.assign_per = t->assign_words_per_thread;
     h->tun.merge_planes = t->merge_planes_per_thread;
     h->tun.stats_bpsm = t->stats_blocks_per_sm;
+    h->tun.step_overlap = t->step_overlap;
     return GVOM_OK;
 }
 
@@ -1183,6 +1318,7 @@ int gvom_get_tuning(GvomHandle *h, GvomTuning *t) {
     t->assign_words_per_thread = h->tun.assign_per;
     t->merge_planes_per_thread = h->tun.merge_planes;
     t->stats_blocks_per_sm = h->tun.stats_bpsm;
+    t->step_overlap = h->tun.step_overlap;
     return GVOM_OK;
 }
 

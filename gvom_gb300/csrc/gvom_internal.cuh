@@ -30,8 +30,9 @@ struct Tuning {
     int assign_per;     // count words per k_assign thread: 4, 8 or 16
     int merge_planes;   // z planes per k_merge thread: 4, 8 or 16
     int stats_bpsm;     // k_merge_stats blocks per multiprocessor: 2, 4 or 8
+    int step_overlap;   // gvom_step runs the index merge beside the statistics kernels: 0 or 1
 };
-constexpr Tuning kDefaultTuning = {256, 8, 8, 4};
+constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
 constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
@@ -192,8 +193,11 @@ constexpr int kCombineKernels = 4;  // merge, merge_stats, columns, maps2d
 constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev, int pts_block);
+                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign);
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
+cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st);
+cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
+                                cudaEvent_t *ev);
 cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
                            cudaEvent_t *ev = nullptr);
 cudaError_t launch_debug_count(const int *idx, long long V, int *counts, int nblocks, cudaStream_t st);

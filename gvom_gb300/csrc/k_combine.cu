@@ -813,25 +813,48 @@ __global__ void k_debug_maps(DebugMapParams p) {
 // launchers
 // ---------------------------------------------------------------------------
 template <int NSRC>
-static void launch_merge(const MergeParams &mp, cudaStream_t st, cudaEvent_t *ev) {
+static void launch_merge_idx(const MergeParams &mp, cudaStream_t st) {
     const int X = mp.g.X, Z = mp.g.Z, zc = mp.planes;
     dim3 gm((X + 31) / 32, (X + 7) / 8, (Z + zc - 1) / zc);
     if (zc == 4) k_merge<NSRC, 4><<<gm, dim3(32, 8), 0, st>>>(mp);
     else if (zc == 16) k_merge<NSRC, 16><<<gm, dim3(32, 8), 0, st>>>(mp);
     else k_merge<NSRC, 8><<<gm, dim3(32, 8), 0, st>>>(mp);
-    if (ev) cudaEventRecord(ev[1], st);
+}
+
+template <int NSRC>
+static void launch_merge_stats(const MergeParams &mp, cudaStream_t st) {
     k_merge_stats<NSRC><<<mp.num_sms * mp.stats_bpsm, 256, 0, st>>>(mp);
 }
 
-cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
-                           cudaEvent_t *ev) {
+// source-count class of a merge (2, 3, 5, 9 or 17 sources)
+template <template <int> class F>
+static void by_nsrc(const MergeParams &mp, cudaStream_t st) {
+    if (mp.nsrc <= 2) F<2>::run(mp, st);
+    else if (mp.nsrc <= 3) F<3>::run(mp, st);
+    else if (mp.nsrc <= 5) F<5>::run(mp, st);
+    else if (mp.nsrc <= 9) F<9>::run(mp, st);
+    else F<kMaxSources>::run(mp, st);
+}
+template <int N>
+struct MergeIdx {
+    static void run(const MergeParams &mp, cudaStream_t st) { launch_merge_idx<N>(mp, st); }
+};
+template <int N>
+struct MergeStats {
+    static void run(const MergeParams &mp, cudaStream_t st) { launch_merge_stats<N>(mp, st); }
+};
+
+cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st) {
+    by_nsrc<MergeIdx>(mp, st);
+    return cudaGetLastError();
+}
+
+// statistics merge, columns and 2-D maps (events ev[1..4] when timing)
+cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
+                                cudaEvent_t *ev) {
     const int X = mp.g.X;
-    if (ev) cudaEventRecord(ev[0], st);
-    if (mp.nsrc <= 2) launch_merge<2>(mp, st, ev);
-    else if (mp.nsrc <= 3) launch_merge<3>(mp, st, ev);
-    else if (mp.nsrc <= 5) launch_merge<5>(mp, st, ev);
-    else if (mp.nsrc <= 9) launch_merge<9>(mp, st, ev);
-    else launch_merge<kMaxSources>(mp, st, ev);
+    if (ev) cudaEventRecord(ev[1], st);
+    by_nsrc<MergeStats>(mp, st);
     if (ev) cudaEventRecord(ev[2], st);
     dim3 gc((X + 31) / 32, (X + 7) / 8);
     k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);
@@ -840,6 +863,13 @@ cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const 
     k_maps2d<<<g2, dim3(kTY, kTX), 0, st>>>(m2);
     if (ev) cudaEventRecord(ev[4], st);
     return cudaGetLastError();
+}
+
+cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
+                           cudaEvent_t *ev) {
+    if (ev) cudaEventRecord(ev[0], st);
+    by_nsrc<MergeIdx>(mp, st);
+    return launch_combine_rest(mp, cp, m2, st, ev);
 }
 
 cudaError_t launch_debug_count(const int *idx, long long V, int *counts, int nblocks, cudaStream_t st) {

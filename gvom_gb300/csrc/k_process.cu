@@ -602,7 +602,7 @@ __global__ void __launch_bounds__(256) k_cleanup(const ProcessConst pc, const __
 template <int NS>
 static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int total_blocks, int max_n, int dtype,
                              float4 *prec, int *prank, float4 *sorted, CellMom *mom, cudaStream_t st, cudaEvent_t *ev,
-                             int bs) {
+                             int bs, cudaEvent_t after_assign) {
     ScanTable<NS> tab;
     for (int i = 0; i < NS; i++) tab.s[i] = i < pc.nscans ? table[i] : table[0];
     if (total_blocks < 1) total_blocks = 1;
@@ -622,6 +622,7 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
         else if (per == 16) k_assign<NS, 16><<<ga, 256, 0, st>>>(pc, tab);
         else k_assign<NS, 8><<<ga, 256, 0, st>>>(pc, tab);
     }
+    if (after_assign) cudaEventRecord(after_assign, st);
     mark(2);
     k_scatter<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank, sorted);
     mark(3);
@@ -638,13 +639,16 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
 
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev, int pts_block) {
+                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign) {
     CellMom *mom = static_cast<CellMom *>(moments);
     if (nscans == 1)
-        return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block);
+        return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
+                            after_assign);
     if (nscans <= 4)
-        return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block);
-    return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block);
+        return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
+                            after_assign);
+    return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
+                                after_assign);
 }
 
 }  // namespace gvom

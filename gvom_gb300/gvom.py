@@ -203,9 +203,7 @@ class Gvom:
     # ------------------------------------------------------------------
     # extensions
     # ------------------------------------------------------------------
-    def process_batch(self, scans):
-        """Process several scans [(pointcloud, ego, transform), ...] in one set of launches;
-        equivalent to calling Process_pointcloud on each in order."""
+    def _scan_array(self, scans):
         arr = (GvomScan * len(scans))()
         keep = []
         on_dev = None
@@ -225,10 +223,39 @@ class Gvom:
             arr[i].row_stride = stride
             arr[i].ego[:] = list(e)
             arr[i].transform = tptr
+        return arr, keep, bool(on_dev)
+
+    def process_batch(self, scans):
+        """Process several scans [(pointcloud, ego, transform), ...] in one set of launches;
+        equivalent to calling Process_pointcloud on each in order."""
+        arr, keep, on_dev = self._scan_array(scans)
         check(self._l.gvom_process_batch(self._h, arr, len(scans), 1 if on_dev else 0))
         if on_dev:
             self.synchronize()
         del keep
+
+    def step(self, scans, device_outputs=None):
+        """process_batch(scans) then combine_maps() in one call (the index merge
+        overlaps the statistics kernels; one graph in graph mode).  Returns
+        combine_maps()'s tuple, or with `device_outputs` = (pos, neg, rough,
+        vis) CUDA tensors fills them stream-ordered and returns the origin."""
+        arr, keep, on_dev = self._scan_array(scans)
+        origin = np.zeros(3, np.float64)
+        P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        if device_outputs is not None:
+            ptrs = [C.c_void_p(t.data_ptr()) for t in device_outputs]
+            check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, P(origin), *ptrs, 1))
+            del keep
+            return origin
+        X = self.xy_size
+        pos = np.empty((X, X), np.int32)
+        neg = np.empty((X, X), np.int32)
+        rough = np.empty((X, X), np.float64)
+        vis = np.empty((X, X), np.int32)
+        check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, P(origin), P(pos), P(neg), P(rough),
+                                P(vis), 0))
+        del keep
+        return origin, pos, neg, rough, vis
 
     def combine_maps_device(self, pos, neg, rough, vis):
         """combine_maps into preallocated CUDA tensors (int32, int32, float64, int32; (X, X)),

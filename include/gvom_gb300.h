@@ -104,6 +104,15 @@ int gvom_combine(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, do
 int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t *d_neg,
                         double *d_roughness, int32_t *d_visibility);
 
+/* One scan-to-map step: gvom_process_batch followed by gvom_combine (host
+ * outputs) or gvom_combine_device (outputs_on_device != 0), with the same
+ * results; no counterpart in the reference.  Submitted together, the index
+ * merge of the combine runs beside the process call's statistics kernels
+ * (it needs only the ring's index maps), and in graph mode the whole step is
+ * one executable graph. */
+int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device, double origin[3],
+              int32_t *pos, int32_t *neg, double *roughness, int32_t *visibility, int32_t outputs_on_device);
+
 /* Replaces Gvom.make_debug_voxel_map (scripts/gvom.py:395-410, 481-503):
  * rows [x, y, z, hit/total, hit, l0-l1, l1-l2, l2] of every occupied voxel of
  * the combined map, in ascending voxel-id order.  *rows = number of rows; at
@@ -174,12 +183,13 @@ int gvom_synchronize(GvomHandle *h);
  * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
 /* Launch shapes chosen by the autotuner (gvom_gb300/autotune.py); no
  * counterpart in the reference.  They change speed only, never results.
- * Defaults: 256, 8, 8, 4. */
+ * Defaults: 256, 8, 8, 4, 1. */
 typedef struct GvomTuning {
     int32_t points_per_block;         /* point-parallel kernels: 128 or 256 */
     int32_t assign_words_per_thread;  /* index assignment: 4, 8 or 16 */
     int32_t merge_planes_per_thread;  /* index merge: 4, 8 or 16 z planes */
     int32_t stats_blocks_per_sm;      /* statistics merge: 2, 4 or 8 */
+    int32_t step_overlap;             /* gvom_step: index merge beside the statistics kernels, 0 or 1 */
 } GvomTuning;
 int gvom_set_tuning(GvomHandle *h, const GvomTuning *t);
 int gvom_get_tuning(GvomHandle *h, GvomTuning *t);

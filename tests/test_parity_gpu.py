@@ -248,3 +248,24 @@ def test_precision_form_os1_128_far_vs_float64_oracle(Gvom):
     print("PRECISION os1_128_far " + json.dumps(errs))
     assert errs["height_abs"] <= 1e-4 and errs["inferred_abs"] <= 1e-4
     assert errs["roughness_rel"] <= 1e-3 and errs["slope_x_rel"] <= 1e-3 and errs["slope_y_rel"] <= 1e-3
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_step_equals_process_then_combine(Gvom, graphs):
+    """gvom_step (process + combine, index merge forked beside the statistics
+    kernels) == process_batch followed by combine_maps."""
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["small_32x512"]
+    scans = make_workload_scans(w, 7)
+    params = w.gvom_args()[:4] + (4,) + w.gvom_args()[5:]
+    a, b = Gvom(*params), Gvom(*params)
+    b.set_graphs(graphs)
+    for k, idx in enumerate([[0], [1, 2], [3], [4, 5, 6], [0]]):
+        batch = [(scans[i].points, scans[i].ego, scans[i].transform) for i in idx]
+        a.process_batch(batch)
+        ra = a.combine_maps()
+        rb = b.step(batch)
+        for x, y in zip(ra, rb):
+            np.testing.assert_array_equal(x, y)
+        assert a.ring_state() == b.ring_state()
+        compare_slot(canonical_state(a.combined_state()), canonical_state(b.combined_state()), f"combined {k}")
