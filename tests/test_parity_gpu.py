@@ -269,3 +269,62 @@ def test_step_equals_process_then_combine(Gvom, graphs):
             np.testing.assert_array_equal(x, y)
         assert a.ring_state() == b.ring_state()
         compare_slot(canonical_state(a.combined_state()), canonical_state(b.combined_state()), f"combined {k}")
+
+
+def _compare_runs(Gvom, params, runs):
+    """runs: [(points, ego, T), ...] each followed by a combine."""
+    g, o = Gvom(*params), OracleGvom(*params)
+    for i, (pts, ego, T) in enumerate(runs):
+        g.Process_pointcloud(pts, ego, T)
+        o.Process_pointcloud(pts, ego, T)
+        assert g.last_process_stats() == o.last_process_stats(), (g.last_process_stats(), o.last_process_stats())
+        _, last = g.ring_state()
+        compare_slot(canonical_state(g.slot_state(last)), canonical_state(o.slot_state(last)), f"scan {i}")
+        out, ref = g.combine_maps(), o.combine_maps()
+        refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
+        compare_combine(out, refd, g.maps_state(), params, f"combine {i}")
+
+
+def test_rays_inside_the_sliver_below_zero(Gvom):
+    """Ray positions in (-2^-20, 0) voxels with a non-zero grid origin: the one
+    range where floor(p) - origin differs from the float64 formula."""
+    params = (0.2, 0.2, 64, 16, 2, 0.1, 0.5, 0.5, 0.3, 2.0, 1.0, 1.0, 1, 1)
+    rng = np.random.default_rng(11)
+    # ego x = -1e-21 m: every position of a ray in the plane x = ego x is
+    # -5e-21 voxels, where float64 rounds p - origin back up to -origin while
+    # floor(p) - origin is one less
+    ex = np.float32(-1.0e-21)
+    ego = (float(ex), 0.05, 1.0)
+    n = 3000
+    pts = np.empty((n, 3), np.float32)
+    pts[:, 0] = ex  # rays in the plane x = ego x: x stays inside the sliver for every step
+    pts[:, 1] = rng.uniform(-6, 6, n)
+    pts[:, 2] = rng.uniform(-1.5, 2.5, n)
+    pts[: n // 3, 0] = np.float32(-1e-9) * rng.uniform(0, 1, n // 3).astype(np.float32)  # small negative x ends
+    pts2 = pts.copy()
+    pts2[:, 0] = np.float32(-4.0e-7)
+    _compare_runs(Gvom, params, [(pts, ego, None), (pts2, (-2.0e-7, -0.03, 0.8), None)])
+
+
+def test_origin_beyond_float32_floor_range(Gvom):
+    """A world origin past 2^22 voxels: ray indices take the float64 path."""
+    from gvom_gb300.synthetic import Lidar, Terrain, make_scan, make_trajectory
+    t = Terrain.make(0, extent=12.8, path_len=2.0, offset=(5.0e5, -2.0e5, 0.0))
+    lid = Lidar(beams=16, columns=256)
+    params = (0.1, 0.1, 128, 32, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)  # 5e5 m / 0.1 m = 5e6 voxels
+    runs = []
+    for i, p in enumerate(make_trajectory(2)):
+        s = make_scan(t, lid, p, i, transform_dtype=np.float64)
+        runs.append((s.points, s.ego, s.transform))
+    _compare_runs(Gvom, params, runs)
+
+
+def test_odd_grid_and_row_length(Gvom):
+    """xy_size 63 (extended rows of 65 cells) and eigen distances (1, 2)."""
+    from gvom_gb300.synthetic import Lidar, Terrain, make_scan, make_trajectory
+    t = Terrain.make(0, extent=12.6, path_len=2.0)
+    lid = Lidar(beams=16, columns=512)
+    params = (0.2, 0.2, 63, 21, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 2)
+    runs = [(s.points, s.ego, s.transform) for s in
+            (make_scan(t, lid, p, i) for i, p in enumerate(make_trajectory(2)))]
+    _compare_runs(Gvom, params, runs)
