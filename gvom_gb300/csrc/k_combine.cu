@@ -468,14 +468,18 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
     float (*sml)[kSY] = reinterpret_cast<float (*)[kSY]>(fit_buf + kSX * kSY * 4);
     double (*qres)[3] = reinterpret_cast<double (*)[3]>(fit_buf);
     __shared__ int qcell[kTX * kTY];
-    __shared__ int qn;
+    __shared__ int qn, qtake;
     __shared__ unsigned char kn[kSX][kSY];
     __shared__ unsigned char nky[kSX][kSY + 2];  // next known y index (in tile coords) at or after sy, kSY if none
     __shared__ unsigned char nkx[kSY][kSX + 2];  // next known x index at or after sx
     const int X = mp.X;
     const int x0t = blockIdx.y * kTX, y0t = blockIdx.x * kTY;
     const int tid = threadIdx.y * kTY + threadIdx.x;
-    if (tid == 0) qn = 0;
+    if (tid == 0) {
+        qn = 0;
+        qtake = 0;
+    }
+#pragma unroll
     for (int k = tid; k < kSX * kSY; k += kTX * kTY) {
         const int sx = k / kSY, sy = k % kSY;
         const int gx = x0t + sx - kHalo, gy = y0t + sy - kHalo;
@@ -488,19 +492,34 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
         sml[sx][sy] = in ? mp.mlow[c] : 0.f;
     }
     __syncthreads();
-    for (int k = tid; k < kSX + kSY; k += kTX * kTY) {
-        if (k < kSX) {
-            unsigned char nxt = kSY;
-            for (int sy = kSY - 1; sy >= 0; sy--) {
-                if (kn[k][sy]) nxt = (unsigned char)sy;
-                nky[k][sy] = nxt;
+    // next-known tables, one warp per row or column: the known flags of up to
+    // 64 entries as two ballots, and for each entry the lowest set bit at or
+    // after it
+    {
+        const int lane = tid & 31, warp = tid >> 5;
+        for (int r = warp; r < kSX + kSY; r += (kTX * kTY) / 32) {
+            const bool is_row = r < kSX;  // row sx: along y (kSY entries); else column sy: along x (kSX entries)
+            const int len = is_row ? kSY : kSX;
+            const int fixed = is_row ? r : r - kSX;
+            unsigned m[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int j = h * 32 + lane;
+                const bool k = j < len && (is_row ? kn[fixed][j] : kn[j][fixed]);
+                m[h] = __ballot_sync(0xffffffffu, k);
             }
-        } else {
-            const int sy = k - kSX;
-            unsigned char nxt = kSX;
-            for (int sx = kSX - 1; sx >= 0; sx--) {
-                if (kn[sx][sy]) nxt = (unsigned char)sx;
-                nkx[sy][sx] = nxt;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int j = h * 32 + lane;
+                if (j >= len) continue;
+                const unsigned below = (1u << lane) - 1u;
+                int nxt;
+                const unsigned a = m[h] & ~below;
+                if (a) nxt = h * 32 + __ffs(a) - 1;
+                else if (h == 0 && m[1]) nxt = 32 + __ffs(m[1]) - 1;
+                else nxt = len;
+                if (is_row) nky[fixed][j] = (unsigned char)nxt;
+                else nkx[fixed][j] = (unsigned char)nxt;
             }
         }
     }
@@ -611,30 +630,12 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
     // cells that need the float64 sequence are compacted into a queue so that
     // whole warps run it, instead of one lane in every warp that has one
     __syncthreads();  // queue complete; szl / sml no longer read
-    {
-        const int nq = qn;
-        for (int q = tid; q < nq; q += kTX * kTY) {
-            const int t = qcell[q];
-            double r = -1.0, a = 0.0, b = 0.0;
-            slope_f64(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, X, mp.xy_res, r, a, b);
-            qres[t][0] = r;
-            qres[t][1] = a;
-            qres[t][2] = b;
-        }
-    }
-    __syncthreads();
-    if (!valid) return;
-    if (need_exact) {
-        rough = qres[tid][0];
-        slx = qres[tid][1];
-        sly = qres[tid][2];
-    }
 
     // __guess_height (scripts/gvom.py:592-714), loop-condition and y_nh quirks
     // included; each ring segment is scanned in increasing order, so its first
     // known cell is one lookup in the next-known tables
     double guess = 0.0;
-    if (!known && !(mp.inferred[cell] == -1000.0)) {
+    if (valid && !known && !(mp.inferred[cell] == -1000.0)) {
         bool xpd = false, xnd = false, ypd = false, ynd = false;
         int xp = x0, xn = x0, yp = y0, yn = y0;
         double xph = -1000.0, xnh = -1000.0, yph = -1000.0, ynh = -1000.0;
@@ -691,6 +692,29 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
         const double dh = __dsub_rn(mx, mn);
         if (dh > 0.0) guess = dh;
     }
+    // the float64 queue, taken item by item by the threads as they finish
+    // their guess search (the queue is the block's longest chain)
+    {
+        const int nq = qn;
+        while (true) {
+            const int q = atomicAdd(&qtake, 1);
+            if (q >= nq) break;
+            const int t = qcell[q];
+            double r = -1.0, a = 0.0, b = 0.0;
+            slope_f64(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, X, mp.xy_res, r, a, b);
+            qres[t][0] = r;
+            qres[t][1] = a;
+            qres[t][2] = b;
+        }
+    }
+    __syncthreads();
+    if (!valid) return;
+    if (need_exact) {
+        rough = qres[tid][0];
+        slx = qres[tid][1];
+        sly = qres[tid][2];
+    }
+
     // __make_positive_obstacle_map slope gate (scripts/gvom.py:524-526): in
     // float32 unless |slope| is near the threshold
     bool steep;
