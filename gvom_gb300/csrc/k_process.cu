@@ -467,10 +467,11 @@ __global__ void __launch_bounds__(256) k_scatter(const ProcessConst pc, const __
 // Neighbourhood statistics (scripts/gvom.py:1249-1421) in two steps.
 //
 // k_cell_moments: one thread per cell that holds points (the thread of the
-// cell's rank-0 point).  Over the cell's points, in ascending point order:
-// count, mean of the in-cell fraction and the second moments about that mean
-// (float32, Kahan-compensated, coordinates centred on the cell centre), and
-// the minimum height fraction (exact).  Stored at the cell's group offset.
+// cell's rank-0 point); cells of more than kSmallCell points are handed to a
+// whole warp.  Over the cell's points: count, mean of the in-cell fraction
+// and the second moments about that mean (float32, Kahan-compensated,
+// coordinates centred on the cell centre), and the minimum height fraction
+// (exact).  Stored at the cell's group offset.
 //
 // k_voxel_stats: one thread per occupied voxel.  Combines the moments of
 // the (2exy+1)^2 (2ez+1) neighbour cells, each shifted by its offset from the
@@ -486,53 +487,162 @@ struct __align__(16) CellMom {
     float pad;
 };
 
+constexpr int kSmallCell = 16;  // cells with more points are summed by a whole warp
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
 template <int NS>
 __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
                                                      const float4 *__restrict__ prec, const int *__restrict__ prank,
                                                      const float4 *__restrict__ sorted, CellMom *__restrict__ mom) {
+    __shared__ int hq_off[256], hq_n[256];
+    __shared__ int hq_count;
     const int s = find_scan(tab, pc.nscans, blockIdx.x);
     const ScanDesc &sd = tab.s[s];
+    if (threadIdx.x == 0) hq_count = 0;
+    __syncthreads();
     const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
-    if (i >= sd.n) return;
-    const long long gi = sd.pt_base + i;
-    const int cell = __float_as_int(prec[gi].w);
-    if (cell < 0 || prank[gi] != 0) return;
-    const unsigned long long v = sd.cnt[cell];
-    const int off = (int)(v >> 32), n = (int)(v & 0xffffffffull);
-    const float4 *__restrict__ P = sorted + sd.pt_base + off;
-    KSum sx, sy, sz;
-    sx.init(); sy.init(); sz.init();
-    float mh = 1.0f;
-    for (int j = 0; j < n; j++) {
-        const float4 p = P[j];
-        sx.add(__fsub_rn(p.x, 0.5f));
-        sy.add(__fsub_rn(p.y, 0.5f));
-        sz.add(__fsub_rn(p.z, 0.5f));
-        mh = fminf(mh, p.z);
+    bool mine = false;
+    int off = 0, n = 0;
+    if (i < sd.n) {
+        const long long gi = sd.pt_base + i;
+        const int cell = __float_as_int(prec[gi].w);
+        if (cell >= 0 && prank[gi] == 0) {
+            const unsigned long long v = sd.cnt[cell];
+            off = (int)(v >> 32);
+            n = (int)(v & 0xffffffffull);
+            if (n > kSmallCell) {
+                const int q = atomicAdd(&hq_count, 1);
+                hq_off[q] = off;
+                hq_n[q] = n;
+            } else {
+                mine = true;
+            }
+        }
     }
-    const float nf = (float)n;
-    const float mx = __fdiv_rn(__fsub_rn(sx.s, sx.c), nf), my = __fdiv_rn(__fsub_rn(sy.s, sy.c), nf);
-    const float mz = __fdiv_rn(__fsub_rn(sz.s, sz.c), nf);
-    KSum cxx, cxy, cxz, cyy, cyz, czz;
-    cxx.init(); cxy.init(); cxz.init(); cyy.init(); cyz.init(); czz.init();
-    for (int j = 0; j < n; j++) {
-        const float4 p = P[j];
-        const float ux = __fsub_rn(__fsub_rn(p.x, 0.5f), mx), uy = __fsub_rn(__fsub_rn(p.y, 0.5f), my);
-        const float uz = __fsub_rn(__fsub_rn(p.z, 0.5f), mz);
-        cxx.add(__fmul_rn(ux, ux));
-        cxy.add(__fmul_rn(ux, uy));
-        cxz.add(__fmul_rn(ux, uz));
-        cyy.add(__fmul_rn(uy, uy));
-        cyz.add(__fmul_rn(uy, uz));
-        czz.add(__fmul_rn(uz, uz));
+    if (mine) {
+        // the cell's points in ascending order, Kahan-compensated
+        const float4 *__restrict__ P = sorted + sd.pt_base + off;
+        KSum sx, sy, sz;
+        sx.init(); sy.init(); sz.init();
+        float mh = 1.0f;
+        for (int j = 0; j < n; j++) {
+            const float4 p = P[j];
+            sx.add(__fsub_rn(p.x, 0.5f));
+            sy.add(__fsub_rn(p.y, 0.5f));
+            sz.add(__fsub_rn(p.z, 0.5f));
+            mh = fminf(mh, p.z);
+        }
+        const float nf = (float)n;
+        const float mx = __fdiv_rn(__fsub_rn(sx.s, sx.c), nf), my = __fdiv_rn(__fsub_rn(sy.s, sy.c), nf);
+        const float mz = __fdiv_rn(__fsub_rn(sz.s, sz.c), nf);
+        KSum cxx, cxy, cxz, cyy, cyz, czz;
+        cxx.init(); cxy.init(); cxz.init(); cyy.init(); cyz.init(); czz.init();
+        for (int j = 0; j < n; j++) {
+            const float4 p = P[j];
+            const float ux = __fsub_rn(__fsub_rn(p.x, 0.5f), mx), uy = __fsub_rn(__fsub_rn(p.y, 0.5f), my);
+            const float uz = __fsub_rn(__fsub_rn(p.z, 0.5f), mz);
+            cxx.add(__fmul_rn(ux, ux));
+            cxy.add(__fmul_rn(ux, uy));
+            cxz.add(__fmul_rn(ux, uz));
+            cyy.add(__fmul_rn(uy, uy));
+            cyz.add(__fmul_rn(uy, uz));
+            czz.add(__fmul_rn(uz, uz));
+        }
+        float4 *o = reinterpret_cast<float4 *>(&mom[sd.pt_base + off]);
+        o[0] = make_float4(mx, my, mz, nf);
+        o[1] = make_float4(__fsub_rn(cxx.s, cxx.c), __fsub_rn(cxy.s, cxy.c), __fsub_rn(cxz.s, cxz.c),
+                           __fsub_rn(cyy.s, cyy.c));
+        o[2] = make_float4(__fsub_rn(cyz.s, cyz.c), __fsub_rn(czz.s, czz.c), mh, 0.f);
     }
-    float4 *o = reinterpret_cast<float4 *>(&mom[sd.pt_base + off]);
-    o[0] = make_float4(mx, my, mz, nf);
-    o[1] = make_float4(__fsub_rn(cxx.s, cxx.c), __fsub_rn(cxy.s, cxy.c), __fsub_rn(cxz.s, cxz.c), __fsub_rn(cyy.s, cyy.c));
-    o[2] = make_float4(__fsub_rn(cyz.s, cyz.c), __fsub_rn(czz.s, czz.c), mh, 0.f);
+    __syncthreads();
+    // cells with many points: one warp each, lanes striding over the points with
+    // compensated partial sums, combined across the warp
+    const int nh = hq_count, lane = threadIdx.x & 31;
+    for (int q = threadIdx.x >> 5; q < nh; q += blockDim.x >> 5) {
+        const int qo = hq_off[q], qn = hq_n[q];
+        const float4 *__restrict__ P = sorted + sd.pt_base + qo;
+        KSum sx, sy, sz;
+        sx.init(); sy.init(); sz.init();
+        float mh = 1.0f;
+        for (int j = lane; j < qn; j += 32) {
+            const float4 p = P[j];
+            sx.add(__fsub_rn(p.x, 0.5f));
+            sy.add(__fsub_rn(p.y, 0.5f));
+            sz.add(__fsub_rn(p.z, 0.5f));
+            mh = fminf(mh, p.z);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mh = fminf(mh, __shfl_xor_sync(0xffffffffu, mh, o));
+        const float nf = (float)qn;
+        const float mx = __fdiv_rn(warp_sum(__fsub_rn(sx.s, sx.c)), nf);
+        const float my = __fdiv_rn(warp_sum(__fsub_rn(sy.s, sy.c)), nf);
+        const float mz = __fdiv_rn(warp_sum(__fsub_rn(sz.s, sz.c)), nf);
+        KSum cxx, cxy, cxz, cyy, cyz, czz;
+        cxx.init(); cxy.init(); cxz.init(); cyy.init(); cyz.init(); czz.init();
+        for (int j = lane; j < qn; j += 32) {
+            const float4 p = P[j];
+            const float ux = __fsub_rn(__fsub_rn(p.x, 0.5f), mx), uy = __fsub_rn(__fsub_rn(p.y, 0.5f), my);
+            const float uz = __fsub_rn(__fsub_rn(p.z, 0.5f), mz);
+            cxx.add(__fmul_rn(ux, ux));
+            cxy.add(__fmul_rn(ux, uy));
+            cxz.add(__fmul_rn(ux, uz));
+            cyy.add(__fmul_rn(uy, uy));
+            cyz.add(__fmul_rn(uy, uz));
+            czz.add(__fmul_rn(uz, uz));
+        }
+        const float c0 = warp_sum(__fsub_rn(cxx.s, cxx.c)), c1 = warp_sum(__fsub_rn(cxy.s, cxy.c));
+        const float c2 = warp_sum(__fsub_rn(cxz.s, cxz.c)), c3 = warp_sum(__fsub_rn(cyy.s, cyy.c));
+        const float c4 = warp_sum(__fsub_rn(cyz.s, cyz.c)), c5 = warp_sum(__fsub_rn(czz.s, czz.c));
+        if (lane == 0) {
+            float4 *o = reinterpret_cast<float4 *>(&mom[sd.pt_base + qo]);
+            o[0] = make_float4(mx, my, mz, nf);
+            o[1] = make_float4(c0, c1, c2, c3);
+            o[2] = make_float4(c4, c5, mh, 0.f);
+        }
+    }
 }
 
-template <int NS>
+// Chan update of the running neighbourhood statistics with one cell's moments,
+// the cell mean shifted into this voxel's frame (centred on the voxel centre)
+struct NbAcc {
+    float n, m0, m1, m2, C0, C1, C2, C3, C4, C5;
+    __device__ __forceinline__ void init() { n = m0 = m1 = m2 = C0 = C1 = C2 = C3 = C4 = C5 = 0.f; }
+    __device__ __forceinline__ void add(const CellMom &cm, int dx, int dy, int dz) {
+        const float b0 = __fadd_rn(cm.m[0], (float)dx), b1 = __fadd_rn(cm.m[1], (float)dy);
+        const float b2 = __fadd_rn(cm.m[2], (float)dz);
+        const float nb = cm.n, nn = __fadd_rn(n, nb);
+        const float d0 = __fsub_rn(b0, m0), d1 = __fsub_rn(b1, m1), d2 = __fsub_rn(b2, m2);
+        const float wb = __fdiv_rn(nb, nn);
+        const float f = __fmul_rn(n, wb);  // n * nb / (n + nb)
+        m0 = __fadd_rn(m0, __fmul_rn(d0, wb));
+        m1 = __fadd_rn(m1, __fmul_rn(d1, wb));
+        m2 = __fadd_rn(m2, __fmul_rn(d2, wb));
+        C0 = __fadd_rn(__fadd_rn(C0, cm.c[0]), __fmul_rn(__fmul_rn(d0, d0), f));
+        C1 = __fadd_rn(__fadd_rn(C1, cm.c[1]), __fmul_rn(__fmul_rn(d0, d1), f));
+        C2 = __fadd_rn(__fadd_rn(C2, cm.c[2]), __fmul_rn(__fmul_rn(d0, d2), f));
+        C3 = __fadd_rn(__fadd_rn(C3, cm.c[3]), __fmul_rn(__fmul_rn(d1, d1), f));
+        C4 = __fadd_rn(__fadd_rn(C4, cm.c[4]), __fmul_rn(__fmul_rn(d1, d2), f));
+        C5 = __fadd_rn(__fadd_rn(C5, cm.c[5]), __fmul_rn(__fmul_rn(d2, d2), f));
+        n = nn;
+    }
+    __device__ __forceinline__ void store(VoxelRec *r, float mh) const {
+        float4 *o = reinterpret_cast<float4 *>(r);
+        o[0] = make_float4(__fadd_rn(m0, 0.5f), __fadd_rn(m1, 0.5f), __fadd_rn(m2, 0.5f), __fdiv_rn(C0, n));
+        o[1] = make_float4(__fdiv_rn(C1, n), __fdiv_rn(C2, n), __fdiv_rn(C3, n), __fdiv_rn(C4, n));
+        reinterpret_cast<float2 *>(r)[4] = make_float2(__fdiv_rn(C5, n), n);
+        r->min_h = mh;
+    }
+};
+
+// E3 = 1: the 3 x 3 x 3 neighbourhood of eigen distances (1, 1) with every
+// load unrolled (27 count words, then the moments of the cells that hold
+// points); E3 = 0: any distances, cell by cell.  Same cells, same order.
+template <int NS, int E3>
 __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
                                                     const CellMom *__restrict__ mom) {
     const ScanDesc &sd = tab.s[blockIdx.y];
@@ -544,39 +654,35 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
         const int gid = __float_as_int(r->aux[0]);
         const int x = gid % g.X, y = (gid / g.X) % g.X, z = gid / (g.X * g.X);
         const int e0 = (x + g.exy) + (y + g.exy) * g.Xe + (z + g.ez) * g.Xe * g.Xe;
-        float n = 0.f, m0 = 0.f, m1 = 0.f, m2 = 0.f;
-        float C0 = 0.f, C1 = 0.f, C2 = 0.f, C3 = 0.f, C4 = 0.f, C5 = 0.f;
+        NbAcc a;
+        a.init();
         float mh = 1.0f;
-        for (int dz = -g.ez; dz <= g.ez; dz++)
-            for (int dy = -g.exy; dy <= g.exy; dy++)
-                for (int dx = -g.exy; dx <= g.exy; dx++) {
-                    const unsigned long long v = sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe];
-                    if (!(v & 0xffffffffull)) continue;
-                    const CellMom cm = M[(int)(v >> 32)];
-                    if (dx == 0 && dy == 0 && dz == 0) mh = cm.min_h;
-                    // cell mean in this voxel's frame, centred on the voxel centre
-                    const float b0 = __fadd_rn(cm.m[0], (float)dx), b1 = __fadd_rn(cm.m[1], (float)dy);
-                    const float b2 = __fadd_rn(cm.m[2], (float)dz);
-                    const float nb = cm.n, nn = __fadd_rn(n, nb);
-                    const float d0 = __fsub_rn(b0, m0), d1 = __fsub_rn(b1, m1), d2 = __fsub_rn(b2, m2);
-                    const float wb = __fdiv_rn(nb, nn);
-                    const float f = __fmul_rn(n, wb);  // n * nb / (n + nb)
-                    m0 = __fadd_rn(m0, __fmul_rn(d0, wb));
-                    m1 = __fadd_rn(m1, __fmul_rn(d1, wb));
-                    m2 = __fadd_rn(m2, __fmul_rn(d2, wb));
-                    C0 = __fadd_rn(__fadd_rn(C0, cm.c[0]), __fmul_rn(__fmul_rn(d0, d0), f));
-                    C1 = __fadd_rn(__fadd_rn(C1, cm.c[1]), __fmul_rn(__fmul_rn(d0, d1), f));
-                    C2 = __fadd_rn(__fadd_rn(C2, cm.c[2]), __fmul_rn(__fmul_rn(d0, d2), f));
-                    C3 = __fadd_rn(__fadd_rn(C3, cm.c[3]), __fmul_rn(__fmul_rn(d1, d1), f));
-                    C4 = __fadd_rn(__fadd_rn(C4, cm.c[4]), __fmul_rn(__fmul_rn(d1, d2), f));
-                    C5 = __fadd_rn(__fadd_rn(C5, cm.c[5]), __fmul_rn(__fmul_rn(d2, d2), f));
-                    n = nn;
-                }
-        float4 *o = reinterpret_cast<float4 *>(r);
-        o[0] = make_float4(__fadd_rn(m0, 0.5f), __fadd_rn(m1, 0.5f), __fadd_rn(m2, 0.5f), __fdiv_rn(C0, n));
-        o[1] = make_float4(__fdiv_rn(C1, n), __fdiv_rn(C2, n), __fdiv_rn(C3, n), __fdiv_rn(C4, n));
-        reinterpret_cast<float2 *>(r)[4] = make_float2(__fdiv_rn(C5, n), n);
-        r->min_h = mh;
+        if (E3) {
+            unsigned long long v[27];
+#pragma unroll
+            for (int k = 0; k < 27; k++) {
+                const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+                v[k] = __ldg(&sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe]);
+            }
+#pragma unroll
+            for (int k = 0; k < 27; k++) {
+                if (!(v[k] & 0xffffffffull)) continue;
+                const CellMom cm = M[(int)(v[k] >> 32)];
+                if (k == 13) mh = cm.min_h;
+                a.add(cm, k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1);
+            }
+        } else {
+            for (int dz = -g.ez; dz <= g.ez; dz++)
+                for (int dy = -g.exy; dy <= g.exy; dy++)
+                    for (int dx = -g.exy; dx <= g.exy; dx++) {
+                        const unsigned long long v = sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe];
+                        if (!(v & 0xffffffffull)) continue;
+                        const CellMom cm = M[(int)(v >> 32)];
+                        if (dx == 0 && dy == 0 && dz == 0) mh = cm.min_h;
+                        a.add(cm, dx, dy, dz);
+                    }
+        }
+        a.store(r, mh);
     }
 }
 
@@ -630,7 +736,8 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
     mark(4);
     const int want = (max_n + 255) / 256;
     dim3 gs((unsigned)std::max(1, std::min(want, 152 * 8)), pc.nscans);
-    k_voxel_stats<NS><<<gs, 256, 0, st>>>(pc, tab, mom);
+    if (pc.g.exy == 1 && pc.g.ez == 1) k_voxel_stats<NS, 1><<<gs, 256, 0, st>>>(pc, tab, mom);
+    else k_voxel_stats<NS, 0><<<gs, 256, 0, st>>>(pc, tab, mom);
     mark(5);
     k_cleanup<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
     mark(6);
