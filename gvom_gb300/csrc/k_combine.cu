@@ -150,9 +150,12 @@ __device__ __forceinline__ void merge_voxel(const MergeParams &mp, int vid) {
             const float o_m[3] = {a.x, a.y, a.z};
             const float o_c[6] = {a.w, bq.x, bq.y, bq.z, bq.w, cc.x};
             const float den = __fadd_rn(n, n2);
-            const float nm0 = __fdiv_rn(__fadd_rn(__fmul_rn(m0, n), __fmul_rn(o_m[0], n2)), den);
-            const float nm1 = __fdiv_rn(__fadd_rn(__fmul_rn(m1, n), __fmul_rn(o_m[1], n2)), den);
-            const float nm2 = __fdiv_rn(__fadd_rn(__fmul_rn(m2, n), __fmul_rn(o_m[2], n2)), den);
+            // one rounded reciprocal per source instead of nine divisions (the
+            // merged statistics are compared at a tolerance, not bit for bit)
+            const float inv = __frcp_rn(den);
+            const float nm0 = __fmul_rn(__fadd_rn(__fmul_rn(m0, n), __fmul_rn(o_m[0], n2)), inv);
+            const float nm1 = __fmul_rn(__fadd_rn(__fmul_rn(m1, n), __fmul_rn(o_m[1], n2)), inv);
+            const float nm2 = __fmul_rn(__fadd_rn(__fmul_rn(m2, n), __fmul_rn(o_m[2], n2)), inv);
             const float cm[3] = {m0, m1, m2};
             const float mn[3] = {nm0, nm1, nm2};
             const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
@@ -164,7 +167,7 @@ __device__ __forceinline__ void merge_voxel(const MergeParams &mp, int vid) {
                     __fmul_rn(__fmul_rn(n, __fsub_rn(cm[pa[t]], mn[pa[t]])), __fsub_rn(cm[pb[t]], mn[pb[t]]));
                 const float t4 =
                     __fmul_rn(__fmul_rn(n2, __fsub_rn(o_m[pa[t]], mn[pa[t]])), __fsub_rn(o_m[pb[t]], mn[pb[t]]));
-                C[t] = __fdiv_rn(__fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), t4), den);
+                C[t] = __fmul_rn(__fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), t4), inv);
             }
             m0 = nm0;
             m1 = nm1;
