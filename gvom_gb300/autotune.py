@@ -1,6 +1,6 @@
 """Autotuner for the launch shapes of the GB300 mapper (GvomTuning).
 
-Five choices, tuned one at a time (coordinate search) on sample steps of
+Six choices, tuned one at a time (coordinate search) on sample steps of
 the caller's workload:
 
   points_per_block         128 / 256   k_voxelize_trace, k_scatter, k_cell_moments, k_cleanup
@@ -8,8 +8,9 @@ the caller's workload:
   merge_planes_per_thread  4 / 8 / 16  k_merge, k_columns
   stats_blocks_per_sm      2 / 4 / 8   k_merge_stats
   step_overlap             0 / 1       gvom_step: the index merge beside the statistics kernels
+  maps_tile_cells          64/128/256  k_maps2d (smaller tiles spread the float64 plane fits)
 
-The first four each affect their own kernels only and are timed with the
+The others each affect their own kernels only and are timed with the
 per-kernel CUDA events of the mapper's stage timer (direct launches); the
 overlap changes how kernels share the GPU, so it is timed on whole steps.
 Candidates run on a private mapper of the same parameters, so the caller's
@@ -29,6 +30,7 @@ CHOICES = {
     "merge_planes_per_thread": (4, 8, 16),
     "stats_blocks_per_sm": (2, 4, 8),
     "step_overlap": (0, 1),
+    "maps_tile_cells": (64, 128, 256),
 }
 AFFECTS = {
     "points_per_block": ("k_voxelize_trace", "k_scatter", "k_cell_moments", "k_cleanup"),
@@ -36,9 +38,10 @@ AFFECTS = {
     "merge_planes_per_thread": ("k_merge", "k_columns"),
     "stats_blocks_per_sm": ("k_merge_stats",),
     "step_overlap": None,  # whole steps
+    "maps_tile_cells": ("k_maps2d",),
 }
 DEFAULT = {"points_per_block": 256, "assign_words_per_thread": 8, "merge_planes_per_thread": 8,
-           "stats_blocks_per_sm": 4, "step_overlap": 1}
+           "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 256}
 
 
 def cache_path() -> str:

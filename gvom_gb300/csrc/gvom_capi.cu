@@ -860,6 +860,7 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
     m2.pos = h->pos;
     m2.neg = h->neg;
     m2.vis = h->vis;
+    m2.tile_cells = h->tun.maps_tile;
     return GVOM_OK;
 }
 
@@ -1302,12 +1303,15 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     if (!(t->stats_blocks_per_sm == 2 || t->stats_blocks_per_sm == 4 || t->stats_blocks_per_sm == 8))
         return fail(GVOM_ERR_ARG, "stats_blocks_per_sm must be 2, 4 or 8");
     if (!(t->step_overlap == 0 || t->step_overlap == 1)) return fail(GVOM_ERR_ARG, "step_overlap must be 0 or 1");
+    if (!(t->maps_tile_cells == 64 || t->maps_tile_cells == 128 || t->maps_tile_cells == 256))
+        return fail(GVOM_ERR_ARG, "maps_tile_cells must be 64, 128 or 256");
     std::lock_guard<std::mutex> lk(h->mu);
     h->tun.pts_block = t->points_per_block;
     h->tun.assign_per = t->assign_words_per_thread;
     h->tun.merge_planes = t->merge_planes_per_thread;
     h->tun.stats_bpsm = t->stats_blocks_per_sm;
     h->tun.step_overlap = t->step_overlap;
+    h->tun.maps_tile = t->maps_tile_cells;
     return GVOM_OK;
 }
 
@@ -1319,6 +1323,7 @@ int gvom_get_tuning(GvomHandle *h, GvomTuning *t) {
     t->merge_planes_per_thread = h->tun.merge_planes;
     t->stats_blocks_per_sm = h->tun.stats_bpsm;
     t->step_overlap = h->tun.step_overlap;
+    t->maps_tile_cells = h->tun.maps_tile;
     return GVOM_OK;
 }
 

@@ -31,8 +31,9 @@ struct Tuning {
     int merge_planes;   // z planes per k_merge thread: 4, 8 or 16
     int stats_bpsm;     // k_merge_stats blocks per multiprocessor: 2, 4 or 8
     int step_overlap;   // gvom_step runs the index merge beside the statistics kernels: 0 or 1
+    int maps_tile;      // k_maps2d tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) cells
 };
-constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1};
+constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1, 256};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
 constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
@@ -162,6 +163,7 @@ struct Maps2DParams {
     const float *mlow;
     double *slope_x, *slope_y, *rough, *guess;
     int *pos, *neg, *vis;
+    int tile_cells;        // Tuning::maps_tile_cells: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16)
 };
 
 struct DebugVoxParams {

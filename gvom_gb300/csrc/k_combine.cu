@@ -298,6 +298,7 @@ __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnP
     if (x >= X || y >= X) return;
     const int plane = X * X;
     int occ_z = Z, free_z = Z;
+#pragma unroll 8
     for (int ch = 0; ch * cp.planes < Z; ch++) {
         const int2 ci = cp.colinfo[ch * plane + y * X + x];
         if (occ_z == Z) occ_z = ci.x;
@@ -330,6 +331,7 @@ __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnP
         }
         if (zmin >= 0 && zmin < Z && zmax >= 0 && zmax < Z) {
             long long nn = 0, dens = 0;
+#pragma unroll 4
             for (int z = zmin; z <= zmax; z++) {
                 const int idx = cp.idx[x + y * X + z * plane];
                 if (idx >= 0) {
@@ -380,8 +382,7 @@ __global__ void k_gather_records(const VoxelRec *__restrict__ rec, const int *__
 // known-height flags and, per column / row, the next known cell (so each
 // ring segment of the guess search is one lookup).
 // ---------------------------------------------------------------------------
-constexpr int kTX = 8, kTY = 32, kHalo = 15;
-constexpr int kSX = kTX + 2 * kHalo, kSY = kTY + 2 * kHalo;
+constexpr int kHalo = 15;
 
 // h > -1000.0 on the bit pattern (no float64 compare)
 __device__ __forceinline__ bool height_known(double h) {
@@ -399,6 +400,7 @@ __device__ __forceinline__ double slope_angle(double a, double m, double im) {
 
 // __calculate_slope (scripts/gvom.py:717-805) in the reference's float64
 // operation order up to the final log / atan2.
+template <int kSY>
 __device__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY], int x0t, int y0t, int x0, int y0,
                           int X, double res, double &rough, double &slx, double &sly) {
 #define H(gx, gy) sh[(gx) - x0t + kHalo][(gy) - y0t + kHalo]
@@ -462,7 +464,10 @@ __device__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY
     sly = slope_angle(a1, m, im);
 }
 
-__global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DParams mp) {
+template <int kTX, int kTY>
+__global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Maps2DParams mp) {
+    constexpr int kSX = kTX + 2 * kHalo, kSY = kTY + 2 * kHalo;
+    static_assert(kSX <= 64 && kSY <= 64 && (kTX * kTY) % 32 == 0, "tile shape");
     __shared__ double sh[kSX][kSY];
     // lowest occupied z and in-voxel height per column for the float32 plane
     // fit; afterwards reused for the results of the float64 queue
@@ -704,7 +709,7 @@ __global__ void __launch_bounds__(256) k_maps2d(const __grid_constant__ Maps2DPa
             if (q >= nq) break;
             const int t = qcell[q];
             double r = -1.0, a = 0.0, b = 0.0;
-            slope_f64(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, X, mp.xy_res, r, a, b);
+            slope_f64<kSY>(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, X, mp.xy_res, r, a, b);
             qres[t][0] = r;
             qres[t][1] = a;
             qres[t][2] = b;
@@ -839,6 +844,12 @@ __global__ void k_debug_maps(DebugMapParams p) {
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+template <int TX, int TY>
+static void launch_maps2d(const Maps2DParams &m2, cudaStream_t st) {
+    const int X = m2.X;
+    dim3 g2((X + TY - 1) / TY, (X + TX - 1) / TX);
+    k_maps2d<TX, TY><<<g2, dim3(TY, TX), 0, st>>>(m2);
+}
 template <int NSRC>
 static void launch_merge_idx(const MergeParams &mp, cudaStream_t st) {
     const int X = mp.g.X, Z = mp.g.Z, zc = mp.planes;
@@ -886,8 +897,9 @@ cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, c
     dim3 gc((X + 31) / 32, (X + 7) / 8);
     k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);
     if (ev) cudaEventRecord(ev[3], st);
-    dim3 g2((X + kTY - 1) / kTY, (X + kTX - 1) / kTX);
-    k_maps2d<<<g2, dim3(kTY, kTX), 0, st>>>(m2);
+    if (m2.tile_cells == 64) launch_maps2d<4, 16>(m2, st);
+    else if (m2.tile_cells == 128) launch_maps2d<8, 16>(m2, st);
+    else launch_maps2d<8, 32>(m2, st);
     if (ev) cudaEventRecord(ev[4], st);
     return cudaGetLastError();
 }

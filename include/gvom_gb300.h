@@ -183,13 +183,14 @@ int gvom_synchronize(GvomHandle *h);
  * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
 /* Launch shapes chosen by the autotuner (gvom_gb300/autotune.py); no
  * counterpart in the reference.  They change speed only, never results.
- * Defaults: 256, 8, 8, 4, 1. */
+ * Defaults: 256, 8, 8, 4, 1, 256. */
 typedef struct GvomTuning {
     int32_t points_per_block;         /* point-parallel kernels: 128 or 256 */
     int32_t assign_words_per_thread;  /* index assignment: 4, 8 or 16 */
     int32_t merge_planes_per_thread;  /* index merge: 4, 8 or 16 z planes */
     int32_t stats_blocks_per_sm;      /* statistics merge: 2, 4 or 8 */
     int32_t step_overlap;             /* gvom_step: index merge beside the statistics kernels, 0 or 1 */
+    int32_t maps_tile_cells;          /* 2-D maps tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) */
 } GvomTuning;
 int gvom_set_tuning(GvomHandle *h, const GvomTuning *t);
 int gvom_get_tuning(GvomHandle *h, GvomTuning *t);

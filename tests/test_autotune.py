@@ -13,7 +13,7 @@ class FakeMapper:
     """Stage times depend on the tuning: each knob has one best value."""
 
     BEST = {"points_per_block": 128, "assign_words_per_thread": 16, "merge_planes_per_thread": 4,
-            "stats_blocks_per_sm": 8, "step_overlap": 0}
+            "stats_blocks_per_sm": 8, "step_overlap": 0, "maps_tile_cells": 64}
 
     def __init__(self, params=(0.15, 0.15, 256, 64, 4, 1, .5, .5, .3, 2, 4, 1, 1, 1)):
         self.params = params
@@ -99,9 +99,9 @@ def test_every_launch_shape_gives_identical_maps(gpu_lib):
     params = w.gvom_args()[:4] + (3,) + w.gvom_args()[5:]
     shapes = [dict(AT.DEFAULT),
               {"points_per_block": 128, "assign_words_per_thread": 4, "merge_planes_per_thread": 16,
-               "stats_blocks_per_sm": 2, "step_overlap": 0},
+               "stats_blocks_per_sm": 2, "step_overlap": 0, "maps_tile_cells": 64},
               {"points_per_block": 256, "assign_words_per_thread": 16, "merge_planes_per_thread": 4,
-               "stats_blocks_per_sm": 8, "step_overlap": 1}]
+               "stats_blocks_per_sm": 8, "step_overlap": 1, "maps_tile_cells": 128}]
     results = []
     for t in shapes:
         g = Gvom(*params)

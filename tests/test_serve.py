@@ -47,8 +47,9 @@ def test_served_mix_equals_alone(gpu_lib):
             reqs.append(srv.submit(inst, s.points, s.ego, s.transform))
             time.sleep(gap)
 
-    ta = threading.Thread(target=feed, args=(0, list(range(12)), 0.0005))
-    tb = threading.Thread(target=feed, args=(1, list(range(11, -1, -1)), 0.0007))
+    # bursts: while an instance's first batch runs, the rest of its requests queue
+    ta = threading.Thread(target=feed, args=(0, list(range(12)), 0.0))
+    tb = threading.Thread(target=feed, args=(1, list(range(11, -1, -1)), 0.0))
     ta.start(); tb.start(); ta.join(); tb.join()
     for r in reqs:
         assert r.done.wait(60)
