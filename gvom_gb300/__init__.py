@@ -9,7 +9,7 @@
 The work runs in libgvom_gb300.so (hand-written sm_103a CUDA behind the C ABI
 of include/gvom_gb300.h).  Build it with `python gvom_gb300/build.py`.
 """
-from .gvom import Gvom  # noqa: F401
+from .gvom import Gvom, pose_to_transform  # noqa: F401
 
-__all__ = ["Gvom"]
+__all__ = ["Gvom", "pose_to_transform"]
 __version__ = "0.1.0"

@@ -31,6 +31,7 @@ EXPORTS = (
     "gvom_synchronize", "gvom_last_process_stats", "gvom_device_bytes", "gvom_last_error",
     "gvom_version", "gvom_set_stage_timing", "gvom_stage_times", "gvom_stage_name",
     "gvom_debug_voxel_map_noalloc", "gvom_set_graphs", "gvom_set_tuning", "gvom_get_tuning", "gvom_step",
+    "gvom_ros_grids", "gvom_process_pointcloud2", "gvom_pose_to_transform",
 )
 GVOM_STAGES = 10
 
@@ -59,6 +60,10 @@ class GvomTuning(C.Structure):
     _fields_ = [("points_per_block", C.c_int32), ("assign_words_per_thread", C.c_int32),
                 ("merge_planes_per_thread", C.c_int32), ("stats_blocks_per_sm", C.c_int32),
                 ("step_overlap", C.c_int32), ("maps_tile_cells", C.c_int32)]
+
+
+class GvomRosParams(C.Structure):
+    _fields_ = [("density_threshold", C.c_double), ("min_roughness", C.c_double), ("max_roughness", C.c_double)]
 
 
 class GvomError(RuntimeError):
@@ -94,6 +99,9 @@ def load(path: str | None = None):
         "gvom_debug_voxel_map_noalloc": ([P, P, i64, C.POINTER(i64)], C.c_int),
         "gvom_set_graphs": ([P, i32], C.c_int),
         "gvom_step": ([P, C.POINTER(GvomScan), i32, i32, P, P, P, P, P, i32], C.c_int),
+        "gvom_ros_grids": ([P, C.POINTER(GvomRosParams), P, P, P, P, P, i32], C.c_int),
+        "gvom_process_pointcloud2": ([P, P, i64, i32, P, i32, i32, P, P, P], C.c_int),
+        "gvom_pose_to_transform": ([P, P, P], C.c_int),
         "gvom_set_tuning": ([P, C.POINTER(GvomTuning)], C.c_int),
         "gvom_get_tuning": ([P, C.POINTER(GvomTuning)], C.c_int),
         "gvom_debug_height_map": ([P, P], C.c_int),

@@ -1,7 +1,8 @@
 """Build the CUDA library libgvom_gb300.so in-tree (gvom_gb300/_build/).
 
-nvcc, sm_103a only, -fmad=false (no contraction of multiply-adds anywhere in
-the library: integer outputs depend on exact float rounding), static CUDA
+nvcc, sm_103a only, -fmad=false and the host compiler's -ffp-contract=off (no
+contraction of multiply-adds anywhere in the library, device or host code:
+integer outputs depend on exact float rounding), static CUDA
 runtime, translation units compiled in parallel.
 """
 from __future__ import annotations
@@ -19,7 +20,8 @@ LIB = os.path.join(OUT_DIR, "libgvom_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+NVFLAGS = ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
+           "--expt-relaxed-constexpr",
            "-Xcudafe", "--diag_suppress=177"]
 
 

@@ -150,6 +150,7 @@ struct GvomHandle {
     bool have_maps = false;
     // debug
     int *d_dbg = nullptr;
+    int8_t *d_ros = nullptr;  // staging of the five OccupancyGrid payloads
     long long bytes = 0;
     int pageable_access = 0;
     int num_sms = 1;
@@ -342,6 +343,8 @@ struct ScanIn {
     long long n, stride;
     double ego[3];
     double T[16];
+    int pc2 = 0;           // PointCloud2 bytes: stride = point step in bytes, float32 fields at off[]
+    int off[3] = {0, 0, 0};
 };
 
 // Enqueue the per-scan pipeline for `k` scans whose points are in device memory.
@@ -400,6 +403,8 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
         d.pts = s.dev_pts;
         d.n = s.n;
         d.stride = s.stride;
+        d.pc2 = s.pc2;
+        for (int a = 0; a < 3; a++) d.off[a] = s.off[a];
         d.tmode = s.tdtype == GVOM_NONE ? 0 : (s.tdtype == GVOM_F32 ? 1 : 2);
         for (int r = 0; r < 12; r++) {
             d.T[r] = s.T[r];
@@ -670,6 +675,7 @@ int gvom_destroy(GvomHandle *h) {
     cudaFree(h->colinfo);
     cudaFree(h->occ_list);
     cudaFree(h->d_dbg);
+    cudaFree(h->d_ros);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
     return GVOM_OK;
@@ -693,6 +699,40 @@ int gvom_process(GvomHandle *h, const void *points, int32_t dtype, int64_t n, in
     if ((rc = enqueue_scans(h, v))) return rc;
     if (bytes && is_pinned_host(points)) CUDA_TRY(cudaStreamSynchronize(h->st));  // caller may reuse its buffer
     return GVOM_OK;
+}
+
+// tf's fromTranslationRotation (ROS tf 1.13, tf/listener.py: the product of
+// transformations.translation_matrix and transformations.quaternion_matrix):
+// the quaternion q = (x, y, z, w) scaled by sqrt(2 / q.q), its outer product
+// Q, R = [[1-Q11-Q22, Q01-Q23, Q02+Q13], [Q01+Q23, 1-Q00-Q22, Q12-Q03],
+// [Q02-Q13, Q12+Q03, 1-Q00-Q11]] evaluated left to right, translation in the
+// last column; identity rotation when q.q is below 4 machine epsilons.  q.q
+// accumulates with fused multiply-adds in index order, as numpy's dot of two
+// float64 4-vectors does (OpenBLAS ddot).
+static void pose_matrix(const double t[3], const double qin[4], double T[16]) {
+    double q[4] = {qin[0], qin[1], qin[2], qin[3]};
+    double nq = 0.0;
+    for (int k = 0; k < 4; k++) nq = std::fma(q[k], q[k], nq);
+    for (int r = 0; r < 16; r++) T[r] = (r % 5 == 0) ? 1.0 : 0.0;
+    if (!(nq < 4.0 * 2.220446049250313e-16)) {
+        const double sc = std::sqrt(2.0 / nq);
+        for (int k = 0; k < 4; k++) q[k] *= sc;
+        double Q[4][4];
+        for (int a = 0; a < 4; a++)
+            for (int b = 0; b < 4; b++) Q[a][b] = q[a] * q[b];
+        T[0] = (1.0 - Q[1][1]) - Q[2][2];
+        T[1] = Q[0][1] - Q[2][3];
+        T[2] = Q[0][2] + Q[1][3];
+        T[4] = Q[0][1] + Q[2][3];
+        T[5] = (1.0 - Q[0][0]) - Q[2][2];
+        T[6] = Q[1][2] - Q[0][3];
+        T[8] = Q[0][2] - Q[1][3];
+        T[9] = Q[1][2] + Q[0][3];
+        T[10] = (1.0 - Q[0][0]) - Q[1][1];
+    }
+    T[3] = t[0];
+    T[7] = t[1];
+    T[11] = t[2];
 }
 
 int gvom_process_device(GvomHandle *h, const void *d_points, int32_t dtype, int64_t n, int64_t row_stride,
@@ -746,6 +786,51 @@ static int stage_batch(GvomHandle *h, const GvomScan *scans, int n_scans, int po
         v[j].dev_pts = static_cast<char *>(h->dpts) + off;
         off = (off + b + 255) & ~(size_t)255;
     }
+    return GVOM_OK;
+}
+
+int gvom_pose_to_transform(const double translation[3], const double rotation_xyzw[4], double out[16]) {
+    if (!translation || !rotation_xyzw || !out) return fail(GVOM_ERR_ARG, "NULL argument");
+    pose_matrix(translation, rotation_xyzw, out);
+    return GVOM_OK;
+}
+
+int gvom_process_pointcloud2(GvomHandle *h, const void *data, int64_t n_points, int32_t point_step,
+                             const int32_t xyz_offsets[3], int32_t field_dtype, int32_t data_on_device,
+                             const double ego[3], const double translation[3], const double rotation_xyzw[4]) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    if (!xyz_offsets || !ego || !translation || !rotation_xyzw) return fail(GVOM_ERR_ARG, "NULL argument");
+    if (field_dtype != GVOM_F32 && field_dtype != GVOM_F64)
+        return fail(GVOM_ERR_ARG, "x / y / z fields must be float32 or float64");
+    const int fb = bytes_of(field_dtype);
+    if (n_points < 0) return fail(GVOM_ERR_ARG, "negative point count");
+    if (n_points > 0 && !data) return fail(GVOM_ERR_ARG, "data is NULL");
+    if (point_step <= 0 || point_step % fb) return fail(GVOM_ERR_ARG, "point_step must be a positive multiple of the field size");
+    for (int a = 0; a < 3; a++)
+        if (xyz_offsets[a] < 0 || xyz_offsets[a] % fb || xyz_offsets[a] + fb > point_step)
+            return fail(GVOM_ERR_ARG, "x / y / z offsets must be aligned to the field size and inside the point");
+    if (data_on_device && n_points > 0 && ((uintptr_t)data % (uintptr_t)fb))
+        return fail(GVOM_ERR_ARG, "device data must be aligned to the field size");
+    std::lock_guard<std::mutex> lk(h->mu);
+    ScanIn s;
+    double T[16];
+    pose_matrix(translation, rotation_xyzw, T);
+    int rc = fill_scan(h, s, GVOM_F64, n_points, 3, ego, T, GVOM_F64);
+    if (rc) return rc;
+    s.pc2 = field_dtype == GVOM_F32 ? 1 : 2;
+    s.stride = point_step;
+    for (int a = 0; a < 3; a++) s.off[a] = xyz_offsets[a];
+    const size_t bytes = (size_t)n_points * (size_t)point_step;
+    if (data_on_device) {
+        s.dev_pts = data;
+    } else {
+        if ((rc = ensure_dpts(h, bytes))) return rc;
+        if (bytes) CUDA_TRY(cudaMemcpyAsync(h->dpts, data, bytes, cudaMemcpyHostToDevice, h->st));
+        s.dev_pts = h->dpts;
+    }
+    std::vector<ScanIn> v{s};
+    if ((rc = enqueue_scans(h, v))) return rc;
+    if (!data_on_device && bytes && is_pinned_host(data)) CUDA_TRY(cudaStreamSynchronize(h->st));
     return GVOM_OK;
 }
 
@@ -1097,6 +1182,47 @@ int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_r
     CUDA_TRY(cudaMemcpyAsync(&total, scratch + nblocks, sizeof(int), cudaMemcpyDeviceToHost, h->st));
     CUDA_TRY(cudaStreamSynchronize(h->st));
     if (rows) *rows = total;
+    return GVOM_OK;
+}
+
+int gvom_ros_grids(GvomHandle *h, const GvomRosParams *rp, int8_t *hard, int8_t *soft, int8_t *certainty,
+                   int8_t *negative, int8_t *roughness, int32_t outputs_on_device) {
+    if (!h || !rp) return fail(GVOM_ERR_ARG, "handle or params is NULL");
+    if (!(rp->max_roughness != rp->min_roughness)) return fail(GVOM_ERR_ARG, "max_roughness must differ from min_roughness");
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->have_maps) return fail(GVOM_NO_DATA, "No data");
+    const size_t X2 = (size_t)h->g.X * h->g.X;
+    int8_t *outs[5] = {hard, soft, certainty, negative, roughness};
+    RosGridParams p;
+    p.X = h->g.X;
+    p.pos = h->pos;
+    p.neg = h->neg;
+    p.vis = h->vis;
+    p.rough = h->rough;
+    p.density_thr = rp->density_threshold;
+    p.min_r = rp->min_roughness;
+    p.max_r = rp->max_roughness;
+    signed char *dst[5];
+    if (outputs_on_device) {
+        for (int k = 0; k < 5; k++) dst[k] = reinterpret_cast<signed char *>(outs[k]);
+    } else {
+        if (!h->d_ros) {
+            int rc = dalloc(h, reinterpret_cast<void **>(&h->d_ros), X2 * 5);
+            if (rc) return rc;
+        }
+        for (int k = 0; k < 5; k++) dst[k] = outs[k] ? reinterpret_cast<signed char *>(h->d_ros) + k * X2 : nullptr;
+    }
+    p.hard = dst[0];
+    p.soft = dst[1];
+    p.certainty = dst[2];
+    p.negative = dst[3];
+    p.roughness = dst[4];
+    CUDA_TRY(launch_ros_grids(p, h->st));
+    if (!outputs_on_device) {
+        for (int k = 0; k < 5; k++)
+            if (outs[k]) CUDA_TRY(cudaMemcpyAsync(outs[k], dst[k], X2, cudaMemcpyDeviceToHost, h->st));
+        CUDA_TRY(cudaStreamSynchronize(h->st));
+    }
     return GVOM_OK;
 }
 

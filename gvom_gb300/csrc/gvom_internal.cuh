@@ -70,7 +70,9 @@ struct ScanCounters {
 
 struct ScanDesc {
     const void *pts;       // device points
-    long long n, stride;   // rows, elements per row
+    long long n, stride;   // rows, elements per row (bytes per point for PointCloud2 data)
+    int pc2;               // PointCloud2 data: x, y, z at byte offsets off[] of each point, 1 float32, 2 float64
+    int off[3];
     int tmode;             // 0 none, 1 float32 transform, 2 float64 transform
     int fast_floor;        // |origin| + grid < 2^22: float32 ray voxel indices (see ray_index)
     int exact_ok;          // |origin| < 2^31: integer hit-voxel arithmetic (gx_coord)
@@ -166,6 +168,14 @@ struct Maps2DParams {
     int tile_cells;        // Tuning::maps_tile_cells: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16)
 };
 
+struct RosGridParams {
+    int X;
+    const int *pos, *neg, *vis;
+    const double *rough;
+    double density_thr, min_r, max_r;
+    signed char *hard, *soft, *certainty, *negative, *roughness;  // X * X each, x fastest; nullable
+};
+
 struct DebugVoxParams {
     const int *idx;
     const VoxelRec *rec;
@@ -206,6 +216,7 @@ cudaError_t launch_debug_count(const int *idx, long long V, int *counts, int nbl
 cudaError_t launch_debug_voxels(const DebugVoxParams &p, int nblocks, cudaStream_t st);
 cudaError_t launch_debug_maps(const DebugMapParams &p, cudaStream_t st);
 int debug_chunk();
+cudaError_t launch_ros_grids(const RosGridParams &p, cudaStream_t st);
 
 // allocation-free debug voxel export (k_debug_static.cu): per-block scratch of
 // kStaticDebugBlocks + 1 words in a fixed device array

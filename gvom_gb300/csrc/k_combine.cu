@@ -741,6 +741,48 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
 }
 
 // ---------------------------------------------------------------------------
+// k_ros_grids: the OccupancyGrid payloads of the reference's ROS node
+// (scripts/gvom_ros.py:141-164) from the last combine's maps, one thread per
+// cell, written in the node's column-major order (x fastest).  Each value is
+// cast to int8 as numpy does on the node's x86 host: truncation toward zero,
+// then the low 8 bits.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ signed char int8_wrap(double v) {
+    if (!(fabs(v) < 9.2e18)) return 0;  // NaN / out of int64 range: numpy gives INT64_MIN, low byte 0
+    const long long t = (long long)v;   // truncation toward zero
+    return (signed char)(unsigned char)(t & 0xff);
+}
+
+__global__ void __launch_bounds__(256) k_ros_grids(const __grid_constant__ RosGridParams p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;  // payload index x + y X
+    const int X = p.X;
+    if (i >= X * X) return;
+    const int x = i % X, y = i / X, c = x * X + y;  // maps are [x, y], y fastest
+    const double obs = (double)p.pos[c];
+    const int neg = p.neg[c];
+    if (p.hard) {  // max(100 (obs > density threshold), neg)   (:142)
+        const int h = obs > p.density_thr ? 100 : 0;
+        p.hard[i] = int8_wrap((double)(h > neg ? h : neg));
+    }
+    if (p.soft) p.soft[i] = (obs <= p.density_thr && obs > 0.0) ? 100 : 0;  // (:147)
+    if (p.certainty) p.certainty[i] = int8_wrap((double)(p.vis[c] * 100));      // (:152)
+    if (p.negative) p.negative[i] = int8_wrap((double)neg);                     // (:158)
+    if (p.roughness) {  // ((clip(r, min, max) + min) / (max - min)) * 100     (:162-164)
+        const double r = p.rough[c];
+        double v = (r < p.max_r || isnan(r)) ? r : p.max_r;  // np.minimum / np.maximum keep NaN
+        v = (v > p.min_r || isnan(v)) ? v : p.min_r;
+        v = __dmul_rn(__ddiv_rn(__dadd_rn(v, p.min_r), __dsub_rn(p.max_r, p.min_r)), 100.0);
+        p.roughness[i] = int8_wrap(v);
+    }
+}
+
+cudaError_t launch_ros_grids(const RosGridParams &p, cudaStream_t st) {
+    const int n = p.X * p.X;
+    k_ros_grids<<<(n + 255) / 256, 256, 0, st>>>(p);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // debug exporters
 // ---------------------------------------------------------------------------
 constexpr int kDbgChunk = 1024;  // voxels per block (256 threads x 4)

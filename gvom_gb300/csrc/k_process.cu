@@ -35,6 +35,31 @@ __device__ __forceinline__ void load_point(const ScanDesc &sd, long long i, PT &
     z = p[2];
 }
 
+// float64 processing also serves PointCloud2 data: float32 fields widened to
+// float64, as the reference's ROS node converts a cloud before mapping it
+// (scripts/gvom_ros.py:108)
+template <>
+__device__ __forceinline__ void load_point<double>(const ScanDesc &sd, long long i, double &x, double &y,
+                                                   double &z) {
+    if (sd.pc2) {
+        const char *b = static_cast<const char *>(sd.pts) + i * sd.stride;
+        if (sd.pc2 == 1) {
+            x = (double)*reinterpret_cast<const float *>(b + sd.off[0]);
+            y = (double)*reinterpret_cast<const float *>(b + sd.off[1]);
+            z = (double)*reinterpret_cast<const float *>(b + sd.off[2]);
+        } else {
+            x = *reinterpret_cast<const double *>(b + sd.off[0]);
+            y = *reinterpret_cast<const double *>(b + sd.off[1]);
+            z = *reinterpret_cast<const double *>(b + sd.off[2]);
+        }
+        return;
+    }
+    const double *p = static_cast<const double *>(sd.pts) + i * sd.stride;
+    x = p[0];
+    y = p[1];
+    z = p[2];
+}
+
 // __transform_pointcloud (scripts/gvom.py:1121-1138): all-float32 when both
 // operands are float32, float64 otherwise; the result is stored back in the
 // point dtype.

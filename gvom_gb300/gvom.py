@@ -86,6 +86,18 @@ def _ego3(ego_position):
     return e
 
 
+def pose_to_transform(translation, rotation_xyzw) -> np.ndarray:
+    """float64 4x4 of tf's fromTranslationRotation (translation, quaternion
+    x, y, z, w), as the reference's ROS node builds Process_pointcloud's
+    transform (scripts/gvom_ros.py:93-105)."""
+    t = np.ascontiguousarray(np.asarray(translation, np.float64).reshape(3))
+    q = np.ascontiguousarray(np.asarray(rotation_xyzw, np.float64).reshape(4))
+    out = np.empty((4, 4), np.float64)
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    check(_lib.load().gvom_pose_to_transform(P(t), P(q), P(out)))
+    return out
+
+
 class Gvom:
     """GB300 implementation of the reference `Gvom` (scripts/gvom.py:8-442)."""
 
@@ -166,6 +178,50 @@ class Gvom:
             return None
         check(rc)
         return origin, pos, neg, rough, vis
+
+    def process_pointcloud2(self, data, n_points, point_step, xyz_offsets, ego_position, translation,
+                            rotation_xyzw, field_dtype=np.float32):
+        """Map a PointCloud2 payload as the reference's ROS node does
+        (scripts/gvom_ros.py:85-109): x / y / z fields (`field_dtype` float32
+        or float64, little-endian) at byte offsets `xyz_offsets` of each
+        `point_step`-byte point, widened to float64, non-finite points
+        dropped, pose from tf translation + quaternion (x, y, z, w).  `data`:
+        bytes / uint8 numpy array, or a CUDA uint8 tensor (read in place)."""
+        fd = np.dtype(field_dtype)
+        if fd not in (np.dtype(np.float32), np.dtype(np.float64)):
+            raise ValueError("x / y / z fields must be float32 or float64")
+        fdt = GVOM_F32 if fd == np.float32 else GVOM_F64
+        offs = (C.c_int32 * 3)(*[int(v) for v in xyz_offsets])
+        ego = _ego3(ego_position)
+        t = np.ascontiguousarray(np.asarray(translation, np.float64).reshape(3))
+        q = np.ascontiguousarray(np.asarray(rotation_xyzw, np.float64).reshape(4))
+        P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        if hasattr(data, "data_ptr") and getattr(data, "is_cuda", False):
+            check(self._l.gvom_process_pointcloud2(self._h, C.c_void_p(data.data_ptr()), int(n_points), int(point_step),
+                                                   offs, fdt, 1, P(ego), P(t), P(q)))
+            self.synchronize()
+            return
+        buf = np.frombuffer(data, np.uint8) if isinstance(data, (bytes, bytearray, memoryview)) else \
+            np.ascontiguousarray(data).view(np.uint8).reshape(-1)
+        if buf.size < int(n_points) * int(point_step):
+            raise ValueError("data is shorter than n_points * point_step")
+        check(self._l.gvom_process_pointcloud2(self._h, P(buf), int(n_points), int(point_step), offs, fdt, 0,
+                                               P(ego), P(t), P(q)))
+
+    def ros_grids(self, density_threshold=50, min_roughness=-10, max_roughness=0):
+        """The ROS node's OccupancyGrid payloads from the last combine_maps
+        (scripts/gvom_ros.py:141-164): {'hard', 'soft', 'certainty',
+        'negative', 'roughness'} -> int8[xy_size**2] in column-major order, or
+        None before the first combine."""
+        X2 = self.xy_size * self.xy_size
+        names = ("hard", "soft", "certainty", "negative", "roughness")
+        out = {k: np.empty(X2, np.int8) for k in names}
+        p = _lib.GvomRosParams(float(density_threshold), float(min_roughness), float(max_roughness))
+        rc = self._l.gvom_ros_grids(self._h, C.byref(p), *[out[k].ctypes.data_as(C.c_void_p) for k in names], 0)
+        if rc == GVOM_NO_DATA:
+            return None
+        check(rc)
+        return out
 
     def make_debug_voxel_map(self):
         """[x, y, z, hit/total, hit, l0-l1, l1-l2, l2] per occupied voxel (scripts/gvom.py:395-410)."""

@@ -87,6 +87,21 @@ int gvom_process_device(GvomHandle *h, const void *d_points, int32_t dtype, int6
                         int64_t row_stride, const double ego[3], const void *transform,
                         int32_t transform_dtype);
 
+/* A PointCloud2 scan as the reference's ROS node maps it (scripts/gvom_ros.py:
+ * 85-109): the cloud's little-endian x / y / z fields (field_dtype GVOM_F32 or
+ * GVOM_F64, byte offsets in xyz_offsets, point_step bytes per point) widened
+ * to float64 as ros_numpy's pointcloud2_to_xyz_array does, points with a
+ * non-finite coordinate dropped, and the sensor pose given as the tf lookup's
+ * translation and quaternion (x, y, z, w) turned into the float64 4x4
+ * transform of tf's fromTranslationRotation; then Process_pointcloud.
+ * `data` is host memory (copied) or, with data_on_device, device memory. */
+int gvom_process_pointcloud2(GvomHandle *h, const void *data, int64_t n_points, int32_t point_step,
+                             const int32_t xyz_offsets[3], int32_t field_dtype, int32_t data_on_device,
+                             const double ego[3], const double translation[3], const double rotation_xyzw[4]);
+
+/* The float64 4x4 transform of tf's fromTranslationRotation (row major). */
+int gvom_pose_to_transform(const double translation[3], const double rotation_xyzw[4], double out[16]);
+
 /* Several scans, equivalent to calling gvom_process on each in order, run as
  * one set of launches over all scans.  No reference counterpart; it serves
  * multi-sensor callers of Process_pointcloud (README.md:49). */
@@ -133,6 +148,23 @@ int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64
  * serialised by a process-wide lock held until their device work is done.
  * Returns after the rows are written (host waits on the instance stream). */
 int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_rows, int64_t *rows);
+
+/* The OccupancyGrid payloads the reference's ROS node builds from
+ * combine_maps' result (scripts/gvom_ros.py:141-164), computed on the device
+ * from the last combine: hard obstacles max(100 (pos > density_threshold),
+ * neg); soft obstacles 100 (0 < pos <= density_threshold); ground certainty
+ * 100 vis; negative obstacles; roughness ((clip(r, min, max) + min) /
+ * (max - min)) 100.  Each is xy_size^2 int8 in the node's column-major order
+ * (x fastest), cast as numpy does on an x86 host (truncation, low 8 bits).
+ * Any output may be NULL.  Node defaults: density_threshold 50,
+ * min_roughness -10, max_roughness 0 (launch/gvom_node.launch:17-20). */
+typedef struct GvomRosParams {
+    double density_threshold;
+    double min_roughness;
+    double max_roughness;
+} GvomRosParams;
+int gvom_ros_grids(GvomHandle *h, const GvomRosParams *params, int8_t *hard, int8_t *soft, int8_t *certainty,
+                   int8_t *negative, int8_t *roughness, int32_t outputs_on_device);
 
 /* Replace make_debug_height_map / make_debug_inferred_height_map
  * (scripts/gvom.py:412-442, 455-479): (xy_size^2, 7) and (xy_size^2, 3) float32. */
