@@ -1,6 +1,6 @@
 """Autotuner for the launch shapes of the GB300 mapper (GvomTuning).
 
-Six choices, tuned one at a time (coordinate search) on sample steps of
+Seven choices, tuned one at a time (coordinate search) on sample steps of
 the caller's workload:
 
   points_per_block         128 / 256   k_voxelize_trace, k_scatter, k_cell_moments, k_cleanup
@@ -9,10 +9,12 @@ the caller's workload:
   stats_blocks_per_sm      2 / 4 / 8   k_merge_stats
   step_overlap             0 / 1       gvom_step: the index merge beside the statistics kernels
   maps_tile_cells          64/128/256  k_maps2d (smaller tiles spread the float64 plane fits)
+  trace_ahead              0 / 1       gvom_step: ray tracing beside the previous step's combine
 
 The others each affect their own kernels only and are timed with the
 per-kernel CUDA events of the mapper's stage timer (direct launches); the
-overlap changes how kernels share the GPU, so it is timed on whole steps.
+two overlap choices change how kernels share the GPU, so they are timed on
+whole steps submitted back to back.
 Candidates run on a private mapper of the same parameters, so the caller's
 map state is untouched.  Results are cached in a JSON file keyed by
 GPU name, grid and scans per step ($GVOM_TUNING_CACHE, default
@@ -31,6 +33,7 @@ CHOICES = {
     "stats_blocks_per_sm": (2, 4, 8),
     "step_overlap": (0, 1),
     "maps_tile_cells": (64, 128, 256),
+    "trace_ahead": (0, 1),
 }
 AFFECTS = {
     "points_per_block": ("k_voxelize_trace", "k_scatter", "k_cell_moments", "k_cleanup"),
@@ -39,9 +42,10 @@ AFFECTS = {
     "stats_blocks_per_sm": ("k_merge_stats",),
     "step_overlap": None,  # whole steps
     "maps_tile_cells": ("k_maps2d",),
+    "trace_ahead": None,  # whole steps
 }
 DEFAULT = {"points_per_block": 256, "assign_words_per_thread": 8, "merge_planes_per_thread": 8,
-           "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 256}
+           "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 256, "trace_ahead": 1}
 
 
 def cache_path() -> str:

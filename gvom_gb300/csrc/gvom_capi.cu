@@ -159,10 +159,16 @@ struct GvomHandle {
     // CUDA graphs: each process / combine launch sequence is captured and
     // replayed through an executable graph updated in place
     bool graphs = false;
-    cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};  // [0] process, [1] combine, [2] step
+    // [0] process, [1] combine, [2] step, [3] a step's trace ahead, [4] the rest of that step
+    cudaGraphExec_t gexec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // a step forks the index merge onto `side` once the index maps are done
     cudaStream_t side = nullptr;
     cudaEvent_t ev_idx = nullptr, ev_join = nullptr;
+    // trace ahead: a step's k_voxelize_trace runs on `tr` as soon as the
+    // previous process is done with the per-scan scratch (ev_scratch), beside
+    // the previous step's combine; the rest of the step waits for ev_traced
+    cudaStream_t tr = nullptr;
+    cudaEvent_t ev_scratch = nullptr, ev_traced = nullptr;
 };
 
 namespace {
@@ -199,12 +205,13 @@ long long ext_cells(const Geom &g) { return (long long)g.Xe * g.Xe * g.Ze; }
 // the executable graph `which`, updated in place when the captured topology
 // matches the previous one and re-instantiated otherwise.
 template <class F>
-int run_graphed(GvomHandle *h, int which, F &&enqueue) {
+int run_graphed(GvomHandle *h, int which, F &&enqueue, cudaStream_t st = nullptr) {
+    if (!st) st = h->st;
     if (!h->graphs) return enqueue();
-    CUDA_TRY(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     const int rc = enqueue();
     cudaGraph_t g = nullptr;
-    const cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc || e != cudaSuccess || !g) {
         if (g) cudaGraphDestroy(g);
         cudaGetLastError();
@@ -226,7 +233,7 @@ int run_graphed(GvomHandle *h, int which, F &&enqueue) {
         x = nullptr;
         return fail(GVOM_ERR_CUDA, std::string("graph instantiation: ") + cudaGetErrorString(ei));
     }
-    CUDA_TRY(cudaGraphLaunch(x, h->st));
+    CUDA_TRY(cudaGraphLaunch(x, st));
     return GVOM_OK;
 }
 
@@ -460,11 +467,16 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
 
 // stream-ordered work of a prepared process call on h->st; `after_assign`
 // (nullable) is recorded once the ring slots' index maps are complete
-int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bool timing) {
-    CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * pl.k, h->st));
+// `part` as in launch_process: 1 (the trace, on stream `st`) and 2 (the rest,
+// on h->st) split one process call in two
+int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bool timing, int part = 0,
+                 cudaStream_t st = nullptr) {
+    if (!st) st = h->st;
+    if (part != 2) CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * pl.k, st));
     CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec, h->prank, h->sorted,
-                            h->moments, h->st, timing ? h->timer.begin(0, kProcessKernels) : nullptr,
-                            h->tun.pts_block, after_assign));
+                            h->moments, st, (timing && !part) ? h->timer.begin(0, kProcessKernels) : nullptr,
+                            h->tun.pts_block, after_assign, part));
+    if (part == 1) return GVOM_OK;
     for (int i = 0; i < pl.k; i++)
         CUDA_TRY(cudaMemcpyAsync(h->d_slotC + pl.slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
                                  h->st));
@@ -491,6 +503,7 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
     if (rc) return rc;
     rc = run_graphed(h, 0, [&]() -> int { return launch_scans(h, pl, nullptr, !h->graphs); });
     if (rc) return rc;
+    CUDA_TRY(cudaEventRecord(h->ev_scratch, h->st));  // a later trace ahead may reuse the scratch
     commit_scans(h, pl);
     return GVOM_OK;
 }
@@ -586,8 +599,11 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     }
     h->st = h->own;
     if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&h->tr, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_idx, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_scratch, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_traced, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         gvom_destroy(h);
         return fail(GVOM_ERR_CUDA, "stream / event creation failed");
@@ -641,8 +657,14 @@ int gvom_destroy(GvomHandle *h) {
         cudaStreamSynchronize(h->side);
         cudaStreamDestroy(h->side);
     }
+    if (h->tr) {
+        cudaStreamSynchronize(h->tr);
+        cudaStreamDestroy(h->tr);
+    }
     if (h->ev_idx) cudaEventDestroy(h->ev_idx);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
+    if (h->ev_scratch) cudaEventDestroy(h->ev_scratch);
+    if (h->ev_traced) cudaEventDestroy(h->ev_traced);
     for (auto &s : h->slots) {
         cudaFree(s.idx);
         cudaFree(s.rec);
@@ -1033,12 +1055,30 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     CombPlan cp;
     if ((rc = prepare_combine(h, cp))) return rc;
     const bool timing = !h->graphs && h->timer.on;
-    rc = run_graphed(h, 2, [&]() -> int {
-        // with stage timing the kernels run in sequence so that each interval is one kernel
-        cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
-        if ((rc = launch_scans(h, pp, idx, timing))) return rc;
-        return launch_comb(h, cp, idx, timing);
-    });
+    // with stage timing the kernels run in sequence so that each interval is one kernel
+    cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
+    if (h->tun.trace_ahead && !timing) {
+        // the trace waits only for the previous process to release the scratch,
+        // so it runs beside the previous step's combine
+        CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_scratch, 0));
+        rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
+        CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_traced, 0));
+        rc = run_graphed(h, 4, [&]() -> int {
+            if ((rc = launch_scans(h, pp, idx, false, 2))) return rc;
+            // in graph mode an event-record node of the graph
+            if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_scratch, h->st, cudaEventRecordExternal));
+            else CUDA_TRY(cudaEventRecord(h->ev_scratch, h->st));
+            return launch_comb(h, cp, idx, false);
+        });
+    } else {
+        rc = run_graphed(h, 2, [&]() -> int {
+            if ((rc = launch_scans(h, pp, idx, timing))) return rc;
+            return launch_comb(h, cp, idx, timing);
+        });
+        if (!rc) CUDA_TRY(cudaEventRecord(h->ev_scratch, h->st));
+    }
     if (rc) return rc;
     commit_combine(h, cp);
     if ((rc = copy_outputs(h, cp, origin, pos, neg, roughness, visibility, !outputs_on_device))) return rc;
@@ -1431,6 +1471,7 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     if (!(t->step_overlap == 0 || t->step_overlap == 1)) return fail(GVOM_ERR_ARG, "step_overlap must be 0 or 1");
     if (!(t->maps_tile_cells == 64 || t->maps_tile_cells == 128 || t->maps_tile_cells == 256))
         return fail(GVOM_ERR_ARG, "maps_tile_cells must be 64, 128 or 256");
+    if (!(t->trace_ahead == 0 || t->trace_ahead == 1)) return fail(GVOM_ERR_ARG, "trace_ahead must be 0 or 1");
     std::lock_guard<std::mutex> lk(h->mu);
     h->tun.pts_block = t->points_per_block;
     h->tun.assign_per = t->assign_words_per_thread;
@@ -1438,6 +1479,7 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     h->tun.stats_bpsm = t->stats_blocks_per_sm;
     h->tun.step_overlap = t->step_overlap;
     h->tun.maps_tile = t->maps_tile_cells;
+    h->tun.trace_ahead = t->trace_ahead;
     return GVOM_OK;
 }
 
@@ -1450,6 +1492,7 @@ int gvom_get_tuning(GvomHandle *h, GvomTuning *t) {
     t->stats_blocks_per_sm = h->tun.stats_bpsm;
     t->step_overlap = h->tun.step_overlap;
     t->maps_tile_cells = h->tun.maps_tile;
+    t->trace_ahead = h->tun.trace_ahead;
     return GVOM_OK;
 }
 

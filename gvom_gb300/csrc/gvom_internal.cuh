@@ -32,8 +32,9 @@ struct Tuning {
     int stats_bpsm;     // k_merge_stats blocks per multiprocessor: 2, 4 or 8
     int step_overlap;   // gvom_step runs the index merge beside the statistics kernels: 0 or 1
     int maps_tile;      // k_maps2d tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) cells
+    int trace_ahead;    // gvom_step traces its scans beside the previous step's combine: 0 or 1
 };
-constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1, 256};
+constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1, 256, 1};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
 constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
@@ -203,9 +204,11 @@ struct DebugMapParams {
 constexpr int kProcessKernels = 6;  // voxelize_trace, assign, scatter, cell_moments, voxel_stats, cleanup
 constexpr int kCombineKernels = 4;  // merge, merge_stats, columns, maps2d
 constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
+// `part`: 0 every kernel, 1 k_voxelize_trace only, 2 the kernels after it
+// (parts are launched without stage events)
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign);
+                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part = 0);
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
 cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st);
 cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,

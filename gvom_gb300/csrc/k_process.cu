@@ -733,19 +733,22 @@ __global__ void __launch_bounds__(256) k_cleanup(const ProcessConst pc, const __
 template <int NS>
 static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int total_blocks, int max_n, int dtype,
                              float4 *prec, int *prank, float4 *sorted, CellMom *mom, cudaStream_t st, cudaEvent_t *ev,
-                             int bs, cudaEvent_t after_assign) {
+                             int bs, cudaEvent_t after_assign, int part) {
     ScanTable<NS> tab;
     for (int i = 0; i < NS; i++) tab.s[i] = i < pc.nscans ? table[i] : table[0];
     if (total_blocks < 1) total_blocks = 1;
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(ev[i], st);
     };
-    mark(0);
-    if (dtype == 1)
-        k_voxelize_trace<double, NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
-    else
-        k_voxelize_trace<float, NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
-    mark(1);
+    if (part != 2) {
+        mark(0);
+        if (dtype == 1)
+            k_voxelize_trace<double, NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
+        else
+            k_voxelize_trace<float, NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
+        mark(1);
+        if (part == 1) return cudaGetLastError();
+    }
     {
         const int per = pc.assign_per;
         dim3 ga((unsigned)((pc.g.Vext + 256 * per - 1) / (256 * per)), pc.nscans);
@@ -771,16 +774,17 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
 
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign) {
+                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part) {
     CellMom *mom = static_cast<CellMom *>(moments);
+    if (part) ev = nullptr;
     if (nscans == 1)
         return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                            after_assign);
+                            after_assign, part);
     if (nscans <= 4)
         return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                            after_assign);
+                            after_assign, part);
     return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                                after_assign);
+                                after_assign, part);
 }
 
 }  // namespace gvom

@@ -340,7 +340,8 @@ def scene_for(w: Workload, path_len: float | None = None):
 
 def make_workload_scans(w: Workload, n: int | None = None, device="cpu", dropout: float = 0.0):
     n = w.n_scans if n is None else n
-    terrain, veg = scene_for(w)
+    # the scene of the workload's own n_scans; longer runs extend it along the path
+    terrain, veg = scene_for(w, None if n <= w.n_scans else n * 0.4)
     lidar = Lidar(beams=w.beams, columns=w.columns)
     poses = make_trajectory(n)
     return [make_scan(terrain, lidar, p, i, vegetation=veg, footprint=w.xy_size * w.res,

@@ -123,8 +123,11 @@ int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t
  * outputs) or gvom_combine_device (outputs_on_device != 0), with the same
  * results; no counterpart in the reference.  Submitted together, the index
  * merge of the combine runs beside the process call's statistics kernels
- * (it needs only the ring's index maps), and in graph mode the whole step is
- * one executable graph. */
+ * (it needs only the ring's index maps).  With trace_ahead (GvomTuning) the
+ * step's ray tracing runs on a second stream as soon as the previous process
+ * call is done with the per-scan scratch, beside the previous step's combine
+ * when steps are submitted back to back; in graph mode the step is two
+ * executable graphs (trace, rest), else one. */
 int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device, double origin[3],
               int32_t *pos, int32_t *neg, double *roughness, int32_t *visibility, int32_t outputs_on_device);
 
@@ -215,7 +218,7 @@ int gvom_synchronize(GvomHandle *h);
  * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
 /* Launch shapes chosen by the autotuner (gvom_gb300/autotune.py); no
  * counterpart in the reference.  They change speed only, never results.
- * Defaults: 256, 8, 8, 4, 1, 256. */
+ * Defaults: 256, 8, 8, 4, 1, 256, 1. */
 typedef struct GvomTuning {
     int32_t points_per_block;         /* point-parallel kernels: 128 or 256 */
     int32_t assign_words_per_thread;  /* index assignment: 4, 8 or 16 */
@@ -223,6 +226,7 @@ typedef struct GvomTuning {
     int32_t stats_blocks_per_sm;      /* statistics merge: 2, 4 or 8 */
     int32_t step_overlap;             /* gvom_step: index merge beside the statistics kernels, 0 or 1 */
     int32_t maps_tile_cells;          /* 2-D maps tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) */
+    int32_t trace_ahead;              /* gvom_step: trace a step's scans beside the previous step's combine, 0 or 1 */
 } GvomTuning;
 int gvom_set_tuning(GvomHandle *h, const GvomTuning *t);
 int gvom_get_tuning(GvomHandle *h, GvomTuning *t);

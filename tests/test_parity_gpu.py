@@ -271,6 +271,49 @@ def test_step_equals_process_then_combine(Gvom, graphs):
         compare_slot(canonical_state(a.combined_state()), canonical_state(b.combined_state()), f"combined {k}")
 
 
+@pytest.mark.parametrize("graphs", [False, True])
+@pytest.mark.parametrize("ahead", [0, 1])
+def test_steps_back_to_back_equal_sequential_calls(Gvom, graphs, ahead):
+    """Steps submitted without a host wait in between (device outputs), so that
+    with trace_ahead a step's ray tracing runs beside the previous step's
+    combine, with plain process / combine calls in the middle of the sequence:
+    every step's maps equal those of process_batch + combine_maps."""
+    import torch
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["small_32x512"]
+    scans = make_workload_scans(w, 7)
+    params = w.gvom_args()[:4] + (3,) + w.gvom_args()[5:]
+    X = params[2]
+    a, b = Gvom(*params), Gvom(*params)
+    b.set_graphs(graphs)
+    b.set_tuning(dict(b.get_tuning(), trace_ahead=ahead))
+    dev = [torch.from_numpy(np.ascontiguousarray(s.points)).cuda() for s in scans]
+    order = [[0], [1, 2], [3], [4], "plain", [5, 6], [0], [2], [1, 3], [4]]
+    want, got = [], []
+    for k, idx in enumerate(order):
+        if idx == "plain":  # the reference-style calls on the same instance, between steps
+            s = scans[5]
+            a.Process_pointcloud(s.points, s.ego, s.transform)
+            b.Process_pointcloud(s.points, s.ego, s.transform)
+            want.append(a.combine_maps())
+            got.append(b.combine_maps())
+            continue
+        a.process_batch([(scans[i].points, scans[i].ego, scans[i].transform) for i in idx])
+        want.append(a.combine_maps())
+        outs = [torch.empty((X, X), dtype=d, device="cuda") for d in (torch.int32, torch.int32, torch.float64,
+                                                                        torch.int32)]
+        origin = b.step([(dev[i], scans[i].ego, scans[i].transform) for i in idx], device_outputs=outs)
+        got.append((origin, outs))
+    torch.cuda.synchronize()
+    for k, (ra, rb) in enumerate(zip(want, got)):
+        if isinstance(rb[1], list):
+            rb = (rb[0], *[t.cpu().numpy() for t in rb[1]])
+        for x, y in zip(ra, rb):
+            np.testing.assert_array_equal(x, y, f"step {k}")
+    assert a.ring_state() == b.ring_state()
+    compare_slot(canonical_state(a.combined_state()), canonical_state(b.combined_state()), "combined")
+
+
 def _compare_runs(Gvom, params, runs):
     """runs: [(points, ego, T), ...] each followed by a combine."""
     g, o = Gvom(*params), OracleGvom(*params)
