@@ -60,7 +60,7 @@ class GvomTuning(C.Structure):
     _fields_ = [("points_per_block", C.c_int32), ("assign_words_per_thread", C.c_int32),
                 ("merge_planes_per_thread", C.c_int32), ("stats_blocks_per_sm", C.c_int32),
                 ("step_overlap", C.c_int32), ("maps_tile_cells", C.c_int32),
-                ("trace_ahead", C.c_int32)]
+                ("step_pipeline", C.c_int32)]
 
 
 class GvomRosParams(C.Structure):

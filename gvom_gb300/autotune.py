@@ -9,7 +9,8 @@ the caller's workload:
   stats_blocks_per_sm      2 / 4 / 8   k_merge_stats
   step_overlap             0 / 1       gvom_step: the index merge beside the statistics kernels
   maps_tile_cells          64/128/256  k_maps2d (smaller tiles spread the float64 plane fits)
-  trace_ahead              0 / 1       gvom_step: ray tracing beside the previous step's combine
+  step_pipeline            0 / 1 / 2   gvom_step: ray tracing beside the previous step's combine (1),
+                                       and the process + merge beside its columns and maps (2)
 
 The others each affect their own kernels only and are timed with the
 per-kernel CUDA events of the mapper's stage timer (direct launches); the
@@ -33,7 +34,7 @@ CHOICES = {
     "stats_blocks_per_sm": (2, 4, 8),
     "step_overlap": (0, 1),
     "maps_tile_cells": (64, 128, 256),
-    "trace_ahead": (0, 1),
+    "step_pipeline": (0, 1, 2),
 }
 AFFECTS = {
     "points_per_block": ("k_voxelize_trace", "k_scatter", "k_cell_moments", "k_cleanup"),
@@ -42,10 +43,10 @@ AFFECTS = {
     "stats_blocks_per_sm": ("k_merge_stats",),
     "step_overlap": None,  # whole steps
     "maps_tile_cells": ("k_maps2d",),
-    "trace_ahead": None,  # whole steps
+    "step_pipeline": None,  # whole steps
 }
 DEFAULT = {"points_per_block": 256, "assign_words_per_thread": 8, "merge_planes_per_thread": 8,
-           "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 256, "trace_ahead": 1}
+           "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 256, "step_pipeline": 2}
 
 
 def cache_path() -> str:

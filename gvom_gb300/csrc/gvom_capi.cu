@@ -127,15 +127,18 @@ struct GvomHandle {
     double cod[2][3] = {{0, 0, 0}, {0, 0, 0}};
     int cur = 0;
     bool have_comb = false;
-    // per-scan scratch
-    std::vector<unsigned long long *> cnt;  // one dense count array per concurrent scan
-    float4 *prec = nullptr, *sorted = nullptr;
-    int *prank = nullptr;
+    // per-scan scratch, in two sets used by alternate process calls (a step's
+    // trace fills one set while the previous step's process reads the other)
+    std::vector<unsigned long long *> cnt[2];  // one dense count array per concurrent scan
+    float4 *prec[2] = {nullptr, nullptr};
+    int *prank[2] = {nullptr, nullptr};
+    float4 *sorted = nullptr;
+    int sset = 0;  // scratch set of the next process call
     char *moments = nullptr;  // per point slot, kCellMomBytes each
     long long pcap = 0;
     void *dpts = nullptr;
     size_t dpts_bytes = 0;
-    ScanCounters *d_ctr = nullptr;  // kMaxBatch
+    ScanCounters *d_ctr = nullptr;  // 2 x kMaxBatch (one block per scratch set)
     int *d_slotC = nullptr;         // per ring slot occupied count
     int *d_combC = nullptr;         // [0..1] occupied count per combined buffer, [2] float64 eigen refinements
     int last_ctr = -1;              // counters of the last processed scan
@@ -145,7 +148,7 @@ struct GvomHandle {
     int *pos_density = nullptr, *pos = nullptr, *neg = nullptr, *vis = nullptr;
     int *zlow = nullptr;
     float *mlow = nullptr;
-    int2 *colinfo = nullptr;  // (Z / 8 chunks) x X x X
+    int2 *colinfo[2] = {nullptr, nullptr};  // (Z / 8 chunks) x X x X, one per combined buffer
     int *occ_list = nullptr;  // occupied voxel ids of the combined map being built (V)
     bool have_maps = false;
     // debug
@@ -159,16 +162,28 @@ struct GvomHandle {
     // CUDA graphs: each process / combine launch sequence is captured and
     // replayed through an executable graph updated in place
     bool graphs = false;
-    // [0] process, [1] combine, [2] step, [3] a step's trace ahead, [4] the rest of that step
-    cudaGraphExec_t gexec[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ merge at
+    // level 2), [5] its columns and maps (level 2)
+    cudaGraphExec_t gexec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // a step forks the index merge onto `side` once the index maps are done
     cudaStream_t side = nullptr;
     cudaEvent_t ev_idx = nullptr, ev_join = nullptr;
-    // trace ahead: a step's k_voxelize_trace runs on `tr` as soon as the
-    // previous process is done with the per-scan scratch (ev_scratch), beside
-    // the previous step's combine; the rest of the step waits for ev_traced
-    cudaStream_t tr = nullptr;
-    cudaEvent_t ev_scratch = nullptr, ev_traced = nullptr;
+    // step pipeline (Tuning::step_pipeline): a step stages its points and
+    // runs k_voxelize_trace on `tr` as soon as the process call that last used
+    // its scratch set (the one before the previous call) is done with it
+    // (ev_scratch[set]).  At level 1 the rest of the step follows on the
+    // instance stream after ev_traced.  At level 2 the rest of the process
+    // and the merge run on `bs` (after ev_traced, and after the columns pass
+    // that last read the combined buffer they write, ev_cols[buffer]) beside
+    // the previous step's columns and maps on the instance stream, which
+    // waits for ev_merged.  Work queued on the instance stream by other calls
+    // sets st_dirty: the next level-2 step first orders `tr` and `bs` after
+    // it (ev_host).
+    cudaStream_t tr = nullptr, bs = nullptr;
+    cudaEvent_t ev_scratch[2] = {nullptr, nullptr};  // the process call that last used the set is done with it
+    cudaEvent_t ev_traced = nullptr, ev_merged = nullptr, ev_host = nullptr;
+    cudaEvent_t ev_cols[2] = {nullptr, nullptr};
+    bool st_dirty = false;
 };
 
 namespace {
@@ -262,17 +277,21 @@ int ensure_points(GvomHandle *h, long long n) {
     cap = std::max<long long>(cap, 4096);
     if (cap >= (1LL << 31)) return fail(GVOM_ERR_ARG, "too many points");
     CUDA_TRY(cudaStreamSynchronize(h->st));
-    dfree(h, h->prec, h->pcap * sizeof(float4));
+    for (int b = 0; b < 2; b++) {
+        dfree(h, h->prec[b], h->pcap * sizeof(float4));
+        dfree(h, h->prank[b], h->pcap * sizeof(int));
+        h->prec[b] = nullptr;
+        h->prank[b] = nullptr;
+    }
     dfree(h, h->sorted, h->pcap * sizeof(float4));
-    dfree(h, h->prank, h->pcap * sizeof(int));
     dfree(h, h->moments, h->pcap * kCellMomBytes);
-    h->prec = h->sorted = nullptr;
-    h->prank = nullptr;
+    h->sorted = nullptr;
     h->moments = nullptr;
     h->pcap = 0;
     int rc;
-    if ((rc = dalloc_t(h, &h->prec, cap)) || (rc = dalloc_t(h, &h->sorted, cap)) || (rc = dalloc_t(h, &h->prank, cap)) ||
-        (rc = dalloc(h, reinterpret_cast<void **>(&h->moments), (size_t)cap * kCellMomBytes)))
+    for (int b = 0; b < 2; b++)
+        if ((rc = dalloc_t(h, &h->prec[b], cap)) || (rc = dalloc_t(h, &h->prank[b], cap))) return rc;
+    if ((rc = dalloc_t(h, &h->sorted, cap)) || (rc = dalloc(h, reinterpret_cast<void **>(&h->moments), (size_t)cap * kCellMomBytes)))
         return rc;
     h->pcap = cap;
     return GVOM_OK;
@@ -291,15 +310,15 @@ int ensure_dpts(GvomHandle *h, size_t bytes) {
     return GVOM_OK;
 }
 
-int ensure_cnt(GvomHandle *h, int nscans) {
-    while ((int)h->cnt.size() < nscans) {
+int ensure_cnt(GvomHandle *h, int nscans, int set) {
+    while ((int)h->cnt[set].size() < nscans) {
         unsigned long long *c = nullptr;
         // padded to whole k_assign blocks of cells; the padding stays zero
         const long long ve = (ext_cells(h->g) + kAssignPadCells - 1) / kAssignPadCells * kAssignPadCells;
         int rc = dalloc_t(h, &c, (size_t)ve);
         if (rc) return rc;
         CUDA_TRY(cudaMemsetAsync(c, 0, (size_t)ve * 8, h->st));
-        h->cnt.push_back(c);
+        h->cnt[set].push_back(c);
     }
     return GVOM_OK;
 }
@@ -361,6 +380,7 @@ struct ProcPlan {
     ProcessConst pc;
     ScanDesc table[kMaxBatch];
     int k = 0, block = 0, max_n = 0, dtype = GVOM_F32;
+    int set = 0;  // scratch set
     int slot_of[kMaxBatch];
     double last_ego[3];
 };
@@ -370,7 +390,8 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
     pl.k = k;
     if (k == 0) return GVOM_OK;
     int rc;
-    if ((rc = ensure_cnt(h, k))) return rc;
+    pl.set = h->sset;
+    if ((rc = ensure_cnt(h, k, pl.set))) return rc;
     long long total_pts = 0, max_n = 0;
     for (auto &s : scans) {
         total_pts += s.n;
@@ -452,11 +473,11 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
         block += d.nblocks;
         d.pt_base = base;
         base += s.n;
-        d.cnt = h->cnt[i];
+        d.cnt = h->cnt[pl.set][i];
         d.idx = h->slots[slot].idx;
         d.rec = h->slots[slot].rec;
         d.rec_cap = h->slots[slot].cap;
-        d.ctr = h->d_ctr + i;
+        d.ctr = h->d_ctr + pl.set * kMaxBatch + i;
     }
     pl.block = block;
     pl.max_n = (int)std::min<long long>(max_n, h->g.V);
@@ -472,14 +493,15 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
 int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bool timing, int part = 0,
                  cudaStream_t st = nullptr) {
     if (!st) st = h->st;
-    if (part != 2) CUDA_TRY(cudaMemsetAsync(h->d_ctr, 0, sizeof(ScanCounters) * pl.k, st));
-    CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec, h->prank, h->sorted,
+    ScanCounters *ctr = h->d_ctr + pl.set * kMaxBatch;
+    if (part != 2) CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(ScanCounters) * pl.k, st));
+    CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec[pl.set], h->prank[pl.set], h->sorted,
                             h->moments, st, (timing && !part) ? h->timer.begin(0, kProcessKernels) : nullptr,
                             h->tun.pts_block, after_assign, part));
     if (part == 1) return GVOM_OK;
     for (int i = 0; i < pl.k; i++)
-        CUDA_TRY(cudaMemcpyAsync(h->d_slotC + pl.slot_of[i], &h->d_ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
-                                 h->st));
+        CUDA_TRY(cudaMemcpyAsync(h->d_slotC + pl.slot_of[i], &ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
+                                 st));
     return GVOM_OK;
 }
 
@@ -493,17 +515,19 @@ void commit_scans(GvomHandle *h, const ProcPlan &pl) {
     for (int a = 0; a < 3; a++) h->ego[a] = pl.last_ego[a];
     h->last_buffer_index = pl.slot_of[pl.k - 1];
     h->buffer_index = (pl.slot_of[pl.k - 1] + 1) % h->B;
-    h->last_ctr = pl.k - 1;
+    h->last_ctr = pl.set * kMaxBatch + pl.k - 1;
+    h->sset = pl.set ^ 1;
 }
 
 int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
+    h->st_dirty = true;  // work on the instance stream: see the step pipeline
     if (scans.empty()) return GVOM_OK;
     ProcPlan pl;
     int rc = prepare_scans(h, scans, pl);
     if (rc) return rc;
     rc = run_graphed(h, 0, [&]() -> int { return launch_scans(h, pl, nullptr, !h->graphs); });
     if (rc) return rc;
-    CUDA_TRY(cudaEventRecord(h->ev_scratch, h->st));  // a later trace ahead may reuse the scratch
+    CUDA_TRY(cudaEventRecord(h->ev_scratch[pl.set], h->st));  // a later pipelined trace may reuse the set
     commit_scans(h, pl);
     return GVOM_OK;
 }
@@ -600,9 +624,15 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     h->st = h->own;
     if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
         cudaStreamCreateWithPriority(&h->tr, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&h->bs, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_merged, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_host, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_cols[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_cols[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_idx, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_scratch, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_scratch[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_scratch[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_traced, cudaEventDisableTiming) != cudaSuccess) {
         cudaGetLastError();
         gvom_destroy(h);
@@ -620,7 +650,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         if ((rc = dalloc_t(h, &h->crec[b], (size_t)g.V))) return bail(rc);
     }
     // counters + scan table
-    if ((rc = dalloc(h, reinterpret_cast<void **>(&h->d_ctr), sizeof(ScanCounters) * kMaxBatch)))
+    if ((rc = dalloc(h, reinterpret_cast<void **>(&h->d_ctr), sizeof(ScanCounters) * 2 * kMaxBatch)))
         return bail(rc);
     if ((rc = dalloc_t(h, &h->d_slotC, (size_t)h->B))) return bail(rc);
     if ((rc = dalloc_t(h, &h->d_combC, 4))) return bail(rc);
@@ -631,14 +661,15 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     for (auto m : imaps)
         if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
     if ((rc = dalloc_t(h, &h->mlow, (size_t)X2))) return bail(rc);
-    if ((rc = dalloc_t(h, &h->colinfo, (size_t)X2 * ((g.Z + 3) / 4)))) return bail(rc);  // chunks of >= 4 planes
+    for (int b = 0; b < 2; b++)  // chunks of >= 4 planes
+        if ((rc = dalloc_t(h, &h->colinfo[b], (size_t)X2 * ((g.Z + 3) / 4)))) return bail(rc);
     if ((rc = dalloc_t(h, &h->occ_list, (size_t)g.V))) return bail(rc);
     if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->B, h->st) != cudaSuccess ||
         cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 4, h->st) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(GVOM_ERR_CUDA, "memset failed"));
     }
-    if ((rc = ensure_cnt(h, 1))) return bail(rc);
+    if ((rc = ensure_cnt(h, 1, 0)) || (rc = ensure_cnt(h, 1, 1))) return bail(rc);
     if (cudaStreamSynchronize(h->st) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(GVOM_ERR_CUDA, "initialisation failed"));
@@ -657,13 +688,17 @@ int gvom_destroy(GvomHandle *h) {
         cudaStreamSynchronize(h->side);
         cudaStreamDestroy(h->side);
     }
-    if (h->tr) {
-        cudaStreamSynchronize(h->tr);
-        cudaStreamDestroy(h->tr);
-    }
+    for (cudaStream_t s : {h->tr, h->bs})
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    for (cudaEvent_t e : {h->ev_merged, h->ev_host, h->ev_cols[0], h->ev_cols[1]})
+        if (e) cudaEventDestroy(e);
     if (h->ev_idx) cudaEventDestroy(h->ev_idx);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
-    if (h->ev_scratch) cudaEventDestroy(h->ev_scratch);
+    for (cudaEvent_t e : h->ev_scratch)
+        if (e) cudaEventDestroy(e);
     if (h->ev_traced) cudaEventDestroy(h->ev_traced);
     for (auto &s : h->slots) {
         cudaFree(s.idx);
@@ -673,10 +708,12 @@ int gvom_destroy(GvomHandle *h) {
         cudaFree(h->cidx[b]);
         cudaFree(h->crec[b]);
     }
-    for (auto c : h->cnt) cudaFree(c);
-    cudaFree(h->prec);
+    for (int b = 0; b < 2; b++) {
+        for (auto c : h->cnt[b]) cudaFree(c);
+        cudaFree(h->prec[b]);
+        cudaFree(h->prank[b]);
+    }
     cudaFree(h->sorted);
-    cudaFree(h->prank);
     cudaFree(h->moments);
     cudaFree(h->dpts);
     cudaFree(h->d_ctr);
@@ -694,7 +731,8 @@ int gvom_destroy(GvomHandle *h) {
     cudaFree(h->vis);
     cudaFree(h->zlow);
     cudaFree(h->mlow);
-    cudaFree(h->colinfo);
+    cudaFree(h->colinfo[0]);
+    cudaFree(h->colinfo[1]);
     cudaFree(h->occ_list);
     cudaFree(h->d_dbg);
     cudaFree(h->d_ros);
@@ -775,7 +813,8 @@ int gvom_process_device(GvomHandle *h, const void *d_points, int32_t dtype, int6
 // overwrites (ring wrap) are dropped; `pinned` tells whether a host buffer
 // was page-locked (the copy must then finish before the call returns).
 static int stage_batch(GvomHandle *h, const GvomScan *scans, int n_scans, int points_on_device,
-                       std::vector<ScanIn> &v, bool &pinned) {
+                       std::vector<ScanIn> &v, bool &pinned, cudaStream_t st = nullptr) {
+    if (!st) st = h->st;
     const int first = std::max(0, n_scans - std::min(h->B, kMaxBatch));
     const int dt = scans[first].dtype;
     size_t total_bytes = 0;
@@ -802,7 +841,7 @@ static int stage_batch(GvomHandle *h, const GvomScan *scans, int n_scans, int po
         const GvomScan &sc = scans[first + (int)j];
         const size_t b = (size_t)v[j].n * (size_t)v[j].stride * (size_t)bytes_of(v[j].dtype);
         if (b) {
-            CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h->dpts) + off, sc.points, b, cudaMemcpyHostToDevice, h->st));
+            CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(h->dpts) + off, sc.points, b, cudaMemcpyHostToDevice, st));
             pinned = pinned || is_pinned_host(sc.points);
         }
         v[j].dev_pts = static_cast<char *>(h->dpts) + off;
@@ -917,7 +956,7 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
     mp.num_sms = h->num_sms;
     mp.planes = h->tun.merge_planes;
     mp.stats_bpsm = h->tun.stats_bpsm;
-    mp.colinfo = h->colinfo;
+    mp.colinfo = h->colinfo[nb];
     ColumnParams &cp = pl.cp;
     std::memset(&cp, 0, sizeof(cp));
     cp.X = h->g.X;
@@ -925,7 +964,7 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
     cp.planes = h->tun.merge_planes;
     cp.idx = mp.out_idx;
     cp.rec = mp.out_rec;
-    cp.colinfo = h->colinfo;
+    cp.colinfo = h->colinfo[nb];
     for (int a = 0; a < 3; a++) {
         cp.co[a] = mp.co[a];
         cp.ego[a] = h->ego[a];
@@ -975,14 +1014,31 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
 // index merge runs on the side stream as soon as that event (recorded when
 // the ring's index maps are complete) has fired, overlapping the rest of the
 // process kernels, and joins back before the statistics merge.
-int launch_comb(GvomHandle *h, const CombPlan &pl, cudaEvent_t idx_ready, bool timing) {
+// `part`: 0 the whole combine on h->st; 1 the merge and merge_stats on `st`;
+// 2 columns and maps on h->st, with ev_cols[buffer] recorded between them
+int launch_comb(GvomHandle *h, const CombPlan &pl, cudaEvent_t idx_ready, bool timing, int part = 0,
+                cudaStream_t st = nullptr) {
+    if (!st) st = h->st;
+    if (part == 2) {
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 2));
+        if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_cols[pl.nb], h->st, cudaEventRecordExternal));
+        else CUDA_TRY(cudaEventRecord(h->ev_cols[pl.nb], h->st));
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 3));
+        return GVOM_OK;
+    }
     if (idx_ready) {
         CUDA_TRY(cudaStreamWaitEvent(h->side, idx_ready, 0));
         CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->side));
         CUDA_TRY(launch_merge_index(pl.mp, h->side));
         CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
-        CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_join, 0));
-        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr));
+        CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, st, nullptr, part));
+        return GVOM_OK;
+    }
+    if (part == 1) {
+        CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), st));
+        CUDA_TRY(launch_merge_index(pl.mp, st));
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, st, nullptr, 1));
         return GVOM_OK;
     }
     CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->st));
@@ -1021,6 +1077,7 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
                         bool to_host) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
+    h->st_dirty = true;  // work on the instance stream: see the step pipeline
     CombPlan pl;
     int rc = prepare_combine(h, pl);
     if (rc) return rc;
@@ -1044,23 +1101,52 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     if (n_scans < 1 || !scans) return fail(GVOM_ERR_ARG, "a step needs at least one scan");
     std::lock_guard<std::mutex> lk(h->mu);
+    const bool timing = !h->graphs && h->timer.on;
+    // with stage timing the kernels run in sequence so that each interval is one kernel
+    const int pipe = timing ? 0 : h->tun.step_pipeline;
+    if (pipe == 2 && h->st_dirty) {  // order the pipeline streams after other calls' work
+        CUDA_TRY(cudaEventRecord(h->ev_host, h->st));
+        CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_host, 0));
+        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_host, 0));
+        h->st_dirty = false;
+    }
+    // a pipelined step stages its points and traces on `tr`, once the previous
+    // process is done with the per-scan scratch and the staging buffer
+    if (pipe) CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_scratch[h->sset], 0));
     std::vector<ScanIn> v;
     bool pinned = false;
     int rc;
-    if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned))) return rc;
+    if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned, pipe ? h->tr : h->st))) return rc;
     ProcPlan pp;
     if ((rc = prepare_scans(h, v, pp))) return rc;
     commit_scans(h, pp);  // host ring bookkeeping; the combine plan reads the ring after this batch
     for (int a = 0; a < 3; a++) h->ego[a] = scans[n_scans - 1].ego[a];
     CombPlan cp;
     if ((rc = prepare_combine(h, cp))) return rc;
-    const bool timing = !h->graphs && h->timer.on;
-    // with stage timing the kernels run in sequence so that each interval is one kernel
     cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
-    if (h->tun.trace_ahead && !timing) {
+    if (pipe == 2) {
+        rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
+        // the rest of the process and the merge: after the trace, and after the
+        // columns pass that last read the combined buffer this merge writes
+        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_traced, 0));
+        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_cols[cp.nb], 0));
+        rc = run_graphed(h, 4, [&]() -> int {
+            if ((rc = launch_scans(h, pp, idx, false, 2, h->bs))) return rc;
+            if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_scratch[pp.set], h->bs, cudaEventRecordExternal));
+            else CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->bs));
+            return launch_comb(h, cp, idx, false, 1, h->bs);
+        }, h->bs);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_merged, h->bs));
+        // columns and maps on the instance stream, beside the next step's process
+        CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_merged, 0));
+        rc = run_graphed(h, 5, [&]() -> int { return launch_comb(h, cp, nullptr, false, 2); });
+    } else if (pipe == 1) {
+        h->st_dirty = true;
         // the trace waits only for the previous process to release the scratch,
         // so it runs beside the previous step's combine
-        CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_scratch, 0));
         rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
@@ -1068,27 +1154,29 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         rc = run_graphed(h, 4, [&]() -> int {
             if ((rc = launch_scans(h, pp, idx, false, 2))) return rc;
             // in graph mode an event-record node of the graph
-            if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_scratch, h->st, cudaEventRecordExternal));
-            else CUDA_TRY(cudaEventRecord(h->ev_scratch, h->st));
+            if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_scratch[pp.set], h->st, cudaEventRecordExternal));
+            else CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->st));
             return launch_comb(h, cp, idx, false);
         });
     } else {
+        h->st_dirty = true;
         rc = run_graphed(h, 2, [&]() -> int {
             if ((rc = launch_scans(h, pp, idx, timing))) return rc;
             return launch_comb(h, cp, idx, timing);
         });
-        if (!rc) CUDA_TRY(cudaEventRecord(h->ev_scratch, h->st));
+        if (!rc) CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->st));
     }
     if (rc) return rc;
     commit_combine(h, cp);
     if ((rc = copy_outputs(h, cp, origin, pos, neg, roughness, visibility, !outputs_on_device))) return rc;
-    if (pinned) CUDA_TRY(cudaStreamSynchronize(h->st));
+    if (pinned) CUDA_TRY(cudaStreamSynchronize(pipe ? h->tr : h->st));  // the caller may reuse its buffers
     return GVOM_OK;
 }
 
 int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64_t *rows) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
+    h->st_dirty = true;  // work on the instance stream: see the step pipeline
     if (!h->have_comb) return fail(GVOM_NO_DATA, "No data");
     const long long V = h->g.V;
     const int chunk = debug_chunk();
@@ -1136,6 +1224,7 @@ int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64
 static int debug_maps(GvomHandle *h, float *out_h, float *out_i) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
+    h->st_dirty = true;  // work on the instance stream: see the step pipeline
     if (!h->have_maps) return fail(GVOM_NO_DATA, "No data");
     if (!out_h && !out_i) return fail(GVOM_ERR_ARG, "output is NULL");
     const size_t X2 = (size_t)h->g.X * h->g.X;
@@ -1180,6 +1269,7 @@ int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_r
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     if (capacity_rows < 0) return fail(GVOM_ERR_ARG, "capacity_rows is negative");
     std::lock_guard<std::mutex> lk(h->mu);
+    h->st_dirty = true;  // work on the instance stream: see the step pipeline
     const long long V = h->g.V;
     const int chunk = debug_chunk();
     const long long nblocks = (V + chunk - 1) / chunk;
@@ -1230,6 +1320,7 @@ int gvom_ros_grids(GvomHandle *h, const GvomRosParams *rp, int8_t *hard, int8_t 
     if (!h || !rp) return fail(GVOM_ERR_ARG, "handle or params is NULL");
     if (!(rp->max_roughness != rp->min_roughness)) return fail(GVOM_ERR_ARG, "max_roughness must differ from min_roughness");
     std::lock_guard<std::mutex> lk(h->mu);
+    h->st_dirty = true;  // work on the instance stream: see the step pipeline
     if (!h->have_maps) return fail(GVOM_NO_DATA, "No data");
     const size_t X2 = (size_t)h->g.X * h->g.X;
     int8_t *outs[5] = {hard, soft, certainty, negative, roughness};
@@ -1422,6 +1513,7 @@ int gvom_get_maps(GvomHandle *h, double *height, double *inferred, double *slope
 int gvom_set_stream(GvomHandle *h, void *stream) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
+    h->st_dirty = true;  // work on the instance stream: see the step pipeline
     cudaStream_t ns = stream ? static_cast<cudaStream_t>(stream) : h->own;
     if (ns != h->st) {
         // order the new stream after everything queued so far
@@ -1471,7 +1563,7 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     if (!(t->step_overlap == 0 || t->step_overlap == 1)) return fail(GVOM_ERR_ARG, "step_overlap must be 0 or 1");
     if (!(t->maps_tile_cells == 64 || t->maps_tile_cells == 128 || t->maps_tile_cells == 256))
         return fail(GVOM_ERR_ARG, "maps_tile_cells must be 64, 128 or 256");
-    if (!(t->trace_ahead == 0 || t->trace_ahead == 1)) return fail(GVOM_ERR_ARG, "trace_ahead must be 0 or 1");
+    if (!(t->step_pipeline >= 0 && t->step_pipeline <= 2)) return fail(GVOM_ERR_ARG, "step_pipeline must be 0, 1 or 2");
     std::lock_guard<std::mutex> lk(h->mu);
     h->tun.pts_block = t->points_per_block;
     h->tun.assign_per = t->assign_words_per_thread;
@@ -1479,7 +1571,7 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     h->tun.stats_bpsm = t->stats_blocks_per_sm;
     h->tun.step_overlap = t->step_overlap;
     h->tun.maps_tile = t->maps_tile_cells;
-    h->tun.trace_ahead = t->trace_ahead;
+    h->tun.step_pipeline = t->step_pipeline;
     return GVOM_OK;
 }
 
@@ -1492,7 +1584,7 @@ int gvom_get_tuning(GvomHandle *h, GvomTuning *t) {
     t->stats_blocks_per_sm = h->tun.stats_bpsm;
     t->step_overlap = h->tun.step_overlap;
     t->maps_tile_cells = h->tun.maps_tile;
-    t->trace_ahead = h->tun.trace_ahead;
+    t->step_pipeline = h->tun.step_pipeline;
     return GVOM_OK;
 }
 

@@ -32,9 +32,10 @@ struct Tuning {
     int stats_bpsm;     // k_merge_stats blocks per multiprocessor: 2, 4 or 8
     int step_overlap;   // gvom_step runs the index merge beside the statistics kernels: 0 or 1
     int maps_tile;      // k_maps2d tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) cells
-    int trace_ahead;    // gvom_step traces its scans beside the previous step's combine: 0 or 1
+    int step_pipeline;  // gvom_step: 0 one stream; 1 the trace beside the previous step's combine; 2 also the
+                        // rest of the process and the merge beside the previous step's columns and maps
 };
-constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1, 256, 1};
+constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1, 256, 2};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
 constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
@@ -211,8 +212,10 @@ cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int ns
                            cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part = 0);
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
 cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st);
+// `part`: 0 merge_stats, columns, maps2d; 1 merge_stats; 2 columns; 3 maps2d
+// (parts are launched without stage events)
 cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
-                                cudaEvent_t *ev);
+                                cudaEvent_t *ev, int part = 0);
 cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
                            cudaEvent_t *ev = nullptr);
 cudaError_t launch_debug_count(const int *idx, long long V, int *counts, int nblocks, cudaStream_t st);

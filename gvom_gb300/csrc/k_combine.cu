@@ -931,17 +931,22 @@ cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st) {
 
 // statistics merge, columns and 2-D maps (events ev[1..4] when timing)
 cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
-                                cudaEvent_t *ev) {
+                                cudaEvent_t *ev, int part) {
     const int X = mp.g.X;
+    if (part) ev = nullptr;
     if (ev) cudaEventRecord(ev[1], st);
-    by_nsrc<MergeStats>(mp, st);
+    if (part == 0 || part == 1) by_nsrc<MergeStats>(mp, st);
     if (ev) cudaEventRecord(ev[2], st);
-    dim3 gc((X + 31) / 32, (X + 7) / 8);
-    k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);
+    if (part == 0 || part == 2) {
+        dim3 gc((X + 31) / 32, (X + 7) / 8);
+        k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);
+    }
     if (ev) cudaEventRecord(ev[3], st);
-    if (m2.tile_cells == 64) launch_maps2d<4, 16>(m2, st);
-    else if (m2.tile_cells == 128) launch_maps2d<8, 16>(m2, st);
-    else launch_maps2d<8, 32>(m2, st);
+    if (part == 0 || part == 3) {
+        if (m2.tile_cells == 64) launch_maps2d<4, 16>(m2, st);
+        else if (m2.tile_cells == 128) launch_maps2d<8, 16>(m2, st);
+        else launch_maps2d<8, 32>(m2, st);
+    }
     if (ev) cudaEventRecord(ev[4], st);
     return cudaGetLastError();
 }

@@ -123,11 +123,13 @@ int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t
  * outputs) or gvom_combine_device (outputs_on_device != 0), with the same
  * results; no counterpart in the reference.  Submitted together, the index
  * merge of the combine runs beside the process call's statistics kernels
- * (it needs only the ring's index maps).  With trace_ahead (GvomTuning) the
- * step's ray tracing runs on a second stream as soon as the previous process
- * call is done with the per-scan scratch, beside the previous step's combine
- * when steps are submitted back to back; in graph mode the step is two
- * executable graphs (trace, rest), else one. */
+ * (it needs only the ring's index maps).  With step_pipeline (GvomTuning),
+ * steps submitted back to back overlap: at 1 a step's ray tracing runs on a
+ * second stream beside the previous step's combine; at 2 the rest of its
+ * process and its merge also run, on a third stream, beside the previous
+ * step's columns and 2-D maps.  The maps are complete in stream order of the
+ * instance stream either way; in graph mode each stream's part of a step is
+ * one executable graph. */
 int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device, double origin[3],
               int32_t *pos, int32_t *neg, double *roughness, int32_t *visibility, int32_t outputs_on_device);
 
@@ -218,7 +220,7 @@ int gvom_synchronize(GvomHandle *h);
  * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
 /* Launch shapes chosen by the autotuner (gvom_gb300/autotune.py); no
  * counterpart in the reference.  They change speed only, never results.
- * Defaults: 256, 8, 8, 4, 1, 256, 1. */
+ * Defaults: 256, 8, 8, 4, 1, 256, 2. */
 typedef struct GvomTuning {
     int32_t points_per_block;         /* point-parallel kernels: 128 or 256 */
     int32_t assign_words_per_thread;  /* index assignment: 4, 8 or 16 */
@@ -226,7 +228,8 @@ typedef struct GvomTuning {
     int32_t stats_blocks_per_sm;      /* statistics merge: 2, 4 or 8 */
     int32_t step_overlap;             /* gvom_step: index merge beside the statistics kernels, 0 or 1 */
     int32_t maps_tile_cells;          /* 2-D maps tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) */
-    int32_t trace_ahead;              /* gvom_step: trace a step's scans beside the previous step's combine, 0 or 1 */
+    int32_t step_pipeline;            /* gvom_step streams: 0 one; 1 the trace beside the previous step's combine;
+                                         2 also the process and merge beside the previous step's columns and maps */
 } GvomTuning;
 int gvom_set_tuning(GvomHandle *h, const GvomTuning *t);
 int gvom_get_tuning(GvomHandle *h, GvomTuning *t);

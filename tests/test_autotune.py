@@ -13,7 +13,7 @@ class FakeMapper:
     """Stage times depend on the tuning: each knob has one best value."""
 
     BEST = {"points_per_block": 128, "assign_words_per_thread": 16, "merge_planes_per_thread": 4,
-            "stats_blocks_per_sm": 8, "step_overlap": 0, "maps_tile_cells": 64, "trace_ahead": 0}
+            "stats_blocks_per_sm": 8, "step_overlap": 0, "maps_tile_cells": 64, "step_pipeline": 0}
 
     def __init__(self, params=(0.15, 0.15, 256, 64, 4, 1, .5, .5, .3, 2, 4, 1, 1, 1)):
         self.params = params
@@ -50,7 +50,7 @@ class FakeMapper:
     def step(self, b):
         # whole-step wall time stands in for the overlap knob
         import time
-        for knob in ("step_overlap", "trace_ahead"):
+        for knob in ("step_overlap", "step_pipeline"):
             if self.t[knob] != self.BEST[knob]:
                 time.sleep(0.002)
 
@@ -100,9 +100,9 @@ def test_every_launch_shape_gives_identical_maps(gpu_lib):
     params = w.gvom_args()[:4] + (3,) + w.gvom_args()[5:]
     shapes = [dict(AT.DEFAULT),
               {"points_per_block": 128, "assign_words_per_thread": 4, "merge_planes_per_thread": 16,
-               "stats_blocks_per_sm": 2, "step_overlap": 0, "maps_tile_cells": 64, "trace_ahead": 0},
+               "stats_blocks_per_sm": 2, "step_overlap": 0, "maps_tile_cells": 64, "step_pipeline": 0},
               {"points_per_block": 256, "assign_words_per_thread": 16, "merge_planes_per_thread": 4,
-               "stats_blocks_per_sm": 8, "step_overlap": 1, "maps_tile_cells": 128, "trace_ahead": 1}]
+               "stats_blocks_per_sm": 8, "step_overlap": 1, "maps_tile_cells": 128, "step_pipeline": 2}]
     results = []
     for t in shapes:
         g = Gvom(*params)

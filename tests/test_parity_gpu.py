@@ -272,12 +272,12 @@ def test_step_equals_process_then_combine(Gvom, graphs):
 
 
 @pytest.mark.parametrize("graphs", [False, True])
-@pytest.mark.parametrize("ahead", [0, 1])
-def test_steps_back_to_back_equal_sequential_calls(Gvom, graphs, ahead):
+@pytest.mark.parametrize("pipeline", [0, 1, 2])
+def test_steps_back_to_back_equal_sequential_calls(Gvom, graphs, pipeline):
     """Steps submitted without a host wait in between (device outputs), so that
-    with trace_ahead a step's ray tracing runs beside the previous step's
-    combine, with plain process / combine calls in the middle of the sequence:
-    every step's maps equal those of process_batch + combine_maps."""
+    with step_pipeline a step's work overlaps the previous step's, with plain
+    process / combine calls in the middle of the sequence and host-input steps
+    among them: every step's maps equal those of process_batch + combine_maps."""
     import torch
     from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
     w = WORKLOADS["small_32x512"]
@@ -286,7 +286,7 @@ def test_steps_back_to_back_equal_sequential_calls(Gvom, graphs, ahead):
     X = params[2]
     a, b = Gvom(*params), Gvom(*params)
     b.set_graphs(graphs)
-    b.set_tuning(dict(b.get_tuning(), trace_ahead=ahead))
+    b.set_tuning(dict(b.get_tuning(), step_pipeline=pipeline))
     dev = [torch.from_numpy(np.ascontiguousarray(s.points)).cuda() for s in scans]
     order = [[0], [1, 2], [3], [4], "plain", [5, 6], [0], [2], [1, 3], [4]]
     want, got = [], []
@@ -302,7 +302,8 @@ def test_steps_back_to_back_equal_sequential_calls(Gvom, graphs, ahead):
         want.append(a.combine_maps())
         outs = [torch.empty((X, X), dtype=d, device="cuda") for d in (torch.int32, torch.int32, torch.float64,
                                                                         torch.int32)]
-        origin = b.step([(dev[i], scans[i].ego, scans[i].transform) for i in idx], device_outputs=outs)
+        pts = (lambda i: scans[i].points) if k % 3 == 2 else (lambda i: dev[i])  # some steps with host inputs
+        origin = b.step([(pts(i), scans[i].ego, scans[i].transform) for i in idx], device_outputs=outs)
         got.append((origin, outs))
     torch.cuda.synchronize()
     for k, (ra, rb) in enumerate(zip(want, got)):
