@@ -403,7 +403,10 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
     # each step alone after an L2 flush (its latency), direct launches back to
     # back for comparison, and a pass with per-kernel CUDA events
     n_aux = max(10, min(n_steps, 300))
+    # (one step at a time: no overlap with the neighbouring steps either)
+    g.set_tuning(dict(tuning, step_pipeline=0))
     step_ms, t_flushed, pts_flushed, _, _, _ = timed(n_aux, graphs, False)
+    g.set_tuning(tuning)
     ms_direct, t_direct, pts_direct, _, _, _ = timed(n_aux, False, False, back_to_back=True)
     _, _, _, _, _, stages = timed(n_aux, False, True)
 
@@ -487,7 +490,7 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
                            "flush: l2_flushed_per_step")),
         "direct_launches": {"value": pts_direct / t_direct, "ms_per_step": 1e3 * t_direct / n_aux, "steps": n_aux},
         "l2_flushed_per_step": {"value": pts_flushed / t_flushed, "ms_per_step": 1e3 * t_flushed / n_aux,
-                                "steps": n_aux},
+                                "steps": n_aux, "step_pipeline": 0},
         "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
                        "e2e_p50": 1e3 * float(np.percentile(ref_times, 50)),
                        "e2e_p99": 1e3 * float(np.percentile(ref_times, 99))},

@@ -330,4 +330,81 @@ GX_HD bool gx_coord(float p, const ExactRes &R, long long o, float &end, long lo
     return gx_make_f32(0u, f24, fe - kk, frac);
 }
 
+// Number of iterations of the reference's ray-length loop
+//     L = 0; K = 0; while (L < R && K < cap) { K++; L = RN64(L + inc); }
+// (scripts/gvom.py:1206-1231: R = ray_length - 1, inc = |1.0 / slope|, both
+// float64), without float64 arithmetic.  After the first iteration L = inc
+// and every later value is a multiple of inc's ulp u0; L is kept as q 2^s u0
+// with q in [2^52, 2^53), so one addition is q + n + f / 2^s with
+// n = I >> s, f = I mod 2^s (I = inc / u0).  Inside one binade that sum
+// rounds the same way at every step -- q + n + (2f > 2^s) -- unless the
+// fraction is a tie, so runs of steps are taken at once up to the binade's
+// end or to R; ties and binade crossings are single steps, rounded to nearest
+// even at the grid of the result.  Requires R, inc finite, inc > 0.
+GX_HD unsigned long long gx_d2u(double d) {
+#ifdef __CUDA_ARCH__
+    return (unsigned long long)__double_as_longlong(d);
+#else
+    unsigned long long u;
+    memcpy(&u, &d, 8);
+    return u;
+#endif
+}
+
+GX_HD int gx_step_count(double R, double inc, int cap) {
+    if (!(R > 0.0) || cap <= 0) return 0;
+    const unsigned long long ib = gx_d2u(inc), rb = gx_d2u(R);
+    const int ie = (int)((ib >> 52) & 0x7ff), re = (int)((rb >> 52) & 0x7ff);
+    if (ie == 0 || ie == 0x7ff || re == 0x7ff) return -1;  // subnormal or non-finite: caller's float64 path
+    const unsigned long long I = (ib & 0xfffffffffffffull) | (1ull << 52);
+    // R / u0 = mR 2^(re - ie); R subnormal: exponent as for re = 1, no implicit bit
+    const unsigned long long mR = re ? ((rb & 0xfffffffffffffull) | (1ull << 52)) : (rb & 0xfffffffffffffull);
+    const int rsh = (re ? re : 1) - ie;
+    const unsigned long long top = 1ull << 53;
+    unsigned long long q = I;
+    int s = 0, K = 1;
+    while (true) {
+        // Rq = ceil(R / (u0 2^s)), clamped far above any q
+        unsigned long long Rq;
+        const int sh = rsh - s;
+        if (sh >= 10) Rq = ~0ull;
+        else if (sh >= 0) Rq = mR << sh;
+        else if (sh > -64) Rq = (mR >> -sh) + ((mR & ((1ull << -sh) - 1ull)) ? 1ull : 0ull);
+        else Rq = 1ull;
+        if (q >= Rq) return K;
+        if (K >= cap) return cap;
+        if (s >= 52) return -1;  // far beyond any ray; caller's float64 path
+        const unsigned long long n = I >> s, f = I & ((1ull << s) - 1ull), half = s ? 1ull << (s - 1) : 0ull;
+        if (!(s > 0 && f == half) && q + n + 1ull < top) {
+            // a run of steps inside the binade, each adding d
+            const unsigned long long d = n + ((s > 0 && f > half) ? 1ull : 0ull);
+            const unsigned long long tb = (top - 2ull - n - q) / d + 1ull;  // steps whose exact sum stays below 2^53
+            const unsigned long long tr = Rq == ~0ull ? ~0ull : (Rq - q + d - 1ull) / d;  // steps until q >= Rq
+            unsigned long long t = tb < tr ? tb : tr;
+            if (t > (unsigned long long)(cap - K)) t = (unsigned long long)(cap - K);
+            q += t * d;
+            K += (int)t;
+            continue;
+        }
+        // one step: exact sum T + f / 2^s in units of 2^s
+        const unsigned long long T = q + n;
+        unsigned long long nq;
+        if (T < top) {  // stays below 2^53: round at grid 2^s
+            const bool up = s > 0 && (f > half || (f == half && (T & 1ull)));
+            nq = T + (up ? 1ull : 0ull);
+        } else {  // crosses into the next binade: grid 2^(s+1)
+            if (!(T & 1ull)) nq = T >> 1;
+            else if (f > 0ull) nq = (T >> 1) + 1ull;
+            else nq = ((T >> 1) & 1ull) ? (T >> 1) + 1ull : (T >> 1);  // tie: to even
+            s++;
+        }
+        if (nq >= top) {  // rounded up to the next power of two
+            nq >>= 1;
+            s++;
+        }
+        q = nq;
+        K++;
+    }
+}
+
 }  // namespace gvom

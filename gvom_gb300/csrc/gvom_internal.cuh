@@ -60,8 +60,8 @@ struct Geom {
     long long V, Vext;
 };
 
-struct ScanCounters {
-    int C;                      // occupied voxels allocated
+struct __align__(8) ScanCounters {
+    int C;                      // occupied voxels allocated (k_assign reserves C and pts with one 64-bit atomic)
     int pts;                    // points placed into cell groups
     int overflow;               // capacity exceeded (should never happen)
     int pad;
@@ -112,6 +112,7 @@ struct ProcessConst {
     int num_sms;           // multiprocessors of the device (persistent grids)
     int assign_per;        // Tuning::assign_per
     unsigned long long xe_magic;  // floor((2^64 - 1) / Xe) + 1 (divisions by the extended row length)
+    int adv[3];            // extended coordinates (x, y, z) of cell index 256
 };
 
 struct MergeSrc {
@@ -269,7 +270,8 @@ __device__ __forceinline__ bool in_sliver(float p) {
 // the count is ceil(R / inc).  R / inc = R |sk| (1 + O(2^-53)); R = rl - 1 is
 // exact in float32 for 1 < rl < 2^23 and the float32 product adds at most
 // 2^-24 relative error, so a 2^-18 relative margin decides it; otherwise the
-// float64 loop is replayed exactly.
+// float64 loop's count is computed exactly in integer arithmetic
+// (gx_step_count), or replayed in float64 where that declines.
 __device__ __forceinline__ int ray_step_count(float rl, float sk, int cap) {
     if (!(rl > 1.0f)) return 0;  // R <= 0 (or NaN)
     if (rl < 8388608.0f) {
@@ -281,6 +283,8 @@ __device__ __forceinline__ int ray_step_count(float rl, float sk, int cap) {
     }
     const double R = __dsub_rn((double)rl, 1.0);
     const double inc = fabs(__ddiv_rn(1.0, (double)sk));
+    const int Kx = gx_step_count(R, inc, cap);  // the float64 loop's count in integer arithmetic
+    if (Kx >= 0) return Kx;
     double L = 0.0;
     int K = 0;
     while (L < R && K < cap) {

@@ -277,7 +277,10 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
 }
 
 template <int NSRC>
-__global__ void __launch_bounds__(256) k_merge_stats(const __grid_constant__ MergeParams mp) {
+#ifndef GVOM_MERGE_STATS_MINB
+#define GVOM_MERGE_STATS_MINB 1  // minimum resident blocks per SM asked of the register allocator
+#endif
+__global__ void __launch_bounds__(256, GVOM_MERGE_STATS_MINB) k_merge_stats(const __grid_constant__ MergeParams mp) {
     const int n = *mp.out_count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         merge_voxel<NSRC>(mp, mp.list[i]);
@@ -331,14 +334,21 @@ __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnP
         }
         if (zmin >= 0 && zmin < Z && zmax >= 0 && zmax < Z) {
             long long nn = 0, dens = 0;
-#pragma unroll 4
-            for (int z = zmin; z <= zmax; z++) {
-                const int idx = cp.idx[x + y * X + z * plane];
-                if (idx >= 0) {
-                    const float2 ht = reinterpret_cast<const float2 *>(&cp.rec[idx])[5];  // hit, total
-                    const int hit = __float_as_int(ht.x);
+            // 16 planes at a time: every index load, then every record load, in flight together
+            for (int z0 = zmin; z0 <= zmax; z0 += 16) {
+                int idx[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++) idx[j] = z0 + j <= zmax ? cp.idx[x + y * X + (z0 + j) * plane] : -1;
+                float2 ht[16];
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    ht[j] = idx[j] >= 0 ? reinterpret_cast<const float2 *>(&cp.rec[idx[j]])[5]  // hit, total
+                                        : make_float2(0.f, 0.f);
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int hit = __float_as_int(ht[j].x);
                     if (hit > 10) {
-                        nn += __float_as_int(ht.y);
+                        nn += __float_as_int(ht[j].y);
                         dens += hit;
                     }
                 }

@@ -173,7 +173,9 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
     if (active) {
         const long long gi = sd.pt_base + i;
         float4 rec = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
-        int rank = 0;
+        // the hit atomic's return value (the point's rank in its cell) is read
+        // only after the march, which hides the atomic's round trip
+        unsigned long long hit_old = 0;
         PT x, y, z;
         load_point<PT>(sd, i, x, y, z);
         if (sd.tmode) transform_point<PT>(sd, x, y, z);
@@ -226,8 +228,7 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
                 const bool in_grid = bx >= 0 && bx < g.X && by >= 0 && by < g.X && bz >= 0 && bz < g.Z;
                 const int cell = (bx + g.exy) + (by + g.exy) * Xe + (bz + g.ez) * XeXe;
                 const unsigned long long inc = in_grid ? ((1ull << 32) | 1ull) : (1ull << 32);
-                const unsigned long long old = atomicAdd(&sd.cnt[cell], inc);
-                rank = (int)(old >> 32);
+                hit_old = atomicAdd(&sd.cnt[cell], inc);
                 rec = make_float4(fr0, fr1, fr2, __int_as_float(cell));
                 n_hit = in_grid;
             }
@@ -325,12 +326,26 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
             n_steps = st;
         }
         prec[gi] = rec;
-        prank[gi] = rank;
+        prank[gi] = (int)(hit_old >> 32);
     }
-    warp_add_u64(&sd.ctr->valid, n_valid);
-    warp_add_u64(&sd.ctr->hits, n_hit);
-    warp_add_u64(&sd.ctr->steps, n_steps);
+    // scan counters: one atomic per block and counter (valid, hits, steps are
+    // adjacent words)
+    __shared__ unsigned long long wsum[3][8];
+    {
+        unsigned long long v3[3] = {n_valid, n_hit, n_steps};
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v3[j] += __shfl_down_sync(0xffffffffu, v3[j], o);
+            if (lane_id() == 0) wsum[j][threadIdx.x >> 5] = v3[j];
+        }
+    }
     __syncthreads();
+    if (threadIdx.x < 3) {
+        unsigned long long t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += wsum[threadIdx.x][w];
+        if (t) atomicAdd(&sd.ctr->valid + threadIdx.x, t);
+    }
     if (kHash)
         for (int k = threadIdx.x; k < (1 << kHashBits); k += blockDim.x) {
             const unsigned t = htag[k];
@@ -431,19 +446,43 @@ __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __g
     block_scan2(n_occ, n_pts, eo, ep, to, tp);
     __shared__ int bases[2];
     if (threadIdx.x == 0) {
-        bases[0] = to ? atomicAdd(&sd.ctr->C, to) : 0;
-        bases[1] = tp ? atomicAdd(&sd.ctr->pts, tp) : 0;
+        // C and pts are adjacent 32-bit words: one 64-bit atomic reserves both
+        // (C stays far below 2^32, so nothing carries into pts)
+        unsigned long long old = 0;
+        if (to | tp)
+            old = atomicAdd(reinterpret_cast<unsigned long long *>(&sd.ctr->C),
+                            ((unsigned long long)(unsigned)tp << 32) | (unsigned)to);
+        bases[0] = (int)(unsigned)(old & 0xffffffffull);
+        bases[1] = (int)(unsigned)(old >> 32);
     }
     __syncthreads();
     int c = bases[0] + eo, off = bases[1] + ep;
+    // the words' extended coordinates: one division for the first, then
+    // steps of 256 cells with carries (pc.adv = coordinates of 256)
+    int ex, ey, ez;
+    {
+        const unsigned row = pc.xe_magic ? (unsigned)__umul64hi((unsigned long long)base, pc.xe_magic) : (unsigned)base;
+        const unsigned zz = pc.xe_magic ? (unsigned)__umul64hi((unsigned long long)row, pc.xe_magic) : row;
+        ex = (int)((unsigned)base - row * (unsigned)g.Xe);
+        ey = (int)(row - zz * (unsigned)g.Xe);
+        ez = (int)zz;
+    }
 #pragma unroll
     for (int k = 0; k < PER; k++) {
         const int e = base + k * 256;
         if (e >= Vext) break;
         const int hit = (int)(v[k] >> 32);
         const int total = (int)(v[k] & 0xffffffffull);
-        int gid;
-        if (cell_in_grid((unsigned)e, g, pc.xe_magic, gid)) {
+        const int gx = ex - g.exy, gy = ey - g.exy, gz = ez - g.ez;
+        const int gid = gx + g.X * (gy + g.X * gz);
+        ex += pc.adv[0];
+        const int cx = ex >= g.Xe;
+        ex -= cx ? g.Xe : 0;
+        ey += pc.adv[1] + cx;
+        const int cy = ey >= g.Xe;
+        ey -= cy ? g.Xe : 0;
+        ez += pc.adv[2] + cy;
+        if ((unsigned)gx < (unsigned)g.X && (unsigned)gy < (unsigned)g.X && (unsigned)gz < (unsigned)g.Z) {
             if (hit > 0) {
                 if (c < sd.rec_cap) {
                     VoxelRec *r = &sd.rec[c];
@@ -655,6 +694,42 @@ struct NbAcc {
         C5 = __fadd_rn(__fadd_rn(C5, cm.c[5]), __fmul_rn(__fmul_rn(d2, d2), f));
         n = nn;
     }
+    // Chan combination with another partial sum in the same voxel frame
+    __device__ __forceinline__ void merge(const NbAcc &o) {
+        if (o.n == 0.f) return;
+        if (n == 0.f) {
+            *this = o;
+            return;
+        }
+        const float nn = __fadd_rn(n, o.n);
+        const float d0 = __fsub_rn(o.m0, m0), d1 = __fsub_rn(o.m1, m1), d2 = __fsub_rn(o.m2, m2);
+        const float wb = __fdiv_rn(o.n, nn);
+        const float f = __fmul_rn(n, wb);
+        m0 = __fadd_rn(m0, __fmul_rn(d0, wb));
+        m1 = __fadd_rn(m1, __fmul_rn(d1, wb));
+        m2 = __fadd_rn(m2, __fmul_rn(d2, wb));
+        C0 = __fadd_rn(__fadd_rn(C0, o.C0), __fmul_rn(__fmul_rn(d0, d0), f));
+        C1 = __fadd_rn(__fadd_rn(C1, o.C1), __fmul_rn(__fmul_rn(d0, d1), f));
+        C2 = __fadd_rn(__fadd_rn(C2, o.C2), __fmul_rn(__fmul_rn(d0, d2), f));
+        C3 = __fadd_rn(__fadd_rn(C3, o.C3), __fmul_rn(__fmul_rn(d1, d1), f));
+        C4 = __fadd_rn(__fadd_rn(C4, o.C4), __fmul_rn(__fmul_rn(d1, d2), f));
+        C5 = __fadd_rn(__fadd_rn(C5, o.C5), __fmul_rn(__fmul_rn(d2, d2), f));
+        n = nn;
+    }
+    __device__ __forceinline__ NbAcc shfl_down(int delta) const {
+        NbAcc o;
+        o.n = __shfl_down_sync(0xffffffffu, n, delta);
+        o.m0 = __shfl_down_sync(0xffffffffu, m0, delta);
+        o.m1 = __shfl_down_sync(0xffffffffu, m1, delta);
+        o.m2 = __shfl_down_sync(0xffffffffu, m2, delta);
+        o.C0 = __shfl_down_sync(0xffffffffu, C0, delta);
+        o.C1 = __shfl_down_sync(0xffffffffu, C1, delta);
+        o.C2 = __shfl_down_sync(0xffffffffu, C2, delta);
+        o.C3 = __shfl_down_sync(0xffffffffu, C3, delta);
+        o.C4 = __shfl_down_sync(0xffffffffu, C4, delta);
+        o.C5 = __shfl_down_sync(0xffffffffu, C5, delta);
+        return o;
+    }
     __device__ __forceinline__ void store(VoxelRec *r, float mh) const {
         float4 *o = reinterpret_cast<float4 *>(r);
         o[0] = make_float4(__fadd_rn(m0, 0.5f), __fadd_rn(m1, 0.5f), __fadd_rn(m2, 0.5f), __fdiv_rn(C0, n));
@@ -664,9 +739,11 @@ struct NbAcc {
     }
 };
 
-// E3 = 1: the 3 x 3 x 3 neighbourhood of eigen distances (1, 1) with every
-// load unrolled (27 count words, then the moments of the cells that hold
-// points); E3 = 0: any distances, cell by cell.  Same cells, same order.
+// E3 = 1: the 3 x 3 x 3 neighbourhood of eigen distances (1, 1), four lanes
+// per voxel: lane j of the group sums cells 7j .. 7j + 6 (z-major; the
+// voxel's own cell, 13, in lane 1) with every count load issued first, and
+// the four partial sums are combined as (0 + 1) + (2 + 3).  E3 = 0: any
+// distances, one thread per voxel, cell by cell.
 template <int NS, int E3>
 __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
                                                     const CellMom *__restrict__ mom) {
@@ -674,6 +751,45 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
     const Geom g = pc.g;
     const int C = min(*(volatile int *)&sd.ctr->C, (int)sd.rec_cap);
     const CellMom *__restrict__ M = mom + sd.pt_base;
+    if (E3) {
+        const int lane = (int)lane_id(), sub = lane & 3;
+        const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+        const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+        const int XeXe = g.Xe * g.Xe;
+        for (int base = warp * 8; base < C; base += nwarps * 8) {  // warp-uniform trip count
+            const int c = base + (lane >> 2);
+            NbAcc a;
+            a.init();
+            float mh = 1.0f;
+            if (c < C) {
+                const int gid = __float_as_int(sd.rec[c].aux[0]);
+                const int x = gid % g.X, y = (gid / g.X) % g.X, z = gid / (g.X * g.X);
+                const int e0 = (x + g.exy) + (y + g.exy) * g.Xe + (z + g.ez) * XeXe;
+                unsigned long long v[7];
+#pragma unroll
+                for (int j = 0; j < 7; j++) {
+                    const int k = sub * 7 + j;
+                    const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+                    v[j] = k < 27 ? __ldg(&sd.cnt[e0 + dx + dy * g.Xe + dz * XeXe]) : 0ull;
+                }
+#pragma unroll
+                for (int j = 0; j < 7; j++) {
+                    const int k = sub * 7 + j;
+                    if (!(v[j] & 0xffffffffull)) continue;
+                    const CellMom cm = M[(int)(v[j] >> 32)];
+                    if (k == 13) mh = cm.min_h;
+                    a.add(cm, k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1);
+                }
+            }
+            NbAcc o = a.shfl_down(1);
+            if (!(sub & 1)) a.merge(o);
+            o = a.shfl_down(2);
+            if (sub == 0) a.merge(o);
+            mh = __shfl_sync(0xffffffffu, mh, (lane & ~3) | 1);
+            if (c < C && sub == 0) a.store(&sd.rec[c], mh);
+        }
+        return;
+    }
     for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
         VoxelRec *r = &sd.rec[c];
         const int gid = __float_as_int(r->aux[0]);
@@ -682,31 +798,15 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
         NbAcc a;
         a.init();
         float mh = 1.0f;
-        if (E3) {
-            unsigned long long v[27];
-#pragma unroll
-            for (int k = 0; k < 27; k++) {
-                const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
-                v[k] = __ldg(&sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe]);
-            }
-#pragma unroll
-            for (int k = 0; k < 27; k++) {
-                if (!(v[k] & 0xffffffffull)) continue;
-                const CellMom cm = M[(int)(v[k] >> 32)];
-                if (k == 13) mh = cm.min_h;
-                a.add(cm, k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1);
-            }
-        } else {
-            for (int dz = -g.ez; dz <= g.ez; dz++)
-                for (int dy = -g.exy; dy <= g.exy; dy++)
-                    for (int dx = -g.exy; dx <= g.exy; dx++) {
-                        const unsigned long long v = sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe];
-                        if (!(v & 0xffffffffull)) continue;
-                        const CellMom cm = M[(int)(v >> 32)];
-                        if (dx == 0 && dy == 0 && dz == 0) mh = cm.min_h;
-                        a.add(cm, dx, dy, dz);
-                    }
-        }
+        for (int dz = -g.ez; dz <= g.ez; dz++)
+            for (int dy = -g.exy; dy <= g.exy; dy++)
+                for (int dx = -g.exy; dx <= g.exy; dx++) {
+                    const unsigned long long v = sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe];
+                    if (!(v & 0xffffffffull)) continue;
+                    const CellMom cm = M[(int)(v >> 32)];
+                    if (dx == 0 && dy == 0 && dz == 0) mh = cm.min_h;
+                    a.add(cm, dx, dy, dz);
+                }
         a.store(r, mh);
     }
 }
@@ -762,9 +862,10 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
     mark(3);
     k_cell_moments<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank, sorted, mom);
     mark(4);
-    const int want = (max_n + 255) / 256;
-    dim3 gs((unsigned)std::max(1, std::min(want, 152 * 8)), pc.nscans);
-    if (pc.g.exy == 1 && pc.g.ez == 1) k_voxel_stats<NS, 1><<<gs, 256, 0, st>>>(pc, tab, mom);
+    const bool e3 = pc.g.exy == 1 && pc.g.ez == 1;  // four lanes per voxel
+    const long long want = ((e3 ? 4LL : 1LL) * max_n + 255) / 256;
+    dim3 gs((unsigned)std::max<long long>(1, std::min<long long>(want, (long long)pc.num_sms * 8)), pc.nscans);
+    if (e3) k_voxel_stats<NS, 1><<<gs, 256, 0, st>>>(pc, tab, mom);
     else k_voxel_stats<NS, 0><<<gs, 256, 0, st>>>(pc, tab, mom);
     mark(5);
     k_cleanup<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);

@@ -74,5 +74,47 @@ int main(int argc, char **argv) {
         }
     }
     printf("%ld cases, %ld declined (non-normal input), %ld mismatches\n", total, declined, bad);
-    return bad ? 1 : 0;
+
+    // ray step count: gx_step_count against the float64 loop it replaces,
+    // on random rays and on rays whose length sits at a step boundary
+    long sbad = 0, stotal = 0, sdecl = 0;
+    std::uniform_int_distribution<int> Ucap(1, 4200);
+    for (long i = 0; i < 40 * n; i++) {
+        const int mode = (int)(i % 5);
+        const double u = U(g), u2 = U(g);
+        // sk: the dominant component of a unit float32 direction, |sk| in [1/sqrt(3), 1]
+        float sk = (float)(0.57735026918962573 + u * (1.0 - 0.57735026918962573));
+        if (u2 < 0.5) sk = -sk;
+        if (mode == 3) sk = (u2 < 0.5) ? -1.0f : 1.0f;
+        double inc = std::fabs(1.0 / (double)sk);
+        if (mode == 4 && (i / 5) % 2 == 0) {
+            // increments whose mantissa ends at bit s0: additions tie at the 2^s0 grid
+            const int s0 = 1 + (int)(g() % 13);
+            inc = 1.0 + std::ldexp((double)(2 * (g() % 1000003) + 1), s0 - 1 - 52 + 1) * (u2 < 0.5 ? 1.0 : 0.5);
+        }
+        float rl;
+        int cap = mode == 4 ? Ucap(g) : 520;
+        if (mode == 0) rl = (float)(1.0 + U(g) * 600.0);
+        else if (mode == 1 || mode == 3) {  // (rl - 1) |sk| within 1e-5 of an integer: the float32 margin fails here
+            const double k = std::floor(U(g) * 400.0) + 1.0;
+            rl = (float)(1.0 + (k + (U(g) - 0.5) * 2e-5) * inc);
+        } else if (mode == 2) rl = (float)(1.0 + U(g) * 3.0);          // short rays
+        else rl = (float)(1.0 + U(g) * 8000.0);                         // long rays, any cap
+        const double R = (double)rl - 1.0;
+        double L = 0.0;
+        int Kref = 0;
+        while (L < R && Kref < cap) {
+            Kref++;
+            L = L + inc;
+        }
+        const int K = gx_step_count(R, inc, cap);
+        stotal++;
+        if (K < 0) { sdecl++; continue; }
+        if (K != Kref) {
+            if (sbad < 20) printf("STEP MISMATCH rl=%.9g sk=%.9g cap=%d: %d vs %d\n", rl, sk, cap, K, Kref);
+            sbad++;
+        }
+    }
+    printf("%ld step-count cases, %ld declined, %ld step-count mismatches\n", stotal, sdecl, sbad);
+    return (bad || sbad) ? 1 : 0;
 }

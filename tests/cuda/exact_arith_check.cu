@@ -63,6 +63,15 @@ __global__ void check(double res, ExactRes R, int mode, unsigned long long seed,
                 while (L < R && Kref < (1 << 20)) { Kref++; L = __dadd_rn(L, inc); }
             }
             if (K != Kref) rs_bad++;
+            // rays whose length sits at a step boundary (the float32 margin fails): the
+            // integer count of the float64 loop, on the device, against that loop
+            const double incb = fabs(__ddiv_rn(1.0, (double)sk));
+            const float rb = (float)(1.0 + (floor(u * 500.0) + 1.0 + (u2 - 0.5) * 2e-5) * incb);
+            const double Rb = __dsub_rn((double)rb, 1.0);
+            int Kb = 0;
+            double Lb = 0.0;
+            while (Lb < Rb && Kb < 520) { Kb++; Lb = __dadd_rn(Lb, incb); }
+            if (gx_step_count(Rb, incb, 520) != Kb || ray_step_count(rb, sk, 520) != Kb) rs_bad++;
         }
         // ray index fast floor
         {
