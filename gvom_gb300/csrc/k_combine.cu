@@ -408,6 +408,19 @@ __device__ __forceinline__ double slope_angle(double a, double m, double im) {
     return (double)atan2f((float)a, (float)im);
 }
 
+// log and atan2 of exact float64 values in float32: the results are compared
+// at 1e-3 relative, and the float32 functions stay within a few 1e-7 relative
+// here.  log(err) near err = 1 goes through log1p of the exact err - 1;
+// values outside the float32 range keep float64.  err = 0 stays 0.
+__device__ __forceinline__ double rough_of(double err) {
+    if (err > 0.0) {
+        if (err >= 0.5 && err <= 2.0) return (double)log1pf((float)__dsub_rn(err, 1.0));
+        if (err > 1e-30 && err < 1e30) return (double)logf((float)err);
+        return log(err);
+    }
+    return err;
+}
+
 // __calculate_slope (scripts/gvom.py:717-805) in the reference's float64
 // operation order up to the final log / atan2.
 template <int kSY>
@@ -459,16 +472,7 @@ __device__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY
         err = __dadd_rn(err, __dmul_rn(e, e));
     }
     err = __ddiv_rn(err, (double)n_good);
-    // log and atan2 of these exact float64 values in float32: the results are
-    // compared at 1e-3 relative, and the float32 functions stay within a few
-    // 1e-7 relative here.  log(err) near err = 1 goes through log1p of the
-    // exact err - 1; values outside the float32 range keep float64.
-    if (err > 0.0) {
-        if (err >= 0.5 && err <= 2.0) err = (double)log1pf((float)__dsub_rn(err, 1.0));
-        else if (err > 1e-30 && err < 1e30) err = (double)logf((float)err);
-        else err = log(err);
-    }
-    rough = err;
+    rough = rough_of(err);
     const double im = __ddiv_rn(1.0, m);
     slx = slope_angle(a0, m, im);
     sly = slope_angle(a1, m, im);
@@ -548,20 +552,22 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
     const int cell = x0 * X + y0;
     const bool known = kn[tx][ty];
 
-    // slope / roughness: float32 plane fit where every neighbour height comes
-    // from an occupied voxel (height differences are then exact sums of a
-    // voxel count and an in-voxel fraction); the reference's float64 sequence
-    // where a neighbour is a robot-disc height or the float32 fit is near a
-    // cancellation (singular normal matrix, residual far below the height
-    // spread, log near 0, a slope component near 0)
+    // slope / roughness: a float32 plane fit on the neighbours' height
+    // differences (exact sums of a voxel count and an in-voxel fraction, or
+    // a float64 difference where a neighbour is a robot-disc height); the
+    // reference's float64 sequence where the fit is near a cancellation
+    // (singular normal matrix, residual far below the height spread, log near
+    // 0, a slope component near 0); closed form where every neighbour has
+    // the same height
     double rough = -1.0, slx = 0.0, sly = 0.0;
     bool need_exact = false;
     {
         const int xl = max(0, x0 - 1), xh = min(X, x0 + 2), yl = max(0, y0 - 1), yh = min(X, y0 + 2);
-        int n_good = 0, sxi = 0, syi = 0;
-        bool all_vox = true;
+        int n_good = 0, sxi = 0, syi = 0, sxxi = 0, syyi = 0, sxyi = 0;
+        bool all_vox = true, all_eq = true;
         int zr = 0;
         float mr = 0.f;
+        double h0 = 0.0;
         for (int xx = xl; xx < xh; xx++)
             for (int yy = yl; yy < yh; yy++) {
                 const int sx = xx - x0t + kHalo, sy = yy - y0t + kHalo;
@@ -569,15 +575,37 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
                     if (n_good == 0) {
                         zr = szl[sx][sy];
                         mr = sml[sx][sy];
+                        h0 = sh[sx][sy];
                     }
                     all_vox = all_vox && szl[sx][sy] >= 0;
+                    all_eq = all_eq && sh[sx][sy] == h0;
                     n_good++;
                     sxi += xx - x0;
                     syi += yy - y0;
+                    sxxi += (xx - x0) * (xx - x0);
+                    syyi += (yy - y0) * (yy - y0);
+                    sxyi += (xx - x0) * (yy - y0);
                 }
             }
-        if (valid && n_good >= 3) {
-            bool exact = !all_vox;
+        // the neighbours' offsets are not collinear (the float64 normal matrix is then regular)
+        const int dxx = n_good * sxxi - sxi * sxi, dyy = n_good * syyi - syi * syi, dxy = n_good * sxyi - sxi * syi;
+        if (valid && n_good >= 3 && all_eq && dxx * dyy - dxy * dxy != 0) {
+            // Every known neighbour has the same height h (the robot disc, or a
+            // flat floor): in the float64 sequence every residual height is
+            // dz = h - mean(h), so sxz and syz are dz times a sum of rounded
+            // offsets from their mean (|sum| < 1e-13 m), the fitted slopes stay
+            // below 1e-12 |dz| / res and err = dz^2 (1 + O(1e-13)).  So slope
+            // 0 and roughness log(dz^2), with dz from the reference's own
+            // sequential mean -- equal to the float64 sequence far inside the
+            // 1e-3 tolerance, without its ~350 dependent float64 operations.
+            double sum = 0.0;
+            for (int j = 0; j < n_good; j++) sum = __dadd_rn(sum, h0);
+            const double dz = __dsub_rn(h0, __ddiv_rn(sum, (double)n_good));
+            rough = rough_of(__dmul_rn(dz, dz));
+            slx = 0.0;
+            sly = 0.0;
+        } else if (valid && n_good >= 3) {
+            bool exact = false;
             float a0 = 0.f, a1 = 0.f, m = 1.f, err = 0.f, szz = 0.f;
             const float nf = (float)n_good;
             if (!exact) {
@@ -592,7 +620,10 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
                         if (kn[sx][sy]) {
                             dxs[i] = ((float)(xx - x0) - cx) * res;
                             dys[i] = ((float)(yy - y0) - cy) * res;
-                            dzs[i] = ((sml[sx][sy] - mr) + (float)(szl[sx][sy] - zr)) * zres;
+                            // from voxels: an exact count plus a fraction; with a robot-disc
+                            // height: the float64 difference, rounded once
+                            dzs[i] = all_vox ? ((sml[sx][sy] - mr) + (float)(szl[sx][sy] - zr)) * zres
+                                             : (float)__dsub_rn(sh[sx][sy], h0);
                             zsum += dzs[i];
                             i++;
                         }
@@ -633,7 +664,10 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
                 // a slope component much smaller than the other is ill-conditioned in any
                 // precision: take the reference's float64 sequence for it
                 const float big = fmaxf(fabsf(sxf), fabsf(syf)), small = fminf(fabsf(sxf), fabsf(syf));
-                exact = !(err > 1e-4f * (szz / nf)) || fabsf(rf) < 1.0f || small < 5e-3f * big || big < 2e-3f;
+                // the residual keeps at least 1e-4 of the height spread, so err is
+                // good to ~1e-5 relative and log(err) to ~1e-5 absolute: exact where
+                // that is not far below 1e-3 of |log err|
+                exact = !(err > 1e-4f * (szz / nf)) || fabsf(rf) < 0.1f || small < 5e-3f * big || big < 2e-3f;
             }
             if (exact) {
                 need_exact = true;
