@@ -119,7 +119,14 @@ struct GvomHandle {
     cudaStream_t own = nullptr, st = nullptr;
     std::mutex mu;
     std::vector<Slot> slots;
-    long long buffer_index = 0, last_buffer_index = 0;
+    long long buffer_index = 0, last_buffer_index = 0;  // the reference's ring positions (mod B)
+    // physical slots: B + E (E = the most scans one call processes), so a
+    // call's new scans never overwrite a slot that the previous combine reads;
+    // scan number n lives in physical slot n mod P, and phys_of maps a ring
+    // position to the physical slot of its scan (-1: none yet)
+    int P = 0;
+    std::vector<int> phys_of;
+    long long scans_total = 0;
     double ego[3] = {0, 0, 0};
     // combined map, double buffered (current / previous)
     int *cidx[2] = {nullptr, nullptr};
@@ -163,8 +170,9 @@ struct GvomHandle {
     // replayed through an executable graph updated in place
     bool graphs = false;
     // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ merge at
-    // level 2), [5] its columns and maps (level 2)
-    cudaGraphExec_t gexec[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // level 2), [5] its columns and maps (levels 2, 3), [6] its k_assign, [7] the rest of its process,
+    // [8] its index merge, [9] its statistics merge (level 3)
+    cudaGraphExec_t gexec[10] = {};
     // a step forks the index merge onto `side` once the index maps are done
     cudaStream_t side = nullptr;
     cudaEvent_t ev_idx = nullptr, ev_join = nullptr;
@@ -180,6 +188,13 @@ struct GvomHandle {
     // sets st_dirty: the next level-2 step first orders `tr` and `bs` after
     // it (ev_host).
     cudaStream_t tr = nullptr, bs = nullptr;
+    // level 3: the merge of step k (index merge after ev_idx, statistics merge
+    // after ev_b1) runs on `mg` beside the process of step k + 1, whose
+    // k_assign waits for the merge that last read the physical slots it
+    // writes, two steps back (ev_b2[parity])
+    cudaStream_t mg = nullptr;
+    cudaEvent_t ev_b1 = nullptr, ev_b2[2] = {nullptr, nullptr};
+    int spar = 0;
     cudaEvent_t ev_scratch[2] = {nullptr, nullptr};  // the process call that last used the set is done with it
     cudaEvent_t ev_traced = nullptr, ev_merged = nullptr, ev_host = nullptr;
     cudaEvent_t ev_cols[2] = {nullptr, nullptr};
@@ -427,7 +442,7 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
     int *slot_of = pl.slot_of;
     for (int i = 0; i < k; i++) {
         const ScanIn &s = scans[i];
-        const int slot = (int)((h->buffer_index + i) % h->B);
+        const int slot = (int)((h->scans_total + i) % h->P);  // physical; ring position (buffer_index + i) mod B
         slot_of[i] = slot;
         if ((rc = ensure_slot(h, slot, s.n))) return rc;
         ScanDesc &d = table[i];
@@ -497,11 +512,11 @@ int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bo
                  cudaStream_t st = nullptr) {
     if (!st) st = h->st;
     ScanCounters *ctr = h->d_ctr + pl.set * kMaxBatch;
-    if (part != 2) CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(ScanCounters) * pl.k, st));
+    if (part == 0 || part == 1) CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(ScanCounters) * pl.k, st));
     CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec[pl.set], h->prank[pl.set], h->sorted,
                             h->moments, st, (timing && !part) ? h->timer.begin(0, kProcessKernels) : nullptr,
                             h->tun.pts_block, after_assign, part));
-    if (part == 1) return GVOM_OK;
+    if (part == 1 || part == 3) return GVOM_OK;
     for (int i = 0; i < pl.k; i++)
         CUDA_TRY(cudaMemcpyAsync(h->d_slotC + pl.slot_of[i], &ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
                                  st));
@@ -516,8 +531,10 @@ void commit_scans(GvomHandle *h, const ProcPlan &pl) {
         sl.valid = true;
     }
     for (int a = 0; a < 3; a++) h->ego[a] = pl.last_ego[a];
-    h->last_buffer_index = pl.slot_of[pl.k - 1];
-    h->buffer_index = (pl.slot_of[pl.k - 1] + 1) % h->B;
+    for (int i = 0; i < pl.k; i++) h->phys_of[(h->buffer_index + i) % h->B] = pl.slot_of[i];
+    h->last_buffer_index = (h->buffer_index + pl.k - 1) % h->B;
+    h->buffer_index = (h->buffer_index + pl.k) % h->B;
+    h->scans_total += pl.k;
     h->last_ctr = pl.set * kMaxBatch + pl.k - 1;
     h->sset = pl.set ^ 1;
 }
@@ -595,13 +612,15 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     g.V = (long long)g.X * g.X * g.Z;
     g.Vext = ext_cells(g);
     h->B = params->buffer_size;
-    h->slots.resize(h->B);
+    h->P = h->B + std::min(h->B, kMaxBatch);
+    h->slots.resize(h->P);
+    h->phys_of.assign(h->B, -1);
     cudaDeviceGetAttribute(&h->pageable_access, cudaDevAttrPageableMemoryAccess, dev);
     if (cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || h->num_sms < 1)
         h->num_sms = 1;
     // admission: the resident footprint must fit in free device memory with margin
     const long long X2 = (long long)g.X * g.X;
-    const long long need = (long long)h->B * g.V * 4 + 2 * g.V * (4 + (long long)sizeof(VoxelRec)) + g.V * 4 +
+    const long long need = (long long)h->P * g.V * 4 + 2 * g.V * (4 + (long long)sizeof(VoxelRec)) + g.V * 4 +
                            g.Vext * 8 +
                            X2 * (6 * 8 + 4 * 4) + (64LL << 20);
     size_t fr = 0, tot = 0;
@@ -628,6 +647,10 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
         cudaStreamCreateWithPriority(&h->tr, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
         cudaStreamCreateWithPriority(&h->bs, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&h->mg, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_b1, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_b2[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_b2[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_merged, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_host, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_cols[0], cudaEventDisableTiming) != cudaSuccess ||
@@ -645,7 +668,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         gvom_destroy(h);
         return code;
     };
-    for (int s = 0; s < h->B; s++) {
+    for (int s = 0; s < h->P; s++) {
         if ((rc = dalloc_t(h, &h->slots[s].idx, (size_t)g.V))) return bail(rc);
     }
     for (int b = 0; b < 2; b++) {
@@ -655,7 +678,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     // counters + scan table
     if ((rc = dalloc(h, reinterpret_cast<void **>(&h->d_ctr), sizeof(ScanCounters) * 2 * kMaxBatch)))
         return bail(rc);
-    if ((rc = dalloc_t(h, &h->d_slotC, (size_t)h->B))) return bail(rc);
+    if ((rc = dalloc_t(h, &h->d_slotC, (size_t)h->P))) return bail(rc);
     if ((rc = dalloc_t(h, &h->d_combC, 4))) return bail(rc);
     double **maps[6] = {&h->height, &h->inferred, &h->slope_x, &h->slope_y, &h->rough, &h->guess};
     for (auto m : maps)
@@ -667,7 +690,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     for (int b = 0; b < 2; b++)  // chunks of >= 4 planes
         if ((rc = dalloc_t(h, &h->colinfo[b], (size_t)X2 * ((g.Z + 3) / 4)))) return bail(rc);
     if ((rc = dalloc_t(h, &h->occ_list, (size_t)g.V))) return bail(rc);
-    if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->B, h->st) != cudaSuccess ||
+    if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->P, h->st) != cudaSuccess ||
         cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 4, h->st) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(GVOM_ERR_CUDA, "memset failed"));
@@ -691,12 +714,12 @@ int gvom_destroy(GvomHandle *h) {
         cudaStreamSynchronize(h->side);
         cudaStreamDestroy(h->side);
     }
-    for (cudaStream_t s : {h->tr, h->bs})
+    for (cudaStream_t s : {h->tr, h->bs, h->mg})
         if (s) {
             cudaStreamSynchronize(s);
             cudaStreamDestroy(s);
         }
-    for (cudaEvent_t e : {h->ev_merged, h->ev_host, h->ev_cols[0], h->ev_cols[1]})
+    for (cudaEvent_t e : {h->ev_merged, h->ev_host, h->ev_cols[0], h->ev_cols[1], h->ev_b1, h->ev_b2[0], h->ev_b2[1]})
         if (e) cudaEventDestroy(e);
     if (h->ev_idx) cudaEventDestroy(h->ev_idx);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
@@ -922,8 +945,9 @@ struct CombPlan {
 };
 
 int prepare_combine(GvomHandle *h, CombPlan &pl) {
-    const Slot &ls = h->slots[h->last_buffer_index];
-    if (!ls.valid) return fail(GVOM_NO_DATA, "ERROR: No data in buffer");
+    const int lp = h->phys_of[h->last_buffer_index];
+    if (lp < 0 || !h->slots[lp].valid) return fail(GVOM_NO_DATA, "ERROR: No data in buffer");
+    const Slot &ls = h->slots[lp];
     const int nb = h->have_comb ? 1 - h->cur : 0;  // buffer receiving the new combined map
     pl.nb = nb;
     MergeParams &mp = pl.mp;
@@ -931,8 +955,9 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
     mp.g = h->g;
     for (int a = 0; a < 3; a++) mp.co[a] = ls.od[a];
     int ns = 0;
-    for (int i = 0; i < h->B; i++) {
-        const Slot &s = h->slots[i];
+    for (int i = 0; i < h->B; i++) {  // ring order, as the reference merges
+        if (h->phys_of[i] < 0) continue;
+        const Slot &s = h->slots[h->phys_of[i]];
         if (!s.valid) continue;
         MergeSrc &m = mp.src[ns++];
         m.idx = s.idx;
@@ -1107,10 +1132,11 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     const bool timing = !h->graphs && h->timer.on;
     // with stage timing the kernels run in sequence so that each interval is one kernel
     const int pipe = timing ? 0 : h->tun.step_pipeline;
-    if (pipe == 2 && h->st_dirty) {  // order the pipeline streams after other calls' work
+    if (pipe >= 2 && h->st_dirty) {  // order the pipeline streams after other calls' work
         CUDA_TRY(cudaEventRecord(h->ev_host, h->st));
         CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_host, 0));
         CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_host, 0));
+        CUDA_TRY(cudaStreamWaitEvent(h->mg, h->ev_host, 0));
         h->st_dirty = false;
     }
     // a pipelined step stages its points and traces on `tr`, once the previous
@@ -1127,7 +1153,44 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     CombPlan cp;
     if ((rc = prepare_combine(h, cp))) return rc;
     cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
-    if (pipe == 2) {
+    if (pipe == 3) {
+        rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
+        // the process: after the trace, and after the merge two steps back (the
+        // last one to read the physical slots this process writes)
+        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_traced, 0));
+        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_b2[h->spar], 0));
+        if ((rc = run_graphed(h, 6, [&]() -> int { return launch_scans(h, pp, nullptr, false, 3, h->bs); }, h->bs)))
+            return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_idx, h->bs));
+        if ((rc = run_graphed(h, 7, [&]() -> int { return launch_scans(h, pp, nullptr, false, 4, h->bs); }, h->bs)))
+            return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->bs));
+        CUDA_TRY(cudaEventRecord(h->ev_b1, h->bs));
+        // the merge: the index merge once the new index maps exist and the
+        // columns pass two steps back has read the combined buffer it writes;
+        // the statistics merge once the process is complete
+        CUDA_TRY(cudaStreamWaitEvent(h->mg, h->ev_idx, 0));
+        CUDA_TRY(cudaStreamWaitEvent(h->mg, h->ev_cols[cp.nb], 0));
+        if ((rc = run_graphed(h, 8, [&]() -> int {
+                 CUDA_TRY(cudaMemsetAsync(cp.mp.out_count, 0, sizeof(int), h->mg));
+                 CUDA_TRY(launch_merge_index(cp.mp, h->mg));
+                 return GVOM_OK;
+             }, h->mg)))
+            return rc;
+        CUDA_TRY(cudaStreamWaitEvent(h->mg, h->ev_b1, 0));
+        if ((rc = run_graphed(h, 9, [&]() -> int {
+                 CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->mg, nullptr, 1));
+                 return GVOM_OK;
+             }, h->mg)))
+            return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_b2[h->spar], h->mg));
+        h->spar ^= 1;
+        // columns and maps on the instance stream
+        CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_b2[h->spar ^ 1], 0));
+        rc = run_graphed(h, 5, [&]() -> int { return launch_comb(h, cp, nullptr, false, 2); });
+    } else if (pipe == 2) {
         rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
@@ -1382,12 +1445,13 @@ int gvom_slot_count(GvomHandle *h, int32_t slot, int64_t *count) {
     if (!h || !count) return fail(GVOM_ERR_ARG, "NULL argument");
     std::lock_guard<std::mutex> lk(h->mu);
     if (slot < 0 || slot >= h->B) return fail(GVOM_ERR_ARG, "slot out of range");
-    if (!h->slots[slot].valid) {
+    const int p = h->phys_of[slot];
+    if (p < 0 || !h->slots[p].valid) {
         *count = -1;
         return GVOM_OK;
     }
     int c = 0;
-    int rc = read_int(h, h->d_slotC + slot, &c);
+    int rc = read_int(h, h->d_slotC + p, &c);
     if (rc) return rc;
     *count = c;
     return GVOM_OK;
@@ -1428,10 +1492,11 @@ int gvom_get_slot(GvomHandle *h, int32_t slot, int32_t *index, int32_t *hit, int
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
     if (slot < 0 || slot >= h->B) return fail(GVOM_ERR_ARG, "slot out of range");
-    const Slot &s = h->slots[slot];
-    if (!s.valid) return fail(GVOM_NO_DATA, "slot is empty");
+    const int p = h->phys_of[slot];
+    if (p < 0 || !h->slots[p].valid) return fail(GVOM_NO_DATA, "slot is empty");
+    const Slot &s = h->slots[p];
     int C = 0;
-    int rc = read_int(h, h->d_slotC + slot, &C);
+    int rc = read_int(h, h->d_slotC + p, &C);
     if (rc) return rc;
     if (index) {
         CUDA_TRY(cudaMemcpyAsync(index, s.idx, sizeof(int) * h->g.V, cudaMemcpyDeviceToHost, h->st));
@@ -1566,7 +1631,7 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     if (!(t->step_overlap == 0 || t->step_overlap == 1)) return fail(GVOM_ERR_ARG, "step_overlap must be 0 or 1");
     if (!(t->maps_tile_cells == 64 || t->maps_tile_cells == 128 || t->maps_tile_cells == 256))
         return fail(GVOM_ERR_ARG, "maps_tile_cells must be 64, 128 or 256");
-    if (!(t->step_pipeline >= 0 && t->step_pipeline <= 2)) return fail(GVOM_ERR_ARG, "step_pipeline must be 0, 1 or 2");
+    if (!(t->step_pipeline >= 0 && t->step_pipeline <= 3)) return fail(GVOM_ERR_ARG, "step_pipeline must be 0 to 3");
     std::lock_guard<std::mutex> lk(h->mu);
     h->tun.pts_block = t->points_per_block;
     h->tun.assign_per = t->assign_words_per_thread;

@@ -33,7 +33,8 @@ struct Tuning {
     int step_overlap;   // gvom_step runs the index merge beside the statistics kernels: 0 or 1
     int maps_tile;      // k_maps2d tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) cells
     int step_pipeline;  // gvom_step: 0 one stream; 1 the trace beside the previous step's combine; 2 also the
-                        // rest of the process and the merge beside the previous step's columns and maps
+                        // rest of the process and the merge beside the previous step's columns and maps;
+                        // 3 also the process beside the previous step's merge
 };
 constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1, 256, 2};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
@@ -206,8 +207,9 @@ struct DebugMapParams {
 constexpr int kProcessKernels = 6;  // voxelize_trace, assign, scatter, cell_moments, voxel_stats, cleanup
 constexpr int kCombineKernels = 4;  // merge, merge_stats, columns, maps2d
 constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
-// `part`: 0 every kernel, 1 k_voxelize_trace only, 2 the kernels after it
-// (parts are launched without stage events)
+// `part`: 0 every kernel, 1 k_voxelize_trace only, 2 the kernels after it,
+// 3 k_assign only, 4 the kernels after k_assign (parts are launched without
+// stage events)
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
                            cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part = 0);

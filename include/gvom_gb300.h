@@ -127,7 +127,8 @@ int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t
  * steps submitted back to back overlap: at 1 a step's ray tracing runs on a
  * second stream beside the previous step's combine; at 2 the rest of its
  * process and its merge also run, on a third stream, beside the previous
- * step's columns and 2-D maps.  The maps are complete in stream order of the
+ * step's columns and 2-D maps; at 3 its process also runs beside the
+ * previous step's merge (the ring keeps spare physical slots for that).  The maps are complete in stream order of the
  * instance stream either way; in graph mode each stream's part of a step is
  * one executable graph. */
 int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device, double origin[3],
@@ -229,7 +230,8 @@ typedef struct GvomTuning {
     int32_t step_overlap;             /* gvom_step: index merge beside the statistics kernels, 0 or 1 */
     int32_t maps_tile_cells;          /* 2-D maps tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) */
     int32_t step_pipeline;            /* gvom_step streams: 0 one; 1 the trace beside the previous step's combine;
-                                         2 also the process and merge beside the previous step's columns and maps */
+                                         2 also the process and merge beside the previous step's columns and maps;
+                                         3 also the process beside the previous step's merge */
 } GvomTuning;
 int gvom_set_tuning(GvomHandle *h, const GvomTuning *t);
 int gvom_get_tuning(GvomHandle *h, GvomTuning *t);
