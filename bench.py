@@ -55,7 +55,7 @@ sys.path.insert(0, HERE)
 METRIC = "scan->map points/sec (process_pointcloud + combine_maps per scan)"
 UNIT = "points/s"
 L2_FLUSH_BYTES = 256 << 20
-KERNELS_PER_STEP = 10  # 6 process kernels (all scans of a step in one set) + 4 combine kernels
+KERNELS_PER_STEP = 11  # 6 process kernels (all scans of a step in one set) + 5 combine kernels
 # distinct steps the timed inputs cycle through: 200 plain scans (228 MB of
 # points) and 48 batched steps (256 MB), more than the 129 MB of L2
 HEAD_DISTINCT_STEPS = 200
@@ -79,6 +79,8 @@ def stage_bytes(name, n, ns, V, Vext, X2, C_new, C_sum, Cc, nsrc):
         return 20 * n
     if name == "k_merge":
         return 4 * V * nsrc + 4 * V + 4 * Cc + 8 * X2 * ((V // X2 + 7) // 8)
+    if name == "k_merge_counts":  # index words of the sources, hit / total / min height of their records
+        return 4 * Cc + 4 * nsrc * Cc + 12 * (C_sum + Cc) + 12 * Cc
     if name == "k_merge_stats":
         return 4 * Cc + 4 * nsrc * Cc + 64 * (C_sum + Cc) + 64 * Cc
     if name == "k_columns":

@@ -33,7 +33,7 @@ EXPORTS = (
     "gvom_debug_voxel_map_noalloc", "gvom_set_graphs", "gvom_set_tuning", "gvom_get_tuning", "gvom_step",
     "gvom_ros_grids", "gvom_process_pointcloud2", "gvom_pose_to_transform",
 )
-GVOM_STAGES = 10
+GVOM_STAGES = 11
 
 
 class GvomParams(C.Structure):

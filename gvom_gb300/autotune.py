@@ -9,9 +9,8 @@ the caller's workload:
   stats_blocks_per_sm      2 / 4 / 8   k_merge_stats
   step_overlap             0 / 1       gvom_step: the index merge beside the statistics kernels
   maps_tile_cells          64/128/256  k_maps2d (smaller tiles spread the float64 plane fits)
-  step_pipeline            0 .. 3      gvom_step: ray tracing beside the previous step's combine (1),
-                                       the process + merge beside its columns and maps (2), the
-                                       process beside its merge (3)
+  step_pipeline            0 / 1 / 2   gvom_step: ray tracing beside the previous step's combine (1),
+                                       and the process + merge beside its columns and maps (2)
 
 The others each affect their own kernels only and are timed with the
 per-kernel CUDA events of the mapper's stage timer (direct launches); the
@@ -35,7 +34,7 @@ CHOICES = {
     "stats_blocks_per_sm": (2, 4, 8),
     "step_overlap": (0, 1),
     "maps_tile_cells": (64, 128, 256),
-    "step_pipeline": (0, 1, 2, 3),
+    "step_pipeline": (0, 1, 2),
 }
 AFFECTS = {
     "points_per_block": ("k_voxelize_trace", "k_scatter", "k_cell_moments", "k_cleanup"),

@@ -34,8 +34,9 @@ int fail(int code, const std::string &msg) {
     } while (0)
 
 constexpr int kStages = kProcessKernels + kCombineKernels;
-const char *kStageNames[kStages] = {"k_voxelize_trace", "k_assign", "k_scatter", "k_cell_moments", "k_voxel_stats",
-                                    "k_cleanup", "k_merge", "k_merge_stats", "k_columns", "k_maps2d"};
+const char *kStageNames[kStages] = {"k_voxelize_trace", "k_assign", "k_scatter",     "k_cell_moments",
+                                    "k_voxel_stats",    "k_cleanup", "k_merge",       "k_merge_counts",
+                                    "k_merge_stats",    "k_columns", "k_maps2d"};
 
 // CUDA events around each kernel launch, harvested when the host waits.
 struct StageTimer {
@@ -120,10 +121,9 @@ struct GvomHandle {
     std::mutex mu;
     std::vector<Slot> slots;
     long long buffer_index = 0, last_buffer_index = 0;  // the reference's ring positions (mod B)
-    // physical slots: B + E (E = the most scans one call processes), so a
-    // call's new scans never overwrite a slot that the previous combine reads;
-    // scan number n lives in physical slot n mod P, and phys_of maps a ring
-    // position to the physical slot of its scan (-1: none yet)
+    // physical slots (P = B): scan number n lives in physical slot n mod P,
+    // and phys_of maps a ring position to the physical slot of its scan (-1:
+    // none yet)
     int P = 0;
     std::vector<int> phys_of;
     long long scans_total = 0;
@@ -156,7 +156,7 @@ struct GvomHandle {
     int *zlow = nullptr;
     float *mlow = nullptr;
     int2 *colinfo[2] = {nullptr, nullptr};  // (Z / 8 chunks) x X x X, one per combined buffer
-    int *occ_list = nullptr;  // occupied voxel ids of the combined map being built (V)
+    int *occ_list[2] = {nullptr, nullptr};  // occupied voxel ids of each combined buffer (V)
     bool have_maps = false;
     // debug
     int *d_dbg = nullptr;
@@ -169,10 +169,9 @@ struct GvomHandle {
     // CUDA graphs: each process / combine launch sequence is captured and
     // replayed through an executable graph updated in place
     bool graphs = false;
-    // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ merge at
-    // level 2), [5] its columns and maps (levels 2, 3), [6] its k_assign, [7] the rest of its process,
-    // [8] its index merge, [9] its statistics merge (level 3)
-    cudaGraphExec_t gexec[10] = {};
+    // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ merge and
+    // count merge at level 2), [5] its columns and maps, [6] its statistics merge (level 2)
+    cudaGraphExec_t gexec[7] = {};
     // a step forks the index merge onto `side` once the index maps are done
     cudaStream_t side = nullptr;
     cudaEvent_t ev_idx = nullptr, ev_join = nullptr;
@@ -188,13 +187,10 @@ struct GvomHandle {
     // sets st_dirty: the next level-2 step first orders `tr` and `bs` after
     // it (ev_host).
     cudaStream_t tr = nullptr, bs = nullptr;
-    // level 3: the merge of step k (index merge after ev_idx, statistics merge
-    // after ev_b1) runs on `mg` beside the process of step k + 1, whose
-    // k_assign waits for the merge that last read the physical slots it
-    // writes, two steps back (ev_b2[parity])
-    cudaStream_t mg = nullptr;
-    cudaEvent_t ev_b1 = nullptr, ev_b2[2] = {nullptr, nullptr};
-    int spar = 0;
+    // the statistics merge runs beside the columns and maps: on `side` after
+    // the count merge (ev_ms) and joined at the end of a combine (ev_msj), or
+    // at level 2 as its own graph, ev_stats[buffer] marking its end
+    cudaEvent_t ev_ms = nullptr, ev_msj = nullptr, ev_stats[2] = {nullptr, nullptr};
     cudaEvent_t ev_scratch[2] = {nullptr, nullptr};  // the process call that last used the set is done with it
     cudaEvent_t ev_traced = nullptr, ev_merged = nullptr, ev_host = nullptr;
     cudaEvent_t ev_cols[2] = {nullptr, nullptr};
@@ -516,7 +512,7 @@ int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bo
     CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec[pl.set], h->prank[pl.set], h->sorted,
                             h->moments, st, (timing && !part) ? h->timer.begin(0, kProcessKernels) : nullptr,
                             h->tun.pts_block, after_assign, part));
-    if (part == 1 || part == 3) return GVOM_OK;
+    if (part == 1) return GVOM_OK;
     for (int i = 0; i < pl.k; i++)
         CUDA_TRY(cudaMemcpyAsync(h->d_slotC + pl.slot_of[i], &ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
                                  st));
@@ -612,7 +608,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     g.V = (long long)g.X * g.X * g.Z;
     g.Vext = ext_cells(g);
     h->B = params->buffer_size;
-    h->P = h->B + std::min(h->B, kMaxBatch);
+    h->P = h->B;
     h->slots.resize(h->P);
     h->phys_of.assign(h->B, -1);
     cudaDeviceGetAttribute(&h->pageable_access, cudaDevAttrPageableMemoryAccess, dev);
@@ -647,10 +643,10 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     if (cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
         cudaStreamCreateWithPriority(&h->tr, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
         cudaStreamCreateWithPriority(&h->bs, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
-        cudaStreamCreateWithPriority(&h->mg, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_b1, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_b2[0], cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_b2[1], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_ms, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_msj, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_stats[0], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_stats[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_merged, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_host, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_cols[0], cudaEventDisableTiming) != cudaSuccess ||
@@ -689,7 +685,8 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     if ((rc = dalloc_t(h, &h->mlow, (size_t)X2))) return bail(rc);
     for (int b = 0; b < 2; b++)  // chunks of >= 4 planes
         if ((rc = dalloc_t(h, &h->colinfo[b], (size_t)X2 * ((g.Z + 3) / 4)))) return bail(rc);
-    if ((rc = dalloc_t(h, &h->occ_list, (size_t)g.V))) return bail(rc);
+    for (int b = 0; b < 2; b++)
+        if ((rc = dalloc_t(h, &h->occ_list[b], (size_t)g.V))) return bail(rc);
     if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->P, h->st) != cudaSuccess ||
         cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 4, h->st) != cudaSuccess) {
         cudaGetLastError();
@@ -714,12 +711,13 @@ int gvom_destroy(GvomHandle *h) {
         cudaStreamSynchronize(h->side);
         cudaStreamDestroy(h->side);
     }
-    for (cudaStream_t s : {h->tr, h->bs, h->mg})
+    for (cudaStream_t s : {h->tr, h->bs})
         if (s) {
             cudaStreamSynchronize(s);
             cudaStreamDestroy(s);
         }
-    for (cudaEvent_t e : {h->ev_merged, h->ev_host, h->ev_cols[0], h->ev_cols[1], h->ev_b1, h->ev_b2[0], h->ev_b2[1]})
+    for (cudaEvent_t e : {h->ev_merged, h->ev_host, h->ev_cols[0], h->ev_cols[1], h->ev_ms, h->ev_msj, h->ev_stats[0],
+                          h->ev_stats[1]})
         if (e) cudaEventDestroy(e);
     if (h->ev_idx) cudaEventDestroy(h->ev_idx);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
@@ -759,7 +757,8 @@ int gvom_destroy(GvomHandle *h) {
     cudaFree(h->mlow);
     cudaFree(h->colinfo[0]);
     cudaFree(h->colinfo[1]);
-    cudaFree(h->occ_list);
+    cudaFree(h->occ_list[0]);
+    cudaFree(h->occ_list[1]);
     cudaFree(h->d_dbg);
     cudaFree(h->d_ros);
     if (h->own) cudaStreamDestroy(h->own);
@@ -980,7 +979,7 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
     mp.out_idx = h->cidx[nb];
     mp.out_rec = h->crec[nb];
     mp.out_count = h->d_combC + nb;
-    mp.list = h->occ_list;
+    mp.list = h->occ_list[nb];
     mp.num_sms = h->num_sms;
     mp.planes = h->tun.merge_planes;
     mp.stats_bpsm = h->tun.stats_bpsm;
@@ -1044,6 +1043,12 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
 // process kernels, and joins back before the statistics merge.
 // `part`: 0 the whole combine on h->st; 1 the merge and merge_stats on `st`;
 // 2 columns and maps on h->st, with ev_cols[buffer] recorded between them
+// `part`: 0 the whole combine on h->st (the index merge on `side` after
+// `idx_ready` when given; the statistics merge forked onto `side` after the
+// count merge, beside the columns and maps, and joined at the end); 1 the
+// index and count merges on `st`; 2 columns and maps on h->st, with
+// ev_cols[buffer] recorded between them.  With `timing` every kernel runs in
+// sequence on h->st.
 int launch_comb(GvomHandle *h, const CombPlan &pl, cudaEvent_t idx_ready, bool timing, int part = 0,
                 cudaStream_t st = nullptr) {
     if (!st) st = h->st;
@@ -1054,23 +1059,30 @@ int launch_comb(GvomHandle *h, const CombPlan &pl, cudaEvent_t idx_ready, bool t
         CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 3));
         return GVOM_OK;
     }
+    if (timing) {
+        CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->st));
+        CUDA_TRY(launch_combine(pl.mp, pl.cp, pl.m2, h->st, h->timer.begin(kProcessKernels, kCombineKernels)));
+        return GVOM_OK;
+    }
     if (idx_ready) {
         CUDA_TRY(cudaStreamWaitEvent(h->side, idx_ready, 0));
         CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->side));
         CUDA_TRY(launch_merge_index(pl.mp, h->side));
         CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
         CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
-        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, st, nullptr, part));
-        return GVOM_OK;
-    }
-    if (part == 1) {
+    } else {
         CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), st));
         CUDA_TRY(launch_merge_index(pl.mp, st));
-        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, st, nullptr, 1));
-        return GVOM_OK;
     }
-    CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->st));
-    CUDA_TRY(launch_combine(pl.mp, pl.cp, pl.m2, h->st, timing ? h->timer.begin(kProcessKernels, kCombineKernels) : nullptr));
+    CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, st, nullptr, 1));
+    if (part == 1) return GVOM_OK;
+    CUDA_TRY(cudaEventRecord(h->ev_ms, h->st));
+    CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_ms, 0));
+    CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->side, nullptr, 4));
+    CUDA_TRY(cudaEventRecord(h->ev_msj, h->side));
+    CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 2));
+    CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 3));
+    CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_msj, 0));
     return GVOM_OK;
 }
 
@@ -1136,7 +1148,6 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         CUDA_TRY(cudaEventRecord(h->ev_host, h->st));
         CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_host, 0));
         CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_host, 0));
-        CUDA_TRY(cudaStreamWaitEvent(h->mg, h->ev_host, 0));
         h->st_dirty = false;
     }
     // a pipelined step stages its points and traces on `tr`, once the previous
@@ -1153,44 +1164,7 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     CombPlan cp;
     if ((rc = prepare_combine(h, cp))) return rc;
     cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
-    if (pipe == 3) {
-        rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
-        if (rc) return rc;
-        CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
-        // the process: after the trace, and after the merge two steps back (the
-        // last one to read the physical slots this process writes)
-        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_traced, 0));
-        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_b2[h->spar], 0));
-        if ((rc = run_graphed(h, 6, [&]() -> int { return launch_scans(h, pp, nullptr, false, 3, h->bs); }, h->bs)))
-            return rc;
-        CUDA_TRY(cudaEventRecord(h->ev_idx, h->bs));
-        if ((rc = run_graphed(h, 7, [&]() -> int { return launch_scans(h, pp, nullptr, false, 4, h->bs); }, h->bs)))
-            return rc;
-        CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->bs));
-        CUDA_TRY(cudaEventRecord(h->ev_b1, h->bs));
-        // the merge: the index merge once the new index maps exist and the
-        // columns pass two steps back has read the combined buffer it writes;
-        // the statistics merge once the process is complete
-        CUDA_TRY(cudaStreamWaitEvent(h->mg, h->ev_idx, 0));
-        CUDA_TRY(cudaStreamWaitEvent(h->mg, h->ev_cols[cp.nb], 0));
-        if ((rc = run_graphed(h, 8, [&]() -> int {
-                 CUDA_TRY(cudaMemsetAsync(cp.mp.out_count, 0, sizeof(int), h->mg));
-                 CUDA_TRY(launch_merge_index(cp.mp, h->mg));
-                 return GVOM_OK;
-             }, h->mg)))
-            return rc;
-        CUDA_TRY(cudaStreamWaitEvent(h->mg, h->ev_b1, 0));
-        if ((rc = run_graphed(h, 9, [&]() -> int {
-                 CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->mg, nullptr, 1));
-                 return GVOM_OK;
-             }, h->mg)))
-            return rc;
-        CUDA_TRY(cudaEventRecord(h->ev_b2[h->spar], h->mg));
-        h->spar ^= 1;
-        // columns and maps on the instance stream
-        CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_b2[h->spar ^ 1], 0));
-        rc = run_graphed(h, 5, [&]() -> int { return launch_comb(h, cp, nullptr, false, 2); });
-    } else if (pipe == 2) {
+    if (pipe == 2) {
         rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
@@ -1198,6 +1172,7 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         // columns pass that last read the combined buffer this merge writes
         CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_traced, 0));
         CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_cols[cp.nb], 0));
+        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_stats[cp.nb], 0));
         rc = run_graphed(h, 4, [&]() -> int {
             if ((rc = launch_scans(h, pp, idx, false, 2, h->bs))) return rc;
             if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_scratch[pp.set], h->bs, cudaEventRecordExternal));
@@ -1206,9 +1181,18 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         }, h->bs);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(h->ev_merged, h->bs));
+        // the statistics merge beside the columns and maps
+        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_merged, 0));
+        rc = run_graphed(h, 6, [&]() -> int {
+            CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->side, nullptr, 4));
+            return GVOM_OK;
+        }, h->side);
+        if (rc) return rc;
+        CUDA_TRY(cudaEventRecord(h->ev_stats[cp.nb], h->side));
         // columns and maps on the instance stream, beside the next step's process
         CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_merged, 0));
         rc = run_graphed(h, 5, [&]() -> int { return launch_comb(h, cp, nullptr, false, 2); });
+        if (!rc) CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_stats[cp.nb], 0));  // later calls see whole records
     } else if (pipe == 1) {
         h->st_dirty = true;
         // the trace waits only for the previous process to release the scratch,
@@ -1631,7 +1615,7 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     if (!(t->step_overlap == 0 || t->step_overlap == 1)) return fail(GVOM_ERR_ARG, "step_overlap must be 0 or 1");
     if (!(t->maps_tile_cells == 64 || t->maps_tile_cells == 128 || t->maps_tile_cells == 256))
         return fail(GVOM_ERR_ARG, "maps_tile_cells must be 64, 128 or 256");
-    if (!(t->step_pipeline >= 0 && t->step_pipeline <= 3)) return fail(GVOM_ERR_ARG, "step_pipeline must be 0 to 3");
+    if (!(t->step_pipeline >= 0 && t->step_pipeline <= 2)) return fail(GVOM_ERR_ARG, "step_pipeline must be 0, 1 or 2");
     std::lock_guard<std::mutex> lk(h->mu);
     h->tun.pts_block = t->points_per_block;
     h->tun.assign_per = t->assign_words_per_thread;

@@ -33,8 +33,7 @@ struct Tuning {
     int step_overlap;   // gvom_step runs the index merge beside the statistics kernels: 0 or 1
     int maps_tile;      // k_maps2d tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) cells
     int step_pipeline;  // gvom_step: 0 one stream; 1 the trace beside the previous step's combine; 2 also the
-                        // rest of the process and the merge beside the previous step's columns and maps;
-                        // 3 also the process beside the previous step's merge
+                        // rest of the process and the merge beside the previous step's columns and maps
 };
 constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1, 256, 2};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
@@ -205,18 +204,18 @@ struct DebugMapParams {
 // `ev` (nullable): kProcessKernels + 1 (resp. kCombineKernels + 1) events,
 // recorded before the first kernel and after each kernel.
 constexpr int kProcessKernels = 6;  // voxelize_trace, assign, scatter, cell_moments, voxel_stats, cleanup
-constexpr int kCombineKernels = 4;  // merge, merge_stats, columns, maps2d
+constexpr int kCombineKernels = 5;  // merge, merge_counts, merge_stats, columns, maps2d
 constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
-// `part`: 0 every kernel, 1 k_voxelize_trace only, 2 the kernels after it,
-// 3 k_assign only, 4 the kernels after k_assign (parts are launched without
-// stage events)
+// `part`: 0 every kernel, 1 k_voxelize_trace only, 2 the kernels after it
+// (parts are launched without stage events)
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
                            cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part = 0);
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
 cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st);
-// `part`: 0 merge_stats, columns, maps2d; 1 merge_stats; 2 columns; 3 maps2d
-// (parts are launched without stage events)
+// `part`: 0 counts, statistics, columns, maps2d in sequence; 1 the count
+// merge; 4 the statistics merge; 2 columns; 3 maps2d (parts are launched
+// without stage events)
 cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
                                 cudaEvent_t *ev, int part = 0);
 cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,

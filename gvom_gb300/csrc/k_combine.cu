@@ -124,8 +124,6 @@ __device__ __forceinline__ void merge_voxel(const MergeParams &mp, int vid) {
     }
     float n = 0.f, m0 = 0.f, m1 = 0.f, m2 = 0.f;
     float C[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    int hit = 0, total = 0;
-    float minh = 1.0f;
 #pragma unroll
     for (int s0 = 0; s0 < NSRC; s0 += kMergeChunk) {
         float4 ra[kMergeChunk], rb[kMergeChunk], rc[kMergeChunk], rd[kMergeChunk];
@@ -173,18 +171,51 @@ __device__ __forceinline__ void merge_voxel(const MergeParams &mp, int vid) {
             m1 = nm1;
             m2 = nm2;
             n = den;
-            hit += __float_as_int(cc.z);
-            total += __float_as_int(cc.w);
-            minh = fminf(minh, d.x);
+            (void)d;
         }
     }
     float e[3];
     eigen3(C, e);
-    float4 *out = reinterpret_cast<float4 *>(&mp.out_rec[vid]);
-    out[0] = make_float4(m0, m1, m2, C[0]);
-    out[1] = make_float4(C[1], C[2], C[3], C[4]);
-    out[2] = make_float4(C[5], n, __int_as_float(hit), __int_as_float(total));
-    out[3] = make_float4(minh, e[0], e[1], e[2]);
+    // every field but hit, total and min_h, which k_merge_counts writes
+    float *out = reinterpret_cast<float *>(&mp.out_rec[vid]);
+    reinterpret_cast<float4 *>(out)[0] = make_float4(m0, m1, m2, C[0]);
+    reinterpret_cast<float4 *>(out)[1] = make_float4(C[1], C[2], C[3], C[4]);
+    reinterpret_cast<float2 *>(out)[4] = make_float2(C[5], n);
+    out[13] = e[0];
+    reinterpret_cast<float2 *>(out)[7] = make_float2(e[1], e[2]);
+}
+
+// hit and total counts (sums) and the lowest in-voxel height (minimum) of a
+// listed voxel over its sources -- everything the columns pass reads, so the
+// 2-D maps need not wait for the statistics merge
+template <int NSRC>
+__device__ __forceinline__ void merge_counts(const MergeParams &mp, int vid) {
+    const int X = mp.g.X, Z = mp.g.Z;
+    const int x = vid % X, y = (vid / X) % X, z = vid / (X * X);
+    int o[NSRC];
+#pragma unroll
+    for (int s = 0; s < NSRC; s++) {
+        o[s] = -1;
+        if (s < mp.nsrc) {
+            const int xs = x + mp.src[s].dx, ys = y + mp.src[s].dy, zs = z + mp.src[s].dz;
+            if ((unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X && (unsigned)zs < (unsigned)Z)
+                o[s] = __ldg(&mp.src[s].idx[xs + ys * X + zs * X * X]);
+        }
+    }
+    int hit = 0, total = 0;
+    float minh = 1.0f;
+#pragma unroll
+    for (int s = 0; s < NSRC; s++) {
+        if (!(s < NSRC && o[s] >= 0)) continue;
+        const VoxelRec *r = &mp.src[s].rec[o[s]];
+        const int2 ht = __ldg(reinterpret_cast<const int2 *>(&r->hit));
+        hit += ht.x;
+        total += ht.y;
+        minh = fminf(minh, __ldg(&r->min_h));
+    }
+    VoxelRec *out = &mp.out_rec[vid];
+    *reinterpret_cast<int2 *>(&out->hit) = make_int2(hit, total);
+    out->min_h = minh;
 }
 
 // k_merge: every thread decides its ZC voxels (index merge), writes the
@@ -284,6 +315,13 @@ __global__ void __launch_bounds__(256, GVOM_MERGE_STATS_MINB) k_merge_stats(cons
     const int n = *mp.out_count;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         merge_voxel<NSRC>(mp, mp.list[i]);
+}
+
+template <int NSRC>
+__global__ void __launch_bounds__(256) k_merge_counts(const __grid_constant__ MergeParams mp) {
+    const int n = *mp.out_count;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        merge_counts<NSRC>(mp, mp.list[i]);
 }
 
 // ---------------------------------------------------------------------------
@@ -950,6 +988,11 @@ static void launch_merge_stats(const MergeParams &mp, cudaStream_t st) {
     k_merge_stats<NSRC><<<mp.num_sms * mp.stats_bpsm, 256, 0, st>>>(mp);
 }
 
+template <int NSRC>
+static void launch_merge_counts(const MergeParams &mp, cudaStream_t st) {
+    k_merge_counts<NSRC><<<mp.num_sms * 8, 256, 0, st>>>(mp);
+}
+
 // source-count class of a merge (2, 3, 5, 9 or 17 sources)
 template <template <int> class F>
 static void by_nsrc(const MergeParams &mp, cudaStream_t st) {
@@ -967,36 +1010,42 @@ template <int N>
 struct MergeStats {
     static void run(const MergeParams &mp, cudaStream_t st) { launch_merge_stats<N>(mp, st); }
 };
+template <int N>
+struct MergeCounts {
+    static void run(const MergeParams &mp, cudaStream_t st) { launch_merge_counts<N>(mp, st); }
+};
 
 cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st) {
     by_nsrc<MergeIdx>(mp, st);
     return cudaGetLastError();
 }
 
-// statistics merge, columns and 2-D maps (events ev[1..4] when timing)
+// count merge, statistics merge, columns and 2-D maps (events ev[1..5] when timing)
 cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
                                 cudaEvent_t *ev, int part) {
     const int X = mp.g.X;
     if (part) ev = nullptr;
     if (ev) cudaEventRecord(ev[1], st);
-    if (part == 0 || part == 1) by_nsrc<MergeStats>(mp, st);
+    if (part == 0 || part == 1) by_nsrc<MergeCounts>(mp, st);
     if (ev) cudaEventRecord(ev[2], st);
+    if (part == 0 || part == 4) by_nsrc<MergeStats>(mp, st);
+    if (ev) cudaEventRecord(ev[3], st);
     if (part == 0 || part == 2) {
         dim3 gc((X + 31) / 32, (X + 7) / 8);
         k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);
     }
-    if (ev) cudaEventRecord(ev[3], st);
+    if (ev) cudaEventRecord(ev[4], st);
     if (part == 0 || part == 3) {
         if (m2.tile_cells == 64) launch_maps2d<4, 16>(m2, st);
         else if (m2.tile_cells == 128) launch_maps2d<8, 16>(m2, st);
         else launch_maps2d<8, 32>(m2, st);
     }
-    if (ev) cudaEventRecord(ev[4], st);
+    if (ev) cudaEventRecord(ev[5], st);
     return cudaGetLastError();
 }
 
 cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
-                           cudaEvent_t *ev) {
+                           cudaEvent_t *ev) {  // every kernel in sequence on `st`
     if (ev) cudaEventRecord(ev[0], st);
     by_nsrc<MergeIdx>(mp, st);
     return launch_combine_rest(mp, cp, m2, st, ev);

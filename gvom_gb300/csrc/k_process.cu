@@ -849,14 +849,13 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
         mark(1);
         if (part == 1) return cudaGetLastError();
     }
-    if (part != 4) {
+    {
         const int per = pc.assign_per;
         dim3 ga((unsigned)((pc.g.Vext + 256 * per - 1) / (256 * per)), pc.nscans);
         if (per == 4) k_assign<NS, 4><<<ga, 256, 0, st>>>(pc, tab);
         else if (per == 16) k_assign<NS, 16><<<ga, 256, 0, st>>>(pc, tab);
         else k_assign<NS, 8><<<ga, 256, 0, st>>>(pc, tab);
         if (after_assign) cudaEventRecord(after_assign, st);
-        if (part == 3) return cudaGetLastError();
     }
     mark(2);
     k_scatter<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank, sorted);

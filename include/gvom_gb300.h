@@ -127,8 +127,7 @@ int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t
  * steps submitted back to back overlap: at 1 a step's ray tracing runs on a
  * second stream beside the previous step's combine; at 2 the rest of its
  * process and its merge also run, on a third stream, beside the previous
- * step's columns and 2-D maps; at 3 its process also runs beside the
- * previous step's merge (the ring keeps spare physical slots for that).  The maps are complete in stream order of the
+ * step's columns and 2-D maps.  The maps are complete in stream order of the
  * instance stream either way; in graph mode each stream's part of a step is
  * one executable graph. */
 int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device, double origin[3],
@@ -230,8 +229,7 @@ typedef struct GvomTuning {
     int32_t step_overlap;             /* gvom_step: index merge beside the statistics kernels, 0 or 1 */
     int32_t maps_tile_cells;          /* 2-D maps tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) */
     int32_t step_pipeline;            /* gvom_step streams: 0 one; 1 the trace beside the previous step's combine;
-                                         2 also the process and merge beside the previous step's columns and maps;
-                                         3 also the process beside the previous step's merge */
+                                         2 also the process and merge beside the previous step's columns and maps */
 } GvomTuning;
 int gvom_set_tuning(GvomHandle *h, const GvomTuning *t);
 int gvom_get_tuning(GvomHandle *h, GvomTuning *t);
@@ -243,7 +241,7 @@ int gvom_get_tuning(GvomHandle *h, GvomTuning *t);
  * per-kernel launch gaps.  Stage timing records nothing while it is on. */
 int gvom_set_graphs(GvomHandle *h, int32_t on);
 
-#define GVOM_STAGES 10
+#define GVOM_STAGES 11
 int gvom_set_stage_timing(GvomHandle *h, int32_t on);
 int gvom_stage_times(GvomHandle *h, double *total_ms, int64_t *launches, int32_t n_stages);
 const char *gvom_stage_name(int32_t stage);

@@ -272,7 +272,7 @@ def test_step_equals_process_then_combine(Gvom, graphs):
 
 
 @pytest.mark.parametrize("graphs", [False, True])
-@pytest.mark.parametrize("pipeline", [0, 1, 2, 3])
+@pytest.mark.parametrize("pipeline", [0, 1, 2])
 def test_steps_back_to_back_equal_sequential_calls(Gvom, graphs, pipeline):
     """Steps submitted without a host wait in between (device outputs), so that
     with step_pipeline a step's work overlaps the previous step's, with plain
