@@ -459,6 +459,15 @@ __device__ __forceinline__ double rough_of(double err) {
     return err;
 }
 
+// The reference's mean of n copies of the coordinate c * res (float64,
+// summed in order, then divided by n) equals c * res exactly.
+__device__ __forceinline__ bool axis_mean_exact(int c, double res, int n) {
+    const double v = __dmul_rn((double)c, res);
+    double sum = 0.0;
+    for (int j = 0; j < n; j++) sum = __dadd_rn(sum, v);
+    return __ddiv_rn(sum, (double)n) == v;
+}
+
 // __calculate_slope (scripts/gvom.py:717-805) in the reference's float64
 // operation order up to the final log / atan2.
 template <int kSY>
@@ -606,6 +615,7 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
         int zr = 0;
         float mr = 0.f;
         double h0 = 0.0;
+        int xf = 0, yf = 0;  // the first known neighbour
         for (int xx = xl; xx < xh; xx++)
             for (int yy = yl; yy < yh; yy++) {
                 const int sx = xx - x0t + kHalo, sy = yy - y0t + kHalo;
@@ -614,6 +624,8 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
                         zr = szl[sx][sy];
                         mr = sml[sx][sy];
                         h0 = sh[sx][sy];
+                        xf = xx;
+                        yf = yy;
                     }
                     all_vox = all_vox && szl[sx][sy] >= 0;
                     all_eq = all_eq && sh[sx][sy] == h0;
@@ -640,6 +652,15 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
             for (int j = 0; j < n_good; j++) sum = __dadd_rn(sum, h0);
             const double dz = __dsub_rn(h0, __ddiv_rn(sum, (double)n_good));
             rough = rough_of(__dmul_rn(dz, dz));
+            slx = 0.0;
+            sly = 0.0;
+        } else if (valid && n_good >= 3 && (dxx == 0 || dyy == 0) &&
+                   axis_mean_exact(dxx == 0 ? xf : yf, mp.xy_res, n_good)) {
+            // every known neighbour in one row (column) of the map, whose float64
+            // coordinate the reference's sequential mean gives back exactly: every
+            // offset along that axis is 0, so its normal matrix has det = 0 and it
+            // leaves roughness -1 and the slopes 0 (scripts/gvom.py:769-771)
+            rough = -1.0;
             slx = 0.0;
             sly = 0.0;
         } else if (valid && n_good >= 3) {
