@@ -121,9 +121,9 @@ struct GvomHandle {
     std::mutex mu;
     std::vector<Slot> slots;
     long long buffer_index = 0, last_buffer_index = 0;  // the reference's ring positions (mod B)
-    // physical slots (P = B): scan number n lives in physical slot n mod P,
-    // and phys_of maps a ring position to the physical slot of its scan (-1:
-    // none yet)
+    // scan number n lives in physical slot n mod P, and phys_of maps a ring
+    // position to the physical slot of its scan (-1: none yet); with P = B
+    // the map is the identity once the ring is full
     int P = 0;
     std::vector<int> phys_of;
     long long scans_total = 0;
