@@ -286,9 +286,11 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 
 def _reduce_max_sum(torch, dist, t_val, pts):
+    """(max over ranks of the timed seconds, sum over ranks of the points)."""
     if not dist:
         return t_val, float(pts)
-    t = torch.tensor([t_val, float(pts)], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([t_val, float(pts)], dtype=torch.float64, device=dev)
     tm = t.clone()
     dist.all_reduce(tm, op=dist.ReduceOp.MAX)
     ts = t.clone()
