@@ -149,6 +149,14 @@ class Clocks:
                 "samples": len(rows), "reasons": sorted(reasons)}
 
 
+def _safe(fn):
+    """fn() or None: an auxiliary figure never breaks the bench line."""
+    try:
+        return fn()
+    except Exception:
+        return None
+
+
 def measured_peak_hbm():
     try:
         with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
@@ -284,6 +292,20 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # GPU measurement of one form
 # ---------------------------------------------------------------------------
+
+def step_roofline(n_pts, ns, V, X2, B, C_new, C_sum, Cc, hits, steps, peak_gbs, ms_per_step):
+    """The whole step against HBM, with the per-unit work of the scan->map
+    roofline accounting: process = 12N + 64 + 4V + 52C per scan, combine =
+    4V (B + 1) + 4V + 52 sum(C_i) + 2 52 Cc + 20 X^2; int32 atomics = 2H + S
+    per scan (H, S of the last scan, times the scans of a step)."""
+    process = 12 * n_pts + ns * (64 + 4 * V) + 52 * C_new
+    combine = 4 * V * (B + 1) + 4 * V + 52 * C_sum + 2 * 52 * Cc + 20 * X2
+    b = process + combine
+    t_hbm = b / (peak_gbs * 1e9)
+    return {"bytes_per_step": int(b), "atomics_per_step": int(ns * (2 * hits + steps)),
+            "hbm_bound_ms": 1e3 * t_hbm, "ms_per_step": ms_per_step,
+            "frac_of_measured_hbm": t_hbm / (ms_per_step / 1e3)}
+
 
 def _reduce_max_sum(torch, dist, t_val, pts):
     """(max over ranks of the timed seconds, sum over ranks of the points)."""
@@ -507,6 +529,9 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
                      "peak_source": peak_kind, "unit": "GB/s", "frac": dom["gbs"] / peak,
                      "alg_bytes_per_launch": dom["alg_bytes"], "ms_per_launch": dom["ms_per_launch"],
                      "traffic": profiled_traffic(dom_name, form.name)},
+        "step_roofline": _safe(lambda: step_roofline(n_mean, ns, V, X * X, w.buffer_size, C_new, C_sum, ncc.value,
+                                                     ray["hits"], ray["ray_steps"], peak,
+                                                     1e3 * t_dev_max / n_steps)),
         "stages": stage_tab,
         "ray_last_scan": ray,
         "wall_s_timed": wall_timed,
@@ -625,7 +650,8 @@ def run_gpu(args):
             "data": "synthetic (seeded terrain / lidar / trajectory generator)",
             "config": dict(res["config"], parallelism=f"replicas x{world}"),
             "latency_ms": res["latency_ms"], "e2e": res["e2e"], "gpu_launches": res["gpu_launches"],
-            "roofline": res["roofline"], "stages": res["stages"], "ray_last_scan": res["ray_last_scan"],
+            "roofline": res["roofline"], "step_roofline": res.get("step_roofline"), "stages": res["stages"],
+            "ray_last_scan": res["ray_last_scan"],
             "direct_launches": res["direct_launches"], "l2_flushed_per_step": res["l2_flushed_per_step"],
             "wall_s_timed": res["wall_s_timed"], "clocks": res["clocks"], "cpu_baseline": cpu,
             "forms": forms,

@@ -1,0 +1,23 @@
+"""bench.py's host-side accounting on CPU: the whole-step roofline follows
+the per-unit work of the scan->map accounting, and an auxiliary figure that
+fails never breaks the bench line."""
+import bench
+
+
+def test_step_roofline_per_unit_work():
+    V, X2, B = 4194304, 65536, 4
+    r = bench.step_roofline(n_pts=1000, ns=1, V=V, X2=X2, B=B, C_new=10, C_sum=40, Cc=30, hits=7, steps=500,
+                            peak_gbs=1000.0, ms_per_step=1.0)
+    process = 12 * 1000 + 64 + 4 * V + 52 * 10
+    combine = 4 * V * (B + 1) + 4 * V + 52 * 40 + 2 * 52 * 30 + 20 * X2
+    assert r["bytes_per_step"] == process + combine
+    assert r["atomics_per_step"] == 2 * 7 + 500
+    assert abs(r["hbm_bound_ms"] - (process + combine) / 1e12 * 1e3) < 1e-12
+    assert abs(r["frac_of_measured_hbm"] - r["hbm_bound_ms"] / 1.0) < 1e-12
+    # the combine's index maps: (B + 2) x 4V, 101 MB at 256 x 256 x 64 with B = 4
+    assert abs(4 * V * (B + 2) / 1e6 - 100.7) < 0.1
+
+
+def test_safe_returns_none_on_failure():
+    assert bench._safe(lambda: 1 / 0) is None
+    assert bench._safe(lambda: 3) == 3
