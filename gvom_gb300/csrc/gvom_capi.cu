@@ -329,6 +329,8 @@ int ensure_cnt(GvomHandle *h, int nscans, int set) {
         int rc = dalloc_t(h, &c, (size_t)ve);
         if (rc) return rc;
         CUDA_TRY(cudaMemsetAsync(c, 0, (size_t)ve * 8, h->st));
+        // complete before a pipelined trace on another stream adds into it
+        CUDA_TRY(cudaStreamSynchronize(h->st));
         h->cnt[set].push_back(c);
     }
     return GVOM_OK;
