@@ -116,6 +116,85 @@ def scene_kat_guess():
     return kat_params(X=16, Z=8, robot_radius=0.5), [P(pts, ego), ("C",)]
 
 
+def _cell_point(cx, cy, cz, f=(0.5, 0.5, 0.5)):
+    """World point at fraction f inside voxel (cx, cy, cz) of the kat_params() grid (origin -8, -8, -4)."""
+    return (cx - 8 + f[0], cy - 8 + f[1], cz - 4 + f[2])
+
+
+# Point clusters of known covariance, one per voxel (offsets from the voxel centre, 1 m voxels);
+# the eigenvalues of each voxel's covariance in closed form (tests/test_oracle_golden.py).
+EIGEN_CLUSTERS = {
+    "isotropic": ((12, 12, 2), [(0.25, 0, 0), (0, 0.25, 0), (0, 0, 0.25)]),
+    "planar": ((4, 12, 2), [(0.25, 0, 0), (0, 0.25, 0)]),
+    "linear": ((12, 4, 2), [(0.125, 0, 0), (0.25, 0, 0)]),
+    "diagonal_line": ((4, 4, 2), [(0.125, 0.125, 0), (0.25, 0.25, 0)]),
+    "tilted_plane": ((8, 13, 5), [(0.125, 0, 0.125), (0, 0.25, 0)]),
+    "anisotropic": ((13, 8, 1), [(0.125, 0, 0), (0, 0.1875, 0), (0, 0, 0.25)]),
+    "pair_a": ((8, 2, 1), [(0.25, 0, 0)]),
+    "pair_b": ((9, 2, 1), [(0, 0.25, 0)]),
+}
+
+
+def scene_kat_eigen():
+    """Voxels whose covariance has eigenvalues in closed form (isotropic, planar, linear, rotated,
+    distinct), one single-point voxel and two adjacent voxels sharing their neighbourhoods; the
+    same scan twice into two slots, then two combines (gvom.py:1249-1371, 888-980, 1423-1487)."""
+    pts = []
+    for (c, offs) in EIGEN_CLUSTERS.values():
+        ctr = np.array(_cell_point(*c))
+        for o in offs:
+            pts += [tuple(ctr + o), tuple(ctr - np.asarray(o))]
+    pts.append(_cell_point(2, 8, 1, (0.6, 0.3, 0.55)))  # single point: zero covariance
+    ego = (0.5, 0.5, 0.5)
+    return kat_params(B=2), [P(pts, ego), P(pts, ego), ("C",), ("C",)]
+
+
+def _stack(cx, cy, cz, n, entry):
+    """`n` points in voxel (cx, cy, cz).  With `entry` they sit just past the face that a ray from
+    (0.5, 0.5, 0.5) enters by, so that its last march step falls short of the voxel (one count per
+    point); otherwise near the middle, where the last step counts the voxel again (two)."""
+    out = []
+    for k in range(n):
+        if entry:
+            fx = 0.5 if cx == 8 else (0.05 + 0.002 * k if cx > 8 else 0.95 - 0.002 * k)
+            fy = 0.5 if cy == 8 else (0.05 + 0.003 * k if cy > 8 else 0.95 - 0.003 * k)
+        else:
+            fx, fy = 0.3 + 0.4 * k / max(1, n - 1), 0.6
+        out.append(_cell_point(cx, cy, cz, (fx, fy, 0.4 + 0.01 * k)))
+    return out
+
+
+# Columns for the positive-obstacle band (gvom.py:515-555): cell -> (ground voxel z, min-height
+# fraction, {z: (points, entry)}).  With 1 m voxels, pos_thr 0.5 and robot_h 2 the band is
+# [zg + 1, zg + 2] for a fraction below 0.5 and [zg + 2, zg + 2] from 0.5 on.
+POSOBS_COLUMNS = {
+    "A": ((12, 8), 1, 0.25, {2: (11, False), 3: (10, False)}),  # hit 10 at z=3 is left out
+    "B": ((8, 12), 1, 0.5, {2: (20, True), 3: (11, False)}),    # band starts one voxel higher
+    "C": ((4, 8), 1, 0.25, {2: (10, False), 3: (10, False)}),   # nothing above 10 hits: 0
+    "D": ((8, 4), 6, 0.25, {7: (11, False)}),                   # band top outside the grid: 0
+    "E": ((13, 13), 1, 0.25, {2: (29, True)}),                  # 29 / 50: int(57.99999999999999)
+    "F": ((4, 12), 1, 0.25, {2: (12, True), 3: (11, False)}),   # both band voxels summed
+    "H": ((12, 3), 1, 0.0, {3: (11, True), 4: (15, False)}),    # fraction 0: z=4 is above the band
+    "J": ((1, 10), 1, 0.5 - 2.0 ** -22, {2: (20, True), 3: (11, False)}),  # just below 0.5
+}
+
+
+def scene_kat_posobs():
+    """Obstacle-band columns at the thresholds (hit > 10, band ends, int() truncation) and a
+    steep 3 x 3 patch whose slope alone makes it an obstacle."""
+    pts = []
+    for (cx, cy), zg, frac, stacks in POSOBS_COLUMNS.values():
+        pts.append(_cell_point(cx, cy, zg, (0.5, 0.5, frac)))
+        for z, (n, entry) in stacks.items():
+            pts += _stack(cx, cy, z, n, entry)
+    pts += [(20.5, 20.5, -7.5)] * 21  # rays through column E's band voxel, ending outside the grid
+    for i in range(3):
+        for j in range(3):
+            pts.append(_cell_point(3 + i, 3 + j, 1, (0.5, 0.5, 0.25 + 0.5 * i + 0.25 * j)))
+    ego = (0.5, 0.5, 0.5)
+    return kat_params(B=1), [P(pts, ego), ("C",)]
+
+
 def scene_synthetic(name, X=32, Z=16, res=0.5, B=3, beams=16, columns=256, n_scans=6,
                     combine_after=(1, 2, 4, 5), tdtype=np.float32, pdtype=np.float32,
                     veg=0.0, dropout=0.0, eig=(1, 1)):
@@ -153,6 +232,8 @@ SCENES = {
     "kat_shift": scene_kat_shift,
     "kat_planes": scene_kat_planes,
     "kat_guess": scene_kat_guess,
+    "kat_eigen": scene_kat_eigen,
+    "kat_posobs": scene_kat_posobs,
     "synth_f32": lambda: scene_synthetic("synth_f32"),
     "synth_f64T_veg": lambda: scene_synthetic("synth_f64T_veg", tdtype=np.float64, veg=2.0, n_scans=5,
                                               combine_after=(0, 2, 4)),

@@ -137,3 +137,69 @@ def test_parallel_oracle_integer_results_match_sequential():
             ca, cb = canonical_state(a.combined_state()), canonical_state(b.combined_state())
             for k in ("occ", "free", "hit", "total", "min_h"):
                 np.testing.assert_array_equal(ca[k], cb[k])
+
+
+def _comb_row(fx, ci, key, x, y, z, X=16):
+    occ = fx[f"c{ci}_comb_occ"]
+    r = np.searchsorted(occ, x + y * X + z * X * X)
+    assert r < len(occ) and occ[r] == x + y * X + z * X * X, f"voxel {(x, y, z)} not occupied"
+    return fx[f"c{ci}_comb_{key}"][r]
+
+
+# kat_eigen: voxel -> (points per scan, mean in voxel units, eigenvalues in closed form).
+# Symmetric clusters about the voxel centre; pair_a / pair_b are adjacent voxels whose
+# neighbourhoods take in each other's points (gvom.py:1249-1371).
+EIGEN_KAT = {
+    (12, 12, 2): (6, (0.5, 0.5, 0.5), (1 / 48, 1 / 48, 1 / 48)),    # isotropic
+    (4, 12, 2): (4, (0.5, 0.5, 0.5), (1 / 32, 1 / 32, 0.0)),        # planar
+    (12, 4, 2): (4, (0.5, 0.5, 0.5), (5 / 128, 0.0, 0.0)),          # linear along x
+    (4, 4, 2): (4, (0.5, 0.5, 0.5), (5 / 64, 0.0, 0.0)),            # linear along x = y
+    (8, 13, 5): (4, (0.5, 0.5, 0.5), (1 / 32, 1 / 64, 0.0)),        # plane tilted about y
+    (13, 8, 1): (6, (0.5, 0.5, 0.5), (1 / 48, 3 / 256, 1 / 192)),   # distinct axes, sorted
+    (2, 8, 1): (1, (0.6, 0.3, 0.55), (0.0, 0.0, 0.0)),              # one point
+    (8, 2, 1): (4, (1.0, 0.5, 0.5), (9 / 32, 1 / 32, 0.0)),         # pair_a
+    (9, 2, 1): (4, (0.0, 0.5, 0.5), (9 / 32, 1 / 32, 0.0)),         # pair_b
+}
+
+
+def test_kat_eigenvalues_closed_form():
+    """The reference's combined statistics and eigenvalues (gvom.py:888-980, 1423-1487) for
+    covariances known in closed form; the same scan in two slots, then two combines, so the
+    counts double on the second combine through the last combined map."""
+    fx = load(os.path.join(GOLDEN, "kat_eigen.npz"))
+    for ci, mult in ((0, 2), (1, 4)):
+        assert len(fx[f"c{ci}_comb_occ"]) == len(EIGEN_KAT)
+        for (x, y, z), (n, mean, lam) in EIGEN_KAT.items():
+            m = _comb_row(fx, ci, "metrics", x, y, z)
+            assert m[9] == mult * n, ((x, y, z), m[9])
+            np.testing.assert_allclose(m[:3], mean, rtol=1e-6, err_msg=str((x, y, z)))
+            np.testing.assert_allclose(_comb_row(fx, ci, "eigen", x, y, z), lam, rtol=1e-6, atol=1e-12,
+                                       err_msg=str((x, y, z)))
+
+
+# kat_posobs: cell -> positive-obstacle value, with the band sums behind it
+# (1 m voxels, positive threshold 0.5 m, robot height 2 m; gvom.py:515-555).
+POSOBS_KAT = {
+    (12, 8): 57,   # band z 2..3: z=2 hit 11 / total 19; z=3 hit 10 is not > 10
+    (8, 12): 50,   # fraction 0.5: band z 3..3, hit 11 / total 22 (z=2 would add 20 / 20)
+    (4, 8): 0,     # hits of 10 only: no density
+    (8, 4): 0,     # band top at z = 8, outside the grid: left at 0
+    (13, 13): 57,  # 29 / 50 = 0.58, and 0.58 * 100 = 57.99999999999999 truncates to 57
+    (4, 12): 67,   # both band voxels: (12 + 11) / (12 + 22)
+    (12, 3): 100,  # fraction 0: band z 2..3, hit 11 / total 11; z=4 is above the band
+    (1, 10): 81,   # fraction 0.5 - 2^-22: band z 2..3, (20 + 11) / (20 + 18)
+}
+
+
+def test_kat_positive_obstacle_band():
+    fx = load(os.path.join(GOLDEN, "kat_posobs.npz"))
+    pos = fx["c0_pos"]
+    for (x, y), want in POSOBS_KAT.items():
+        assert pos[x, y] == want, ((x, y), pos[x, y], want)
+    assert int(29 / 50 * 100) == 57  # the float64 quirk the kernel keeps
+    hit = _comb_row(fx, 0, "hit", 13, 13, 2)
+    total = _comb_row(fx, 0, "total", 13, 13, 2)
+    assert (hit, total) == (29, 50)
+    # a steep 3 x 3 patch (slope above 0.3 rad) is an obstacle whatever its band holds
+    assert (pos[3:6, 3:6] == 100).all()
+    assert np.hypot(fx["c0_slope_x"][4, 4], fx["c0_slope_y"][4, 4]) >= 0.3
