@@ -197,7 +197,7 @@ def scene_kat_posobs():
 
 def scene_synthetic(name, X=32, Z=16, res=0.5, B=3, beams=16, columns=256, n_scans=6,
                     combine_after=(1, 2, 4, 5), tdtype=np.float32, pdtype=np.float32,
-                    veg=0.0, dropout=0.0, eig=(1, 1)):
+                    veg=0.0, dropout=0.0, eig=(1, 1), zres=None):
     from gvom_gb300.synthetic import Lidar, Terrain, Vegetation, make_scan, make_trajectory
     terrain = Terrain.make(0, extent=X * res, path_len=n_scans * 0.4)
     vegetation = None
@@ -206,7 +206,7 @@ def scene_synthetic(name, X=32, Z=16, res=0.5, B=3, beams=16, columns=256, n_sca
         vegetation = Vegetation.make(terrain, (-ext, ext + n_scans), (-ext, ext), density=veg)
     lidar = Lidar(beams=beams, columns=columns)
     poses = make_trajectory(n_scans)
-    params = (res, res, X, Z, B, 1.0, 0.5, 0.5, 0.3, 2.0, 2.0, 1.0, eig[0], eig[1])
+    params = (res, res if zres is None else zres, X, Z, B, 1.0, 0.5, 0.5, 0.3, 2.0, 2.0, 1.0, eig[0], eig[1])
     ops = []
     for i, pose in enumerate(poses):
         s = make_scan(terrain, lidar, pose, i, vegetation=vegetation, footprint=X * res,
@@ -240,6 +240,12 @@ SCENES = {
     "synth_f64pts_eig20": lambda: scene_synthetic("synth_f64pts_eig20", pdtype=np.float64, eig=(2, 0),
                                                   n_scans=4, combine_after=(1, 3), B=2, dropout=0.3),
     "small_32x512": scene_small_32x512,
+    # the ROS node's default voxels (scripts/gvom_ros.py:24-25): 0.4 m across, 0.2 m high
+    "synth_aniso_z": lambda: scene_synthetic("synth_aniso_z", res=0.4, zres=0.2, n_scans=4, combine_after=(1, 3),
+                                             eig=(1, 2)),
+    # and the other way round, with float64 transforms
+    "synth_aniso_xy": lambda: scene_synthetic("synth_aniso_xy", X=40, Z=12, res=0.25, zres=0.5, n_scans=4,
+                                              combine_after=(0, 3), tdtype=np.float64),
 }
 
 
