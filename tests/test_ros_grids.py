@@ -37,6 +37,29 @@ def test_restatement_matches_numpy_astype_on_x86():
         np.testing.assert_array_equal(got[k], want[k], k)
 
 
+PAYLOAD_OF = {"h_obstacle_map_pub": "hard", "s_obstacle_map_pub": "soft", "g_certainty_pub": "certainty",
+              "a_certainty_pub": "certainty", "n_obstacle_map_pub": "negative", "r_map_pub": "roughness"}
+
+
+def test_restatement_matches_the_reference_callback():
+    """Pinned to the reference node itself: tests/golden/ros_epilogue.npz holds what
+    VoxelMapper.cb_timer (scripts/gvom_ros.py:113-166), run unchanged on x86 by
+    tests/golden/make_ros_golden.py, published for stored combine outputs and edge
+    cases (clip bounds, payloads outside int8, NaN, other node parameters)."""
+    import os
+    from conftest import GOLDEN
+    with np.load(os.path.join(GOLDEN, "ros_epilogue.npz")) as z:
+        fx = {k: z[k] for k in z.files}
+    names = str(fx["cases"]).split(",")
+    assert len(names) >= 6
+    for n in names:
+        thr, lo, hi = fx[f"{n}_params"]
+        got = ros_grids(fx[f"{n}_pos"], fx[f"{n}_neg"], fx[f"{n}_rough"], fx[f"{n}_vis"],
+                        density_threshold=thr, min_roughness=lo, max_roughness=hi)
+        for pub, key in PAYLOAD_OF.items():
+            np.testing.assert_array_equal(got[key], fx[f"{n}_{pub}"], f"{n} {pub}")
+
+
 @pytest.mark.gpu
 def test_device_payloads_equal_oracle(gpu_lib):
     from gvom_gb300 import Gvom
