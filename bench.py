@@ -107,7 +107,10 @@ class Clocks:
     def __init__(self, gpu_index, tag=""):
         self.p = None
         self.gpu = gpu_index
-        self.path = os.path.join(HERE, "gpurun_out", f"clocks_gpu{gpu_index}{tag}.csv")
+        # the raw samples go to $GVOM_CLOCKS_DIR (default: the temporary directory)
+        import tempfile
+        self.path = os.path.join(os.environ.get("GVOM_CLOCKS_DIR") or tempfile.gettempdir(),
+                                 f"gvom_clocks_gpu{gpu_index}{tag}.csv")
 
     def start(self):
         try:
