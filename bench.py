@@ -130,26 +130,33 @@ class Clocks:
         except Exception:
             self.p.kill()
         self.f.close()
-        rows = []
-        for line in open(self.path):
-            parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                rows.append(dict(sm=float(parts[1]), smax=float(parts[2]), active=parts[4],
-                                 hw=parts[5], hwt=parts[6], swt=parts[7], swp=parts[8]))
-            except ValueError:
-                continue
-        if not rows:
-            return None
-        reasons = set()
-        for r in rows:
-            for k, nm in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"), ("swt", "sw_thermal_slowdown"),
-                          ("swp", "sw_power_cap")):
-                if r[k].lower() == "active":
-                    reasons.add(nm)
-        return {"sm_mhz": statistics.median(r["sm"] for r in rows), "sm_max_mhz": max(r["smax"] for r in rows),
-                "samples": len(rows), "reasons": sorted(reasons)}
+        with open(self.path) as f:
+            return summarize_clocks(f)
+
+
+def summarize_clocks(lines):
+    """Median SM clock, its maximum and the throttle reasons seen, from
+    nvidia-smi CSV rows of Clocks.Q (no header, no units); None without rows."""
+    rows = []
+    for line in lines:
+        parts = [x.strip() for x in line.split(",")]
+        if len(parts) < 9:
+            continue
+        try:
+            rows.append(dict(sm=float(parts[1]), smax=float(parts[2]), active=parts[4],
+                             hw=parts[5], hwt=parts[6], swt=parts[7], swp=parts[8]))
+        except ValueError:
+            continue
+    if not rows:
+        return None
+    reasons = set()
+    for r in rows:
+        for k, nm in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"), ("swt", "sw_thermal_slowdown"),
+                      ("swp", "sw_power_cap")):
+            if r[k].lower() == "active":
+                reasons.add(nm)
+    return {"sm_mhz": statistics.median(r["sm"] for r in rows), "sm_max_mhz": max(r["smax"] for r in rows),
+            "samples": len(rows), "reasons": sorted(reasons)}
 
 
 def _safe(fn):

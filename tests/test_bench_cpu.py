@@ -1,4 +1,4 @@
-"""bench.py's host-side accounting on CPU: the whole-step roofline follows
+"""bench.py's host-side accounting on CPU: the clock summary, the whole-step roofline follows
 the per-unit work of the scan->map accounting, and an auxiliary figure that
 fails never breaks the bench line."""
 import bench
@@ -21,3 +21,16 @@ def test_step_roofline_per_unit_work():
 def test_safe_returns_none_on_failure():
     assert bench._safe(lambda: 1 / 0) is None
     assert bench._safe(lambda: 3) == 3
+
+
+def test_clock_summary_reads_nvidia_smi_rows():
+    rows = ["0, 2070, 2070, 900.1, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+            "0, 1980, 2070, 1390.5, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+            "0, 2070, 2070, 1200.0, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+            "0, [N/A], 2070, 0, 0x0, Not Active, Not Active, Not Active, Not Active",  # unreadable: skipped
+            "short row"]
+    s = bench.summarize_clocks(rows)
+    assert s == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "samples": 3, "reasons": ["sw_power_cap"]}
+    hot = bench.summarize_clocks(["0, 1500, 2070, 1400, 0x48, Active, Active, Not Active, Not Active"])
+    assert hot["reasons"] == ["hw_slowdown", "hw_thermal_slowdown"]
+    assert bench.summarize_clocks([]) is None
