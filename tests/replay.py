@@ -217,3 +217,24 @@ def float_errors(got_out, ref: dict, got_maps: dict) -> dict:
         "slope_x_rel": rel(got_maps["slope_x"], ref["slope_x"]),
         "slope_y_rel": rel(got_maps["slope_y"], ref["slope_y"]),
     }
+
+
+def stat_errors(got_state: dict, ref_state: dict) -> dict:
+    """Largest deviations of the combined per-voxel statistics from the oracle,
+    on canonical states with the same occupied set: absolute for the mean and
+    the covariance (voxel units), and for the eigenvalues relative to each
+    voxel's largest eigenvalue magnitude."""
+    g = canonical_state(got_state)
+    r = canonical_state(ref_state)
+    assert_exact(g["occ"], r["occ"], "occupied set")
+    gm = np.asarray(g["metrics"], np.float64)
+    rm = np.asarray(r["metrics"], np.float64)
+    out = {"voxels": int(len(r["occ"])),
+           "mean_abs": float(np.max(np.abs(gm[:, :3] - rm[:, :3]))) if len(rm) else 0.0,
+           "cov_abs": float(np.max(np.abs(gm[:, 3:9] - rm[:, 3:9]))) if len(rm) else 0.0}
+    if "eigen" in g and "eigen" in r and len(rm):
+        ge = np.asarray(g["eigen"], np.float64)
+        re = np.asarray(r["eigen"], np.float64)
+        scale = np.maximum(np.abs(re).max(axis=1, keepdims=True), 1e-30)
+        out["eigen_rel_to_max"] = float(np.max(np.abs(ge - re) / scale))
+    return out

@@ -236,7 +236,7 @@ def test_precision_form_os1_128_far_vs_float64_oracle(Gvom):
     import json
     import torch
     from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
-    from replay import float_errors
+    from replay import float_errors, stat_errors
     w = WORKLOADS["os1_128_far"]
     scans = make_workload_scans(w, 2, device="cuda" if torch.cuda.is_available() else "cpu")
     g, o = _run_both(Gvom, w.gvom_args(), scans)
@@ -246,6 +246,7 @@ def test_precision_form_os1_128_far_vs_float64_oracle(Gvom):
     compare_combine(out, refd, g.maps_state(), w.gvom_args(), "final combine")
     errs = float_errors(out, refd, g.maps_state())
     print("PRECISION os1_128_far " + json.dumps(errs))
+    print("PRECISION os1_128_far stats " + json.dumps(stat_errors(g.combined_state(), o.combined_state())))
     assert errs["height_abs"] <= 1e-4 and errs["inferred_abs"] <= 1e-4
     assert errs["roughness_rel"] <= 1e-3 and errs["slope_x_rel"] <= 1e-3 and errs["slope_y_rel"] <= 1e-3
 
