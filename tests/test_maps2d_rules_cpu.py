@@ -1,0 +1,125 @@
+"""The shortcuts of the 2-D map kernels, restated in numpy and checked
+against the oracle's float64 maps on every golden fixture (CPU):
+
+* k_maps2d answers a cell's slope and roughness with a float32 plane fit
+  unless one of its rules sends the cell to the reference's float64 sequence
+  or a closed form (gvom_gb300/csrc/k_combine.cu, k_maps2d).  Every cell the
+  rules leave to float32 must stay well inside the 1e-3 relative tolerance.
+* k_columns takes the positive-obstacle band ends from float32
+  minh + threshold / z_res unless that lies within 1e-4 of an integer
+  (gvom_gb300/csrc/k_combine.cu, k_columns); outside that margin the band
+  must equal the reference's float64 floor((h + thr) / z_res - oz)
+  (scripts/gvom.py:529-533)."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_files
+from oracle.oracle import OracleGvom
+from replay import load, ops_of, params_of
+
+f32 = np.float32
+
+
+def _combines(name):
+    fx = load(os.path.join(GOLDEN, name))
+    p = params_of(fx)
+    o = OracleGvom(*p)
+    for op in ops_of(fx):
+        if op[0] == "P":
+            o.Process_pointcloud(*op[2:])
+        else:
+            yield p, o, o.combine_maps()
+
+
+def _lowest(o, X, Z):
+    cs = o.combined_state()
+    idx = cs["index"].reshape(Z, X, X)  # [z][y][x]
+    occ = idx >= 0
+    any_occ = occ.any(axis=0)
+    zl = np.where(any_occ, occ.argmax(axis=0), -1).T  # [x][y]
+    ml = np.zeros((X, X), np.float32)
+    xs, ys = np.nonzero(zl >= 0)
+    ml[xs, ys] = cs["min_h"][idx[zl[xs, ys], ys, xs]]
+    return zl, ml
+
+
+def _float32_fit(H, zl, ml, x0, y0, X, res, zres):
+    """(slope_x, slope_y, log err) of the kernel's float32 fit, or None where
+    its rules take the float64 sequence or a closed form instead."""
+    pts = [(xx, yy) for xx in range(max(0, x0 - 1), min(X, x0 + 2))
+           for yy in range(max(0, y0 - 1), min(X, y0 + 2)) if H[xx, yy] > -1000.0]
+    n = len(pts)
+    if n < 3:
+        return None
+    hs = np.array([H[p] for p in pts])
+    ox = np.array([p[0] - x0 for p in pts])
+    oy = np.array([p[1] - y0 for p in pts])
+    dxx = n * (ox * ox).sum() - ox.sum() ** 2
+    dyy = n * (oy * oy).sum() - oy.sum() ** 2
+    dxy = n * (ox * oy).sum() - ox.sum() * oy.sum()
+    if ((hs == hs[0]).all() and dxx * dyy - dxy * dxy != 0) or dxx == 0 or dyy == 0:
+        return None  # closed forms, or a row / column of neighbours
+    dx = (ox.astype(f32) - f32(ox.sum()) / f32(n)) * f32(res)
+    dy = (oy.astype(f32) - f32(oy.sum()) / f32(n)) * f32(res)
+    p0 = pts[0]
+    if all(zl[p] >= 0 for p in pts):
+        dz = np.array([((ml[p] - ml[p0]) + f32(zl[p] - zl[p0])) * f32(zres) for p in pts], f32)
+    else:
+        dz = np.array([f32(H[p] - H[p0]) for p in pts], f32)
+    dz = (dz - f32(dz.sum(dtype=f32) / f32(n))).astype(f32)
+    s = lambda a, b: f32((a * b).sum(dtype=f32))  # noqa: E731
+    sxx, sxy, sxz, syy, syz, szz = s(dx, dx), s(dx, dy), s(dx, dz), s(dy, dy), s(dy, dz), s(dz, dz)
+    det = f32(sxx * syy - sxy * sxy)
+    if not abs(det) > f32(1e-3) * sxx * syy:
+        return None
+    a0 = f32((syy * sxz - sxy * syz) / det)
+    a1 = f32((sxx * syz - sxy * sxz) / det)
+    m = f32(np.sqrt(a0 * a0 + a1 * a1 + f32(1)))
+    a0, a1 = f32(a0 / m), f32(a1 / m)
+    e = (dz - (a0 * dx + a1 * dy)).astype(f32)
+    err = f32((e * e).sum(dtype=f32) / f32(n))
+    rf = float(np.log(err)) if err > 0 else -math.inf
+    sx, sy = float(np.arctan2(a0, 1 / m)), float(np.arctan2(a1, 1 / m))
+    big, small = max(abs(sx), abs(sy)), min(abs(sx), abs(sy))
+    if not err > f32(1e-4) * (szz / f32(n)) or abs(rf) < 0.1 or small < 5e-3 * big or big < 2e-3:
+        return None
+    return sx, sy, rf
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_float32_plane_fit_cells_within_tolerance(name):
+    for p, o, out in _combines(name):
+        res, zres, X, Z = p[0], p[1], p[2], p[3]
+        H = o.maps_state()["height"]
+        m = o.maps_state()
+        zl, ml = _lowest(o, X, Z)
+        worst = 0.0
+        for x0 in range(X):
+            for y0 in range(X):
+                r = _float32_fit(H, zl, ml, x0, y0, X, res, zres)
+                if r is None:
+                    continue
+                for got, ref in zip(r, (m["slope_x"][x0, y0], m["slope_y"][x0, y0], out[3][x0, y0])):
+                    if ref != 0:
+                        worst = max(worst, abs(got - ref) / abs(ref))
+        assert worst < 2.5e-4, (name, worst)
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_float32_band_ends_equal_float64(name):
+    for p, o, out in _combines(name):
+        zres, X, Z, pthr, robh = p[1], p[2], p[3], p[6], p[9]
+        pv, rv = f32(pthr / zres), f32(robh / zres)
+        oz = round(float(out[0][2]) / zres)
+        zl, ml = _lowest(o, X, Z)
+        for x, y in zip(*np.nonzero(zl >= 0)):
+            z, mh = int(zl[x, y]), ml[x, y]
+            wmin, wmax = f32(mh + pv), f32(mh + rv)
+            if min(abs(float(w) - round(float(w))) for w in (wmin, wmax)) <= 1e-4:
+                continue  # the kernel takes the float64 formula
+            h = (float(mh) + z + oz) * zres
+            ref = (math.floor((h + pthr) / zres - oz) + 1, math.floor((h + robh) / zres - oz))
+            assert (z + math.floor(wmin) + 1, z + math.floor(wmax)) == ref, (name, x, y)
