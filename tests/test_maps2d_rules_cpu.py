@@ -9,7 +9,8 @@ against the oracle's float64 maps on every golden fixture (CPU):
   minh + threshold / z_res unless that lies within 1e-4 of an integer
   (gvom_gb300/csrc/k_combine.cu, k_columns); outside that margin the band
   must equal the reference's float64 floor((h + thr) / z_res - oz)
-  (scripts/gvom.py:529-533)."""
+  (scripts/gvom.py:529-533).
+* k_columns decides the robot disc in float32 away from its rim."""
 import math
 import os
 
@@ -123,3 +124,34 @@ def test_float32_band_ends_equal_float64(name):
             h = (float(mh) + z + oz) * zres
             ref = (math.floor((h + pthr) / zres - oz) + 1, math.floor((h + robh) / zres - oz))
             assert (z + math.floor(wmin) + 1, z + math.floor(wmax)) == ref, (name, x, y)
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_float32_robot_disc_equals_float64(name):
+    """k_columns decides the robot disc (scripts/gvom.py:566-570) in float32
+    unless the cell is within 1e-3 r^2 + 1e-4 of the rim; outside that margin
+    the float32 decision must equal the reference's float64 one."""
+    fx = load(os.path.join(GOLDEN, name))
+    p = params_of(fx)
+    res, X, r = p[0], p[2], p[10]
+    ego, ci = None, 0
+    checked = 0
+    for op in ops_of(fx):
+        if op[0] == "P":
+            ego = np.asarray(op[3], np.float64)
+            continue
+        co = fx[f"c{ci}_origin"] / np.array([res, res, p[1]])
+        co = np.round(co)
+        base_x, base_y = f32(co[0] * res - ego[0]), f32(co[1] * res - ego[1])
+        xs = np.arange(X)
+        xp = (base_x + xs.astype(f32) * f32(res)).astype(f32)
+        s = (xp[:, None] * xp[:, None] + (base_y + xs.astype(f32) * f32(res)).astype(f32)[None, :] ** 2).astype(f32)
+        r2f = f32(r * r)
+        far = np.abs(s - r2f) > f32(1e-3) * r2f + f32(1e-4)
+        xd = (co[0] + xs) * res - ego[0]
+        yd = (co[1] + xs) * res - ego[1]
+        ref = (xd[:, None] * xd[:, None] + yd[None, :] * yd[None, :]) <= r * r
+        assert np.array_equal((s <= r2f)[far], ref[far]), name
+        checked += int(far.sum())
+        ci += 1
+    assert checked > 0
