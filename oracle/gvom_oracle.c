@@ -12,6 +12,10 @@
  * with -ffp-contract=off so no multiply-add is fused (the reference's CPU path,
  * the Numba CUDA simulator, evaluates every operation separately too).
  *
+ * Pinned: tests/test_oracle_golden.py checks it, floats included, bit for bit
+ * against the reference's own outputs (tests/golden/*.npz, made by running
+ * scripts/gvom.py unchanged through tests/golden/make_golden.py).
+ *
  * Modes: threads == 1 runs every kernel sequentially in thread-index order
  * (a valid schedule of the reference's launches: its atomics make all integer
  * results order-free, and compact indices are order-dependent but not
