@@ -195,6 +195,33 @@ def scene_kat_posobs():
     return kat_params(B=1), [P(pts, ego), ("C",)]
 
 
+def scene_kat_boundaries():
+    """Points on and next to voxel faces of a 0.2 m grid (p / res lands on, just under or just over
+    an integer in float64), on the min-distance sphere in float32 arithmetic, on the grid's outer
+    faces, and with negative zero coordinates (gvom.py:1145-1171, 1254-1264, 1399-1416)."""
+    res = 0.2
+    pts = []
+    for k in range(-14, 15):  # multiples of 0.1 m along each axis, and diagonals
+        v = np.float32(0.1 * k)
+        pts += [(v, 1.55, 0.15), (1.55, v, 0.15), (1.35, 1.25, v * np.float32(0.5)), (v, v, np.float32(1.1))]
+    for v in (0.6, 1.0, 1.2, 1.4, -0.6, -1.0):  # float32 neighbours of face coordinates
+        f = np.float32(v)
+        for w in (np.nextafter(f, np.float32(-9)), f, np.nextafter(f, np.float32(9))):
+            pts += [(w, -1.45, 0.05), (-1.45, w, 0.05), (1.55, 1.45, w * np.float32(0.5))]
+    for ang in np.linspace(0.0, 2 * np.pi, 24, endpoint=False):  # on the 1 m min-distance sphere
+        pts.append((np.float32(np.cos(ang)), np.float32(np.sin(ang)), np.float32(0.0)))
+    pts += [(-0.0, 1.5, -0.0), (1.5, -0.0, 0.0), (0.0, -0.0, 1.25)]
+    half = 16 * res  # grid of 32 x 32 x 16 around ego (0.1, 0.1, 0.1): x in [-3.2, 3.2)
+    for e in (-half, half):
+        f = np.float32(e)
+        for w in (np.nextafter(f, np.float32(-9)), f, np.nextafter(f, np.float32(9))):
+            pts += [(w, 1.3, 0.05), (1.3, w, 0.05)]
+    params = (res, res, 32, 16, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 2.0, 1.0, 1, 1)
+    pts = np.asarray(pts, np.float32)
+    return params, [("P", pts, (0.1, 0.1, 0.1), None), ("C",),
+                    ("P", pts[::-1].copy(), (0.3, -0.1, 0.1), None), ("C",)]
+
+
 def scene_synthetic(name, X=32, Z=16, res=0.5, B=3, beams=16, columns=256, n_scans=6,
                     combine_after=(1, 2, 4, 5), tdtype=np.float32, pdtype=np.float32,
                     veg=0.0, dropout=0.0, eig=(1, 1), zres=None):
@@ -234,6 +261,7 @@ SCENES = {
     "kat_guess": scene_kat_guess,
     "kat_eigen": scene_kat_eigen,
     "kat_posobs": scene_kat_posobs,
+    "kat_boundaries": scene_kat_boundaries,
     "synth_f32": lambda: scene_synthetic("synth_f32"),
     "synth_f64T_veg": lambda: scene_synthetic("synth_f64T_veg", tdtype=np.float64, veg=2.0, n_scans=5,
                                               combine_after=(0, 2, 4)),
