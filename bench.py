@@ -317,6 +317,23 @@ def step_roofline(n_pts, ns, V, X2, B, C_new, C_sum, Cc, hits, steps, peak_gbs, 
             "frac_of_measured_hbm": t_hbm / (ms_per_step / 1e3)}
 
 
+# Scattered 64-bit L2 reductions (atomicAdd without return to random words of
+# a 35 MB array) sustained 200-225 G/s on this part in a throughput probe; the
+# lower figure is the trace kernel's atomic ceiling.
+RED64_SCATTERED_PER_S = 200e9
+
+
+def trace_atomic_roofline(hits, steps, ms_per_launch, peak=RED64_SCATTERED_PER_S):
+    """The ray-trace kernel against the L2 reduction rate: its int32 atomics
+    (2H + S of the last scan: a hit and a total per hit, one total per ray
+    step) per launch over its measured launch time."""
+    atomics = 2 * hits + steps
+    achieved = atomics / (ms_per_launch / 1e3)
+    return {"bound": "l2_atomics", "atomics_per_launch": int(atomics), "achieved_per_s": achieved,
+            "peak_per_s": peak, "frac": achieved / peak,
+            "peak_source": "scattered 64-bit reduction throughput probe on GB300 (200-225 G/s; lower figure)"}
+
+
 def _reduce_max_sum(torch, dist, t_val, pts):
     """(max over ranks of the timed seconds, sum over ranks of the points)."""
     if not dist:
@@ -542,6 +559,8 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
         "step_roofline": _safe(lambda: step_roofline(n_mean, ns, V, X * X, w.buffer_size, C_new, C_sum, ncc.value,
                                                      ray["hits"], ray["ray_steps"], peak,
                                                      1e3 * t_dev_max / n_steps)),
+        "trace_atomic_roofline": _safe(lambda: trace_atomic_roofline(
+            ray["hits"], ray["ray_steps"], stage_tab["k_voxelize_trace"]["ms_per_launch"])),
         "stages": stage_tab,
         "ray_last_scan": ray,
         "wall_s_timed": wall_timed,
@@ -660,7 +679,8 @@ def run_gpu(args):
             "data": "synthetic (seeded terrain / lidar / trajectory generator)",
             "config": dict(res["config"], parallelism=f"replicas x{world}"),
             "latency_ms": res["latency_ms"], "e2e": res["e2e"], "gpu_launches": res["gpu_launches"],
-            "roofline": res["roofline"], "step_roofline": res.get("step_roofline"), "stages": res["stages"],
+            "roofline": res["roofline"], "step_roofline": res.get("step_roofline"),
+            "trace_atomic_roofline": res.get("trace_atomic_roofline"), "stages": res["stages"],
             "ray_last_scan": res["ray_last_scan"],
             "direct_launches": res["direct_launches"], "l2_flushed_per_step": res["l2_flushed_per_step"],
             "wall_s_timed": res["wall_s_timed"], "clocks": res["clocks"], "cpu_baseline": cpu,
