@@ -33,8 +33,16 @@ from . import _lib
 from ._lib import GVOM_F32, GVOM_F64, GVOM_NO_DATA, GVOM_NONE, GvomParams, GvomScan, check
 
 
+def _native_float(dt) -> bool:
+    return dt.char in "fd" and dt.isnative
+
+
 def _as_points(pointcloud):
     """Return (pointer, dtype code, n, row_stride, keepalive, on_device)."""
+    if type(pointcloud) is np.ndarray:  # the common case, without conversions
+        a = pointcloud
+        if a.ndim == 2 and a.shape[1] >= 3 and _native_float(a.dtype) and a.flags.c_contiguous:
+            return a.ctypes.data, (GVOM_F64 if a.dtype.char == "d" else GVOM_F32), a.shape[0], a.shape[1], a, False
     try:  # torch tensor?
         import torch  # noqa: F401
         is_tensor = type(pointcloud).__module__.startswith("torch")
@@ -62,12 +70,15 @@ def _as_points(pointcloud):
     if not a.flags.c_contiguous:
         a = np.ascontiguousarray(a)
     code = GVOM_F64 if a.dtype == np.float64 else GVOM_F32
-    return a.ctypes.data_as(C.c_void_p), code, a.shape[0], a.shape[1], a, False
+    return a.ctypes.data, code, a.shape[0], a.shape[1], a, False
 
 
 def _as_transform(transform):
     if transform is None:
         return None, GVOM_NONE, None
+    if type(transform) is np.ndarray and transform.shape == (4, 4) and _native_float(transform.dtype) \
+            and transform.flags.c_contiguous:
+        return transform.ctypes.data, (GVOM_F64 if transform.dtype.char == "d" else GVOM_F32), transform
     try:
         import torch
         if isinstance(transform, torch.Tensor):
@@ -78,7 +89,7 @@ def _as_transform(transform):
     if T.dtype not in (np.float32, np.float64):
         T = T.astype(np.float64)
     T = np.ascontiguousarray(T.reshape(4, 4))
-    return T.ctypes.data_as(C.c_void_p), (GVOM_F64 if T.dtype == np.float64 else GVOM_F32), T
+    return T.ctypes.data, (GVOM_F64 if T.dtype == np.float64 else GVOM_F32), T
 
 
 def _ego3(ego_position):
@@ -155,7 +166,7 @@ class Gvom:
         tptr, tcode, tkeep = _as_transform(transform)
         ego = _ego3(ego_position)
         fn = self._l.gvom_process_device if on_dev else self._l.gvom_process
-        check(fn(self._h, ptr, code, n, stride, ego.ctypes.data_as(C.c_void_p), tptr, tcode))
+        check(fn(self._h, ptr, code, n, stride, ego.ctypes.data, tptr, tcode))
         if on_dev:
             # the library runs on its own stream; keep the tensor alive until the scan is consumed
             self.synchronize()
@@ -171,8 +182,8 @@ class Gvom:
         neg = np.empty((X, X), np.int32)
         rough = np.empty((X, X), np.float64)
         vis = np.empty((X, X), np.int32)
-        P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
-        rc = self._l.gvom_combine(self._h, P(origin), P(pos), P(neg), P(rough), P(vis))
+        rc = self._l.gvom_combine(self._h, origin.ctypes.data, pos.ctypes.data, neg.ctypes.data, rough.ctypes.data,
+                                  vis.ctypes.data)
         if rc == GVOM_NO_DATA:
             print("ERROR: No data in buffer")
             return None
@@ -297,7 +308,7 @@ class Gvom:
         vis) CUDA tensors fills them stream-ordered and returns the origin."""
         arr, keep, on_dev = self._scan_array(scans)
         origin = np.zeros(3, np.float64)
-        P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        P = lambda a: a.ctypes.data  # noqa: E731
         if device_outputs is not None:
             ptrs = [C.c_void_p(t.data_ptr()) for t in device_outputs]
             check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, P(origin), *ptrs, 1))
