@@ -283,13 +283,14 @@ class Gvom:
             tptr, tcode, tk = _as_transform(T)
             keep += [k, tk]
             e = _ego3(ego)
-            arr[i].points = ptr
-            arr[i].dtype = code
-            arr[i].transform_dtype = tcode
-            arr[i].n = n
-            arr[i].row_stride = stride
-            arr[i].ego[:] = list(e)
-            arr[i].transform = tptr
+            sc = arr[i]
+            sc.points = ptr
+            sc.dtype = code
+            sc.transform_dtype = tcode
+            sc.n = n
+            sc.row_stride = stride
+            sc.ego[:] = e.tolist()
+            sc.transform = tptr
         return arr, keep, bool(on_dev)
 
     def process_batch(self, scans):
