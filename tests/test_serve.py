@@ -1,5 +1,5 @@
-"""Served form (gvom_gb300/serve.py): admission policy and arrival process on
-the CPU; on the GPU, two instances served concurrently with continuous
+"""Served form (gvom_gb300/serve.py): admission policy, arrival process and
+the request loop (with a stand-in mapper) on the CPU; on the GPU, two instances served concurrently with continuous
 batching give, batch by batch, the same maps as the same batches run alone."""
 import numpy as np
 import pytest
@@ -68,3 +68,92 @@ def test_served_mix_equals_alone(gpu_lib):
         for a, b in zip(alone, served):
             for x, y in zip(a, b):
                 np.testing.assert_array_equal(x, y)
+
+
+class _FakeMapper:
+    """Stands in for Gvom in the request loop (CPU): records the calls, blocks
+    the first process call until released, numbers its combines."""
+    gate = None
+    entered = {}
+    calls = []
+
+    def __init__(self, *params):
+        self.params = params
+        self.combines = 0
+        self.first = True
+
+    def set_stream(self, s):
+        pass
+
+    def set_graphs(self, on):
+        pass
+
+    def _process(self, kind, scans):
+        if self.first and _FakeMapper.gate is not None:
+            self.first = False
+            _FakeMapper.entered[self.params[4]].set()
+            _FakeMapper.gate.wait(10)
+        if any(np.isnan(p).any() for p, _, _ in scans):
+            raise RuntimeError("bad scan")
+        _FakeMapper.calls.append((self.params[4], kind, [p.shape[0] for p, _, _ in scans]))
+
+    def Process_pointcloud(self, points, ego, transform=None):
+        self._process("one", [(points, ego, transform)])
+
+    def process_batch(self, scans):
+        self._process("batch", scans)
+
+    def combine_maps(self):
+        self.combines += 1
+        return ("map", self.params[4], self.combines)
+
+    def close(self):
+        pass
+
+
+def test_request_loop_batches_and_answers(monkeypatch):
+    """Continuous batching on CPU with a stand-in mapper: while an instance's
+    first scan is on the (fake) device, later requests queue and go out as one
+    batch, within the ring-slot and point limits; every request is answered
+    with the map of its own batch; a failing batch answers with its error."""
+    import threading
+    import types
+
+    import torch
+
+    from gvom_gb300 import serve
+    monkeypatch.setattr(serve, "Gvom", _FakeMapper)
+    fake_cuda = types.SimpleNamespace(Stream=lambda: types.SimpleNamespace(cuda_stream=0),
+                                      mem_get_info=lambda: (8 << 30, 16 << 30), set_stream=lambda s: None)
+    monkeypatch.setattr(torch, "cuda", fake_cuda)
+    _FakeMapper.gate = threading.Event()
+    _FakeMapper.entered = {4: threading.Event(), 2: threading.Event()}
+    _FakeMapper.calls = []
+    p4 = (0.2, 0.2, 32, 16, 4, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    p2 = p4[:4] + (2,) + p4[5:]
+    srv = serve.MapServer([p4, p2], point_budget=1000)
+    pts = lambda n: np.zeros((n, 3), np.float32)  # noqa: E731
+    first = srv.submit(0, pts(10), (0, 0, 0))
+    assert _FakeMapper.entered[4].wait(10)  # the first scan is on the device alone
+    queued = [srv.submit(0, pts(300), (0, 0, 0)) for _ in range(6)]  # 4 slots, 1000 points -> 3 + 3
+    other = [srv.submit(1, pts(5), (0, 0, 0)) for _ in range(3)]
+    _FakeMapper.gate.set()
+    for r in [first] + queued + other:
+        assert r.done.wait(10)
+    bad = srv.submit(1, np.full((2, 3), np.nan, np.float32), (0, 0, 0))
+    assert bad.done.wait(10)
+    after = srv.submit(1, pts(5), (0, 0, 0))  # the loop goes on after a failed batch
+    assert after.done.wait(10)
+    srv.close()
+    assert first.result == ("map", 4, 1)
+    inst0 = [c for c in _FakeMapper.calls if c[0] == 4]
+    assert inst0[0] == (4, "one", [10])
+    assert [c[2] for c in inst0[1:]] == [[300, 300, 300], [300, 300, 300]]
+    assert [r.result[2] for r in queued] == [2, 2, 2, 3, 3, 3]
+    assert len({r.batch_id for r in queued}) == 2
+    assert all(isinstance(r.result, tuple) and r.result[1] == 2 for r in other)
+    assert isinstance(bad.result, RuntimeError)
+    assert isinstance(after.result, tuple) and after.result[1] == 2
+    seqs = sorted(s for _, b in srv.batches for s in b)
+    assert seqs == list(range(12))
+    assert all(r.latency >= 0 for r in [first] + queued + other)
