@@ -559,8 +559,9 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
         "step_roofline": _safe(lambda: step_roofline(n_mean, ns, V, X * X, w.buffer_size, C_new, C_sum, ncc.value,
                                                      ray["hits"], ray["ray_steps"], peak,
                                                      1e3 * t_dev_max / n_steps)),
+        # one scan per launch only: the counters are the last scan's
         "trace_atomic_roofline": _safe(lambda: trace_atomic_roofline(
-            ray["hits"], ray["ray_steps"], stage_tab["k_voxelize_trace"]["ms_per_launch"])),
+            ray["hits"], ray["ray_steps"], stage_tab["k_voxelize_trace"]["ms_per_launch"])) if ns == 1 else None,
         "stages": stage_tab,
         "ray_last_scan": ray,
         "wall_s_timed": wall_timed,
