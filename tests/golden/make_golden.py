@@ -268,6 +268,10 @@ SCENES = {
     "synth_f64pts_eig20": lambda: scene_synthetic("synth_f64pts_eig20", pdtype=np.float64, eig=(2, 0),
                                                   n_scans=4, combine_after=(1, 3), B=2, dropout=0.3),
     "small_32x512": scene_small_32x512,
+    # a long run: 12 scans through a 2-slot ring, a combine after each (counts and pass counts
+    # accumulate through the last combined map, gvom.py:242-298)
+    "synth_longrun": lambda: scene_synthetic("synth_longrun", B=2, columns=128, n_scans=12,
+                                             combine_after=tuple(range(12))),
     # the ROS node's default voxels (scripts/gvom_ros.py:24-25): 0.4 m across, 0.2 m high
     "synth_aniso_z": lambda: scene_synthetic("synth_aniso_z", res=0.4, zres=0.2, n_scans=4, combine_after=(1, 3),
                                              eig=(1, 2)),
