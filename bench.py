@@ -15,6 +15,13 @@ no dataset, so synthetic scans of the named shapes stand in for its logs):
       0.15 m, buffer 16.  One step = the 8 scans of one vehicle pose through
       one process_batch (one set of launches over all scans) followed by
       combine_maps.
+  served: two device-resident instances behind the request loop of
+      gvom_gb300.serve, Poisson arrivals; p50 / p99 scan->map latency.
+  ros: the reference ROS node's two ends on the headline workload: each step
+      maps one lidar message from host bytes (process_pointcloud2 with the tf
+      translation and quaternion) and reads back combine_maps' outputs and
+      the five OccupancyGrid payloads (ros_grids), beside the host time of
+      the conversions the node would run for the same message and maps.
 
 Metric: points/sec = points ingested per step / step time.
 
@@ -41,6 +48,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -332,6 +340,99 @@ def trace_atomic_roofline(hits, steps, ms_per_launch, peak=RED64_SCATTERED_PER_S
     return {"bound": "l2_atomics", "atomics_per_launch": int(atomics), "achieved_per_s": achieved,
             "peak_per_s": peak, "frac": achieved / peak,
             "peak_source": "scattered 64-bit reduction throughput probe on GB300 (200-225 G/s; lower figure)"}
+
+
+def _quat_xyzw(R):
+    """Unit quaternion (x, y, z, w) of a rotation matrix (Shepperd's method)."""
+    R = np.asarray(R, np.float64)
+    tr = R[0, 0] + R[1, 1] + R[2, 2]
+    if tr > 0.0:
+        s = 2.0 * math.sqrt(tr + 1.0)
+        return np.array([(R[2, 1] - R[1, 2]) / s, (R[0, 2] - R[2, 0]) / s, (R[1, 0] - R[0, 1]) / s, 0.25 * s])
+    i = int(np.argmax(np.diag(R)))
+    j, k = (i + 1) % 3, (i + 2) % 3
+    s = 2.0 * math.sqrt(1.0 + R[i, i] - R[j, j] - R[k, k])
+    q = np.empty(4)
+    q[i] = 0.25 * s
+    q[j] = (R[j, i] + R[i, j]) / s
+    q[k] = (R[k, i] + R[i, k]) / s
+    q[3] = (R[k, j] - R[j, k]) / s
+    return q
+
+
+def lidar_message(points, rng, point_step=48):
+    """A PointCloud2-style payload of `points`: float32 x, y, z at byte
+    offsets 0, 4, 8 of each `point_step`-byte point, other fields random."""
+    rows = rng.random((points.shape[0], point_step // 4), dtype=np.float32)
+    rows[:, :3] = points
+    return rows
+
+
+def node_host_work(rows, maps, density_threshold=50, min_roughness=-10, max_roughness=0):
+    """The host conversions the reference's ROS node runs for one message and
+    one map (scripts/gvom_ros.py:108, 141-164), which process_pointcloud2 and
+    ros_grids move to the device: the message's x, y, z fields to a float64
+    (N, 3) array without non-finite rows, and the five int8 payloads."""
+    import warnings
+    xyz = np.empty((rows.shape[0], 3), np.float64)
+    xyz[:, 0], xyz[:, 1], xyz[:, 2] = rows[:, 0], rows[:, 1], rows[:, 2]
+    xyz = xyz[np.isfinite(xyz).all(axis=1)]
+    _, obs, neg, rough, cert = maps
+    F = lambda a: np.reshape(a, -1, order="F")  # noqa: E731
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        out = [F(np.maximum(100 * (obs > density_threshold), neg)).astype(np.int8),
+               F(100 * (obs <= density_threshold) * (obs > 0)).astype(np.int8),
+               F(cert * 100).astype(np.int8), F(neg).astype(np.int8),
+               F(((np.maximum(np.minimum(rough, max_roughness), min_roughness) + min_roughness)
+                  / (max_roughness - min_roughness)) * 100).astype(np.int8)]
+    return xyz, out
+
+
+def measure_ros(form, torch, n_steps=200, warmup=5):
+    """The reference ROS node's two ends on the headline workload: each step
+    maps one lidar message from host memory (process_pointcloud2: bytes,
+    tf translation and quaternion) and reads back combine_maps' outputs and
+    the five OccupancyGrid payloads (ros_grids).  Reported beside the host
+    time of the conversions the node itself would run for the same message
+    and maps."""
+    from gvom_gb300 import Gvom
+    rng = np.random.default_rng(5)
+    msgs = []
+    for st in form.steps[:24]:
+        s = st[0]
+        T = np.asarray(s.transform, np.float64)
+        msgs.append((lidar_message(s.points, rng), s.points.shape[0], s.ego, T[:3, 3].copy(), _quat_xyzw(T[:3, :3])))
+    g = Gvom(*form.w.gvom_args())
+    t_in, t_comb, t_grid, pts, maps = [], [], [], 0, None
+    for k in range(warmup + n_steps):
+        rows, n, ego, t, q = msgs[k % len(msgs)]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.process_pointcloud2(rows, n, 48, (0, 4, 8), ego, t, q)
+        t1 = time.perf_counter()
+        maps = g.combine_maps()
+        t2 = time.perf_counter()
+        g.ros_grids()
+        t3 = time.perf_counter()
+        if k >= warmup:
+            t_in.append(t1 - t0)
+            t_comb.append(t2 - t1)
+            t_grid.append(t3 - t2)
+            pts += n
+    g.close()
+    host = []
+    for k in range(20):
+        t0 = time.perf_counter()
+        node_host_work(msgs[k % len(msgs)][0], maps)
+        host.append(time.perf_counter() - t0)
+    us = lambda v: 1e6 * float(np.median(v))  # noqa: E731
+    total = sum(t_in) + sum(t_comb) + sum(t_grid)
+    return {"workload": form.name, "steps": n_steps, "point_step_bytes": 48,
+            "points_per_s": pts / total,
+            "entry": "process_pointcloud2 (host bytes, translation + quaternion), combine_maps, ros_grids",
+            "us_p50": {"process_pointcloud2": us(t_in), "combine_maps": us(t_comb), "ros_grids": us(t_grid)},
+            "node_host_conversions_us_p50": us(host)}
 
 
 def _reduce_max_sum(torch, dist, t_val, pts):
@@ -665,10 +766,14 @@ def run_gpu(args):
             if world == 1:
                 forms[name] = measure_served(args, torch)
             continue
+        if name == "ros":  # measured below, on the headline workload
+            continue
         fm = Form(name, "cuda", FORM_DISTINCT_STEPS)
         forms[name] = measure_form(fm, args, torch, dist, lrank, flush, headline=False)
         if rank == 0 and world == 1 and not args.no_cpu_baseline:
             forms[name]["cpu_baseline"] = cpu_baseline(fm, budget_s=6.0)
+    if world == 1 and "ros" in [f for f in args.forms.split(",")]:
+        forms["ros"] = _safe(lambda: measure_ros(head, torch))
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(head)
@@ -700,7 +805,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="gvom", choices=["gvom", "reference"])
     ap.add_argument("--workload", default="os1_64_veg", help="headline form")
-    ap.add_argument("--forms", default="batched_8,served", help="comma-separated other forms measured in the same run")
+    ap.add_argument("--forms", default="batched_8,served,ros",
+                    help="comma-separated other forms measured in the same run")
     ap.add_argument("--served-seconds", type=float, default=3.0, help="arrival window of the served form")
     ap.add_argument("--form-steps", type=int, default=300, help="timed steps of each other form")
     ap.add_argument("--no-cpu-baseline", action="store_true")

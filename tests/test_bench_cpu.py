@@ -42,3 +42,32 @@ def test_trace_atomic_roofline():
     assert abs(r["achieved_per_s"] - 6_990_000 / 61.4e-6) < 1.0
     assert abs(r["frac"] - r["achieved_per_s"] / bench.RED64_SCATTERED_PER_S) < 1e-12
     assert 0.5 < r["frac"] < 0.6
+
+
+def test_quaternion_round_trip_and_node_host_work(gpu_lib):
+    """bench.py's message builder: the quaternion of a rotation (all four
+    branches of Shepperd's method) gives back the rotation through the
+    library's tf-style 4x4; the node's host conversions of a message keep the
+    finite x, y, z rows as float64 and give five int8 payloads."""
+    import numpy as np
+    from gvom_gb300 import pose_to_transform
+    from scipy.spatial.transform import Rotation
+    rng = np.random.default_rng(2)
+    Rs = [np.eye(3), np.diag([1.0, -1.0, -1.0]), np.diag([-1.0, 1.0, -1.0]), np.diag([-1.0, -1.0, 1.0])]
+    Rs += list(Rotation.random(200, random_state=3).as_matrix())
+    for R in Rs:
+        q = bench._quat_xyzw(R)
+        assert abs(np.linalg.norm(q) - 1.0) < 1e-12
+        T = pose_to_transform(np.array([1.0, 2.0, 3.0]), q)
+        np.testing.assert_allclose(T[:3, :3], R, atol=1e-12)
+    pts = rng.standard_normal((100, 3)).astype(np.float32)
+    pts[7, 1] = np.nan
+    rows = bench.lidar_message(pts, rng)
+    assert rows.shape == (100, 12) and rows.dtype == np.float32
+    np.testing.assert_array_equal(rows[:, :3], pts)
+    X = 8
+    maps = (np.zeros(3), rng.integers(0, 101, (X, X)).astype(np.int32), np.zeros((X, X), np.int32),
+            rng.uniform(-12, 1, (X, X)), np.ones((X, X), np.int32))
+    xyz, pay = bench.node_host_work(rows, maps)
+    assert xyz.shape == (99, 3) and xyz.dtype == np.float64
+    assert len(pay) == 5 and all(p.dtype == np.int8 and p.shape == (X * X,) for p in pay)
