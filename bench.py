@@ -404,7 +404,7 @@ def measure_ros(form, torch, n_steps=200, warmup=5):
         T = np.asarray(s.transform, np.float64)
         msgs.append((lidar_message(s.points, rng), s.points.shape[0], s.ego, T[:3, 3].copy(), _quat_xyzw(T[:3, :3])))
     g = Gvom(*form.w.gvom_args())
-    t_in, t_comb, t_grid, pts, maps = [], [], [], 0, None
+    t_in, t_comb, t_grid, t_dbg, pts, maps = [], [], [], [], 0, None
     for k in range(warmup + n_steps):
         rows, n, ego, t, q = msgs[k % len(msgs)]
         torch.cuda.synchronize()
@@ -420,6 +420,12 @@ def measure_ros(form, torch, n_steps=200, warmup=5):
             t_comb.append(t2 - t1)
             t_grid.append(t3 - t2)
             pts += n
+        if k >= warmup and k % 10 == 0:  # the node's three debug clouds (scripts/gvom_ros.py:168-190)
+            t4 = time.perf_counter()
+            g.make_debug_voxel_map()
+            g.make_debug_height_map()
+            g.make_debug_inferred_height_map()
+            t_dbg.append(time.perf_counter() - t4)
     g.close()
     host = []
     for k in range(20):
@@ -431,7 +437,8 @@ def measure_ros(form, torch, n_steps=200, warmup=5):
     return {"workload": form.name, "steps": n_steps, "point_step_bytes": 48,
             "points_per_s": pts / total,
             "entry": "process_pointcloud2 (host bytes, translation + quaternion), combine_maps, ros_grids",
-            "us_p50": {"process_pointcloud2": us(t_in), "combine_maps": us(t_comb), "ros_grids": us(t_grid)},
+            "us_p50": {"process_pointcloud2": us(t_in), "combine_maps": us(t_comb), "ros_grids": us(t_grid),
+                       "debug_exports_all_three": us(t_dbg)},
             "node_host_conversions_us_p50": us(host)}
 
 
