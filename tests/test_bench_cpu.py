@@ -71,3 +71,51 @@ def test_quaternion_round_trip_and_node_host_work(gpu_lib):
     xyz, pay = bench.node_host_work(rows, maps)
     assert xyz.shape == (99, 3) and xyz.dtype == np.float64
     assert len(pay) == 5 and all(p.dtype == np.int8 and p.shape == (X * X,) for p in pay)
+
+
+def test_measure_ros_runs_against_a_stand_in_mapper(monkeypatch):
+    """Every line of the ros form on CPU: a stand-in mapper records the
+    calls; the form's numbers come out for the given steps."""
+    import types
+
+    import numpy as np
+
+    import gvom_gb300
+    calls = []
+
+    class FakeGvom:
+        def __init__(self, *params):
+            self.X = params[2]
+
+        def process_pointcloud2(self, data, n, step, offs, ego, t, q):
+            assert np.asarray(data).nbytes >= n * step and tuple(offs) == (0, 4, 8) and len(q) == 4
+            calls.append("pc2")
+
+        def combine_maps(self):
+            X = self.X
+            return (np.zeros(3), np.zeros((X, X), np.int32), np.zeros((X, X), np.int32), np.full((X, X), -1.0),
+                    np.ones((X, X), np.int32))
+
+        def ros_grids(self):
+            calls.append("grids")
+
+        def make_debug_voxel_map(self):
+            calls.append("dbg")
+
+        make_debug_height_map = make_debug_inferred_height_map = make_debug_voxel_map
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(gvom_gb300, "Gvom", FakeGvom)
+    torch = types.SimpleNamespace(cuda=types.SimpleNamespace(synchronize=lambda: None))
+    rng = np.random.default_rng(0)
+    scan = lambda: types.SimpleNamespace(points=rng.standard_normal((50, 3)).astype(np.float32),  # noqa: E731
+                                          ego=(0.0, 0.0, 1.0), transform=np.eye(4, dtype=np.float32))
+    form = types.SimpleNamespace(name="tiny", steps=[[scan()] for _ in range(3)],
+                                 w=types.SimpleNamespace(gvom_args=lambda: (0.2, 0.2, 16, 8, 2, 1.0, 0.5, 0.5, 0.3,
+                                                                            2.0, 4.0, 1.0, 1, 1)))
+    r = bench.measure_ros(form, torch, n_steps=20, warmup=2)
+    assert calls.count("pc2") == 22 and calls.count("grids") == 22 and calls.count("dbg") == 3 * 2
+    assert r["steps"] == 20 and r["points_per_s"] > 0 and r["node_host_conversions_us_p50"] > 0
+    assert set(r["us_p50"]) == {"process_pointcloud2", "combine_maps", "ros_grids", "debug_exports_all_three"}
