@@ -1,0 +1,80 @@
+"""The eigen-solve of the statistics merge (`jacobi_rot` / `eigen3` in
+gvom_gb300/csrc/k_combine.cu: float32 cyclic Jacobi, float64 determinant
+for a near-degenerate smallest eigenvalue), compiled for the host from the
+kernel source, against the reference's closed form (the oracle, pinned to
+scripts/gvom.py:1423-1487) on the combined covariances of every golden
+fixture, at the parity tolerance.  The device's approximate division and
+reciprocal square root are taken as correctly rounded ones here, which
+moves results by a few float32 ulps, far inside the tolerance."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_files
+from oracle.canonical import canonical_state
+from oracle.oracle import OracleGvom
+from replay import assert_eigen, load, ops_of, params_of
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KERNEL = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc", "k_combine.cu")
+
+PRELUDE = r"""
+#include <cmath>
+using std::fabs; using std::sqrt;
+#define __device__
+#define __forceinline__ inline
+static inline float __fdividef(float a, float b) { return a / b; }
+static inline float rsqrtf(float x) { return 1.0f / std::sqrt(x); }
+"""
+
+DRIVER = r"""
+extern "C" void eigen_all(const float *cov, long long n, float *out) {
+    for (long long i = 0; i < n; i++) eigen3(cov + 6 * i, out + 3 * i);
+}
+"""
+
+
+def _kernel_eigen_source():
+    src = open(KERNEL).read()
+    a = src.index("__device__ __forceinline__ void jacobi_rot(")
+    b = src.index("\n}\n", src.index("__device__ __forceinline__ void eigen3(")) + 3
+    return src[a:b]
+
+
+@pytest.fixture(scope="module")
+def eigen_lib(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("eigen")
+    cpp = d / "eigen_host.cpp"
+    cpp.write_text(PRELUDE + _kernel_eigen_source() + DRIVER)
+    so = d / "libeigen.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(so), str(cpp)],
+                   check=True)
+    lib = C.CDLL(str(so))
+    lib.eigen_all.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p]
+    return lib
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_kernel_eigen_solve_within_tolerance_of_reference(eigen_lib, name):
+    fx = load(os.path.join(GOLDEN, name))
+    o = OracleGvom(*params_of(fx))
+    n_checked = 0
+    for op in ops_of(fx):
+        if op[0] == "P":
+            o.Process_pointcloud(*op[2:])
+            continue
+        o.combine_maps()
+        st = canonical_state(o.combined_state())
+        cov = np.ascontiguousarray(np.asarray(st["metrics"], np.float32)[:, 3:9])
+        got = np.empty((len(cov), 3), np.float32)
+        if len(cov):
+            eigen_lib.eigen_all(cov.ctypes.data, len(cov), got.ctypes.data)
+        assert_eigen(got, st["eigen"], f"{name} eigenvalues")
+        n_checked += len(cov)
+    assert n_checked > 0
