@@ -847,12 +847,15 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
 // k_ros_grids: the OccupancyGrid payloads of the reference's ROS node
 // (scripts/gvom_ros.py:141-164) from the last combine's maps, one thread per
 // cell, written in the node's column-major order (x fastest).  Each value is
-// cast to int8 as numpy does on the node's x86 host: truncation toward zero,
-// then the low 8 bits.
+// cast to int8 as numpy does on the node's x86 host: truncation toward zero
+// through a 32-bit integer, then the low 8 bits.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ signed char int8_wrap(double v) {
-    if (!(fabs(v) < 9.2e18)) return 0;  // NaN / out of int64 range: numpy gives INT64_MIN, low byte 0
-    const long long t = (long long)v;   // truncation toward zero
+    // numpy's float64 -> int8 cast on x86 truncates through a 32-bit integer:
+    // a value whose truncation lies outside int32, or NaN, becomes the integer
+    // indefinite 0x80000000, whose low byte is 0
+    if (!(v > -2147483649.0 && v < 2147483648.0)) return 0;
+    const int t = (int)v;  // truncation toward zero
     return (signed char)(unsigned char)(t & 0xff);
 }
 

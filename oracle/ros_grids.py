@@ -4,8 +4,9 @@ gvom_ros_grids / Gvom.ros_grids.  Inputs are combine_maps' outputs
 (pos, neg, roughness, visibility as [x, y] arrays); each payload is flattened
 column-major (x fastest) as the node's np.reshape(..., -1, order='F') does and
 cast to int8 the way numpy does on the node's x86 host: truncation toward
-zero, then the low 8 bits (the roughness payload of the node's defaults lies
-in [-200, -100], outside int8, so the cast rule is part of the result)."""
+zero through a 32-bit integer (0 outside its range, and for NaN), then the
+low 8 bits (the roughness payload of the node's defaults lies in
+[-200, -100], outside int8, so the cast rule is part of the result)."""
 from __future__ import annotations
 
 import numpy as np
@@ -14,7 +15,9 @@ import numpy as np
 def int8_wrap(v: np.ndarray) -> np.ndarray:
     v = np.asarray(v, np.float64)
     out = np.zeros(v.shape, np.int64)
-    ok = np.abs(v) < 9.2e18  # NaN / beyond int64: numpy's conversion gives INT64_MIN, low byte 0
+    # x86 truncates through a 32-bit integer: outside int32, or NaN, gives the
+    # integer indefinite 0x80000000, low byte 0
+    ok = (v > -2147483649.0) & (v < 2147483648.0)
     out[ok] = np.trunc(v[ok]).astype(np.int64)
     b = out & 0xFF
     return np.where(b >= 128, b - 256, b).astype(np.int8)

@@ -11,7 +11,8 @@ published message.  The maps are the combine outputs stored in the other
 golden fixtures plus edge cases: every roughness from -12 to 1 in steps of
 1/8 (the clip bounds, and values whose payload leaves int8), NaN,
 negative-obstacle values of 0 and 100, densities on both sides of the
-threshold, and non-default node parameters.  Run in the build container; the
+threshold, non-default node parameters, and roughness ranges so narrow that
+the payload leaves int32.  Run in the build container; the
 fixture is committed:
 
     python tests/golden/make_ros_golden.py
@@ -135,6 +136,9 @@ def cases():
     e = edge_maps()
     out.append(("edges", e, {}))
     out.append(("edges_params", e, dict(density_threshold=30, min_roughness=-6, max_roughness=-1)))
+    # a roughness range so narrow that the payload leaves int32 (about -2e11) or stays just inside it (-2e9)
+    out.append(("edges_narrow_out", e, dict(min_roughness=-1.0, max_roughness=-1.0 + 1e-9)))
+    out.append(("edges_narrow_in", e, dict(min_roughness=-1.0, max_roughness=-1.0 + 1e-7)))
     return out
 
 

@@ -14,7 +14,9 @@ from oracle.ros_grids import int8_wrap, ros_grids
 def test_restatement_matches_numpy_astype_on_x86():
     import warnings
     rng = np.random.default_rng(5)
-    v = np.concatenate([rng.uniform(-300, 300, 20000), np.arange(-260, 260, 0.25), [-1e10, 1e10, 0.0, -0.0]])
+    v = np.concatenate([rng.uniform(-300, 300, 20000), np.arange(-260, 260, 0.25), rng.uniform(-1e12, 1e12, 2000),
+                        [-1e10, 1e10, 0.0, -0.0, 2.0 ** 31 - 0.5, 2.0 ** 31, 2.0 ** 31 + 255, -2.0 ** 31,
+                         -2.0 ** 31 - 0.5, -2.0 ** 31 - 1, 3e9 + 7, 1e19, -1e19, np.nan, np.inf, -np.inf]])
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         ref = v.astype(np.int8)
@@ -76,3 +78,38 @@ def test_device_payloads_equal_oracle(gpu_lib):
             want = ros_grids(out[1], out[2], out[3], out[4], **kw)
             for k in want:
                 np.testing.assert_array_equal(got[k], want[k], k)
+
+
+def test_kernel_int8_cast_equals_numpy_on_x86(tmp_path):
+    """k_ros_grids' int8 cast (`int8_wrap` in gvom_gb300/csrc/k_combine.cu),
+    compiled for the host from the kernel source, equals numpy's
+    float64 -> int8 astype on x86 (the node's host) and the oracle's."""
+    import ctypes as C
+    import os
+    import shutil
+    import subprocess
+    import warnings
+    if shutil.which("g++") is None or platform.machine() not in ("x86_64", "AMD64"):
+        pytest.skip("needs g++ on x86")
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                            "gvom_gb300", "csrc", "k_combine.cu")).read()
+    a = src.index("__device__ __forceinline__ signed char int8_wrap(")
+    b = src.index("\n}\n", a) + 3
+    cpp = tmp_path / "int8.cpp"
+    cpp.write_text("#include <cmath>\nusing std::fabs;\n#define __device__\n#define __forceinline__ inline\n" + src[a:b] +
+                   'extern "C" void wrap_all(const double *v, long long n, signed char *o) '
+                   "{ for (long long i = 0; i < n; i++) o[i] = int8_wrap(v[i]); }\n")
+    so = tmp_path / "libint8.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-o", str(so), str(cpp)], check=True)
+    lib = C.CDLL(str(so))
+    lib.wrap_all.argtypes = [C.c_void_p, C.c_longlong, C.c_void_p]
+    rng = np.random.default_rng(9)
+    v = np.concatenate([rng.uniform(-300, 300, 50000), np.arange(-260, 260, 0.125), rng.uniform(-1e12, 1e12, 1000),
+                        [np.nan, np.inf, -np.inf, 1e19, -1e19, 0.0, -0.0, 127.9, 128.0, -128.9, -129.0]])
+    got = np.empty(v.size, np.int8)
+    lib.wrap_all(v.ctypes.data, v.size, got.ctypes.data)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        want = v.astype(np.int8)
+    np.testing.assert_array_equal(got, want)
+    np.testing.assert_array_equal(got, int8_wrap(v))
