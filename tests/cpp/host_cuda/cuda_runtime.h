@@ -1,0 +1,56 @@
+/* A host stand-in for <cuda_runtime.h>, so that device code of the library can
+ * be compiled by a host compiler for the CPU tests (tests/test_trace_host.py):
+ * qualifiers become nothing, the correctly rounded intrinsics become plain
+ * IEEE operations (compile with -ffp-contract=off -frounding-math), atomics
+ * become sequential updates.  Not part of the library. */
+#pragma once
+#include <cfenv>
+#include <climits>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+
+#define __device__
+#define __host__
+#define __global__
+#define __forceinline__ inline
+#define __align__(n) alignas(n)
+#define __launch_bounds__(...)
+#define __grid_constant__
+
+struct float4 { float x, y, z, w; };
+struct float2 { float x, y; };
+struct int2 { int x, y; };
+static inline float4 make_float4(float a, float b, float c, float d) { return float4{a, b, c, d}; }
+typedef int cudaError_t;
+typedef struct CUstream_st *cudaStream_t;
+typedef struct CUevent_st *cudaEvent_t;
+struct HostDim3 { unsigned x, y, z; };
+static HostDim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1};
+
+static inline float __fadd_rn(float a, float b) { return a + b; }
+static inline float __fsub_rn(float a, float b) { return a - b; }
+static inline float __fmul_rn(float a, float b) { return a * b; }
+static inline float __fdiv_rn(float a, float b) { return a / b; }
+static inline float __fsqrt_rn(float a) { return std::sqrt(a); }
+static inline float __fadd_rd(float a, float b) {
+    std::fesetround(FE_DOWNWARD);
+    volatile float r = a + b;
+    std::fesetround(FE_TONEAREST);
+    return r;
+}
+static inline double __dadd_rn(double a, double b) { return a + b; }
+static inline double __dsub_rn(double a, double b) { return a - b; }
+static inline double __dmul_rn(double a, double b) { return a * b; }
+static inline double __ddiv_rn(double a, double b) { return a / b; }
+static inline float __double2float_rn(double d) { return (float)d; }
+static inline int __float2int_rd(float f) { return (int)std::floor(f); }
+static inline int __float_as_int(float f) { int i; std::memcpy(&i, &f, 4); return i; }
+static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
+static inline unsigned long long atomicAdd(unsigned long long *p, unsigned long long v) {
+    const unsigned long long o = *p; *p = o + v; return o;
+}
+static inline unsigned atomicAdd(unsigned *p, unsigned v) { const unsigned o = *p; *p = o + v; return o; }
+static inline unsigned atomicCAS(unsigned *p, unsigned cmp, unsigned v) {
+    const unsigned o = *p; if (o == cmp) *p = v; return o;
+}

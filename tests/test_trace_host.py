@@ -1,0 +1,214 @@
+"""The ray-trace kernel's per-point code (k_voxelize_trace in
+gvom_gb300/csrc/k_process.cu: transform, min-distance filter, exact hit
+voxel, float32 march with the fast floor, the sliver, the shared cube and
+hash table and their flush), compiled for the host from the kernel source
+and run thread by thread, against the oracle on every scan of every golden
+fixture: the per-voxel hit and total counts of each slot must be equal.
+The scan descriptor is filled the way the library's host code does
+(prepare_scans in gvom_gb300/csrc/gvom_capi.cu)."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_files
+from oracle.oracle import OracleGvom
+from replay import load, ops_of, params_of
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc")
+
+
+def _matching_block(src, start):
+    """src[start:] begins a line ending in '{': return through its matching '}'."""
+    i = src.index("{", start)
+    depth = 0
+    for j in range(i, len(src)):
+        if src[j] == "{":
+            depth += 1
+        elif src[j] == "}":
+            depth -= 1
+            if depth == 0:
+                return src[start:j + 1]
+    raise AssertionError("unbalanced braces")
+
+
+def _kernel_parts():
+    src = open(os.path.join(CSRC, "k_process.cu")).read()
+    a = src.index("#ifndef GVOM_TRACE_HASH_BITS")
+    b = src.index("constexpr unsigned kHashEmpty = 0xffffffffu;") + len("constexpr unsigned kHashEmpty = 0xffffffffu;")
+    hashc = src[a:b]
+    a = src.index("template <typename PT>\n__device__ __forceinline__ void load_point(")
+    b = src.index("__device__ __forceinline__ void warp_add_u64(")
+    helpers = src[a:b]
+    k = src.index("__global__ void __launch_bounds__(256) k_voxelize_trace(")
+    point = _matching_block(src, src.index("    if (active) {", k))
+    f = src.index("    if (kHash)\n        for (int k = threadIdx.x; k < (1 << kHashBits); k += blockDim.x) {\n"
+                  "            const unsigned t = htag[k];", k)
+    flush_hash = _matching_block(src, f)
+    c = src.index("    if (!sd.cube_on) return;", f)
+    flush_cube = "    if (sd.cube_on)\n" + _matching_block(src, src.index("    for (int k = threadIdx.x; k < kCubeCells;", c))
+    return hashc, helpers, point, flush_hash, flush_cube
+
+
+DRIVER = r"""
+namespace gvom {
+template <typename PT>
+static void trace_block(const ProcessConst &pc, const ScanDesc &sd, long long first, float4 *prec, int *prank) {
+    static unsigned cube[kCubeCells];
+    static unsigned htag[1 << kHashBits], hcnt[1 << kHashBits];
+    for (int k = 0; k < kCubeCells; k++) cube[k] = 0u;
+    for (int k = 0; k < (1 << kHashBits); k++) { htag[k] = kHashEmpty; hcnt[k] = 0u; }
+    const Geom g = pc.g;
+    const int ffloor = sd.fast_floor;
+    const int Xe = g.Xe, XeXe = g.Xe * g.Xe;
+    for (int t = 0; t < 256; t++) {
+        const long long i = first + t;
+        const bool active = i < sd.n;
+        unsigned long long n_valid = 0, n_hit = 0, n_steps = 0;
+%(point)s
+        (void)n_valid; (void)n_hit; (void)n_steps;
+    }
+%(flush_hash)s
+%(flush_cube)s
+}
+}  // namespace gvom
+
+using namespace gvom;
+
+static ExactRes exact_res(double r) {
+    int e;
+    const double f = std::frexp(r, &e);
+    ExactRes R;
+    R.mr = (unsigned long long)std::ldexp(f, 53);
+    R.er = e - 53;
+    unsigned __int128 w = ((unsigned __int128)1 << 116) / R.mr;
+    if (w >> 64) w = ~0ull;
+    R.W = (unsigned long long)w;
+    R.pad = 0;
+    return R;
+}
+
+// prepare_scans (gvom_capi.cu) for one scan; counts of the grid's voxels out
+extern "C" int trace_scan(const void *pts, int dtype, long long n, long long stride, const double *ego,
+                          const double *T, int tmode, double xy_res, double z_res, int X, int Z, int exy, int ez,
+                          double min_distance, int *hit, int *total) {
+    ProcessConst pc;
+    std::memset(&pc, 0, sizeof pc);
+    Geom &g = pc.g;
+    g.X = X; g.Z = Z; g.exy = exy; g.ez = ez; g.Xe = X + 2 * exy; g.Ze = Z + 2 * ez;
+    g.V = (long long)X * X * Z; g.Vext = (long long)g.Xe * g.Xe * g.Ze;
+    pc.xy_res = xy_res; pc.z_res = z_res;
+    pc.md2 = min_distance * min_distance;
+    float f = (float)pc.md2;
+    if ((double)f < pc.md2) f = std::nextafter(f, INFINITY);
+    while ((double)std::nextafter(f, -INFINITY) >= pc.md2) f = std::nextafter(f, -INFINITY);
+    pc.md2_f32 = f;
+    pc.rxy = exact_res(xy_res);
+    pc.rz = exact_res(z_res);
+    pc.step_cap = 2 * std::max(X, Z) + 8;
+    pc.nscans = 1;
+    ScanDesc d;
+    std::memset(&d, 0, sizeof d);
+    d.pts = pts; d.n = n; d.stride = stride; d.tmode = tmode;
+    for (int r = 0; r < 12; r++) { d.T[r] = T ? T[r] : 0.0; d.Tf[r] = (float)d.T[r]; }
+    d.od[0] = std::floor((ego[0] / xy_res) - (double)X / 2.0);
+    d.od[1] = std::floor((ego[1] / xy_res) - (double)X / 2.0);
+    d.od[2] = std::floor((ego[2] / z_res) - (double)Z / 2.0);
+    bool fast = true, exact = true;
+    const double lim = 4194304.0 - (double)std::max(X, Z) - 2.0;
+    for (int a = 0; a < 3; a++) {
+        if (!(std::fabs(d.od[a]) < 2147483648.0)) exact = false;
+        if (!(std::fabs(d.od[a]) < lim)) fast = false;
+    }
+    for (int a = 0; a < 3; a++) d.oi[a] = exact ? (int)d.od[a] : 0;
+    d.fast_floor = fast; d.exact_ok = exact;
+    d.pt0[0] = (float)(ego[0] / xy_res); d.pt0[1] = (float)(ego[1] / xy_res); d.pt0[2] = (float)(ego[2] / z_res);
+    d.cube_on = (fast && X >= kCube && Z >= kCube) ? 1 : 0;
+    for (int a = 0; a < 3; a++) {
+        const int dim = a < 2 ? X : Z;
+        int c = 0;
+        if (d.cube_on) {
+            const double ev = std::floor((double)d.pt0[a] - d.od[a]);
+            c = (int)std::min(std::max(ev - kCube / 2, 0.0), (double)(dim - kCube));
+        }
+        d.cube0[a] = c;
+    }
+    unsigned long long *cnt = new unsigned long long[g.Vext]();
+    float4 *prec = new float4[n > 0 ? n : 1];
+    int *prank = new int[n > 0 ? n : 1];
+    d.cnt = cnt;
+    for (long long b = 0; b < n; b += 256) {
+        if (dtype == 0) trace_block<float>(pc, d, b, prec, prank);
+        else trace_block<double>(pc, d, b, prec, prank);
+    }
+    for (int z = 0; z < Z; z++)
+        for (int y = 0; y < X; y++)
+            for (int x = 0; x < X; x++) {
+                const unsigned long long w = cnt[(x + exy) + (long long)(y + exy) * g.Xe + (long long)(z + ez) * g.Xe * g.Xe];
+                const long long v = x + (long long)y * X + (long long)z * X * X;
+                hit[v] = (int)(w >> 32);
+                total[v] = (int)(w & 0xffffffffu);
+            }
+    delete[] cnt; delete[] prec; delete[] prank;
+    return 0;
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def trace_lib(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    hashc, helpers, point, flush_hash, flush_cube = _kernel_parts()
+    d = tmp_path_factory.mktemp("trace")
+    cpp = d / "trace_host.cpp"
+    cpp.write_text("#include <algorithm>\n#include <cmath>\nusing std::isfinite;\n"
+                   '#include "gvom_internal.cuh"\nnamespace gvom {\n' + hashc + "\n" + helpers + "\n}\n" +
+                   DRIVER % {"point": point, "flush_hash": flush_hash, "flush_cube": flush_cube})
+    so = d / "libtrace.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-frounding-math", "-fPIC", "-shared",
+                    "-I", os.path.join(HERE, "cpp", "host_cuda"), "-I", CSRC, "-o", str(so), str(cpp)], check=True)
+    lib = C.CDLL(str(so))
+    P = C.c_void_p
+    lib.trace_scan.argtypes = [P, C.c_int, C.c_longlong, C.c_longlong, P, P, C.c_int, C.c_double, C.c_double,
+                               C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, P, P]
+    return lib
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_kernel_trace_counts_equal_oracle(trace_lib, name):
+    fx = load(os.path.join(GOLDEN, name))
+    p = params_of(fx)
+    xy, zr, X, Z = p[0], p[1], p[2], p[3]
+    o = OracleGvom(*p)
+    V = X * X * Z
+    for op in ops_of(fx):
+        if op[0] != "P":
+            continue
+        _, pi, pts, ego, T = op
+        pts = np.ascontiguousarray(pts)
+        o.Process_pointcloud(pts, ego, T)
+        _, last = o.ring_state()
+        st = o.slot_state(last)
+        idx = np.asarray(st["index"]).reshape(-1)
+        ref_hit = np.zeros(V, np.int64)
+        ref_total = np.zeros(V, np.int64)
+        occ = idx >= 0
+        ref_hit[occ] = np.asarray(st["hit"])[idx[occ]]
+        ref_total[occ] = np.asarray(st["total"])[idx[occ]]
+        ref_total[~occ] = -idx[~occ].astype(np.int64) - 1
+        Td = None if T is None else np.ascontiguousarray(np.asarray(T, np.float64).reshape(4, 4))
+        tmode = 0 if T is None else (1 if np.asarray(T).dtype == np.float32 else 2)
+        e = np.ascontiguousarray(np.asarray(ego, np.float64))
+        hit = np.empty(V, np.int32)
+        total = np.empty(V, np.int32)
+        rc = trace_lib.trace_scan(pts.ctypes.data, 0 if pts.dtype == np.float32 else 1, pts.shape[0], pts.shape[1],
+                                  e.ctypes.data, None if Td is None else Td.ctypes.data, tmode, xy, zr, X, Z,
+                                  int(p[12]), int(p[13]), p[5], hit.ctypes.data, total.ctypes.data)
+        assert rc == 0
+        np.testing.assert_array_equal(hit, ref_hit, f"{name} scan {pi} hits")
+        np.testing.assert_array_equal(total, ref_total, f"{name} scan {pi} totals")
