@@ -54,3 +54,5 @@ static inline unsigned atomicAdd(unsigned *p, unsigned v) { const unsigned o = *
 static inline unsigned atomicCAS(unsigned *p, unsigned cmp, unsigned v) {
     const unsigned o = *p; if (o == cmp) *p = v; return o;
 }
+static inline int atomicAdd(int *p, int v) { const int o = *p; *p = o + v; return o; }
+static inline long long __double_as_longlong(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
