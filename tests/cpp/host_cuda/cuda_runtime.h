@@ -56,3 +56,4 @@ static inline unsigned atomicCAS(unsigned *p, unsigned cmp, unsigned v) {
 }
 static inline int atomicAdd(int *p, int v) { const int o = *p; *p = o + v; return o; }
 static inline long long __double_as_longlong(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
+static inline int __popc(unsigned v) { return __builtin_popcount(v); }
