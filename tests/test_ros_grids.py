@@ -113,3 +113,53 @@ def test_kernel_int8_cast_equals_numpy_on_x86(tmp_path):
         want = v.astype(np.int8)
     np.testing.assert_array_equal(got, want)
     np.testing.assert_array_equal(got, int8_wrap(v))
+
+
+def test_kernel_payloads_equal_the_reference_callback(tmp_path):
+    """k_ros_grids (gvom_gb300/csrc/k_combine.cu), compiled for the host from
+    the kernel source through the host stand-in header and run cell by cell,
+    on the maps of tests/golden/ros_epilogue.npz: its five payloads equal
+    what the reference node's callback published for them, byte for byte."""
+    import ctypes as C
+    import os
+    import shutil
+    import subprocess
+    from conftest import GOLDEN
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    here = os.path.dirname(os.path.abspath(__file__))
+    csrc = os.path.join(os.path.dirname(here), "gvom_gb300", "csrc")
+    src = open(os.path.join(csrc, "k_combine.cu")).read()
+    a = src.index("__device__ __forceinline__ signed char int8_wrap(")
+    k = src.index("__global__ void __launch_bounds__(256) k_ros_grids(")
+    b = src.index("\n}\n", k) + 3
+    cpp = tmp_path / "ros_host.cpp"
+    cpp.write_text('#include <cmath>\nusing std::fabs; using std::isnan;\n#include "gvom_internal.cuh"\n'
+                   "namespace gvom {\n" + src[a:b] + "}\nusing namespace gvom;\n"
+                   'extern "C" void grids(const RosGridParams *p) {\n'
+                   "    for (int i = 0; i < p->X * p->X; i++) { blockIdx.x = i; threadIdx.x = 0; blockDim.x = 1; k_ros_grids(*p); }\n"
+                   "}\n")
+    so = tmp_path / "libros.so"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I",
+                    os.path.join(here, "cpp", "host_cuda"), "-I", csrc, "-o", str(so), str(cpp)], check=True)
+    lib = C.CDLL(str(so))
+
+    class Params(C.Structure):
+        _fields_ = [("X", C.c_int), ("pos", C.c_void_p), ("neg", C.c_void_p), ("vis", C.c_void_p),
+                    ("rough", C.c_void_p), ("density_thr", C.c_double), ("min_r", C.c_double), ("max_r", C.c_double),
+                    ("hard", C.c_void_p), ("soft", C.c_void_p), ("certainty", C.c_void_p), ("negative", C.c_void_p),
+                    ("roughness", C.c_void_p)]
+    lib.grids.argtypes = [C.POINTER(Params)]
+    with np.load(os.path.join(GOLDEN, "ros_epilogue.npz")) as z:
+        fx = {k: z[k] for k in z.files}
+    for n in str(fx["cases"]).split(","):
+        pos, neg, vis = (np.ascontiguousarray(fx[f"{n}_{k}"], np.int32) for k in ("pos", "neg", "vis"))
+        rough = np.ascontiguousarray(fx[f"{n}_rough"], np.float64)
+        X = pos.shape[0]
+        out = {k: np.zeros(X * X, np.int8) for k in ("hard", "soft", "certainty", "negative", "roughness")}
+        thr, lo, hi = fx[f"{n}_params"]
+        prm = Params(X, pos.ctypes.data, neg.ctypes.data, vis.ctypes.data, rough.ctypes.data, thr, lo, hi,
+                     *[out[k].ctypes.data for k in ("hard", "soft", "certainty", "negative", "roughness")])
+        lib.grids(C.byref(prm))
+        for pub, key in PAYLOAD_OF.items():
+            np.testing.assert_array_equal(out[key], fx[f"{n}_{pub}"], f"{n} {pub}")
