@@ -95,7 +95,7 @@ static ExactRes exact_res(double r) {
 // prepare_scans (gvom_capi.cu) for one scan; counts of the grid's voxels out
 extern "C" int trace_scan(const void *pts, int dtype, long long n, long long stride, const double *ego,
                           const double *T, int tmode, double xy_res, double z_res, int X, int Z, int exy, int ez,
-                          double min_distance, int *hit, int *total) {
+                          double min_distance, int *hit, int *total, int pc2, const int *off) {
     ProcessConst pc;
     std::memset(&pc, 0, sizeof pc);
     Geom &g = pc.g;
@@ -114,6 +114,8 @@ extern "C" int trace_scan(const void *pts, int dtype, long long n, long long str
     ScanDesc d;
     std::memset(&d, 0, sizeof d);
     d.pts = pts; d.n = n; d.stride = stride; d.tmode = tmode;
+    d.pc2 = pc2;
+    for (int a = 0; a < 3; a++) d.off[a] = off ? off[a] : 0;
     for (int r = 0; r < 12; r++) { d.T[r] = T ? T[r] : 0.0; d.Tf[r] = (float)d.T[r]; }
     d.od[0] = std::floor((ego[0] / xy_res) - (double)X / 2.0);
     d.od[1] = std::floor((ego[1] / xy_res) - (double)X / 2.0);
@@ -175,7 +177,7 @@ def trace_lib(tmp_path_factory):
     lib = C.CDLL(str(so))
     P = C.c_void_p
     lib.trace_scan.argtypes = [P, C.c_int, C.c_longlong, C.c_longlong, P, P, C.c_int, C.c_double, C.c_double,
-                               C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, P, P]
+                               C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, P, P, C.c_int, P]
     return lib
 
 
@@ -208,7 +210,49 @@ def test_kernel_trace_counts_equal_oracle(trace_lib, name):
         total = np.empty(V, np.int32)
         rc = trace_lib.trace_scan(pts.ctypes.data, 0 if pts.dtype == np.float32 else 1, pts.shape[0], pts.shape[1],
                                   e.ctypes.data, None if Td is None else Td.ctypes.data, tmode, xy, zr, X, Z,
-                                  int(p[12]), int(p[13]), p[5], hit.ctypes.data, total.ctypes.data)
+                                  int(p[12]), int(p[13]), p[5], hit.ctypes.data, total.ctypes.data, 0, None)
         assert rc == 0
+        np.testing.assert_array_equal(hit, ref_hit, f"{name} scan {pi} hits")
+        np.testing.assert_array_equal(total, ref_total, f"{name} scan {pi} totals")
+
+
+@pytest.mark.parametrize("name", ["synth_f32.npz", "kat_boundaries.npz", "synth_aniso_z.npz"])
+def test_kernel_trace_reads_pointcloud2_bytes(trace_lib, name):
+    """The same per-point code on PointCloud2-style bytes (float32 x, y, z at
+    byte offsets 8, 0, 20 of 28-byte points, widened to float64 as the
+    reference's ROS node does) against the oracle on the float64 points."""
+    fx = load(os.path.join(GOLDEN, name))
+    p = params_of(fx)
+    xy, zr, X, Z = p[0], p[1], p[2], p[3]
+    V = X * X * Z
+    o = OracleGvom(*p)
+    for op in ops_of(fx):
+        if op[0] != "P":
+            continue
+        _, pi, pts, ego, T = op
+        if pts.dtype != np.float32:
+            continue
+        n = pts.shape[0]
+        rows = np.random.default_rng(pi).random((n, 7), dtype=np.float32)
+        rows[:, 2], rows[:, 0], rows[:, 5] = pts[:, 0], pts[:, 1], pts[:, 2]
+        rows = np.ascontiguousarray(rows)
+        xyz = np.ascontiguousarray(pts.astype(np.float64))
+        o.Process_pointcloud(xyz, ego, T)
+        _, last = o.ring_state()
+        st = o.slot_state(last)
+        idx = np.asarray(st["index"]).reshape(-1)
+        occ = idx >= 0
+        ref_hit = np.zeros(V, np.int64)
+        ref_total = np.where(occ, 0, -idx.astype(np.int64) - 1)
+        ref_hit[occ] = np.asarray(st["hit"])[idx[occ]]
+        ref_total[occ] = np.asarray(st["total"])[idx[occ]]
+        Td = None if T is None else np.ascontiguousarray(np.asarray(T, np.float64).reshape(4, 4))
+        e = np.ascontiguousarray(np.asarray(ego, np.float64))
+        off = np.array([8, 0, 20], np.int32)
+        hit = np.empty(V, np.int32)
+        total = np.empty(V, np.int32)
+        assert trace_lib.trace_scan(rows.ctypes.data, 1, n, 28, e.ctypes.data, None if Td is None else Td.ctypes.data,
+                                    0 if T is None else 2, xy, zr, X, Z, int(p[12]), int(p[13]), p[5],
+                                    hit.ctypes.data, total.ctypes.data, 1, off.ctypes.data) == 0
         np.testing.assert_array_equal(hit, ref_hit, f"{name} scan {pi} hits")
         np.testing.assert_array_equal(total, ref_total, f"{name} scan {pi} totals")
