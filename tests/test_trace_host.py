@@ -95,7 +95,7 @@ static ExactRes exact_res(double r) {
 // prepare_scans (gvom_capi.cu) for one scan; counts of the grid's voxels out
 extern "C" int trace_scan(const void *pts, int dtype, long long n, long long stride, const double *ego,
                           const double *T, int tmode, double xy_res, double z_res, int X, int Z, int exy, int ez,
-                          double min_distance, int *hit, int *total, int pc2, const int *off) {
+                          double min_distance, int *hit, int *total, int pc2, const int *off, float *minh) {
     ProcessConst pc;
     std::memset(&pc, 0, sizeof pc);
     Geom &g = pc.g;
@@ -155,6 +155,19 @@ extern "C" int trace_scan(const void *pts, int dtype, long long n, long long str
                 hit[v] = (int)(w >> 32);
                 total[v] = (int)(w & 0xffffffffu);
             }
+    // lowest in-voxel height fraction per voxel from the points' records (cell, fractions)
+    if (minh) {
+        for (long long v = 0; v < g.V; v++) minh[v] = 1.0f;
+        for (long long i = 0; i < n; i++) {
+            const int cell = __float_as_int(prec[i].w);
+            if (cell < 0) continue;
+            const int ex = cell %% g.Xe, ey = (cell / g.Xe) %% g.Xe, ez2 = cell / (g.Xe * g.Xe);
+            const int x = ex - exy, y = ey - exy, z = ez2 - ez;
+            if (x < 0 || x >= X || y < 0 || y >= X || z < 0 || z >= Z) continue;
+            const long long v = x + (long long)y * X + (long long)z * X * X;
+            minh[v] = std::min(minh[v], prec[i].z);
+        }
+    }
     delete[] cnt; delete[] prec; delete[] prank;
     return 0;
 }
@@ -177,7 +190,7 @@ def trace_lib(tmp_path_factory):
     lib = C.CDLL(str(so))
     P = C.c_void_p
     lib.trace_scan.argtypes = [P, C.c_int, C.c_longlong, C.c_longlong, P, P, C.c_int, C.c_double, C.c_double,
-                               C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, P, P, C.c_int, P]
+                               C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, P, P, C.c_int, P, P]
     return lib
 
 
@@ -208,12 +221,17 @@ def test_kernel_trace_counts_equal_oracle(trace_lib, name):
         e = np.ascontiguousarray(np.asarray(ego, np.float64))
         hit = np.empty(V, np.int32)
         total = np.empty(V, np.int32)
+        minh = np.empty(V, np.float32)
         rc = trace_lib.trace_scan(pts.ctypes.data, 0 if pts.dtype == np.float32 else 1, pts.shape[0], pts.shape[1],
                                   e.ctypes.data, None if Td is None else Td.ctypes.data, tmode, xy, zr, X, Z,
-                                  int(p[12]), int(p[13]), p[5], hit.ctypes.data, total.ctypes.data, 0, None)
+                                  int(p[12]), int(p[13]), p[5], hit.ctypes.data, total.ctypes.data, 0, None,
+                                  minh.ctypes.data)
         assert rc == 0
         np.testing.assert_array_equal(hit, ref_hit, f"{name} scan {pi} hits")
         np.testing.assert_array_equal(total, ref_total, f"{name} scan {pi} totals")
+        # the points' z fractions (the exact hit-voxel arithmetic): their minimum per voxel is the slot's min height
+        ref_minh = np.asarray(st["min_h"], np.float32)[idx[occ]]
+        np.testing.assert_array_equal(minh[occ], ref_minh, f"{name} scan {pi} min height")
 
 
 @pytest.mark.parametrize("name", ["synth_f32.npz", "kat_boundaries.npz", "synth_aniso_z.npz"])
@@ -253,6 +271,6 @@ def test_kernel_trace_reads_pointcloud2_bytes(trace_lib, name):
         total = np.empty(V, np.int32)
         assert trace_lib.trace_scan(rows.ctypes.data, 1, n, 28, e.ctypes.data, None if Td is None else Td.ctypes.data,
                                     0 if T is None else 2, xy, zr, X, Z, int(p[12]), int(p[13]), p[5],
-                                    hit.ctypes.data, total.ctypes.data, 1, off.ctypes.data) == 0
+                                    hit.ctypes.data, total.ctypes.data, 1, off.ctypes.data, None) == 0
         np.testing.assert_array_equal(hit, ref_hit, f"{name} scan {pi} hits")
         np.testing.assert_array_equal(total, ref_total, f"{name} scan {pi} totals")
