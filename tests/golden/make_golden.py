@@ -278,6 +278,10 @@ SCENES = {
     # and the other way round, with float64 transforms
     "synth_aniso_xy": lambda: scene_synthetic("synth_aniso_xy", X=40, Z=12, res=0.25, zres=0.5, n_scans=4,
                                               combine_after=(0, 3), tdtype=np.float64),
+    # a 16-slot ring (the largest the library takes): combines with 5, 16 and 17 sources (the ring
+    # full plus the previous combined map), then after the ring has wrapped over its oldest slots
+    "synth_ring16": lambda: scene_synthetic("synth_ring16", B=16, columns=128, n_scans=20,
+                                            combine_after=(3, 15, 16, 19), dropout=0.2),
 }
 
 

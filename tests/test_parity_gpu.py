@@ -373,3 +373,73 @@ def test_odd_grid_and_row_length(Gvom):
     runs = [(s.points, s.ego, s.transform) for s in
             (make_scan(t, lid, p, i) for i, p in enumerate(make_trajectory(2)))]
     _compare_runs(Gvom, params, runs)
+
+
+@pytest.mark.parametrize("B", [1, 2, 4, 8, 12, 16])
+def test_ring_sizes_every_source_class_vs_oracle(Gvom, B):
+    """Rings of 1 to 16 slots, a combine after every scan: the merge runs with
+    every source count from 1 to B + 1, so every source-count class of the
+    index, count and statistics merges (2, 3, 5, 9 and 17 sources) is compared
+    with the oracle, including the 17-source class with the ring full and
+    after it wraps (scripts/gvom.py:242-298)."""
+    import torch
+    from gvom_gb300.synthetic import Lidar, Terrain, make_scan, make_trajectory
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    n = B + 3
+    t = Terrain.make(0, extent=12.8, path_len=n * 0.4)
+    lid = Lidar(beams=16, columns=256)
+    params = (0.2, 0.2, 64, 16, B, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    scans = [make_scan(t, lid, p, i, dropout=0.25, device=dev) for i, p in enumerate(make_trajectory(n))]
+    _run_both(Gvom, params, scans)
+
+
+def test_batched_8_shape_vs_oracle(Gvom):
+    """The batched form's measured shape: 8 sensors of 16,384-262,144 points
+    with 0-60 % whole-beam dropout on 4 mountings, 256 x 256 x 64 at 0.15 m,
+    buffer 16.  Three steps of one process_batch each (one launch per kernel
+    over the 8 scans), a combine after each (17 sources from the second step
+    on): every written slot and every combine equal the oracle's run of the
+    same scans one by one."""
+    import torch
+    from gvom_gb300.synthetic import BATCHED, make_batched_steps
+    w = BATCHED["batched_8"]
+    steps = make_batched_steps(w, 3, device="cuda" if torch.cuda.is_available() else "cpu")
+    params = w.gvom_args()
+    g = Gvom(*params)
+    o = OracleGvom(*params, threads=os.cpu_count() or 1)
+    for k, scans in enumerate(steps):
+        g.process_batch([(s.points, s.ego, s.transform) for s in scans])
+        for s in scans:
+            o.Process_pointcloud(s.points, s.ego, s.transform)
+        assert g.ring_state() == o.ring_state()
+        bi, _ = g.ring_state()
+        for j in range(len(scans)):
+            slot = (bi - len(scans) + j) % w.buffer_size
+            compare_slot(canonical_state(g.slot_state(slot)), canonical_state(o.slot_state(slot)),
+                         f"step {k} slot {slot}")
+        out, ref = g.combine_maps(), o.combine_maps()
+        refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
+        compare_combine(out, refd, g.maps_state(), params, f"step {k} combine")
+        compare_slot(canonical_state(g.combined_state()), canonical_state(o.combined_state()), f"step {k} combined")
+
+
+def test_os1_64_veg_30_scans_combine_each_vs_oracle(Gvom):
+    """The headline workload's first 30 scans (256 x 256 x 64 at 0.15 m,
+    buffer 4, OS1-64 + vegetation, float32 transforms) with a combine after
+    every scan, so the previous combined map is carried through 30 merges."""
+    import torch
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["os1_64_veg"]
+    scans = make_workload_scans(w, 30, device="cuda" if torch.cuda.is_available() else "cpu")
+    g = Gvom(*w.gvom_args())
+    o = OracleGvom(*w.gvom_args(), threads=os.cpu_count() or 1)
+    params = w.gvom_args()
+    for i, s in enumerate(scans):
+        g.Process_pointcloud(s.points, s.ego, s.transform)
+        o.Process_pointcloud(s.points, s.ego, s.transform)
+        _, last = g.ring_state()
+        compare_slot(canonical_state(g.slot_state(last)), canonical_state(o.slot_state(last)), f"scan {i}")
+        out, ref = g.combine_maps(), o.combine_maps()
+        refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
+        compare_combine(out, refd, g.maps_state(), params, f"combine after scan {i}")
+    compare_slot(canonical_state(g.combined_state()), canonical_state(o.combined_state()), "combined")
