@@ -75,8 +75,8 @@ FORM_DISTINCT_STEPS = 48
 def stage_bytes(name, n, ns, V, Vext, X2, C_new, C_sum, Cc, nsrc):
     if name == "k_voxelize_trace":
         return 12 * n + 64 * ns
-    if name == "k_assign":
-        return ns * (8 * Vext + 4 * V) + 12 * C_new
+    if name == "k_assign":  # cell and rank per point; per occupied cell its words, index word and record
+        return 20 * n + 36 * C_new
     if name == "k_scatter":
         return 20 * n + 16 * n
     if name == "k_cell_moments":
@@ -270,7 +270,8 @@ def run_reference(args):
     if rank != 0:
         return 0
     from gvom_gb300 import synthetic as S
-    n = 8 if args.workload in S.BATCHED else min(100, max(8, args.steps + args.warmup))
+    # the GPU arm's distinct steps, cycled the same way (step i = distinct step i mod len)
+    n = FORM_DISTINCT_STEPS if args.workload in S.BATCHED else HEAD_DISTINCT_STEPS
     form = Form(args.workload, "cuda" if _has_cuda() else "cpu", n)
     from oracle.oracle import OracleGvom
     threads = os.cpu_count() or 1
@@ -315,7 +316,7 @@ def step_roofline(n_pts, ns, V, X2, B, C_new, C_sum, Cc, hits, steps, peak_gbs, 
     """The whole step against HBM, with the per-unit work of the scan->map
     roofline accounting: process = 12N + 64 + 4V + 52C per scan, combine =
     4V (B + 1) + 4V + 52 sum(C_i) + 2 52 Cc + 20 X^2; int32 atomics = 2H + S
-    per scan (H, S of the last scan, times the scans of a step)."""
+    per scan (H, S: means per scan over the timed steps)."""
     process = 12 * n_pts + ns * (64 + 4 * V) + 52 * C_new
     combine = 4 * V * (B + 1) + 4 * V + 52 * C_sum + 2 * 52 * Cc + 20 * X2
     b = process + combine
@@ -325,21 +326,40 @@ def step_roofline(n_pts, ns, V, X2, B, C_new, C_sum, Cc, hits, steps, peak_gbs, 
             "frac_of_measured_hbm": t_hbm / (ms_per_step / 1e3)}
 
 
-# Scattered 64-bit L2 reductions (atomicAdd without return to random words of
-# a 35 MB array) sustained 200-225 G/s on this part in a throughput probe; the
-# lower figure is the trace kernel's atomic ceiling.
-RED64_SCATTERED_PER_S = 200e9
+# Scattered 32-bit L2 reductions (atomicAdd without return to hashed words of
+# a 16.8 MB int32 array, the headline slot's index map) sustained this rate on
+# GB300 in a throughput probe (method in the design notes); the trace kernel's
+# atomic ceiling.
+RED32_SCATTERED_PER_S = 200e9
 
 
-def trace_atomic_roofline(hits, steps, ms_per_launch, peak=RED64_SCATTERED_PER_S):
+def trace_atomic_roofline(hits, steps, ms_per_launch, peak=RED32_SCATTERED_PER_S):
     """The ray-trace kernel against the L2 reduction rate: its int32 atomics
-    (2H + S of the last scan: a hit and a total per hit, one total per ray
-    step) per launch over its measured launch time."""
+    per launch (2H + S, mean over the timed scans: a hit and a total per hit,
+    one total per ray step) over its measured launch time."""
     atomics = 2 * hits + steps
     achieved = atomics / (ms_per_launch / 1e3)
     return {"bound": "l2_atomics", "atomics_per_launch": int(atomics), "achieved_per_s": achieved,
             "peak_per_s": peak, "frac": achieved / peak,
-            "peak_source": "scattered 64-bit reduction throughput probe on GB300 (200-225 G/s; lower figure)"}
+            "peak_source": "scattered 32-bit reduction throughput probe on GB300"}
+
+
+def scan_counts(g, form, torch):
+    """Valid points, in-grid hits H and ray steps S of every distinct step
+    (each scan processed alone on `g`, untimed): the timed steps cycle through
+    these, so their means are the timed scans' means."""
+    per_step = []
+    for st in form.steps:
+        h = s_ = v = 0
+        for s in st:
+            g.Process_pointcloud(s.points, s.ego, s.transform)
+            r = g.last_process_stats()
+            h += r["hits"]
+            s_ += r["ray_steps"]
+            v += r["valid_points"]
+        per_step.append((v, h, s_))
+    torch.cuda.synchronize()
+    return per_step
 
 
 def _quat_xyzw(R):
@@ -504,6 +524,9 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
         arr = calls[i % len(calls)]
         check(lib.gvom_step(g._h, arr, len(arr), 1, origin.ctypes.data_as(C.c_void_p), *out_ptrs, 1))
 
+    # H and S of the distinct steps, on a private mapper (its state is not the timed one's)
+    counts = scan_counts(Gvom(*w.gvom_args()), form, torch)
+
     for i in range(args.warmup):
         step_device(i)
     torch.cuda.synchronize()
@@ -561,6 +584,10 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
     # the headline: steps back to back, CUDA-graph replay (or direct launches with graphs=False)
     _, t_dev_max, pts_all, wall_timed, clk, _ = timed(n_steps, graphs, False, "" if headline else "_" + form.name,
                                                       back_to_back=True)
+    # mean H, S per step over the timed steps (steps warmup .. warmup + n_steps - 1)
+    timed_counts = [counts[(args.warmup + k) % len(form)] for k in range(n_steps)]
+    H_mean = float(np.mean([c[1] for c in timed_counts]))
+    S_mean = float(np.mean([c[2] for c in timed_counts]))
     # each step alone after an L2 flush (its latency), direct launches back to
     # back for comparison, and a pass with per-kernel CUDA events
     n_aux = max(10, min(n_steps, 300))
@@ -600,6 +627,11 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
     dom = stage_tab[dom_name]
     peak, peak_kind = measured_peak_hbm()
     ray = g.last_process_stats()
+    # the dominant kernel's roofline time: max(bytes / HBM, atomics / L2 reduction rate)
+    t_bytes = dom["alg_bytes"] / (peak * 1e9)
+    atomics = 2 * H_mean + S_mean if dom_name == "k_voxelize_trace" else 0.0
+    t_atom = atomics / RED32_SCATTERED_PER_S
+    t_roof = max(t_bytes, t_atom)
 
     # ---- e2e through the public API with host buffers ----
     e2e_times = []
@@ -663,13 +695,19 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": dom["gbs"], "peak": peak,
                      "peak_source": peak_kind, "unit": "GB/s", "frac": dom["gbs"] / peak,
                      "alg_bytes_per_launch": dom["alg_bytes"], "ms_per_launch": dom["ms_per_launch"],
-                     "traffic": profiled_traffic(dom_name, form.name)},
+                     "traffic": profiled_traffic(dom_name, form.name),
+                     # the scan->map accounting's two terms for this kernel: bytes / HBM and
+                     # int32 atomics (2H + S, mean over the timed steps) / the L2 reduction rate
+                     "atomics_per_launch": int(atomics), "atomic_peak_per_s": RED32_SCATTERED_PER_S,
+                     "atomic_frac": (atomics / (dom["ms_per_launch"] / 1e3)) / RED32_SCATTERED_PER_S,
+                     "t_roof_ms": 1e3 * t_roof, "t_roof_term": "atomics" if t_atom >= t_bytes else "hbm",
+                     "frac_of_t_roof": 1e3 * t_roof / dom["ms_per_launch"]},
         "step_roofline": _safe(lambda: step_roofline(n_mean, ns, V, X * X, w.buffer_size, C_new, C_sum, ncc.value,
-                                                     ray["hits"], ray["ray_steps"], peak,
+                                                     H_mean / ns, S_mean / ns, peak,
                                                      1e3 * t_dev_max / n_steps)),
-        # one scan per launch only: the counters are the last scan's
         "trace_atomic_roofline": _safe(lambda: trace_atomic_roofline(
-            ray["hits"], ray["ray_steps"], stage_tab["k_voxelize_trace"]["ms_per_launch"])) if ns == 1 else None,
+            H_mean, S_mean, stage_tab["k_voxelize_trace"]["ms_per_launch"])),
+        "scan_counts_mean": {"hits": H_mean, "ray_steps": S_mean, "scans_per_step": ns},
         "stages": stage_tab,
         "ray_last_scan": ray,
         "wall_s_timed": wall_timed,
@@ -794,7 +832,7 @@ def run_gpu(args):
             "latency_ms": res["latency_ms"], "e2e": res["e2e"], "gpu_launches": res["gpu_launches"],
             "roofline": res["roofline"], "step_roofline": res.get("step_roofline"),
             "trace_atomic_roofline": res.get("trace_atomic_roofline"), "stages": res["stages"],
-            "ray_last_scan": res["ray_last_scan"],
+            "ray_last_scan": res["ray_last_scan"], "scan_counts_mean": res.get("scan_counts_mean"),
             "direct_launches": res["direct_launches"], "l2_flushed_per_step": res["l2_flushed_per_step"],
             "wall_s_timed": res["wall_s_timed"], "clocks": res["clocks"], "cpu_baseline": cpu,
             "forms": forms,

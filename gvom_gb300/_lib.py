@@ -31,7 +31,7 @@ EXPORTS = (
     "gvom_synchronize", "gvom_last_process_stats", "gvom_device_bytes", "gvom_last_error",
     "gvom_version", "gvom_set_stage_timing", "gvom_stage_times", "gvom_stage_name",
     "gvom_debug_voxel_map_noalloc", "gvom_set_graphs", "gvom_set_tuning", "gvom_get_tuning", "gvom_step",
-    "gvom_ros_grids", "gvom_process_pointcloud2", "gvom_pose_to_transform",
+    "gvom_ros_grids", "gvom_process_pointcloud2", "gvom_pose_to_transform", "gvom_reserve",
 )
 GVOM_STAGES = 11
 
@@ -57,7 +57,7 @@ class GvomScan(C.Structure):
 
 
 class GvomTuning(C.Structure):
-    _fields_ = [("points_per_block", C.c_int32), ("assign_words_per_thread", C.c_int32),
+    _fields_ = [("points_per_block", C.c_int32),
                 ("merge_planes_per_thread", C.c_int32), ("stats_blocks_per_sm", C.c_int32),
                 ("step_overlap", C.c_int32), ("maps_tile_cells", C.c_int32),
                 ("step_pipeline", C.c_int32)]
@@ -117,6 +117,7 @@ def load(path: str | None = None):
         "gvom_synchronize": ([P], C.c_int),
         "gvom_last_process_stats": ([P, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "gvom_device_bytes": ([P, C.POINTER(i64)], C.c_int),
+        "gvom_reserve": ([P, i32, i64, i64], C.c_int),
         "gvom_last_error": ([], C.c_char_p),
         "gvom_set_stage_timing": ([P, i32], C.c_int),
         "gvom_stage_times": ([P, C.POINTER(C.c_double), C.POINTER(i64), i32], C.c_int),

@@ -1,10 +1,9 @@
 """Autotuner for the launch shapes of the GB300 mapper (GvomTuning).
 
-Seven choices, tuned one at a time (coordinate search) on sample steps of
+Six choices, tuned one at a time (coordinate search) on sample steps of
 the caller's workload:
 
   points_per_block         128 / 256   k_voxelize_trace, k_scatter, k_cell_moments, k_cleanup
-  assign_words_per_thread  4 / 8 / 16  k_assign
   merge_planes_per_thread  4 / 8 / 16  k_merge, k_columns
   stats_blocks_per_sm      2 / 4 / 8   k_merge_stats
   step_overlap             0 / 1       gvom_step: the index merge beside the statistics kernels
@@ -29,7 +28,6 @@ import os
 
 CHOICES = {
     "points_per_block": (128, 256),
-    "assign_words_per_thread": (4, 8, 16),
     "merge_planes_per_thread": (4, 8, 16),
     "stats_blocks_per_sm": (2, 4, 8),
     "step_overlap": (0, 1),
@@ -38,14 +36,13 @@ CHOICES = {
 }
 AFFECTS = {
     "points_per_block": ("k_voxelize_trace", "k_scatter", "k_cell_moments", "k_cleanup"),
-    "assign_words_per_thread": ("k_assign",),
     "merge_planes_per_thread": ("k_merge", "k_columns"),
     "stats_blocks_per_sm": ("k_merge_stats",),
     "step_overlap": None,  # whole steps
     "maps_tile_cells": ("k_maps2d",),
     "step_pipeline": None,  # whole steps
 }
-DEFAULT = {"points_per_block": 256, "assign_words_per_thread": 8, "merge_planes_per_thread": 8,
+DEFAULT = {"points_per_block": 256, "merge_planes_per_thread": 8,
            "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 256, "step_pipeline": 2}
 
 

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <deque>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -111,21 +112,47 @@ struct Slot {
     bool valid = false;
 };
 
+// combine-done events kept per instance (a ring): event e % kCombEvents marks
+// the end of combine e's last reader of the ring slots (its statistics merge)
+constexpr int kCombEvents = 8;
+
+// Makes the instance's device current for the duration of an entry point and
+// restores the caller's device afterwards.
+struct DeviceScope {
+    int prev = -1;
+    bool switched = false;
+    explicit DeviceScope(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) switched = cudaSetDevice(dev) == cudaSuccess;
+        cudaGetLastError();
+    }
+    ~DeviceScope() {
+        if (switched) cudaSetDevice(prev);
+    }
+};
+
 }  // namespace
 
 struct GvomHandle {
     GvomParams p;
     Geom g;
     int B = 0;
+    int dev = 0;  // the device the instance was created on
     cudaStream_t own = nullptr, st = nullptr;
     std::mutex mu;
+    // physical slots: the B the ring needs plus spares (up to kMaxPhysSlots).
+    // phys_of maps a ring position to the physical slot of its scan (-1: none
+    // yet); free_q holds the physical slots the ring does not reference, the
+    // longest unreferenced first.  A scan takes the head of free_q, so with
+    // enough spares it is traced into a slot that no combine still in flight
+    // reads; slot_epoch (the last combine that read a slot) and ev_cdone make
+    // that ordering explicit whatever the number of spares.
     std::vector<Slot> slots;
     long long buffer_index = 0, last_buffer_index = 0;  // the reference's ring positions (mod B)
-    // scan number n lives in physical slot n mod P, and phys_of maps a ring
-    // position to the physical slot of its scan (-1: none yet); with P = B
-    // the map is the identity once the ring is full
-    int P = 0;
     std::vector<int> phys_of;
+    std::deque<int> free_q;
+    std::vector<long long> slot_epoch;
+    long long n_comb = 0;                // combines submitted
+    cudaEvent_t ev_cdone[kCombEvents] = {};
     long long scans_total = 0;
     double ego[3] = {0, 0, 0};
     // combined map, double buffered (current / previous)
@@ -169,9 +196,10 @@ struct GvomHandle {
     // CUDA graphs: each process / combine launch sequence is captured and
     // replayed through an executable graph updated in place
     bool graphs = false;
-    // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ merge and
-    // count merge at level 2), [5] its columns and maps, [6] its statistics merge (level 2)
-    cudaGraphExec_t gexec[7] = {};
+    // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ the combine
+    // at level 1), [5] its columns and maps, [6] its count and statistics merges (level 2), [7] its index
+    // merge (level 2)
+    cudaGraphExec_t gexec[8] = {};
     // a step forks the index merge onto `side` once the index maps are done
     cudaStream_t side = nullptr;
     cudaEvent_t ev_idx = nullptr, ev_join = nullptr;
@@ -324,8 +352,7 @@ int ensure_dpts(GvomHandle *h, size_t bytes) {
 int ensure_cnt(GvomHandle *h, int nscans, int set) {
     while ((int)h->cnt[set].size() < nscans) {
         unsigned long long *c = nullptr;
-        // padded to whole k_assign blocks of cells; the padding stays zero
-        const long long ve = (ext_cells(h->g) + kAssignPadCells - 1) / kAssignPadCells * kAssignPadCells;
+        const long long ve = ext_cells(h->g);
         int rc = dalloc_t(h, &c, (size_t)ve);
         if (rc) return rc;
         CUDA_TRY(cudaMemsetAsync(c, 0, (size_t)ve * 8, h->st));
@@ -349,6 +376,38 @@ int ensure_slot(GvomHandle *h, int s, long long need) {
     int rc = dalloc_t(h, &sl.rec, (size_t)cap);
     if (rc) return rc;
     sl.cap = cap;
+    return GVOM_OK;
+}
+
+// a spare physical slot (its index map; records grow on demand), first in
+// the free queue: it has never been read
+int add_slot(GvomHandle *h) {
+    Slot s;
+    int rc = dalloc_t(h, &s.idx, (size_t)h->g.V);
+    if (rc) return rc;
+    h->slots.push_back(s);
+    h->slot_epoch.push_back(-1);
+    h->free_q.push_front((int)h->slots.size() - 1);
+    return GVOM_OK;
+}
+
+// Stream `s` waits until no combine still reads the physical slots `slot_of`
+// (the end of the last combine that read each, ev_cdone).  A slot read by
+// combine e was read by no later combine than the one that last recorded
+// ev_cdone[e % kCombEvents], so the wait is never short.
+int wait_slots_free(GvomHandle *h, const int *slot_of, int k, cudaStream_t s) {
+    for (int i = 0; i < k; i++) {
+        const long long e = h->slot_epoch[slot_of[i]];
+        if (e >= 0) CUDA_TRY(cudaStreamWaitEvent(s, h->ev_cdone[e % kCombEvents], 0));
+    }
+    return GVOM_OK;
+}
+
+// marks the end of the combine just submitted on stream `s` (after its
+// statistics merge, the last kernel that reads the ring slots)
+int comb_done(GvomHandle *h, cudaStream_t s) {
+    CUDA_TRY(cudaEventRecord(h->ev_cdone[h->n_comb % kCombEvents], s));
+    h->n_comb++;
     return GVOM_OK;
 }
 
@@ -396,9 +455,36 @@ struct ProcPlan {
     int set = 0;  // scratch set
     int slot_of[kMaxBatch];
     double last_ego[3];
+    std::deque<int> free_before;  // the free queue before this plan took its slots
 };
 
-int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl) {
+// Physical slots for the plan's scans.  Scan i overwrites ring position
+// (buffer_index + i) mod B: the slot that position held joins the back of
+// the free queue, and the scan takes the head (the slot unreferenced the
+// longest).  While fewer than `spare` + 1 slots are free, a spare slot is
+// added first (up to kMaxPhysSlots; without memory the plan goes on with
+// fewer spares, still correct through wait_slots_free).  Pipelined steps ask
+// for two steps' worth of spares, so the head was last read two combines back.
+void take_slots(GvomHandle *h, ProcPlan &pl, int spare) {
+    pl.free_before = h->free_q;
+    for (int i = 0; i < pl.k; i++) {
+        const int pos = (int)((h->buffer_index + i) % h->B);
+        if (h->phys_of[pos] >= 0) h->free_q.push_back(h->phys_of[pos]);
+        while ((int)h->free_q.size() < spare + 1 && (int)h->slots.size() < kMaxPhysSlots) {
+            if (add_slot(h)) {
+                cudaGetLastError();
+                break;
+            }
+        }
+        pl.slot_of[i] = h->free_q.front();
+        h->free_q.pop_front();
+    }
+}
+
+// undoes take_slots when the plan is dropped before commit_scans
+void release_slots(GvomHandle *h, ProcPlan &pl) { h->free_q = pl.free_before; }
+
+int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl, int spare = 0) {
     const int k = (int)scans.size();
     pl.k = k;
     if (k == 0) return GVOM_OK;
@@ -427,7 +513,6 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
     }
     pc.step_cap = 2 * std::max(h->g.X, h->g.Z) + 8;
     pc.num_sms = h->num_sms;
-    pc.assign_per = h->tun.assign_per;
     pc.xe_magic = ~0ull / (unsigned long long)h->g.Xe + 1ull;
     pc.adv[0] = 256 % h->g.Xe;
     pc.adv[1] = (256 / h->g.Xe) % h->g.Xe;
@@ -437,12 +522,15 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
     std::memset(pl.table, 0, sizeof(pl.table));
     int block = 0;
     long long base = 0;
+    take_slots(h, pl, spare);
     int *slot_of = pl.slot_of;
     for (int i = 0; i < k; i++) {
         const ScanIn &s = scans[i];
-        const int slot = (int)((h->scans_total + i) % h->P);  // physical; ring position (buffer_index + i) mod B
-        slot_of[i] = slot;
-        if ((rc = ensure_slot(h, slot, s.n))) return rc;
+        const int slot = slot_of[i];
+        if ((rc = ensure_slot(h, slot, s.n))) {
+            release_slots(h, pl);
+            return rc;
+        }
         ScanDesc &d = table[i];
         d.pts = s.dev_pts;
         d.n = s.n;
@@ -502,18 +590,24 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl)
     return GVOM_OK;
 }
 
-// stream-ordered work of a prepared process call on h->st; `after_assign`
-// (nullable) is recorded once the ring slots' index maps are complete
-// `part` as in launch_process: 1 (the trace, on stream `st`) and 2 (the rest,
-// on h->st) split one process call in two
+// stream-ordered work of a prepared process call on stream `st` (default
+// h->st); `after_assign` (nullable) is recorded once the ring slots' index
+// maps are complete (as an external event with `assign_external`).  `part`
+// as in launch_process: 1 (the trace) and 2 (the rest) split one process
+// call in two.  The trace part first fills the slots' index maps with -1
+// (unknown): the trace counts pass-throughs down from there.
 int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bool timing, int part = 0,
-                 cudaStream_t st = nullptr) {
+                 cudaStream_t st = nullptr, bool assign_external = false) {
     if (!st) st = h->st;
     ScanCounters *ctr = h->d_ctr + pl.set * kMaxBatch;
-    if (part == 0 || part == 1) CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(ScanCounters) * pl.k, st));
+    if (part == 0 || part == 1) {
+        CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(ScanCounters) * pl.k, st));
+        for (int i = 0; i < pl.k; i++)
+            CUDA_TRY(cudaMemsetAsync(h->slots[pl.slot_of[i]].idx, 0xff, sizeof(int) * (size_t)h->g.V, st));
+    }
     CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec[pl.set], h->prank[pl.set], h->sorted,
                             h->moments, st, (timing && !part) ? h->timer.begin(0, kProcessKernels) : nullptr,
-                            h->tun.pts_block, after_assign, part));
+                            h->tun.pts_block, after_assign, part, assign_external));
     if (part == 1) return GVOM_OK;
     for (int i = 0; i < pl.k; i++)
         CUDA_TRY(cudaMemcpyAsync(h->d_slotC + pl.slot_of[i], &ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
@@ -543,8 +637,12 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
     ProcPlan pl;
     int rc = prepare_scans(h, scans, pl);
     if (rc) return rc;
-    rc = run_graphed(h, 0, [&]() -> int { return launch_scans(h, pl, nullptr, !h->graphs); });
-    if (rc) return rc;
+    if (!rc) rc = wait_slots_free(h, pl.slot_of, pl.k, h->st);
+    if (!rc) rc = run_graphed(h, 0, [&]() -> int { return launch_scans(h, pl, nullptr, !h->graphs); });
+    if (rc) {
+        release_slots(h, pl);
+        return rc;
+    }
     CUDA_TRY(cudaEventRecord(h->ev_scratch[pl.set], h->st));  // a later pipelined trace may reuse the set
     commit_scans(h, pl);
     return GVOM_OK;
@@ -599,6 +697,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     GvomHandle *h = new GvomHandle();
+    h->dev = dev;
     h->p = *params;
     Geom &g = h->g;
     g.X = params->xy_size;
@@ -610,15 +709,16 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     g.V = (long long)g.X * g.X * g.Z;
     g.Vext = ext_cells(g);
     h->B = params->buffer_size;
-    h->P = h->B;
-    h->slots.resize(h->P);
+    h->slots.resize(h->B);
+    h->slot_epoch.assign(h->B, -1);
+    for (int s = 0; s < h->B; s++) h->free_q.push_back(s);
     h->phys_of.assign(h->B, -1);
     cudaDeviceGetAttribute(&h->pageable_access, cudaDevAttrPageableMemoryAccess, dev);
     if (cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || h->num_sms < 1)
         h->num_sms = 1;
     // admission: the resident footprint must fit in free device memory with margin
     const long long X2 = (long long)g.X * g.X;
-    const long long need = (long long)h->P * g.V * 4 + 2 * g.V * (4 + (long long)sizeof(VoxelRec)) + g.V * 4 +
+    const long long need = (long long)h->B * g.V * 4 + 2 * g.V * (4 + (long long)sizeof(VoxelRec)) + g.V * 4 +
                            g.Vext * 8 +
                            X2 * (6 * 8 + 4 * 4) + (64LL << 20);
     size_t fr = 0, tot = 0;
@@ -662,11 +762,19 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         gvom_destroy(h);
         return fail(GVOM_ERR_CUDA, "stream / event creation failed");
     }
+    for (auto &e : h->ev_cdone) {
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+            e = nullptr;
+            cudaGetLastError();
+            gvom_destroy(h);
+            return fail(GVOM_ERR_CUDA, "event creation failed");
+        }
+    }
     auto bail = [&](int code) {
         gvom_destroy(h);
         return code;
     };
-    for (int s = 0; s < h->P; s++) {
+    for (int s = 0; s < h->B; s++) {
         if ((rc = dalloc_t(h, &h->slots[s].idx, (size_t)g.V))) return bail(rc);
     }
     for (int b = 0; b < 2; b++) {
@@ -676,7 +784,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
     // counters + scan table
     if ((rc = dalloc(h, reinterpret_cast<void **>(&h->d_ctr), sizeof(ScanCounters) * 2 * kMaxBatch)))
         return bail(rc);
-    if ((rc = dalloc_t(h, &h->d_slotC, (size_t)h->P))) return bail(rc);
+    if ((rc = dalloc_t(h, &h->d_slotC, (size_t)kMaxPhysSlots))) return bail(rc);
     if ((rc = dalloc_t(h, &h->d_combC, 4))) return bail(rc);
     double **maps[6] = {&h->height, &h->inferred, &h->slope_x, &h->slope_y, &h->rough, &h->guess};
     for (auto m : maps)
@@ -689,7 +797,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         if ((rc = dalloc_t(h, &h->colinfo[b], (size_t)X2 * ((g.Z + 3) / 4)))) return bail(rc);
     for (int b = 0; b < 2; b++)
         if ((rc = dalloc_t(h, &h->occ_list[b], (size_t)g.V))) return bail(rc);
-    if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * h->P, h->st) != cudaSuccess ||
+    if (cudaMemsetAsync(h->d_slotC, 0, sizeof(int) * kMaxPhysSlots, h->st) != cudaSuccess ||
         cudaMemsetAsync(h->d_combC, 0, sizeof(int) * 4, h->st) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(GVOM_ERR_CUDA, "memset failed"));
@@ -705,6 +813,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
 
 int gvom_destroy(GvomHandle *h) {
     if (!h) return GVOM_OK;
+    DeviceScope ds(h->dev);
     if (h->st) cudaStreamSynchronize(h->st);
     if (h->own) cudaStreamSynchronize(h->own);
     for (auto &x : h->gexec)
@@ -726,6 +835,8 @@ int gvom_destroy(GvomHandle *h) {
     for (cudaEvent_t e : h->ev_scratch)
         if (e) cudaEventDestroy(e);
     if (h->ev_traced) cudaEventDestroy(h->ev_traced);
+    for (cudaEvent_t e : h->ev_cdone)
+        if (e) cudaEventDestroy(e);
     for (auto &s : h->slots) {
         cudaFree(s.idx);
         cudaFree(s.rec);
@@ -771,6 +882,7 @@ int gvom_destroy(GvomHandle *h) {
 int gvom_process(GvomHandle *h, const void *points, int32_t dtype, int64_t n, int64_t row_stride,
                  const double ego[3], const void *transform, int32_t transform_dtype) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     if (n > 0 && !points) return fail(GVOM_ERR_ARG, "points is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
     ScanIn s;
@@ -825,6 +937,7 @@ static void pose_matrix(const double t[3], const double qin[4], double T[16]) {
 int gvom_process_device(GvomHandle *h, const void *d_points, int32_t dtype, int64_t n, int64_t row_stride,
                         const double ego[3], const void *transform, int32_t transform_dtype) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     if (n > 0 && !d_points) return fail(GVOM_ERR_ARG, "points is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
     ScanIn s;
@@ -887,6 +1000,7 @@ int gvom_process_pointcloud2(GvomHandle *h, const void *data, int64_t n_points, 
                              const int32_t xyz_offsets[3], int32_t field_dtype, int32_t data_on_device,
                              const double ego[3], const double translation[3], const double rotation_xyzw[4]) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     if (!xyz_offsets || !ego || !translation || !rotation_xyzw) return fail(GVOM_ERR_ARG, "NULL argument");
     if (field_dtype != GVOM_F32 && field_dtype != GVOM_F64)
         return fail(GVOM_ERR_ARG, "x / y / z fields must be float32 or float64");
@@ -924,6 +1038,7 @@ int gvom_process_pointcloud2(GvomHandle *h, const void *data, int64_t n_points, 
 
 int gvom_process_batch(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     if (n_scans < 0 || (n_scans > 0 && !scans)) return fail(GVOM_ERR_ARG, "bad scan list");
     if (n_scans == 0) return GVOM_OK;
     std::lock_guard<std::mutex> lk(h->mu);
@@ -960,6 +1075,7 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
         if (h->phys_of[i] < 0) continue;
         const Slot &s = h->slots[h->phys_of[i]];
         if (!s.valid) continue;
+        h->slot_epoch[h->phys_of[i]] = h->n_comb;  // read by this combine (see comb_done)
         MergeSrc &m = mp.src[ns++];
         m.idx = s.idx;
         m.rec = s.rec;
@@ -1118,6 +1234,7 @@ int copy_outputs(GvomHandle *h, const CombPlan &pl, double origin[3], int32_t *p
 static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, double *rough, int32_t *vis,
                         bool to_host) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     h->st_dirty = true;  // work on the instance stream: see the step pipeline
     CombPlan pl;
@@ -1125,6 +1242,7 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     if (rc) return rc;
     rc = run_graphed(h, 1, [&]() -> int { return launch_comb(h, pl, nullptr, !h->graphs); });
     if (rc) return rc;
+    if ((rc = comb_done(h, h->st))) return rc;
     commit_combine(h, pl);
     return copy_outputs(h, pl, origin, pos, neg, rough, vis, to_host);
 }
@@ -1141,6 +1259,7 @@ int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t
 int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device, double origin[3],
               int32_t *pos, int32_t *neg, double *roughness, int32_t *visibility, int32_t outputs_on_device) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     if (n_scans < 1 || !scans) return fail(GVOM_ERR_ARG, "a step needs at least one scan");
     std::lock_guard<std::mutex> lk(h->mu);
     const bool timing = !h->graphs && h->timer.on;
@@ -1150,6 +1269,7 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         CUDA_TRY(cudaEventRecord(h->ev_host, h->st));
         CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_host, 0));
         CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_host, 0));
+        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_host, 0));
         h->st_dirty = false;
     }
     // a pipelined step stages its points and traces on `tr`, once the previous
@@ -1160,45 +1280,66 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     int rc;
     if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned, pipe ? h->tr : h->st))) return rc;
     ProcPlan pp;
-    if ((rc = prepare_scans(h, v, pp))) return rc;
+    // pipelined: spare slots for two steps, so the trace never waits for a combine in flight
+    if ((rc = prepare_scans(h, v, pp, pipe ? 2 * (int)v.size() : 0))) return rc;
+    // the trace stream waits until no combine in flight reads the slots it fills
+    if ((rc = wait_slots_free(h, pp.slot_of, pp.k, pipe ? h->tr : h->st))) {
+        release_slots(h, pp);
+        return rc;
+    }
     commit_scans(h, pp);  // host ring bookkeeping; the combine plan reads the ring after this batch
     for (int a = 0; a < 3; a++) h->ego[a] = scans[n_scans - 1].ego[a];
     CombPlan cp;
     if ((rc = prepare_combine(h, cp))) return rc;
     cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
     if (pipe == 2) {
+        // tr: the trace
         rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
-        // the rest of the process and the merge: after the trace, and after the
-        // columns pass that last read the combined buffer this merge writes
+        // bs: the rest of the process, after the trace; ev_idx marks the slots'
+        // index maps complete, ev_scratch[set] the whole process
         CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_traced, 0));
-        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_cols[cp.nb], 0));
-        CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_stats[cp.nb], 0));
         rc = run_graphed(h, 4, [&]() -> int {
-            if ((rc = launch_scans(h, pp, idx, false, 2, h->bs))) return rc;
+            if ((rc = launch_scans(h, pp, h->ev_idx, false, 2, h->bs, h->graphs))) return rc;
             if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_scratch[pp.set], h->bs, cudaEventRecordExternal));
             else CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->bs));
-            return launch_comb(h, cp, idx, false, 1, h->bs);
+            return GVOM_OK;
         }, h->bs);
         if (rc) return rc;
-        CUDA_TRY(cudaEventRecord(h->ev_merged, h->bs));
-        // the statistics merge beside the columns and maps
-        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_merged, 0));
+        // side: the combine's merges, in stream order after the previous step's
+        // statistics merge (which reads the combined buffer this merge writes)
+        // and after the columns pass that last read that buffer; the index merge
+        // once the index maps are complete, beside the statistics kernels
+        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_cols[cp.nb], 0));
+        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_idx, 0));
+        rc = run_graphed(h, 7, [&]() -> int {
+            CUDA_TRY(cudaMemsetAsync(cp.mp.out_count, 0, sizeof(int), h->side));
+            CUDA_TRY(launch_merge_index(cp.mp, h->side));
+            return GVOM_OK;
+        }, h->side);
+        if (rc) return rc;
+        // the count and statistics merges once the slots' records are complete
+        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_scratch[pp.set], 0));
         rc = run_graphed(h, 6, [&]() -> int {
+            CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->side, nullptr, 1));
+            if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_merged, h->side, cudaEventRecordExternal));
+            else CUDA_TRY(cudaEventRecord(h->ev_merged, h->side));
             CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->side, nullptr, 4));
             return GVOM_OK;
         }, h->side);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(h->ev_stats[cp.nb], h->side));
-        // columns and maps on the instance stream, beside the next step's process
+        if ((rc = comb_done(h, h->side))) return rc;
+        // st: columns and maps after the count merge, beside the statistics
+        // merge and the next step's process
         CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_merged, 0));
         rc = run_graphed(h, 5, [&]() -> int { return launch_comb(h, cp, nullptr, false, 2); });
         if (!rc) CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_stats[cp.nb], 0));  // later calls see whole records
     } else if (pipe == 1) {
         h->st_dirty = true;
-        // the trace waits only for the previous process to release the scratch,
-        // so it runs beside the previous step's combine
+        // the trace waits only for the previous process to release the scratch
+        // (and for its slots), so it runs beside the previous step's combine
         rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
         if (rc) return rc;
         CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
@@ -1210,6 +1351,7 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
             else CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->st));
             return launch_comb(h, cp, idx, false);
         });
+        if (!rc) rc = comb_done(h, h->st);
     } else {
         h->st_dirty = true;
         rc = run_graphed(h, 2, [&]() -> int {
@@ -1217,6 +1359,7 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
             return launch_comb(h, cp, idx, timing);
         });
         if (!rc) CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->st));
+        if (!rc) rc = comb_done(h, h->st);
     }
     if (rc) return rc;
     commit_combine(h, cp);
@@ -1227,6 +1370,7 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
 
 int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64_t *rows) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     h->st_dirty = true;  // work on the instance stream: see the step pipeline
     if (!h->have_comb) return fail(GVOM_NO_DATA, "No data");
@@ -1275,6 +1419,7 @@ int gvom_debug_voxel_map(GvomHandle *h, float *out, int64_t capacity_rows, int64
 
 static int debug_maps(GvomHandle *h, float *out_h, float *out_i) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     h->st_dirty = true;  // work on the instance stream: see the step pipeline
     if (!h->have_maps) return fail(GVOM_NO_DATA, "No data");
@@ -1319,6 +1464,7 @@ int *g_static_ptr[kMaxDevices] = {};
 
 int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_rows, int64_t *rows) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     if (capacity_rows < 0) return fail(GVOM_ERR_ARG, "capacity_rows is negative");
     std::lock_guard<std::mutex> lk(h->mu);
     h->st_dirty = true;  // work on the instance stream: see the step pipeline
@@ -1330,8 +1476,9 @@ int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_r
                                       std::to_string((long long)kStaticDebugBlocks * chunk) +
                                       " voxels the allocation-free export supports; use gvom_debug_voxel_map");
     if (!h->have_comb) return fail(GVOM_NO_DATA, "No data");
-    int dev = 0;
-    CUDA_TRY(cudaGetDevice(&dev));
+    // the scratch array and its lock belong to the instance's device (current
+    // here through the DeviceScope)
+    const int dev = h->dev;
     if (dev < 0 || dev >= kMaxDevices) return fail(GVOM_ERR_ARG, "device index out of range");
     std::lock_guard<std::mutex> dl(g_static_mu[dev]);
     if (!g_static_ptr[dev]) {
@@ -1344,9 +1491,12 @@ int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_r
         g_static_ptr[dev] = p;
     }
     int *scratch = g_static_ptr[dev];
-    CUDA_TRY(launch_debug_count(h->cidx[h->cur], V, scratch, (int)nblocks, h->st));
-    CUDA_TRY(launch_debug_offsets(scratch, (int)nblocks, h->st));
-    if (d_out && capacity_rows > 0) {
+    // once a kernel is queued, every exit waits for the stream, so that the
+    // lock covers all device work on the shared scratch array
+    int total = 0;
+    cudaError_t e = launch_debug_count(h->cidx[h->cur], V, scratch, (int)nblocks, h->st);
+    if (e == cudaSuccess) e = launch_debug_offsets(scratch, (int)nblocks, h->st);
+    if (e == cudaSuccess && d_out && capacity_rows > 0) {
         DebugVoxParams p;
         p.idx = h->cidx[h->cur];
         p.rec = h->crec[h->cur];
@@ -1358,11 +1508,15 @@ int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_r
         p.z_res = h->p.z_resolution;
         p.out = d_out;
         p.cap = capacity_rows;
-        CUDA_TRY(launch_debug_voxels(p, (int)nblocks, h->st));
+        e = launch_debug_voxels(p, (int)nblocks, h->st);
     }
-    int total = 0;
-    CUDA_TRY(cudaMemcpyAsync(&total, scratch + nblocks, sizeof(int), cudaMemcpyDeviceToHost, h->st));
-    CUDA_TRY(cudaStreamSynchronize(h->st));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, scratch + nblocks, sizeof(int), cudaMemcpyDeviceToHost, h->st);
+    const cudaError_t es = cudaStreamSynchronize(h->st);
+    if (e == cudaSuccess) e = es;
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(GVOM_ERR_CUDA, std::string("allocation-free debug voxel export: ") + cudaGetErrorString(e));
+    }
     if (rows) *rows = total;
     return GVOM_OK;
 }
@@ -1370,6 +1524,7 @@ int gvom_debug_voxel_map_noalloc(GvomHandle *h, float *d_out, int64_t capacity_r
 int gvom_ros_grids(GvomHandle *h, const GvomRosParams *rp, int8_t *hard, int8_t *soft, int8_t *certainty,
                    int8_t *negative, int8_t *roughness, int32_t outputs_on_device) {
     if (!h || !rp) return fail(GVOM_ERR_ARG, "handle or params is NULL");
+    DeviceScope ds(h->dev);
     if (!(rp->max_roughness != rp->min_roughness)) return fail(GVOM_ERR_ARG, "max_roughness must differ from min_roughness");
     std::lock_guard<std::mutex> lk(h->mu);
     h->st_dirty = true;  // work on the instance stream: see the step pipeline
@@ -1415,6 +1570,7 @@ int gvom_debug_inferred_height_map(GvomHandle *h, float *out) { return debug_map
 
 int gvom_ring_state(GvomHandle *h, int64_t *buffer_index, int64_t *last_buffer_index) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     if (buffer_index) *buffer_index = h->buffer_index;
     if (last_buffer_index) *last_buffer_index = h->last_buffer_index;
@@ -1429,6 +1585,7 @@ static int read_int(GvomHandle *h, const int *d, int *v) {
 
 int gvom_slot_count(GvomHandle *h, int32_t slot, int64_t *count) {
     if (!h || !count) return fail(GVOM_ERR_ARG, "NULL argument");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     if (slot < 0 || slot >= h->B) return fail(GVOM_ERR_ARG, "slot out of range");
     const int p = h->phys_of[slot];
@@ -1476,6 +1633,7 @@ static int copy_records(GvomHandle *h, const VoxelRec *d_rec, long long C, int32
 int gvom_get_slot(GvomHandle *h, int32_t slot, int32_t *index, int32_t *hit, int32_t *total, float *min_height,
                   float *metrics, double origin[3]) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     if (slot < 0 || slot >= h->B) return fail(GVOM_ERR_ARG, "slot out of range");
     const int p = h->phys_of[slot];
@@ -1496,6 +1654,7 @@ int gvom_get_slot(GvomHandle *h, int32_t slot, int32_t *index, int32_t *hit, int
 
 int gvom_combined_count(GvomHandle *h, int64_t *count) {
     if (!h || !count) return fail(GVOM_ERR_ARG, "NULL argument");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     if (!h->have_comb) {
         *count = -1;
@@ -1511,6 +1670,7 @@ int gvom_combined_count(GvomHandle *h, int64_t *count) {
 int gvom_get_combined(GvomHandle *h, int32_t *index, int32_t *hit, int32_t *total, float *min_height, float *metrics,
                       float *eigen, double origin[3]) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     if (!h->have_comb) return fail(GVOM_NO_DATA, "No data");
     // the device map addresses records by voxel id; export them compacted in
@@ -1553,6 +1713,7 @@ int gvom_get_combined(GvomHandle *h, int32_t *index, int32_t *hit, int32_t *tota
 int gvom_get_maps(GvomHandle *h, double *height, double *inferred, double *slope_x, double *slope_y, double *roughness,
                   double *guess) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     if (!h->have_maps) return fail(GVOM_NO_DATA, "No data");
     const size_t b = (size_t)h->g.X * h->g.X * 8;
@@ -1566,6 +1727,7 @@ int gvom_get_maps(GvomHandle *h, double *height, double *inferred, double *slope
 
 int gvom_set_stream(GvomHandle *h, void *stream) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     h->st_dirty = true;  // work on the instance stream: see the step pipeline
     cudaStream_t ns = stream ? static_cast<cudaStream_t>(stream) : h->own;
@@ -1584,6 +1746,7 @@ int gvom_set_stream(GvomHandle *h, void *stream) {
 
 int gvom_synchronize(GvomHandle *h) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     CUDA_TRY(cudaStreamSynchronize(h->st));
     CUDA_TRY(cudaGetLastError());
@@ -1592,6 +1755,7 @@ int gvom_synchronize(GvomHandle *h) {
 
 int gvom_last_process_stats(GvomHandle *h, int64_t *valid_points, int64_t *hits, int64_t *ray_steps) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     if (h->last_ctr < 0) return fail(GVOM_NO_DATA, "no scan processed yet");
     ScanCounters c;
@@ -1608,8 +1772,6 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     if (!h || !t) return fail(GVOM_ERR_ARG, "handle or tuning is NULL");
     if (!(t->points_per_block == 128 || t->points_per_block == 256))
         return fail(GVOM_ERR_ARG, "points_per_block must be 128 or 256");
-    if (!(t->assign_words_per_thread == 4 || t->assign_words_per_thread == 8 || t->assign_words_per_thread == 16))
-        return fail(GVOM_ERR_ARG, "assign_words_per_thread must be 4, 8 or 16");
     if (!(t->merge_planes_per_thread == 4 || t->merge_planes_per_thread == 8 || t->merge_planes_per_thread == 16))
         return fail(GVOM_ERR_ARG, "merge_planes_per_thread must be 4, 8 or 16");
     if (!(t->stats_blocks_per_sm == 2 || t->stats_blocks_per_sm == 4 || t->stats_blocks_per_sm == 8))
@@ -1620,7 +1782,6 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     if (!(t->step_pipeline >= 0 && t->step_pipeline <= 2)) return fail(GVOM_ERR_ARG, "step_pipeline must be 0, 1 or 2");
     std::lock_guard<std::mutex> lk(h->mu);
     h->tun.pts_block = t->points_per_block;
-    h->tun.assign_per = t->assign_words_per_thread;
     h->tun.merge_planes = t->merge_planes_per_thread;
     h->tun.stats_bpsm = t->stats_blocks_per_sm;
     h->tun.step_overlap = t->step_overlap;
@@ -1633,7 +1794,6 @@ int gvom_get_tuning(GvomHandle *h, GvomTuning *t) {
     if (!h || !t) return fail(GVOM_ERR_ARG, "handle or tuning is NULL");
     std::lock_guard<std::mutex> lk(h->mu);
     t->points_per_block = h->tun.pts_block;
-    t->assign_words_per_thread = h->tun.assign_per;
     t->merge_planes_per_thread = h->tun.merge_planes;
     t->stats_blocks_per_sm = h->tun.stats_bpsm;
     t->step_overlap = h->tun.step_overlap;
@@ -1644,6 +1804,7 @@ int gvom_get_tuning(GvomHandle *h, GvomTuning *t) {
 
 int gvom_set_graphs(GvomHandle *h, int32_t on) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     h->graphs = on != 0;
     return GVOM_OK;
@@ -1651,6 +1812,7 @@ int gvom_set_graphs(GvomHandle *h, int32_t on) {
 
 int gvom_set_stage_timing(GvomHandle *h, int32_t on) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     h->timer.reset();
     h->timer.on = on != 0;
@@ -1659,6 +1821,7 @@ int gvom_set_stage_timing(GvomHandle *h, int32_t on) {
 
 int gvom_stage_times(GvomHandle *h, double *total_ms, int64_t *launches, int32_t n_stages) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
     std::lock_guard<std::mutex> lk(h->mu);
     h->timer.harvest();
     for (int i = 0; i < n_stages && i < kStages; i++) {
@@ -1675,6 +1838,28 @@ const char *gvom_stage_name(int32_t stage) {
 int gvom_device_bytes(GvomHandle *h, int64_t *bytes) {
     if (!h || !bytes) return fail(GVOM_ERR_ARG, "NULL argument");
     *bytes = h->bytes;
+    return GVOM_OK;
+}
+
+int gvom_reserve(GvomHandle *h, int32_t max_scans, int64_t max_points, int64_t max_row_bytes) {
+    if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
+    DeviceScope ds(h->dev);
+    if (max_scans < 1 || max_scans > kMaxBatch) return fail(GVOM_ERR_ARG, "max_scans must be in [1, 16]");
+    if (max_points < 0 || max_row_bytes < 0) return fail(GVOM_ERR_ARG, "negative size");
+    std::lock_guard<std::mutex> lk(h->mu);
+    CUDA_TRY(cudaStreamSynchronize(h->st));
+    int rc;
+    for (int set = 0; set < 2; set++)
+        if ((rc = ensure_cnt(h, max_scans, set))) return rc;
+    if ((rc = ensure_points(h, std::max<long long>(max_points, 1)))) return rc;
+    const size_t stage = (size_t)max_points * (size_t)max_row_bytes + 256 * (size_t)max_scans;
+    if ((rc = ensure_dpts(h, stage))) return rc;
+    const int want = std::min(kMaxPhysSlots, h->B + 2 * max_scans);
+    while ((int)h->slots.size() < want)
+        if ((rc = add_slot(h))) return rc;
+    for (int s = 0; s < (int)h->slots.size(); s++)
+        if ((rc = ensure_slot(h, s, max_points))) return rc;
+    CUDA_TRY(cudaStreamSynchronize(h->st));
     return GVOM_OK;
 }
 

@@ -21,13 +21,10 @@
 namespace gvom {
 
 constexpr int kMaxBatch = 16;         // scans per batched launch
-constexpr int kAssignPerMax = 16;     // count words per k_assign thread, at most
-constexpr int kAssignPadCells = 256 * kAssignPerMax;  // count arrays are padded to this many cells
 
 // Launch-shape choices of the autotuner (each affects its own kernels only).
 struct Tuning {
     int pts_block;      // points per block of the point-parallel kernels: 128 or 256
-    int assign_per;     // count words per k_assign thread: 4, 8 or 16
     int merge_planes;   // z planes per k_merge thread: 4, 8 or 16
     int stats_bpsm;     // k_merge_stats blocks per multiprocessor: 2, 4 or 8
     int step_overlap;   // gvom_step runs the index merge beside the statistics kernels: 0 or 1
@@ -35,10 +32,13 @@ struct Tuning {
     int step_pipeline;  // gvom_step: 0 one stream; 1 the trace beside the previous step's combine; 2 also the
                         // rest of the process and the merge beside the previous step's columns and maps
 };
-constexpr Tuning kDefaultTuning = {256, 8, 8, 4, 1, 256, 2};
+constexpr Tuning kDefaultTuning = {256, 8, 4, 1, 256, 2};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
 constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map
+// physical slots of an instance: the ring's B plus spares, so that a step's
+// scans are traced into slots that the combines still in flight do not read
+constexpr int kMaxPhysSlots = (kMaxSources - 1) + 2 * kMaxBatch;
 
 // Per-voxel record.  Ring slots store aux[0] = voxel id (int bits); the
 // combined map stores the three eigenvalues (descending) in aux.
@@ -110,7 +110,6 @@ struct ProcessConst {
     int step_cap;          // upper bound on ray steps inside the grid
     int nscans;
     int num_sms;           // multiprocessors of the device (persistent grids)
-    int assign_per;        // Tuning::assign_per
     unsigned long long xe_magic;  // floor((2^64 - 1) / Xe) + 1 (divisions by the extended row length)
     int adv[3];            // extended coordinates (x, y, z) of cell index 256
 };
@@ -207,10 +206,14 @@ constexpr int kProcessKernels = 6;  // voxelize_trace, assign, scatter, cell_mom
 constexpr int kCombineKernels = 5;  // merge, merge_counts, merge_stats, columns, maps2d
 constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
 // `part`: 0 every kernel, 1 k_voxelize_trace only, 2 the kernels after it
-// (parts are launched without stage events)
+// (parts are launched without stage events).  `after_assign` (nullable) is
+// recorded once the slots' index maps are complete; `assign_external`: as an
+// external event (graph capture: for a wait outside the captured graph).
+// The slots' index maps must already hold -1 when the trace starts.
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part = 0);
+                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part = 0,
+                           bool assign_external = false);
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
 cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st);
 // `part`: 0 counts, statistics, columns, maps2d in sequence; 1 the count

@@ -1,14 +1,23 @@
 // Per-scan kernels: Gvom.Process_pointcloud (scripts/gvom.py:105-217).
 //
+// The slot's index map is the pass-through counter: it is filled with -1
+// (unknown) before the scan, and every ray step and every in-grid hit
+// subtracts one from its voxel's word, which leaves a free voxel at
+// -(total)-1, the reference's encoding (scripts/gvom.py:1233-1240).  The
+// points' cells (grid plus the eigen-neighbourhood halo) count their points
+// in a separate, sparsely touched word array (`cnt`, zero between scans).
+//
 //   k_voxelize_trace  transform + min-distance filter + hit voxel + ray march
 //                     (scripts/gvom.py:1121-1231); also records every point's
-//                     voxel fraction and cell for the statistics
-//   k_assign          compact-index allocation and dense->compact move
+//                     voxel fraction, cell and rank in its cell
+//   k_assign          one thread per point-holding cell (its first point):
+//                     compact index and record of occupied voxels, total =
+//                     -(word)-1 read back from the index map
 //                     (scripts/gvom.py:1233-1247), point-group offsets
 //   k_scatter         groups points by cell (rank from the hit atomic)
 //   k_voxel_stats     neighbourhood mean / covariance / count and in-voxel
 //                     minimum height (scripts/gvom.py:1249-1421)
-//   k_cleanup         returns the dense count array to zero
+//   k_cleanup         returns the cell words to zero
 //
 // All float arithmetic that decides an integer result uses the IEEE-rounded
 // intrinsics in the reference's operand types, without contraction.
@@ -129,15 +138,15 @@ __device__ __forceinline__ void warp_add_u64(unsigned long long *dst, unsigned l
 // ---------------------------------------------------------------------------
 // k_voxelize_trace: one thread per point.
 //
-// Every ray starts at the ego, so the cells around it receive an increment
-// from almost every ray.  A ray's first steps, while they stay inside a
-// kCube^3 block of cells around the ego voxel (sd.cube0, inside the grid),
-// are counted in shared memory and flushed once per block (one global atomic
-// per touched cell).  The remaining steps go through a per-block shared hash
-// table of (cell, count): neighbouring rays of a block cross many of the
-// same cells, and a shared atomic is several times cheaper than a scattered
-// global reduction; a step whose slot holds another cell adds straight into
-// the dense count words.
+// Every ray starts at the ego, so the voxels around it receive a pass from
+// almost every ray.  A ray's first steps, while they stay inside a kCube^3
+// block of voxels around the ego voxel (sd.cube0, inside the grid), are
+// counted in shared memory and flushed once per block (one global atomic per
+// touched voxel).  The remaining steps go through a per-block shared hash
+// table of (voxel, count): neighbouring rays of a block cross many of the
+// same voxels, and a shared atomic is several times cheaper than a scattered
+// global reduction; a step whose slot holds another voxel subtracts straight
+// from the index map word.
 // ---------------------------------------------------------------------------
 
 // per-block shared hash table for the ray steps outside the cube
@@ -170,6 +179,7 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
     const bool active = i < sd.n;
     unsigned long long n_valid = 0, n_hit = 0, n_steps = 0;
     const int Xe = g.Xe, XeXe = g.Xe * g.Xe;
+    const int XX = g.X * g.X;
     if (active) {
         const long long gi = sd.pt_base + i;
         float4 rec = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
@@ -227,8 +237,8 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
             if (in_ext) {
                 const bool in_grid = bx >= 0 && bx < g.X && by >= 0 && by < g.X && bz >= 0 && bz < g.Z;
                 const int cell = (bx + g.exy) + (by + g.exy) * Xe + (bz + g.ez) * XeXe;
-                const unsigned long long inc = in_grid ? ((1ull << 32) | 1ull) : (1ull << 32);
-                hit_old = atomicAdd(&sd.cnt[cell], inc);
+                hit_old = atomicAdd(&sd.cnt[cell], 1ull);  // the point's rank in its cell
+                if (in_grid) atomicAdd(&sd.idx[bx + g.X * by + XX * bz], -1);  // a hit counts toward the total
                 rec = make_float4(fr0, fr1, fr2, __int_as_float(cell));
                 n_hit = in_grid;
             }
@@ -253,7 +263,7 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
             const float iy = k == 1 ? __fdiv_rn(sk, ak) : __fdiv_rn(s1, ak);
             const float iz = k == 2 ? __fdiv_rn(sk, ak) : __fdiv_rn(s2, ak);
             const int K = ray_step_count(rl, sk, pc.step_cap);
-            unsigned long long *__restrict__ cnt = sd.cnt;
+            int *__restrict__ vmap = sd.idx;  // the slot's index map, counting down from -1
             int st = 0;
             if (ffloor) {
                 // float32 voxel indices: floor(p) from the bits of p + 1.5 * 2^23 rounded
@@ -295,18 +305,18 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
                     }
                     if ((unsigned)vx >= (unsigned)g.X || (unsigned)vy >= (unsigned)g.X || (unsigned)vz >= (unsigned)g.Z)
                         break;
-                    const unsigned cell = (unsigned)((vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe);
+                    const unsigned vid = (unsigned)(vx + g.X * vy + XX * vz);
                     if (kHash) {
-                        const unsigned h = (cell * 2654435761u) >> (32 - kHashBits);
+                        const unsigned h = (vid * 2654435761u) >> (32 - kHashBits);
                         unsigned tag = htag[h];
                         if (tag == kHashEmpty) {
-                            tag = atomicCAS(&htag[h], kHashEmpty, cell);
-                            if (tag == kHashEmpty) tag = cell;
+                            tag = atomicCAS(&htag[h], kHashEmpty, vid);
+                            if (tag == kHashEmpty) tag = vid;
                         }
-                        if (tag == cell) atomicAdd(&hcnt[h], 1u);
-                        else atomicAdd(&cnt[cell], 1ull);
+                        if (tag == vid) atomicAdd(&hcnt[h], 1u);
+                        else atomicAdd(&vmap[vid], -1);
                     } else {
-                        atomicAdd(&cnt[cell], 1ull);
+                        atomicAdd(&vmap[vid], -1);
                     }
                 }
             } else {
@@ -320,13 +330,13 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
                     const int vz = ray_index(pz, sd.oi[2], sd.od[2], 0);
                     if ((unsigned)vx >= (unsigned)g.X || (unsigned)vy >= (unsigned)g.X || (unsigned)vz >= (unsigned)g.Z)
                         break;
-                    atomicAdd(&cnt[(vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe], 1ull);
+                    atomicAdd(&vmap[vx + g.X * vy + XX * vz], -1);
                 }
             }
             n_steps = st;
         }
         prec[gi] = rec;
-        prank[gi] = (int)(hit_old >> 32);
+        prank[gi] = (int)(unsigned)(hit_old & 0xffffffffull);
     }
     // scan counters: one atomic per block and counter (valid, hits, steps are
     // adjacent words)
@@ -349,7 +359,7 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
     if (kHash)
         for (int k = threadIdx.x; k < (1 << kHashBits); k += blockDim.x) {
             const unsigned t = htag[k];
-            if (t != kHashEmpty) atomicAdd(&sd.cnt[t], (unsigned long long)hcnt[k]);
+            if (t != kHashEmpty) atomicAdd(&sd.idx[t], -(int)hcnt[k]);
         }
     if (!sd.cube_on) return;
     for (int k = threadIdx.x; k < kCubeCells; k += blockDim.x) {
@@ -357,18 +367,18 @@ __global__ void __launch_bounds__(256) k_voxelize_trace(const ProcessConst pc, c
         if (c) {
             const int vx = sd.cube0[0] + (k % kCube), vy = sd.cube0[1] + ((k / kCube) % kCube),
                       vz = sd.cube0[2] + k / (kCube * kCube);
-            atomicAdd(&sd.cnt[(vx + g.exy) + (vy + g.exy) * Xe + (vz + g.ez) * XeXe], (unsigned long long)c);
+            atomicAdd(&sd.idx[vx + g.X * vy + XX * vz], -(int)c);
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// block-wide exclusive scan of two counters (256 threads); returns this
+// block-wide exclusive scan of two counters (up to 8 warps); returns this
 // thread's exclusive prefixes and the block totals
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void block_scan2(int a, int b, int &ea, int &eb, int &ta, int &tb) {
     __shared__ int wa[8], wb[8];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
     int ia = a, ib = b;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -386,6 +396,7 @@ __device__ __forceinline__ void block_scan2(int a, int b, int &ea, int &eb, int 
     int pa = 0, pb = 0, sa = 0, sb = 0;
 #pragma unroll
     for (int k = 0; k < 8; k++) {
+        if (k >= nw) break;
         if (k < w) {
             pa += wa[k];
             pb += wb[k];
@@ -400,18 +411,19 @@ __device__ __forceinline__ void block_scan2(int a, int b, int &ea, int &eb, int 
 }
 
 // ---------------------------------------------------------------------------
-// k_assign: one pass over the dense count words; a block covers 256 * PER
-// consecutive extended cells, thread i the cells i, i + 256,
-// ... (every load and store of a warp is contiguous), blockIdx.y = scan.
-// In-grid cells: hit > 0 -> compact index and the record's hit/total/voxel
-// id; else -(total)-1 (scripts/gvom.py:1233-1247).  Cells holding points
-// (occupied or halo) get a point-group offset; their count word becomes
-// (offset << 32 | points) for k_scatter / k_voxel_stats.  Free cells are
-// cleared here, point cells by k_cleanup.  One counter atomic per block.
-// The count arrays are padded to whole blocks of cells (zero cells).
+// k_assign: one thread per point; the thread of each cell's first point
+// (rank 0) owns the cell.  An owned in-grid cell is an occupied voxel
+// (hit > 0, scripts/gvom.py:1233-1240): it takes a compact index, and its
+// record gets hit = the cell's point count, total = -(word)-1 of the index
+// map (the ray steps and hits counted there), and the voxel id
+// (scripts/gvom.py:1242-1247); the index map word becomes the compact
+// index.  Every owned cell (occupied or halo) gets its point-group offset:
+// its cell word becomes (offset << 32 | points) for k_scatter /
+// k_voxel_stats.  Compact indices and offsets are reserved with one 64-bit
+// atomic per block.
 // ---------------------------------------------------------------------------
 
-// (x, y, z) of extended cell e: e = x + Xe (y + Xe z), divisions by Xe as a
+// grid voxel of extended cell e = x + Xe (y + Xe z), divisions by Xe as a
 // multiply-high by xe_magic = floor((2^64 - 1) / Xe) + 1, exact for e < 2^32
 // (xe_magic wraps to 0 for Xe = 1, where the quotient is e itself)
 __device__ __forceinline__ bool cell_in_grid(unsigned e, const Geom &g, unsigned long long magic, int &gid) {
@@ -423,27 +435,24 @@ __device__ __forceinline__ bool cell_in_grid(unsigned e, const Geom &g, unsigned
     return (unsigned)gx < (unsigned)g.X && (unsigned)gy < (unsigned)g.X && (unsigned)gz < (unsigned)g.Z;
 }
 
-template <int NS, int PER>
-__global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab) {
-    const ScanDesc &sd = tab.s[blockIdx.y];
-    const Geom g = pc.g;
-    const int Vext = (int)g.Vext;
-    const int base = blockIdx.x * (256 * PER) + threadIdx.x;
-    unsigned long long v[PER];
-#pragma unroll
-    for (int k = 0; k < PER; k++) v[k] = sd.cnt[base + k * 256];  // padded: always in bounds
-    int n_occ = 0, n_pts = 0;
-#pragma unroll
-    for (int k = 0; k < PER; k++) {
-        const int hit = (int)(v[k] >> 32);
-        if (hit > 0) {
-            int gid;
-            n_pts += hit;
-            if (cell_in_grid((unsigned)(base + k * 256), g, pc.xe_magic, gid)) n_occ++;
+template <int NS>
+__global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
+                                               const float4 *__restrict__ prec, const int *__restrict__ prank) {
+    const int s = find_scan(tab, pc.nscans, blockIdx.x);
+    const ScanDesc &sd = tab.s[s];
+    const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
+    int cell = -1, gid = 0, occ = 0, npts = 0;
+    if (i < sd.n) {
+        const long long gi = sd.pt_base + i;
+        const int c = __float_as_int(prec[gi].w);
+        if (c >= 0 && prank[gi] == 0) {
+            cell = c;
+            npts = (int)(unsigned)(sd.cnt[c] & 0xffffffffull);
+            occ = cell_in_grid((unsigned)c, pc.g, pc.xe_magic, gid) ? 1 : 0;
         }
     }
     int eo, ep, to, tp;
-    block_scan2(n_occ, n_pts, eo, ep, to, tp);
+    block_scan2(occ, npts, eo, ep, to, tp);
     __shared__ int bases[2];
     if (threadIdx.x == 0) {
         // C and pts are adjacent 32-bit words: one 64-bit atomic reserves both
@@ -456,54 +465,20 @@ __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __g
         bases[1] = (int)(unsigned)(old >> 32);
     }
     __syncthreads();
-    int c = bases[0] + eo, off = bases[1] + ep;
-    // the words' extended coordinates: one division for the first, then
-    // steps of 256 cells with carries (pc.adv = coordinates of 256)
-    int ex, ey, ez;
-    {
-        const unsigned row = pc.xe_magic ? (unsigned)__umul64hi((unsigned long long)base, pc.xe_magic) : (unsigned)base;
-        const unsigned zz = pc.xe_magic ? (unsigned)__umul64hi((unsigned long long)row, pc.xe_magic) : row;
-        ex = (int)((unsigned)base - row * (unsigned)g.Xe);
-        ey = (int)(row - zz * (unsigned)g.Xe);
-        ez = (int)zz;
-    }
-#pragma unroll
-    for (int k = 0; k < PER; k++) {
-        const int e = base + k * 256;
-        if (e >= Vext) break;
-        const int hit = (int)(v[k] >> 32);
-        const int total = (int)(v[k] & 0xffffffffull);
-        const int gx = ex - g.exy, gy = ey - g.exy, gz = ez - g.ez;
-        const int gid = gx + g.X * (gy + g.X * gz);
-        ex += pc.adv[0];
-        const int cx = ex >= g.Xe;
-        ex -= cx ? g.Xe : 0;
-        ey += pc.adv[1] + cx;
-        const int cy = ey >= g.Xe;
-        ey -= cy ? g.Xe : 0;
-        ez += pc.adv[2] + cy;
-        if ((unsigned)gx < (unsigned)g.X && (unsigned)gy < (unsigned)g.X && (unsigned)gz < (unsigned)g.Z) {
-            if (hit > 0) {
-                if (c < sd.rec_cap) {
-                    VoxelRec *r = &sd.rec[c];
-                    r->hit = hit;
-                    r->total = total;
-                    r->aux[0] = __int_as_float(gid);
-                } else {
-                    atomicOr(&sd.ctr->overflow, 1);
-                }
-                sd.idx[gid] = c;
-                c++;
-            } else {
-                sd.idx[gid] = -total - 1;
-                if (total) sd.cnt[e] = 0ull;
-            }
+    if (cell < 0) return;
+    if (occ) {
+        const int c = bases[0] + eo;
+        const int total = -1 - sd.idx[gid];
+        if (c < sd.rec_cap) {
+            VoxelRec *r = &sd.rec[c];
+            *reinterpret_cast<int2 *>(&r->hit) = make_int2(npts, total);
+            r->aux[0] = __int_as_float(gid);
+        } else {
+            atomicOr(&sd.ctr->overflow, 1);
         }
-        if (hit > 0) {
-            sd.cnt[e] = ((unsigned long long)(unsigned)off << 32) | (unsigned)hit;
-            off += hit;
-        }
+        sd.idx[gid] = c;
     }
+    sd.cnt[cell] = ((unsigned long long)(unsigned)(bases[1] + ep) << 32) | (unsigned)npts;
 }
 
 // ---------------------------------------------------------------------------
@@ -833,7 +808,7 @@ __global__ void __launch_bounds__(256) k_cleanup(const ProcessConst pc, const __
 template <int NS>
 static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int total_blocks, int max_n, int dtype,
                              float4 *prec, int *prank, float4 *sorted, CellMom *mom, cudaStream_t st, cudaEvent_t *ev,
-                             int bs, cudaEvent_t after_assign, int part) {
+                             int bs, cudaEvent_t after_assign, int part, bool assign_external) {
     ScanTable<NS> tab;
     for (int i = 0; i < NS; i++) tab.s[i] = i < pc.nscans ? table[i] : table[0];
     if (total_blocks < 1) total_blocks = 1;
@@ -849,13 +824,10 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
         mark(1);
         if (part == 1) return cudaGetLastError();
     }
-    {
-        const int per = pc.assign_per;
-        dim3 ga((unsigned)((pc.g.Vext + 256 * per - 1) / (256 * per)), pc.nscans);
-        if (per == 4) k_assign<NS, 4><<<ga, 256, 0, st>>>(pc, tab);
-        else if (per == 16) k_assign<NS, 16><<<ga, 256, 0, st>>>(pc, tab);
-        else k_assign<NS, 8><<<ga, 256, 0, st>>>(pc, tab);
-        if (after_assign) cudaEventRecord(after_assign, st);
+    k_assign<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
+    if (after_assign) {
+        if (assign_external) cudaEventRecordWithFlags(after_assign, st, cudaEventRecordExternal);
+        else cudaEventRecord(after_assign, st);
     }
     mark(2);
     k_scatter<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank, sorted);
@@ -875,17 +847,17 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
 
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part) {
+                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part, bool assign_external) {
     CellMom *mom = static_cast<CellMom *>(moments);
     if (part) ev = nullptr;
     if (nscans == 1)
         return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                            after_assign, part);
+                            after_assign, part, assign_external);
     if (nscans <= 4)
         return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                            after_assign, part);
+                            after_assign, part, assign_external);
     return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                                after_assign, part);
+                                after_assign, part, assign_external);
 }
 
 }  // namespace gvom

@@ -377,6 +377,12 @@ class Gvom:
         check(self._l.gvom_device_bytes(self._h, C.byref(b)))
         return b.value
 
+    def reserve(self, max_scans: int, max_points: int, max_row_bytes: int = 12):
+        """Allocate now what calls of up to `max_scans` scans and `max_points`
+        points in all would allocate on first use (gvom_reserve), so that a
+        request loop's latency never includes an allocation."""
+        check(self._l.gvom_reserve(self._h, int(max_scans), int(max_points), int(max_row_bytes)))
+
     # ------------------------------------------------------------------
     # state access (parity checks)
     # ------------------------------------------------------------------

@@ -220,10 +220,9 @@ int gvom_synchronize(GvomHandle *h);
  * counts since timing was (re-)enabled.  Stage names: gvom_stage_name. */
 /* Launch shapes chosen by the autotuner (gvom_gb300/autotune.py); no
  * counterpart in the reference.  They change speed only, never results.
- * Defaults: 256, 8, 8, 4, 1, 256, 2. */
+ * Defaults: 256, 8, 4, 1, 256, 2. */
 typedef struct GvomTuning {
     int32_t points_per_block;         /* point-parallel kernels: 128 or 256 */
-    int32_t assign_words_per_thread;  /* index assignment: 4, 8 or 16 */
     int32_t merge_planes_per_thread;  /* index merge: 4, 8 or 16 z planes */
     int32_t stats_blocks_per_sm;      /* statistics merge: 2, 4 or 8 */
     int32_t step_overlap;             /* gvom_step: index merge beside the statistics kernels, 0 or 1 */
@@ -252,6 +251,16 @@ int gvom_last_process_stats(GvomHandle *h, int64_t *valid_points, int64_t *hits,
 
 /* Bytes of device memory held by the handle. */
 int gvom_device_bytes(GvomHandle *h, int64_t *bytes);
+
+/* Allocates now what later process / step calls of up to `max_scans` scans
+ * (<= 16) and `max_points` points in all would otherwise allocate on first
+ * use: both sets of per-scan scratch, the staging buffer for host points of
+ * up to `max_row_bytes` bytes per point, record capacity for `max_points`
+ * voxels in every ring slot, and the step pipeline's spare slots.  No
+ * counterpart in the reference; for request loops whose latency must not
+ * include an allocation (cudaFree waits for the whole device).  Waits for the
+ * instance's queued work; GVOM_ERR_OOM when device memory is short. */
+int gvom_reserve(GvomHandle *h, int32_t max_scans, int64_t max_points, int64_t max_row_bytes);
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *gvom_last_error(void);

@@ -118,3 +118,4 @@ STUB(gvom_set_stage_timing, GvomHandle *h, int32_t on)
 STUB(gvom_stage_times, GvomHandle *h, double *a, int64_t *b, int32_t n)
 STUB(gvom_last_process_stats, GvomHandle *h, int64_t *a, int64_t *b, int64_t *c)
 STUB(gvom_device_bytes, GvomHandle *h, int64_t *b)
+STUB(gvom_reserve, GvomHandle *h, int32_t s, int64_t p, int64_t b)

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ by running the REFERENCE mapper.
 
 Runs the reference's own scripts/gvom.py, unchanged, from the reference
-checkout (default /root/reference, or $GVOM_REFERENCE) on the host through
+checkout named by $GVOM_REFERENCE (required) on the host through
 the sequential numba stand-in in oracle/numba_shim, for a set of small scenes,
 and writes each scene's inputs and the reference's outputs and internal state
 (in canonical voxel order) to tests/golden/<scene>.npz.
@@ -31,7 +31,9 @@ from numba import cuda as shim_cuda  # noqa: E402
 
 from oracle.canonical import canonical_map  # noqa: E402
 
-REF = os.environ.get("GVOM_REFERENCE", "/root/reference")
+REF = os.environ.get("GVOM_REFERENCE")
+if not REF:
+    raise SystemExit("set GVOM_REFERENCE to the reference checkout (the directory holding scripts/gvom.py)")
 
 
 def load_reference():

@@ -3,8 +3,8 @@ map-publishing callback, unchanged.
 
 `VoxelMapper.cb_timer` of the reference's scripts/gvom_ros.py (:113-166) turns
 combine_maps' outputs into five int8 OccupancyGrid payloads with numpy.  This
-script loads that file from the reference checkout (default /root/reference,
-or $GVOM_REFERENCE) with stand-in modules for rospy, the ROS message types,
+script loads that file from the reference checkout named by $GVOM_REFERENCE
+(required) with stand-in modules for rospy, the ROS message types,
 tf and ros_numpy (none is installed, and the callback uses them only to
 build and publish messages), feeds it maps, and records the `data` of every
 published message.  The maps are the combine outputs stored in the other
@@ -27,7 +27,9 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("GVOM_REFERENCE", "/root/reference")
+REF = os.environ.get("GVOM_REFERENCE")
+if not REF:
+    raise SystemExit("set GVOM_REFERENCE to the reference checkout (the directory holding scripts/gvom.py)")
 
 
 def _stub_modules():

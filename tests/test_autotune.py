@@ -12,7 +12,7 @@ from gvom_gb300 import autotune as AT
 class FakeMapper:
     """Stage times depend on the tuning: each knob has one best value."""
 
-    BEST = {"points_per_block": 128, "assign_words_per_thread": 16, "merge_planes_per_thread": 4,
+    BEST = {"points_per_block": 128, "merge_planes_per_thread": 4,
             "stats_blocks_per_sm": 8, "step_overlap": 0, "maps_tile_cells": 64, "step_pipeline": 0}
 
     def __init__(self, params=(0.15, 0.15, 256, 64, 4, 1, .5, .5, .3, 2, 4, 1, 1, 1)):
@@ -99,9 +99,9 @@ def test_every_launch_shape_gives_identical_maps(gpu_lib):
     scans = make_workload_scans(w, 4)
     params = w.gvom_args()[:4] + (3,) + w.gvom_args()[5:]
     shapes = [dict(AT.DEFAULT),
-              {"points_per_block": 128, "assign_words_per_thread": 4, "merge_planes_per_thread": 16,
+              {"points_per_block": 128, "merge_planes_per_thread": 16,
                "stats_blocks_per_sm": 2, "step_overlap": 0, "maps_tile_cells": 64, "step_pipeline": 0},
-              {"points_per_block": 256, "assign_words_per_thread": 16, "merge_planes_per_thread": 4,
+              {"points_per_block": 256, "merge_planes_per_thread": 4,
                "stats_blocks_per_sm": 8, "step_overlap": 1, "maps_tile_cells": 128, "step_pipeline": 2}]
     results = []
     for t in shapes:

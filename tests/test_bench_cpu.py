@@ -40,7 +40,7 @@ def test_trace_atomic_roofline():
     r = bench.trace_atomic_roofline(hits=95000, steps=6_800_000, ms_per_launch=0.0614)
     assert r["atomics_per_launch"] == 2 * 95000 + 6_800_000
     assert abs(r["achieved_per_s"] - 6_990_000 / 61.4e-6) < 1.0
-    assert abs(r["frac"] - r["achieved_per_s"] / bench.RED64_SCATTERED_PER_S) < 1e-12
+    assert abs(r["frac"] - r["achieved_per_s"] / bench.RED32_SCATTERED_PER_S) < 1e-12
     assert 0.5 < r["frac"] < 0.6
 
 

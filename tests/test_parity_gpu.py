@@ -443,3 +443,60 @@ def test_os1_64_veg_30_scans_combine_each_vs_oracle(Gvom):
         refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
         compare_combine(out, refd, g.maps_state(), params, f"combine after scan {i}")
     compare_slot(canonical_state(g.combined_state()), canonical_state(o.combined_state()), "combined")
+
+
+@pytest.mark.parametrize("form", ["os1_64_veg", "batched_8"])
+def test_pipelined_full_size_steps_equal_one_at_a_time(Gvom, form):
+    """The measured forms at full size, steps submitted back to back from
+    device memory with graphs on and the step pipeline at its deepest level,
+    so that every overlap the pipeline allows happens (the device is held back
+    until all steps are queued): every step's maps equal, and the combined
+    map's statistics and debug voxel rows stay within tolerance of, the same
+    steps run one call at a time with a wait after each (process_batch +
+    combine_maps)."""
+    import torch
+    from gvom_gb300.synthetic import BATCHED, WORKLOADS, make_batched_steps, make_workload_scans
+    from oracle.canonical import sort_debug_voxels
+    from replay import assert_eigen, assert_exact
+    if form in WORKLOADS:
+        w = WORKLOADS[form]
+        steps = [[s] for s in make_workload_scans(w, 12, device="cuda")]
+    else:
+        w = BATCHED[form]
+        steps = make_batched_steps(w, 6, device="cuda")
+    params = w.gvom_args()
+    X = params[2]
+    a, b = Gvom(*params), Gvom(*params)
+    b.set_graphs(True)
+    b.set_tuning(dict(b.get_tuning(), step_pipeline=2))
+    dev = [[torch.from_numpy(np.ascontiguousarray(s.points)).cuda() for s in st] for st in steps]
+    torch.cuda.synchronize()
+    want = []
+    for st in steps:
+        a.process_batch([(s.points, s.ego, s.transform) for s in st])
+        want.append(a.combine_maps())
+    got = []
+    outs_all = [[torch.empty((X, X), dtype=d, device="cuda") for d in (torch.int32, torch.int32, torch.float64,
+                                                                        torch.int32)] for _ in steps]
+    # hold the device back while every step is submitted: the mapper's stream
+    # sleeps first, and the pipeline's streams start after it, so that all
+    # the steps' work is queued before any of it runs
+    hold = torch.cuda.Stream()
+    b.set_stream(hold.cuda_stream)
+    with torch.cuda.stream(hold):
+        torch.cuda._sleep(200_000_000)
+    for k, st in enumerate(steps):
+        origin = b.step([(dev[k][j], s.ego, s.transform) for j, s in enumerate(st)], device_outputs=outs_all[k])
+        got.append((origin, outs_all[k]))
+    b.synchronize()
+    b.set_stream(None)
+    for k, (ra, (origin, outs)) in enumerate(zip(want, got)):
+        rb = (origin, *[t.cpu().numpy() for t in outs])
+        for x, y in zip(ra, rb):
+            np.testing.assert_array_equal(x, y, f"step {k}")
+    compare_slot(canonical_state(a.combined_state()), canonical_state(b.combined_state()), "combined")
+    da, db = sort_debug_voxels(a.make_debug_voxel_map()), sort_debug_voxels(b.make_debug_voxel_map())
+    assert_exact(db[:, :5], da[:, :5], "debug voxel rows")
+    lmax = np.abs(da[:, 5:6] + da[:, 6:7] + da[:, 7:8])
+    assert_eigen(db[:, 5:], da[:, 5:], "debug voxel eigen gaps",
+                 scale=np.maximum(lmax, np.abs(da[:, 5:]).max(axis=1, keepdims=True)))

@@ -3,7 +3,8 @@ gvom_gb300/csrc/k_process.cu: transform, min-distance filter, exact hit
 voxel, float32 march with the fast floor, the sliver, the shared cube and
 hash table and their flush), compiled for the host from the kernel source
 and run thread by thread, against the oracle on every scan of every golden
-fixture: the per-voxel hit and total counts of each slot must be equal.
+fixture: the per-voxel hit counts (the cell words) and totals (the index map
+counted down from -1) of each slot must be equal.
 The scan descriptor is filled the way the library's host code does
 (prepare_scans in gvom_gb300/csrc/gvom_capi.cu)."""
 import ctypes as C
@@ -65,6 +66,7 @@ static void trace_block(const ProcessConst &pc, const ScanDesc &sd, long long fi
     const Geom g = pc.g;
     const int ffloor = sd.fast_floor;
     const int Xe = g.Xe, XeXe = g.Xe * g.Xe;
+    const int XX = g.X * g.X;
     for (int t = 0; t < 256; t++) {
         const long long i = first + t;
         const bool active = i < sd.n;
@@ -140,9 +142,12 @@ extern "C" int trace_scan(const void *pts, int dtype, long long n, long long str
         d.cube0[a] = c;
     }
     unsigned long long *cnt = new unsigned long long[g.Vext]();
+    int *vmap = new int[g.V];
+    for (long long v = 0; v < g.V; v++) vmap[v] = -1;  // the slot's index map before the scan
     float4 *prec = new float4[n > 0 ? n : 1];
     int *prank = new int[n > 0 ? n : 1];
     d.cnt = cnt;
+    d.idx = vmap;
     for (long long b = 0; b < n; b += 256) {
         if (dtype == 0) trace_block<float>(pc, d, b, prec, prank);
         else trace_block<double>(pc, d, b, prec, prank);
@@ -152,8 +157,8 @@ extern "C" int trace_scan(const void *pts, int dtype, long long n, long long str
             for (int x = 0; x < X; x++) {
                 const unsigned long long w = cnt[(x + exy) + (long long)(y + exy) * g.Xe + (long long)(z + ez) * g.Xe * g.Xe];
                 const long long v = x + (long long)y * X + (long long)z * X * X;
-                hit[v] = (int)(w >> 32);
-                total[v] = (int)(w & 0xffffffffu);
+                hit[v] = (int)(w & 0xffffffffu);
+                total[v] = -1 - vmap[v];
             }
     // lowest in-voxel height fraction per voxel from the points' records (cell, fractions)
     if (minh) {
@@ -168,7 +173,7 @@ extern "C" int trace_scan(const void *pts, int dtype, long long n, long long str
             minh[v] = std::min(minh[v], prec[i].z);
         }
     }
-    delete[] cnt; delete[] prec; delete[] prank;
+    delete[] cnt; delete[] vmap; delete[] prec; delete[] prank;
     return 0;
 }
 """
