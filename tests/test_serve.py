@@ -35,7 +35,7 @@ def test_served_mix_equals_alone(gpu_lib):
     from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
 
     wa = WORKLOADS["small_32x512"]
-    pa = wa.gvom_args()[:4] + (8,) + wa.gvom_args()[5:]
+    pa = wa.gvom_args()[:4] + (16,) + wa.gvom_args()[5:]  # a 16-slot ring: merges of up to 17 sources
     pb = (0.2, 0.2, 96, 24, 4, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
     scans = make_workload_scans(wa, 12)
     srv = MapServer([pa, pb], point_budget=60000)
@@ -107,15 +107,36 @@ class _FakeMapper:
         self.combines += 1
         return ("map", self.params[4], self.combines)
 
+    def step(self, scans, device_outputs=None):
+        self._process("one" if len(scans) == 1 else "batch", scans)
+        return self.combine_maps()
+
+    def reserve(self, max_scans, max_points, max_row_bytes=12):
+        _FakeMapper.reserved[self.params[4]] = (max_scans, max_points)
+
     def close(self):
         pass
+
+
+class _FakeOutputSet:
+    """Stands in for serve.OutputSet on the CPU: the step runs when submitted."""
+
+    def __init__(self, X):
+        self.out = None
+
+    def submit(self, mapper, scans, stream):
+        self.out = mapper.step(scans)
+
+    def result(self):
+        return self.out
 
 
 def test_request_loop_batches_and_answers(monkeypatch):
     """Continuous batching on CPU with a stand-in mapper: while an instance's
     first scan is on the (fake) device, later requests queue and go out as one
     batch, within the ring-slot and point limits; every request is answered
-    with the map of its own batch; a failing batch answers with its error."""
+    with the map of its own batch; a failing batch (a scan the mapper rejects)
+    answers with its error and the loop goes on."""
     import threading
     import types
 
@@ -123,12 +144,14 @@ def test_request_loop_batches_and_answers(monkeypatch):
 
     from gvom_gb300 import serve
     monkeypatch.setattr(serve, "Gvom", _FakeMapper)
+    monkeypatch.setattr(serve, "OutputSet", _FakeOutputSet)
     fake_cuda = types.SimpleNamespace(Stream=lambda: types.SimpleNamespace(cuda_stream=0),
                                       mem_get_info=lambda: (8 << 30, 16 << 30), set_stream=lambda s: None)
     monkeypatch.setattr(torch, "cuda", fake_cuda)
     _FakeMapper.gate = threading.Event()
     _FakeMapper.entered = {4: threading.Event(), 2: threading.Event()}
     _FakeMapper.calls = []
+    _FakeMapper.reserved = {}
     p4 = (0.2, 0.2, 32, 16, 4, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
     p2 = p4[:4] + (2,) + p4[5:]
     srv = serve.MapServer([p4, p2], point_budget=1000)
@@ -156,4 +179,77 @@ def test_request_loop_batches_and_answers(monkeypatch):
     assert isinstance(after.result, tuple) and after.result[1] == 2
     seqs = sorted(s for _, b in srv.batches for s in b)
     assert seqs == list(range(12))
+    assert _FakeMapper.reserved == {4: (4, 4 * 262144), 2: (2, 2 * 262144)}  # scratch reserved at start-up
     assert all(r.latency >= 0 for r in [first] + queued + other)
+
+
+def test_submitter_runs_ahead_of_completion(monkeypatch):
+    """The submitter does not wait for a batch's maps: with two output sets a
+    second batch is submitted while the first is still on the (fake) device,
+    and a third waits only for a free output set."""
+    import threading
+    import types
+
+    import torch
+
+    from gvom_gb300 import serve
+
+    release = threading.Event()
+    submitted = []
+
+    class HeldOutputSet(_FakeOutputSet):
+        def submit(self, mapper, scans, stream):
+            submitted.append(len(scans))
+            super().submit(mapper, scans, stream)
+
+        def result(self):
+            assert release.wait(10)
+            return super().result()
+
+    monkeypatch.setattr(serve, "Gvom", _FakeMapper)
+    monkeypatch.setattr(serve, "OutputSet", HeldOutputSet)
+    fake_cuda = types.SimpleNamespace(Stream=lambda: types.SimpleNamespace(cuda_stream=0),
+                                      mem_get_info=lambda: (8 << 30, 16 << 30), set_stream=lambda s: None)
+    monkeypatch.setattr(torch, "cuda", fake_cuda)
+    _FakeMapper.gate = None
+    _FakeMapper.calls = []
+    _FakeMapper.reserved = {}
+    p = (0.2, 0.2, 32, 16, 1, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)  # one slot: one scan per batch
+    srv = serve.MapServer([p], point_budget=1000, reserve_points=0)
+    pts = np.zeros((10, 3), np.float32)
+    reqs = [srv.submit(0, pts, (0, 0, 0)) for _ in range(3)]
+    import time
+    deadline = time.time() + 10
+    while len(submitted) < 2 and time.time() < deadline:
+        time.sleep(0.01)
+    time.sleep(0.1)
+    assert submitted == [1, 1]          # two batches in flight, none answered yet
+    assert not any(r.done.is_set() for r in reqs)
+    release.set()
+    for r in reqs:
+        assert r.done.wait(10)
+    srv.close()
+    assert submitted == [1, 1, 1]
+    assert [r.result[2] for r in reqs] == [1, 2, 3]
+    assert _FakeMapper.reserved == {}  # reserve_points=0: nothing reserved
+
+
+@pytest.mark.gpu
+def test_instance_refused_when_device_memory_is_short(gpu_lib):
+    """gvom_create's admission check: an instance whose resident footprint
+    exceeds the free device memory is refused with GVOM_ERR_OOM before any
+    allocation (2.0e9 voxels need about 300 GB), and the server's constructor
+    raises it; a fitting instance is still admitted afterwards."""
+    import ctypes as C
+
+    from gvom_gb300 import Gvom
+    from gvom_gb300._lib import GVOM_ERR_OOM, GvomError, GvomParams
+    big = (0.2, 0.2, 8192, 29, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    h = C.c_void_p()
+    rc = gpu_lib.gvom_create(C.byref(GvomParams(*big)), C.byref(h))
+    assert rc == GVOM_ERR_OOM, rc
+    assert b"admission refused" in gpu_lib.gvom_last_error()
+    with pytest.raises(GvomError):
+        Gvom(*big)
+    g = Gvom(0.2, 0.2, 64, 16, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    assert g.device_bytes() > 0
