@@ -469,42 +469,70 @@ __device__ __forceinline__ bool axis_mean_exact(int c, double res, int n) {
 }
 
 // __calculate_slope (scripts/gvom.py:717-805) in the reference's float64
-// operation order up to the final log / atan2.
+// operation order up to the final log / atan2.  The reference forms every
+// point's x * res, y * res and their offsets from the means point by point;
+// the neighbourhood has at most three distinct x and three distinct y, so
+// those values (and x * x, y * y, a0 * x, a1 * y of the offsets) are formed
+// once per column / row with the same rounded operations and reused -- the
+// same bits in fewer float64 instructions, all in registers.  Sums run over
+// the known neighbours in the reference's order (x major, y minor).
 template <int kSY>
-__device__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY], int x0t, int y0t, int x0, int y0,
-                          int X, double res, double &rough, double &slx, double &sly) {
-#define H(gx, gy) sh[(gx) - x0t + kHalo][(gy) - y0t + kHalo]
-#define K(gx, gy) kn[(gx) - x0t + kHalo][(gy) - y0t + kHalo]
+__device__ __forceinline__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY], int x0t, int y0t,
+                                          int x0, int y0, int X, double res, double &rough, double &slx, double &sly) {
     const int xl = max(0, x0 - 1), xh = min(X, x0 + 2), yl = max(0, y0 - 1), yh = min(X, y0 + 2);
-    double px[9], py[9], pz[9];
-    int i = 0;
-    double mx = 0.0, my = 0.0, mz = 0.0;
-    for (int xx = xl; xx < xh; xx++)
-        for (int yy = yl; yy < yh; yy++)
-            if (K(xx, yy)) {
-                px[i] = __dmul_rn((double)xx, res);
-                py[i] = __dmul_rn((double)yy, res);
-                pz[i] = H(xx, yy);
-                mx = __dadd_rn(mx, px[i]);
-                my = __dadd_rn(my, py[i]);
-                mz = __dadd_rn(mz, pz[i]);
-                i++;
-            }
-#undef H
-#undef K
-    const int n_good = i;
-    mx = __ddiv_rn(mx, (double)i);
-    my = __ddiv_rn(my, (double)i);
-    mz = __ddiv_rn(mz, (double)i);
-    double sxx = 0.0, sxy = 0.0, sxz = 0.0, syy = 0.0, syz = 0.0;
-    for (int j = 0; j < n_good; j++) {
-        const double dx = __dsub_rn(px[j], mx), dy = __dsub_rn(py[j], my), dz = __dsub_rn(pz[j], mz);
-        sxx = __dadd_rn(sxx, __dmul_rn(dx, dx));
-        sxy = __dadd_rn(sxy, __dmul_rn(dx, dy));
-        sxz = __dadd_rn(sxz, __dmul_rn(dx, dz));
-        syy = __dadd_rn(syy, __dmul_rn(dy, dy));
-        syz = __dadd_rn(syz, __dmul_rn(dy, dz));
+    bool k[3][3];
+    double hz[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            k[a][b] = xl + a < xh && yl + b < yh && kn[xl + a - x0t + kHalo][yl + b - y0t + kHalo];
+            hz[a][b] = k[a][b] ? sh[xl + a - x0t + kHalo][yl + b - y0t + kHalo] : 0.0;
+        }
+    double px[3], py[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        px[a] = __dmul_rn((double)(xl + a), res);
+        py[a] = __dmul_rn((double)(yl + a), res);
     }
+    double mx = 0.0, my = 0.0, mz = 0.0;
+    int n = 0;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+            if (k[a][b]) {
+                mx = __dadd_rn(mx, px[a]);
+                my = __dadd_rn(my, py[b]);
+                mz = __dadd_rn(mz, hz[a][b]);
+                n++;
+            }
+    const double dn = (double)n;
+    mx = __ddiv_rn(mx, dn);
+    my = __ddiv_rn(my, dn);
+    mz = __ddiv_rn(mz, dn);
+    double dx[3], dy[3], dxx[3], dyy[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        dx[a] = __dsub_rn(px[a], mx);
+        dy[a] = __dsub_rn(py[a], my);
+        dxx[a] = __dmul_rn(dx[a], dx[a]);
+        dyy[a] = __dmul_rn(dy[a], dy[a]);
+    }
+    double sxx = 0.0, sxy = 0.0, sxz = 0.0, syy = 0.0, syz = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+            if (k[a][b]) {
+                const double dz = __dsub_rn(hz[a][b], mz);
+                hz[a][b] = dz;  // kept for the residuals
+                sxx = __dadd_rn(sxx, dxx[a]);
+                sxy = __dadd_rn(sxy, __dmul_rn(dx[a], dy[b]));
+                sxz = __dadd_rn(sxz, __dmul_rn(dx[a], dz));
+                syy = __dadd_rn(syy, dyy[b]);
+                syz = __dadd_rn(syz, __dmul_rn(dy[b], dz));
+            }
     const double det = __dsub_rn(__dmul_rn(sxx, syy), __dmul_rn(sxy, sxy));
     if (det == 0.0) return;
     double a0 = __ddiv_rn(__dsub_rn(__dmul_rn(syy, sxz), __dmul_rn(sxy, syz)), det);
@@ -512,23 +540,40 @@ __device__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY
     const double m = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(a0, a0), __dmul_rn(a1, a1)), 1.0));
     a0 = __ddiv_rn(a0, m);
     a1 = __ddiv_rn(a1, m);
-    double err = 0.0;
-    for (int j = 0; j < n_good; j++) {
-        const double e = __dsub_rn(__dsub_rn(pz[j], mz),
-                                   __dadd_rn(__dmul_rn(a0, __dsub_rn(px[j], mx)), __dmul_rn(a1, __dsub_rn(py[j], my))));
-        err = __dadd_rn(err, __dmul_rn(e, e));
+    double ax[3], ay[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        ax[a] = __dmul_rn(a0, dx[a]);
+        ay[a] = __dmul_rn(a1, dy[a]);
     }
-    err = __ddiv_rn(err, (double)n_good);
+    double err = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++)
+            if (k[a][b]) {
+                const double e = __dsub_rn(hz[a][b], __dadd_rn(ax[a], ay[b]));
+                err = __dadd_rn(err, __dmul_rn(e, e));
+            }
+    err = __ddiv_rn(err, dn);
     rough = rough_of(err);
     const double im = __ddiv_rn(1.0, m);
     slx = slope_angle(a0, m, im);
     sly = slope_angle(a1, m, im);
 }
 
+// The block has one thread per cell plus one more warp (kTY = 32: one more
+// row of threads; kTY = 16: two) that takes no cell: once the float64 queue
+// is complete it drains it, 32 cells per warp instruction, while the cell
+// threads run their guess search.  A float64 warp instruction holds the slow
+// float64 pipe as long with one lane active as with 32, so the queue goes
+// through in as few warp instructions as it can.  Cell warps that finish
+// their search early take what is left, also 32 cells at a time.
 template <int kTX, int kTY>
-__global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Maps2DParams mp) {
+__global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant__ Maps2DParams mp) {
     constexpr int kSX = kTX + 2 * kHalo, kSY = kTY + 2 * kHalo;
-    static_assert(kSX <= 64 && kSY <= 64 && (kTX * kTY) % 32 == 0, "tile shape");
+    constexpr int kCells = kTX * kTY, kThreads = kCells + 32;
+    static_assert(kSX <= 64 && kSY <= 64 && kCells % 32 == 0 && 32 % kTY == 0, "tile shape");
     __shared__ double sh[kSX][kSY];
     // lowest occupied z and in-voxel height per column for the float32 plane
     // fit; afterwards reused for the results of the float64 queue
@@ -549,7 +594,7 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
         qtake = 0;
     }
 #pragma unroll
-    for (int k = tid; k < kSX * kSY; k += kTX * kTY) {
+    for (int k = tid; k < kSX * kSY; k += kThreads) {
         const int sx = k / kSY, sy = k % kSY;
         const int gx = x0t + sx - kHalo, gy = y0t + sy - kHalo;
         const bool in = gx >= 0 && gx < X && gy >= 0 && gy < X;
@@ -566,7 +611,7 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
     // after it
     {
         const int lane = tid & 31, warp = tid >> 5;
-        for (int r = warp; r < kSX + kSY; r += (kTX * kTY) / 32) {
+        for (int r = warp; r < kSX + kSY; r += kThreads / 32) {
             const bool is_row = r < kSX;  // row sx: along y (kSY entries); else column sy: along x (kSX entries)
             const int len = is_row ? kSY : kSX;
             const int fixed = is_row ? r : r - kSX;
@@ -594,7 +639,8 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
     }
     __syncthreads();
     const int x0 = x0t + threadIdx.y, y0 = y0t + threadIdx.x;
-    const bool valid = x0 < X && y0 < X;
+    const bool cell_thread = tid < kCells;  // the last warp takes no cell
+    const bool valid = cell_thread && x0 < X && y0 < X;
     const int tx = threadIdx.y + kHalo, ty = threadIdx.x + kHalo;  // this cell in tile coords
     const int cell = x0 * X + y0;
     const bool known = kn[tx][ty];
@@ -670,35 +716,48 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
             if (!exact) {
                 const float res = (float)mp.xy_res, zres = (float)mp.z_res;
                 const float cx = (float)sxi / nf, cy = (float)syi / nf;
-                float dxs[9], dys[9], dzs[9];
+                // neighbour (a, b) is cell (x0 - 1 + a, y0 - 1 + b); its x offset
+                // depends on a only and its y offset on b only
+                bool kk[3][3];
+                float dzs[3][3], dxa[3], dyb[3];
                 float zsum = 0.f;
-                int i = 0;
-                for (int xx = xl; xx < xh; xx++)
-                    for (int yy = yl; yy < yh; yy++) {
+#pragma unroll
+                for (int a = 0; a < 3; a++) {
+                    dxa[a] = ((float)(a - 1) - cx) * res;
+                    dyb[a] = ((float)(a - 1) - cy) * res;
+                }
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int b = 0; b < 3; b++) {
+                        const int xx = x0 - 1 + a, yy = y0 - 1 + b;
                         const int sx = xx - x0t + kHalo, sy = yy - y0t + kHalo;
-                        if (kn[sx][sy]) {
-                            dxs[i] = ((float)(xx - x0) - cx) * res;
-                            dys[i] = ((float)(yy - y0) - cy) * res;
+                        kk[a][b] = xx >= xl && xx < xh && yy >= yl && yy < yh && kn[sx][sy];
+                        dzs[a][b] = 0.f;
+                        if (kk[a][b]) {
                             // from voxels: an exact count plus a fraction; with a robot-disc
                             // height: the float64 difference, rounded once
-                            dzs[i] = all_vox ? ((sml[sx][sy] - mr) + (float)(szl[sx][sy] - zr)) * zres
-                                             : (float)__dsub_rn(sh[sx][sy], h0);
-                            zsum += dzs[i];
-                            i++;
+                            dzs[a][b] = all_vox ? ((sml[sx][sy] - mr) + (float)(szl[sx][sy] - zr)) * zres
+                                                : (float)__dsub_rn(sh[sx][sy], h0);
+                            zsum += dzs[a][b];
                         }
                     }
                 const float zm = zsum / nf;
                 float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f;
-                for (int j = 0; j < i; j++) {
-                    const float dz = dzs[j] - zm;
-                    dzs[j] = dz;
-                    sxx += dxs[j] * dxs[j];
-                    sxy += dxs[j] * dys[j];
-                    sxz += dxs[j] * dz;
-                    syy += dys[j] * dys[j];
-                    syz += dys[j] * dz;
-                    szz += dz * dz;
-                }
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int b = 0; b < 3; b++)
+                        if (kk[a][b]) {
+                            const float dz = dzs[a][b] - zm;
+                            dzs[a][b] = dz;
+                            sxx += dxa[a] * dxa[a];
+                            sxy += dxa[a] * dyb[b];
+                            sxz += dxa[a] * dz;
+                            syy += dyb[b] * dyb[b];
+                            syz += dyb[b] * dz;
+                            szz += dz * dz;
+                        }
                 const float det = sxx * syy - sxy * sxy;
                 exact = !(fabsf(det) > 1e-3f * sxx * syy);
                 if (!exact) {
@@ -707,10 +766,14 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
                     m = sqrtf(a0 * a0 + a1 * a1 + 1.0f);
                     a0 /= m;
                     a1 /= m;
-                    for (int j = 0; j < i; j++) {
-                        const float e = dzs[j] - (a0 * dxs[j] + a1 * dys[j]);
-                        err += e * e;
-                    }
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+#pragma unroll
+                        for (int b = 0; b < 3; b++)
+                            if (kk[a][b]) {
+                                const float e = dzs[a][b] - (a0 * dxa[a] + a1 * dyb[b]);
+                                err += e * e;
+                            }
                     err /= nf;
                 }
             }
@@ -740,7 +803,29 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
     }
     // cells that need the float64 sequence are compacted into a queue so that
     // whole warps run it, instead of one lane in every warp that has one
-    __syncthreads();  // queue complete; szl / sml no longer read
+    __syncthreads();  // queue complete; szl / sml no longer read (qres reuses their space)
+    // the float64 queue, 32 cells per warp: each warp takes the next 32 queued
+    // cells until none are left (called with the warp converged)
+    auto drain = [&]() {
+        const int nq = qn, lane = tid & 31;
+        while (true) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&qtake, 32);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= nq) break;
+            const int q = base + lane;
+            if (q < nq) {
+                const int t = qcell[q];
+                double r = -1.0, a = 0.0, b = 0.0;
+                slope_f64<kSY>(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, X, mp.xy_res, r, a, b);
+                qres[t][0] = r;
+                qres[t][1] = a;
+                qres[t][2] = b;
+            }
+            __syncwarp();
+        }
+    };
+    if (!cell_thread) drain();  // the extra warp starts at once, beside the guess search
 
     // __guess_height (scripts/gvom.py:592-714), loop-condition and y_nh quirks
     // included; each ring segment is scanned in increasing order, so its first
@@ -803,21 +888,9 @@ __global__ void __launch_bounds__(kTX * kTY) k_maps2d(const __grid_constant__ Ma
         const double dh = __dsub_rn(mx, mn);
         if (dh > 0.0) guess = dh;
     }
-    // the float64 queue, taken item by item by the threads as they finish
-    // their guess search (the queue is the block's longest chain)
-    {
-        const int nq = qn;
-        while (true) {
-            const int q = atomicAdd(&qtake, 1);
-            if (q >= nq) break;
-            const int t = qcell[q];
-            double r = -1.0, a = 0.0, b = 0.0;
-            slope_f64<kSY>(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, X, mp.xy_res, r, a, b);
-            qres[t][0] = r;
-            qres[t][1] = a;
-            qres[t][2] = b;
-        }
-    }
+    // cell warps that finish their search take what the extra warp has not
+    __syncwarp();
+    drain();
     __syncthreads();
     if (!valid) return;
     if (need_exact) {
@@ -996,7 +1069,7 @@ template <int TX, int TY>
 static void launch_maps2d(const Maps2DParams &m2, cudaStream_t st) {
     const int X = m2.X;
     dim3 g2((X + TY - 1) / TY, (X + TX - 1) / TX);
-    k_maps2d<TX, TY><<<g2, dim3(TY, TX), 0, st>>>(m2);
+    k_maps2d<TX, TY><<<g2, dim3(TY, TX + 32 / TY), 0, st>>>(m2);
 }
 template <int NSRC>
 static void launch_merge_idx(const MergeParams &mp, cudaStream_t st) {

@@ -69,7 +69,7 @@ POSTLUDE = r"""
 def _kernel_guess_block():
     src = open(KERNEL).read()
     a = src.index("    // __guess_height (scripts/gvom.py:592-714)")
-    b = src.index("    // the float64 queue", a)
+    b = src.index("    // cell warps that finish their search", a)
     return src[a:b]
 
 

@@ -67,7 +67,7 @@ extern "C" int slope_all(const double *H, int X, double res, double *rough, doub
 
 def _kernel_slope_source():
     src = open(KERNEL).read()
-    a = src.index("template <int kSY>\n__device__ void slope_f64")
+    a = src.index("template <int kSY>\n__device__ __forceinline__ void slope_f64")
     b = src.index("template <int kTX, int kTY>", a)
     return src[a:b]
 
