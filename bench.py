@@ -555,12 +555,14 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
             clocks.start()
         t0 = time.perf_counter()
         pts = 0
+        t_sub = None
         if back_to_back:
             starts[0].record(stream)
             for k in range(n):
                 step_device(args.warmup + k)
                 pts += form.points[(args.warmup + k) % len(form)]
             ends[0].record(stream)
+            t_sub = time.perf_counter() - t0  # host time to submit the n steps
         else:
             for k in range(n):
                 flush.zero_()
@@ -580,11 +582,13 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
         st = g.stage_times() if stage_timing else None
         g.set_stage_timing(False)
         t, p = _reduce_max_sum(torch, dist, sum(ms) / 1e3, pts)
+        timed.host_submit_s = t_sub
         return ms, t, p, wall, clk, st
 
     # the headline: steps back to back, CUDA-graph replay (or direct launches with graphs=False)
     _, t_dev_max, pts_all, wall_timed, clk, _ = timed(n_steps, graphs, False, "" if headline else "_" + form.name,
                                                       back_to_back=True)
+    host_submit_s = timed.host_submit_s
     # mean H, S per step over the timed steps (steps warmup .. warmup + n_steps - 1)
     timed_counts = [counts[i] for i in timed_idx]
     H_mean = float(np.mean([c[1] for c in timed_counts]))
@@ -712,6 +716,9 @@ def measure_form(form, args, torch, dist, lrank, flush, headline, graphs=True):
         "stages": stage_tab,
         "ray_last_scan": ray,
         "wall_s_timed": wall_timed,
+        # host time to submit the timed steps (no wait inside): when it is close to the device time the
+        # host's calls, not the GPU, set the pace
+        "host_submit_ms_per_step": 1e3 * host_submit_s / n_steps if host_submit_s else None,
         "clocks": clk,
     }
 
@@ -800,6 +807,33 @@ def measure_served(args, torch):
                     "request of the window at once and reports the points/sec the loop sustains"}
 
 
+def run_profile(args):
+    """A short run for profilers: `--profile-steps` distinct steps of the
+    workload through gvom_step (device inputs and outputs, direct launches,
+    one stream, so each kernel is launched once per step in a fixed order:
+    k_voxelize_trace, k_assign, k_scatter, k_cell_moments, k_voxel_stats,
+    k_cleanup, k_merge, k_merge_counts, k_merge_stats, k_columns, k_maps2d)."""
+    import torch
+
+    from gvom_gb300 import Gvom
+    from gvom_gb300 import build as gb
+    gb.build()
+    form = Form(args.workload, "cuda", args.profile_steps)
+    g = Gvom(*form.w.gvom_args())
+    g.set_tuning(dict(g.get_tuning(), step_pipeline=0))
+    X = form.w.xy_size
+    outs = [torch.empty((X, X), dtype=d, device="cuda") for d in (torch.int32, torch.int32, torch.float64, torch.int32)]
+    dev = [[torch.from_numpy(s.points).cuda() for s in st] for st in form.steps]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k, st in enumerate(form.steps):
+        g.step([(dev[k][j], s.ego, s.transform) for j, s in enumerate(st)], device_outputs=outs)
+    g.synchronize()
+    print(json.dumps({"profile_run": form.name, "steps": len(form.steps), "wall_s": time.perf_counter() - t0}))
+    g.close()
+    return 0
+
+
 def run_gpu(args):
     import torch
 
@@ -844,7 +878,7 @@ def run_gpu(args):
             "trace_atomic_roofline": res.get("trace_atomic_roofline"), "stages": res["stages"],
             "ray_last_scan": res["ray_last_scan"], "scan_counts_mean": res.get("scan_counts_mean"),
             "direct_launches": res["direct_launches"], "l2_flushed_per_step": res["l2_flushed_per_step"],
-            "wall_s_timed": res["wall_s_timed"], "clocks": res["clocks"], "cpu_baseline": cpu,
+            "wall_s_timed": res["wall_s_timed"], "host_submit_ms_per_step": res.get("host_submit_ms_per_step"), "clocks": res["clocks"], "cpu_baseline": cpu,
             "forms": forms,
         }
         print(json.dumps(line), flush=True)
@@ -867,7 +901,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
                     help="default launch shapes instead of tuning them on the workload first")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="only run this many steps of --workload for a profiler (no JSON bench line)")
     args = ap.parse_args()
+    if args.profile_steps > 0:
+        return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -32,6 +32,7 @@ EXPORTS = (
     "gvom_version", "gvom_set_stage_timing", "gvom_stage_times", "gvom_stage_name",
     "gvom_debug_voxel_map_noalloc", "gvom_set_graphs", "gvom_set_tuning", "gvom_get_tuning", "gvom_step",
     "gvom_ros_grids", "gvom_process_pointcloud2", "gvom_pose_to_transform", "gvom_reserve",
+    "gvom_expand_binary", "gvom_lowpass_binary", "gvom_convolve",
 )
 GVOM_STAGES = 11
 
@@ -118,6 +119,9 @@ def load(path: str | None = None):
         "gvom_last_process_stats": ([P, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "gvom_device_bytes": ([P, C.POINTER(i64)], C.c_int),
         "gvom_reserve": ([P, i32, i64, i64], C.c_int),
+        "gvom_expand_binary": ([P, P, i32, C.c_double, P], C.c_int),
+        "gvom_lowpass_binary": ([P, P, i32, i32, C.c_double, P], C.c_int),
+        "gvom_convolve": ([P, P, P, i32, i32, P], C.c_int),
         "gvom_last_error": ([], C.c_char_p),
         "gvom_set_stage_timing": ([P, i32], C.c_int),
         "gvom_stage_times": ([P, C.POINTER(C.c_double), C.POINTER(i64), i32], C.c_int),

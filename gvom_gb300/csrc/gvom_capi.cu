@@ -1841,6 +1841,30 @@ int gvom_device_bytes(GvomHandle *h, int64_t *bytes) {
     return GVOM_OK;
 }
 
+int gvom_expand_binary(const int32_t *d_in, int32_t *d_out, int32_t xy_size, double r, void *stream) {
+    if (!d_in || !d_out || xy_size <= 0) return fail(GVOM_ERR_ARG, "expand_binary: NULL image or size <= 0");
+    if (!(r < 4096.0)) return fail(GVOM_ERR_ARG, "expand_binary: radius must be below 4096");
+    CUDA_TRY(launch_expand_binary(d_in, d_out, xy_size, r, static_cast<cudaStream_t>(stream)));
+    return GVOM_OK;
+}
+
+int gvom_lowpass_binary(const int32_t *d_in, int32_t *d_out, int32_t xy_size, int32_t filter_size,
+                        double filter_fraction, void *stream) {
+    if (!d_in || !d_out || xy_size <= 0) return fail(GVOM_ERR_ARG, "lowpass_binary: NULL image or size <= 0");
+    if (filter_size < 0 || filter_size > 1023) return fail(GVOM_ERR_ARG, "lowpass_binary: filter_size must be in [0, 1023]");
+    CUDA_TRY(launch_lowpass_binary(d_in, d_out, xy_size, filter_size, filter_fraction,
+                                   static_cast<cudaStream_t>(stream)));
+    return GVOM_OK;
+}
+
+int gvom_convolve(const double *d_in, double *d_out, const double *d_kernel, int32_t xy_size, int32_t kernel_size,
+                  void *stream) {
+    if (!d_in || !d_out || !d_kernel || xy_size <= 0) return fail(GVOM_ERR_ARG, "convolve: NULL buffer or size <= 0");
+    if (kernel_size < 1 || kernel_size > 255) return fail(GVOM_ERR_ARG, "convolve: kernel_size must be in [1, 255]");
+    CUDA_TRY(launch_convolve(d_in, d_out, d_kernel, xy_size, kernel_size, static_cast<cudaStream_t>(stream)));
+    return GVOM_OK;
+}
+
 int gvom_reserve(GvomHandle *h, int32_t max_scans, int64_t max_points, int64_t max_row_bytes) {
     if (!h) return fail(GVOM_ERR_ARG, "handle is NULL");
     DeviceScope ds(h->dev);

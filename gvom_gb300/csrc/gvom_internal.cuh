@@ -229,6 +229,11 @@ cudaError_t launch_debug_maps(const DebugMapParams &p, cudaStream_t st);
 int debug_chunk();
 cudaError_t launch_ros_grids(const RosGridParams &p, cudaStream_t st);
 
+// 2-D image kernels with no caller on the path (k_morph.cu)
+cudaError_t launch_expand_binary(const int32_t *in, int32_t *out, int X, double r, cudaStream_t st);
+cudaError_t launch_lowpass_binary(const int32_t *in, int32_t *out, int X, int fs, double frac, cudaStream_t st);
+cudaError_t launch_convolve(const double *in, double *out, const double *kern, int X, int ks, cudaStream_t st);
+
 // allocation-free debug voxel export (k_debug_static.cu): per-block scratch of
 // kStaticDebugBlocks + 1 words in a fixed device array
 constexpr int kStaticDebugBlocks = 32768;

@@ -176,6 +176,31 @@ int gvom_ros_grids(GvomHandle *h, const GvomRosParams *params, int8_t *hard, int
 int gvom_debug_height_map(GvomHandle *h, float *out);
 int gvom_debug_inferred_height_map(GvomHandle *h, float *out);
 
+/* ---- 2-D image kernels that no reference caller launches -----------------
+ * Images are xy_size x xy_size, [x][y] row major (y fastest, the layout of
+ * the maps), in DEVICE memory; the kernels run on `stream` (a cudaStream_t,
+ * NULL for the default stream) without host synchronisation. */
+
+/* Replaces Gvom.__expand_binary (scripts/gvom.py:807-831): out = 1 where a
+ * cell equal to 1 lies within the disc of radius r (float64 row extents
+ * floor(sqrt(r^2 - i^2)), as the reference), else 0.  r < 4096. */
+int gvom_expand_binary(const int32_t *d_in, int32_t *d_out, int32_t xy_size, double r, void *stream);
+
+/* Replaces Gvom.__lowpass_binary (scripts/gvom.py:833-861): out = 0 where in
+ * is 0, else 1 where the mean over the (2 filter_size + 1)^2 window, clipped
+ * to the image, is >= filter_fraction. */
+int gvom_lowpass_binary(const int32_t *d_in, int32_t *d_out, int32_t xy_size, int32_t filter_size,
+                        double filter_fraction, void *stream);
+
+/* Replaces Gvom.__convolve (scripts/gvom.py:863-885) with its indexing as
+ * written: out[x, y] = sum over the kernel's entries [0, 2r] x [0, 2r], in
+ * row order, of in[x + r, y + r] times the entry, 0 where (x + r, y + r) is
+ * outside; r = (kernel_size - 1) / 2 in integers (the reference's float
+ * radius cannot be passed to range(), so its kernel never runs); the
+ * kernel is kernel_size x kernel_size, row major.  kernel_size <= 255. */
+int gvom_convolve(const double *d_in, double *d_out, const double *d_kernel, int32_t xy_size, int32_t kernel_size,
+                  void *stream);
+
 /* ---- state access for parity checks (host copies) ---------------------- */
 
 /* Ring position: next slot to write and last slot written

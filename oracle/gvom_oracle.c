@@ -1067,3 +1067,71 @@ void gvo_last_process_stats(const gvo_map *m, int64_t *ray_steps, int64_t *hits,
     *hits = m->last_hits;
     *valid_points = m->last_valid_points;
 }
+
+/* ------------------------------------------------------------------------- */
+/* 2-D image kernels that no reference caller launches                        */
+/* ------------------------------------------------------------------------- */
+
+/* __expand_binary (scripts/gvom.py:807-831), thread (x, y) in turn. */
+void gvo_expand_binary(const int32_t *in, int32_t *out, int X, double r) {
+    const long long rint_ = (long long)floor(r);
+    for (int x = 0; x < X; x++)
+        for (int y = 0; y < X; y++) {
+            int v = 0;
+            for (long long i = -rint_; i < rint_ + 1 && !v; i++) {
+                const long long dy = (long long)floor(sqrt(r * r - (double)(i * i)));
+                if (x + i < 0 || x + i >= X) continue;
+                for (long long j = -dy; j < dy + 1; j++) {
+                    if (y + j < 0 || y + j >= X) continue;
+                    if (in[(x + i) * (long long)X + (y + j)] == 1) {
+                        v = 1;
+                        break;
+                    }
+                }
+            }
+            out[(long long)x * X + y] = v;
+        }
+}
+
+/* __lowpass_binary (scripts/gvom.py:833-861). */
+void gvo_lowpass_binary(const int32_t *in, int32_t *out, int X, int filter_size, double filter_fraction) {
+    for (int x = 0; x < X; x++)
+        for (int y = 0; y < X; y++) {
+            if (in[(long long)x * X + y] == 0) {
+                out[(long long)x * X + y] = 0;
+                continue;
+            }
+            double tmp_val = 0.0, tmp_count = 0.0;
+            for (int i = -filter_size; i < filter_size + 1; i++) {
+                if (x + i < 0 || x + i >= X) continue;
+                for (int j = -filter_size; j < filter_size + 1; j++) {
+                    if (y + j < 0 || y + j >= X) continue;
+                    tmp_val += (double)in[(long long)(x + i) * X + (y + j)] * 1.0;
+                    tmp_count += 1.0;
+                }
+            }
+            out[(long long)x * X + y] = (tmp_val / tmp_count) >= filter_fraction ? 1 : 0;
+        }
+}
+
+/* __convolve (scripts/gvom.py:863-885) as written, with the radius an
+ * integer: every term reads input[x + r, y + r] and the in-range tests are
+ * on x + r and y + r.  (The reference's float radius cannot be passed to
+ * range(), so its kernel itself never runs.) */
+void gvo_convolve(const double *in, double *out, const double *kernel, int X, int kernel_size) {
+    const int r = (kernel_size - 1) / 2;
+    for (int x = 0; x < X; x++)
+        for (int y = 0; y < X; y++) {
+            double tmp_val = 0.0;
+            for (int i = -r; i < r + 1; i++) {
+                const int x2 = i + r;
+                if (x + r < 0 || x + r >= X) continue;
+                for (int j = -r; j < r + 1; j++) {
+                    const int y2 = j + r;
+                    if (y + r < 0 || y + r >= X) continue;
+                    tmp_val += in[(long long)(x + r) * X + (y + r)] * kernel[x2 * kernel_size + y2];
+                }
+            }
+            out[(long long)x * X + y] = tmp_val;
+        }
+}

@@ -59,8 +59,36 @@ def _load():
     lib.gvo_get_slot.argtypes = [P, C.c_int] + [P] * 6
     lib.gvo_ring_state.argtypes = [P, P, P]
     lib.gvo_last_process_stats.argtypes = [P, P, P, P]
+    lib.gvo_expand_binary.argtypes = [P, P, C.c_int, C.c_double]
+    lib.gvo_lowpass_binary.argtypes = [P, P, C.c_int, C.c_int, C.c_double]
+    lib.gvo_convolve.argtypes = [P, P, P, C.c_int, C.c_int]
     _lib = lib
     return lib
+
+
+def expand_binary(img, r):
+    """__expand_binary (scripts/gvom.py:807-831) on an (X, X) int32 image."""
+    a = np.ascontiguousarray(img, np.int32)
+    out = np.empty_like(a)
+    _load().gvo_expand_binary(_ptr(a), _ptr(out), a.shape[0], float(r))
+    return out
+
+
+def lowpass_binary(img, filter_size, filter_fraction):
+    """__lowpass_binary (scripts/gvom.py:833-861) on an (X, X) int32 image."""
+    a = np.ascontiguousarray(img, np.int32)
+    out = np.empty_like(a)
+    _load().gvo_lowpass_binary(_ptr(a), _ptr(out), a.shape[0], int(filter_size), float(filter_fraction))
+    return out
+
+
+def convolve(img, kernel):
+    """__convolve (scripts/gvom.py:863-885) as written, integer radius."""
+    a = np.ascontiguousarray(img, np.float64)
+    k = np.ascontiguousarray(kernel, np.float64)
+    out = np.empty_like(a)
+    _load().gvo_convolve(_ptr(a), _ptr(out), _ptr(k), a.shape[0], k.shape[0])
+    return out
 
 
 def _ptr(a):

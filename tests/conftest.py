@@ -27,5 +27,6 @@ GOLDEN = os.path.join(HERE, "golden")
 
 
 def golden_files():
-    """The mapper scene fixtures (ros_*.npz hold the ROS node's payloads instead)."""
-    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("ros_"))
+    """The mapper scene fixtures (ros_*.npz hold the ROS node's payloads and
+    morph_*.npz the 2-D image kernels' outputs instead)."""
+    return sorted(f for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith(("ros_", "morph_")))

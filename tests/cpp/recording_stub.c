@@ -119,3 +119,6 @@ STUB(gvom_stage_times, GvomHandle *h, double *a, int64_t *b, int32_t n)
 STUB(gvom_last_process_stats, GvomHandle *h, int64_t *a, int64_t *b, int64_t *c)
 STUB(gvom_device_bytes, GvomHandle *h, int64_t *b)
 STUB(gvom_reserve, GvomHandle *h, int32_t s, int64_t p, int64_t b)
+STUB(gvom_expand_binary, const int32_t *a, int32_t *b, int32_t n, double r, void *s)
+STUB(gvom_lowpass_binary, const int32_t *a, int32_t *b, int32_t n, int32_t f, double q, void *s)
+STUB(gvom_convolve, const double *a, double *b, const double *k, int32_t n, int32_t ks, void *s)

@@ -340,9 +340,46 @@ def run_reference(mod, params, ops):
     return out
 
 
+# The reference's 2-D image kernels that no caller launches (scripts/gvom.py:807-885), run
+# through the stand-in on seeded binary images: sizes, radii / window sizes and fractions that
+# reach the image edges, radii with and without a fraction, windows larger than the image.
+MORPH_CASES = {
+    "expand": [(37, 0.0), (37, 1.0), (37, 1.5), (64, 2.7), (64, 4.0), (23, 30.0), (40, -1.0)],
+    "lowpass": [(37, 0, 0.5), (37, 1, 0.5), (64, 2, 0.3), (64, 1, 0.75), (23, 15, 0.2), (40, 3, 1.0)],
+}
+
+
+def make_morph(mod):
+    """Outputs of __expand_binary and __lowpass_binary; __convolve cannot run (its radius
+    (kernel_size - 1) / 2 is a float, which range() rejects), so it has no fixture."""
+    out = {}
+    rng = np.random.default_rng(21)
+    kexp = mod.Gvom._Gvom__expand_binary
+    klow = mod.Gvom._Gvom__lowpass_binary
+    tpb = (16, 16)
+    for n, (X, r) in enumerate(MORPH_CASES["expand"]):
+        img = (rng.uniform(size=(X, X)) < (0.02 if r > 2 else 0.15)).astype(np.int32)
+        res = np.full((X, X), -7, np.int32)
+        kexp[((X + 15) // 16, (X + 15) // 16), tpb](img, res, X, float(r))
+        out[f"expand{n}_img"], out[f"expand{n}_r"], out[f"expand{n}_out"] = img, np.float64(r), res
+    for n, (X, fs, frac) in enumerate(MORPH_CASES["lowpass"]):
+        img = (rng.uniform(size=(X, X)) < 0.5).astype(np.int32)
+        res = np.full((X, X), -7, np.int32)
+        klow[((X + 15) // 16, (X + 15) // 16), tpb](img, res, X, int(fs), float(frac))
+        out[f"lowpass{n}_img"], out[f"lowpass{n}_fs"] = img, np.int64(fs)
+        out[f"lowpass{n}_frac"], out[f"lowpass{n}_out"] = np.float64(frac), res
+    return out
+
+
 def main(argv):
-    names = argv or list(SCENES)
+    names = argv or list(SCENES) + ["morph_binary"]
     mod = load_reference()
+    if "morph_binary" in names:
+        t = time.time()
+        path = os.path.join(HERE, "morph_binary.npz")
+        np.savez_compressed(path, **make_morph(mod))
+        print(f"morph_binary: {time.time() - t:.1f} s, {os.path.getsize(path) / 1024:.0f} KiB", flush=True)
+        names = [n for n in names if n != "morph_binary"]
     for name in names:
         t = time.time()
         params, ops = SCENES[name]()
