@@ -16,6 +16,137 @@
 #include "gvom_internal.cuh"
 
 
+namespace gvom {
+
+namespace {
+thread_local Recorder t_rec;
+// tags of the non-kernel nodes: the addresses of three distinct bytes
+const char kTags[3] = {0, 1, 2};
+const void *const kTagMemset = &kTags[0];
+const void *const kTagMemcpy = &kTags[1];
+const void *const kTagEvent = &kTags[2];
+}  // namespace
+
+Recorder &recorder() { return t_rec; }
+
+cudaError_t rec_note(cudaStream_t st, const void *tag) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t nd = 0;
+    const cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
+    GraphNodes &g = *t_rec.g;
+    if (cs != cudaStreamCaptureStatusActive || nd != 1) {
+        t_rec.ok = false;  // the sequence cannot be replayed node by node: it is captured every time
+        return cudaSuccess;
+    }
+    g.nodes.push_back(deps[0]);
+    g.tags.push_back(tag);
+    g.mset.push_back(cudaMemsetParams{});
+    g.arg.push_back(0);
+    return cudaSuccess;
+}
+
+cudaGraphNode_t rec_take(const void *tag) {
+    Recorder &r = t_rec;
+    if (!r.ok || r.next >= r.g->nodes.size() || r.g->tags[r.next] != tag) {
+        r.ok = false;
+        return nullptr;
+    }
+    return r.g->nodes[r.next++];
+}
+
+cudaError_t rec_memset(void *p, int value, size_t bytes, cudaStream_t st) {
+    Recorder &r = t_rec;
+    if (r.mode == 2) {
+        const size_t i = r.next;
+        cudaGraphNode_t n = rec_take(kTagMemset);
+        if (!n) return cudaSuccess;
+        // the same value and size as at capture: only the address changes
+        if (r.g->arg[i] != (long long)(((unsigned long long)bytes << 8) | (unsigned)(value & 0xff))) {
+            r.ok = false;
+            return cudaSuccess;
+        }
+        cudaMemsetParams mp = r.g->mset[i];
+        mp.dst = p;
+        if (cudaGraphExecMemsetNodeSetParams(r.g->exec, n, &mp) != cudaSuccess) {
+            cudaGetLastError();
+            r.ok = false;
+        }
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaMemsetAsync(p, value, bytes, st);
+    if (e != cudaSuccess || r.mode != 1) return e;
+    const size_t before = r.g->nodes.size();
+    if ((e = rec_note(st, kTagMemset)) != cudaSuccess) return e;
+    if (r.g->nodes.size() > before) {
+        if (cudaGraphMemsetNodeGetParams(r.g->nodes.back(), &r.g->mset.back()) != cudaSuccess) {
+            cudaGetLastError();
+            r.ok = false;
+        }
+        r.g->arg.back() = (long long)(((unsigned long long)bytes << 8) | (unsigned)(value & 0xff));
+    }
+    return cudaSuccess;
+}
+
+cudaError_t rec_memcpy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+    Recorder &r = t_rec;
+    if (r.mode == 2) {
+        const size_t i = r.next;
+        cudaGraphNode_t n = rec_take(kTagMemcpy);
+        if (!n) return cudaSuccess;
+        if (r.g->arg[i] != (long long)bytes ||
+            cudaGraphExecMemcpyNodeSetParams1D(r.g->exec, n, dst, src, bytes, kind) != cudaSuccess) {
+            cudaGetLastError();
+            r.ok = false;
+        }
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, st);
+    if (e != cudaSuccess || r.mode != 1) return e;
+    const size_t before = r.g->nodes.size();
+    if ((e = rec_note(st, kTagMemcpy)) != cudaSuccess) return e;
+    if (r.g->nodes.size() > before) r.g->arg.back() = (long long)bytes;
+    return cudaSuccess;
+}
+
+cudaError_t rec_event_external(cudaEvent_t ev, cudaStream_t st) {
+    Recorder &r = t_rec;
+    if (r.mode == 2) {
+        const size_t i = r.next;
+        cudaGraphNode_t n = rec_take(kTagEvent);
+        if (!n) return cudaSuccess;
+        // the node's event as last written (it alternates between calls for
+        // double-buffered state): rewrite it only when it changes
+        if (r.g->arg[i] != (long long)(uintptr_t)ev) {
+            if (cudaGraphExecEventRecordNodeSetEvent(r.g->exec, n, ev) != cudaSuccess) {
+                cudaGetLastError();
+                r.ok = false;
+            } else {
+                r.g->arg[i] = (long long)(uintptr_t)ev;
+            }
+        }
+        return cudaSuccess;
+    }
+    if (r.mode == 0) return cudaEventRecord(ev, st);
+    cudaError_t e = cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
+    if (e != cudaSuccess) return e;
+    const size_t before = r.g->nodes.size();
+    if ((e = rec_note(st, kTagEvent)) != cudaSuccess) return e;
+    if (r.g->nodes.size() > before) r.g->arg.back() = (long long)(uintptr_t)ev;
+    return cudaSuccess;
+}
+
+cudaError_t rec_event_internal(cudaEvent_t ev, cudaStream_t st) {
+    return t_rec.mode == 2 ? cudaSuccess : cudaEventRecord(ev, st);
+}
+
+cudaError_t rec_wait_internal(cudaStream_t st, cudaEvent_t ev) {
+    return t_rec.mode == 2 ? cudaSuccess : cudaStreamWaitEvent(st, ev, 0);
+}
+
+}  // namespace gvom
+
 using namespace gvom;
 
 namespace {
@@ -193,13 +324,14 @@ struct GvomHandle {
     int num_sms = 1;
     Tuning tun = kDefaultTuning;
     StageTimer timer;
-    // CUDA graphs: each process / combine launch sequence is captured and
-    // replayed through an executable graph updated in place
+    // CUDA graphs: each process / combine launch sequence is captured once
+    // per shape and replayed through an executable graph whose nodes take
+    // the parameters of each later call (see Recorder)
     bool graphs = false;
     // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ the combine
     // at level 1), [5] its columns and maps, [6] its count and statistics merges (level 2), [7] its index
     // merge (level 2)
-    cudaGraphExec_t gexec[8] = {};
+    GraphNodes gn[8];
     // a step forks the index merge onto `side` once the index maps are done
     cudaStream_t side = nullptr;
     cudaEvent_t ev_idx = nullptr, ev_join = nullptr;
@@ -254,16 +386,47 @@ void dfree(GvomHandle *h, void *p, size_t bytes) {
 
 long long ext_cells(const Geom &g) { return (long long)g.Xe * g.Xe * g.Ze; }
 
-// Runs `enqueue` (stream-ordered work on h->st only, no allocation and no
-// host synchronisation) directly, or in graph mode captures it and launches
-// the executable graph `which`, updated in place when the captured topology
-// matches the previous one and re-instantiated otherwise.
+// Runs `enqueue` (stream-ordered work through the rec_* helpers, no
+// allocation and no host synchronisation) directly, or in graph mode as the
+// executable graph `which`: when that graph exists, `enqueue` writes this
+// call's parameters into its nodes and the graph is launched; when it does
+// not, or the sequence differs in shape, `enqueue` is captured into a new
+// executable graph, which replaces the old one.
 template <class F>
 int run_graphed(GvomHandle *h, int which, F &&enqueue, cudaStream_t st = nullptr) {
     if (!st) st = h->st;
-    if (!h->graphs) return enqueue();
-    CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    Recorder &r = recorder();
+    if (!h->graphs) {
+        r = Recorder{};
+        return enqueue();
+    }
+    GraphNodes &G = h->gn[which];
+    if (G.exec) {
+        r = Recorder{};
+        r.mode = 2;
+        r.g = &G;
+        const int rc = enqueue();
+        const bool done = r.ok && r.next == G.nodes.size();
+        r = Recorder{};
+        if (rc) return rc;
+        if (done) {
+            CUDA_TRY(cudaGraphLaunch(G.exec, st));
+            return GVOM_OK;
+        }
+    }
+    GraphNodes fresh;
+    r = Recorder{};
+    r.mode = 1;
+    r.g = &fresh;
+    const cudaError_t eb = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+    if (eb != cudaSuccess) {
+        r = Recorder{};
+        cudaGetLastError();
+        return fail(GVOM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(eb));
+    }
     const int rc = enqueue();
+    const bool noted = r.ok;
+    r = Recorder{};
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc || e != cudaSuccess || !g) {
@@ -271,23 +434,28 @@ int run_graphed(GvomHandle *h, int which, F &&enqueue, cudaStream_t st = nullptr
         cudaGetLastError();
         return rc ? rc : fail(GVOM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     }
-    cudaGraphExec_t &x = h->gexec[which];
-    if (x) {
-        cudaGraphExecUpdateResultInfo info;
-        if (cudaGraphExecUpdate(x, g, &info) != cudaSuccess) {
-            cudaGetLastError();
-            cudaGraphExecDestroy(x);
-            x = nullptr;
-        }
-    }
-    cudaError_t ei = cudaSuccess;
-    if (!x) ei = cudaGraphInstantiate(&x, g, cudaGraphInstantiateFlagUseNodePriority);
-    cudaGraphDestroy(g);
+    cudaGraphExec_t x = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&x, g, cudaGraphInstantiateFlagUseNodePriority);
     if (ei != cudaSuccess) {
-        x = nullptr;
+        cudaGraphDestroy(g);
+        cudaGetLastError();
         return fail(GVOM_ERR_CUDA, std::string("graph instantiation: ") + cudaGetErrorString(ei));
     }
-    CUDA_TRY(cudaGraphLaunch(x, st));
+    // an executable graph still running is freed when it completes
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    if (G.graph) cudaGraphDestroy(G.graph);
+    G = std::move(fresh);
+    G.graph = g;
+    G.exec = x;
+    if (!noted) {  // nodes not all noted: later calls capture again
+        G.nodes.clear();
+        G.tags.clear();
+        G.mset.clear();
+        G.arg.clear();
+        G.nodes.push_back(nullptr);
+        G.tags.push_back(nullptr);
+    }
+    CUDA_TRY(cudaGraphLaunch(G.exec, st));
     return GVOM_OK;
 }
 
@@ -601,17 +769,16 @@ int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bo
     if (!st) st = h->st;
     ScanCounters *ctr = h->d_ctr + pl.set * kMaxBatch;
     if (part == 0 || part == 1) {
-        CUDA_TRY(cudaMemsetAsync(ctr, 0, sizeof(ScanCounters) * pl.k, st));
+        CUDA_TRY(rec_memset(ctr, 0, sizeof(ScanCounters) * pl.k, st));
         for (int i = 0; i < pl.k; i++)
-            CUDA_TRY(cudaMemsetAsync(h->slots[pl.slot_of[i]].idx, 0xff, sizeof(int) * (size_t)h->g.V, st));
+            CUDA_TRY(rec_memset(h->slots[pl.slot_of[i]].idx, 0xff, sizeof(int) * (size_t)h->g.V, st));
     }
     CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec[pl.set], h->prank[pl.set], h->sorted,
                             h->moments, st, (timing && !part) ? h->timer.begin(0, kProcessKernels) : nullptr,
                             h->tun.pts_block, after_assign, part, assign_external));
     if (part == 1) return GVOM_OK;
     for (int i = 0; i < pl.k; i++)
-        CUDA_TRY(cudaMemcpyAsync(h->d_slotC + pl.slot_of[i], &ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice,
-                                 st));
+        CUDA_TRY(rec_memcpy(h->d_slotC + pl.slot_of[i], &ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice, st));
     return GVOM_OK;
 }
 
@@ -816,8 +983,10 @@ int gvom_destroy(GvomHandle *h) {
     DeviceScope ds(h->dev);
     if (h->st) cudaStreamSynchronize(h->st);
     if (h->own) cudaStreamSynchronize(h->own);
-    for (auto &x : h->gexec)
-        if (x) cudaGraphExecDestroy(x);
+    for (auto &x : h->gn) {
+        if (x.exec) cudaGraphExecDestroy(x.exec);
+        if (x.graph) cudaGraphDestroy(x.graph);
+    }
     if (h->side) {
         cudaStreamSynchronize(h->side);
         cudaStreamDestroy(h->side);
@@ -1172,35 +1341,34 @@ int launch_comb(GvomHandle *h, const CombPlan &pl, cudaEvent_t idx_ready, bool t
     if (!st) st = h->st;
     if (part == 2) {
         CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 2));
-        if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_cols[pl.nb], h->st, cudaEventRecordExternal));
-        else CUDA_TRY(cudaEventRecord(h->ev_cols[pl.nb], h->st));
+        CUDA_TRY(rec_event_external(h->ev_cols[pl.nb], h->st));
         CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 3));
         return GVOM_OK;
     }
     if (timing) {
-        CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->st));
+        CUDA_TRY(rec_memset(pl.mp.out_count, 0, sizeof(int), h->st));
         CUDA_TRY(launch_combine(pl.mp, pl.cp, pl.m2, h->st, h->timer.begin(kProcessKernels, kCombineKernels)));
         return GVOM_OK;
     }
     if (idx_ready) {
-        CUDA_TRY(cudaStreamWaitEvent(h->side, idx_ready, 0));
-        CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), h->side));
+        CUDA_TRY(rec_wait_internal(h->side, idx_ready));
+        CUDA_TRY(rec_memset(pl.mp.out_count, 0, sizeof(int), h->side));
         CUDA_TRY(launch_merge_index(pl.mp, h->side));
-        CUDA_TRY(cudaEventRecord(h->ev_join, h->side));
-        CUDA_TRY(cudaStreamWaitEvent(st, h->ev_join, 0));
+        CUDA_TRY(rec_event_internal(h->ev_join, h->side));
+        CUDA_TRY(rec_wait_internal(st, h->ev_join));
     } else {
-        CUDA_TRY(cudaMemsetAsync(pl.mp.out_count, 0, sizeof(int), st));
+        CUDA_TRY(rec_memset(pl.mp.out_count, 0, sizeof(int), st));
         CUDA_TRY(launch_merge_index(pl.mp, st));
     }
     CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, st, nullptr, 1));
     if (part == 1) return GVOM_OK;
-    CUDA_TRY(cudaEventRecord(h->ev_ms, h->st));
-    CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_ms, 0));
+    CUDA_TRY(rec_event_internal(h->ev_ms, h->st));
+    CUDA_TRY(rec_wait_internal(h->side, h->ev_ms));
     CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->side, nullptr, 4));
-    CUDA_TRY(cudaEventRecord(h->ev_msj, h->side));
+    CUDA_TRY(rec_event_internal(h->ev_msj, h->side));
     CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 2));
     CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 3));
-    CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_msj, 0));
+    CUDA_TRY(rec_wait_internal(h->st, h->ev_msj));
     return GVOM_OK;
 }
 
@@ -1228,6 +1396,17 @@ int copy_outputs(GvomHandle *h, const CombPlan &pl, double origin[3], int32_t *p
     if (rough) CUDA_TRY(cudaMemcpyAsync(rough, h->rough, X2 * 8, kind, h->st));
     if (vis) CUDA_TRY(cudaMemcpyAsync(vis, h->vis, X2 * 4, kind, h->st));
     if (to_host) CUDA_TRY(cudaStreamSynchronize(h->st));
+    return GVOM_OK;
+}
+
+// the four maps into the caller's device buffers, on the instance stream, as
+// part of the sequence (graph) that computes them
+static int enqueue_device_outputs(GvomHandle *h, int32_t *pos, int32_t *neg, double *rough, int32_t *vis) {
+    const size_t X2 = (size_t)h->g.X * h->g.X;
+    if (pos) CUDA_TRY(rec_memcpy(pos, h->pos, X2 * 4, cudaMemcpyDeviceToDevice, h->st));
+    if (neg) CUDA_TRY(rec_memcpy(neg, h->neg, X2 * 4, cudaMemcpyDeviceToDevice, h->st));
+    if (rough) CUDA_TRY(rec_memcpy(rough, h->rough, X2 * 8, cudaMemcpyDeviceToDevice, h->st));
+    if (vis) CUDA_TRY(rec_memcpy(vis, h->vis, X2 * 4, cudaMemcpyDeviceToDevice, h->st));
     return GVOM_OK;
 }
 
@@ -1263,6 +1442,7 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     if (n_scans < 1 || !scans) return fail(GVOM_ERR_ARG, "a step needs at least one scan");
     std::lock_guard<std::mutex> lk(h->mu);
     const bool timing = !h->graphs && h->timer.on;
+    const bool dev_out = outputs_on_device != 0;
     // with stage timing the kernels run in sequence so that each interval is one kernel
     const int pipe = timing ? 0 : h->tun.step_pipeline;
     if (pipe >= 2 && h->st_dirty) {  // order the pipeline streams after other calls' work
@@ -1294,16 +1474,18 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
     if (pipe == 2) {
         // tr: the trace
-        rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
+        rc = run_graphed(h, 3, [&]() -> int {
+            if ((rc = launch_scans(h, pp, nullptr, false, 1, h->tr))) return rc;
+            CUDA_TRY(rec_event_external(h->ev_traced, h->tr));
+            return GVOM_OK;
+        }, h->tr);
         if (rc) return rc;
-        CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
         // bs: the rest of the process, after the trace; ev_idx marks the slots'
         // index maps complete, ev_scratch[set] the whole process
         CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_traced, 0));
         rc = run_graphed(h, 4, [&]() -> int {
-            if ((rc = launch_scans(h, pp, h->ev_idx, false, 2, h->bs, h->graphs))) return rc;
-            if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_scratch[pp.set], h->bs, cudaEventRecordExternal));
-            else CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->bs));
+            if ((rc = launch_scans(h, pp, h->ev_idx, false, 2, h->bs, true))) return rc;
+            CUDA_TRY(rec_event_external(h->ev_scratch[pp.set], h->bs));
             return GVOM_OK;
         }, h->bs);
         if (rc) return rc;
@@ -1314,7 +1496,7 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_cols[cp.nb], 0));
         CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_idx, 0));
         rc = run_graphed(h, 7, [&]() -> int {
-            CUDA_TRY(cudaMemsetAsync(cp.mp.out_count, 0, sizeof(int), h->side));
+            CUDA_TRY(rec_memset(cp.mp.out_count, 0, sizeof(int), h->side));
             CUDA_TRY(launch_merge_index(cp.mp, h->side));
             return GVOM_OK;
         }, h->side);
@@ -1323,47 +1505,56 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_scratch[pp.set], 0));
         rc = run_graphed(h, 6, [&]() -> int {
             CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->side, nullptr, 1));
-            if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_merged, h->side, cudaEventRecordExternal));
-            else CUDA_TRY(cudaEventRecord(h->ev_merged, h->side));
+            CUDA_TRY(rec_event_external(h->ev_merged, h->side));
             CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->side, nullptr, 4));
+            CUDA_TRY(rec_event_external(h->ev_stats[cp.nb], h->side));
             return GVOM_OK;
         }, h->side);
         if (rc) return rc;
-        CUDA_TRY(cudaEventRecord(h->ev_stats[cp.nb], h->side));
         if ((rc = comb_done(h, h->side))) return rc;
         // st: columns and maps after the count merge, beside the statistics
         // merge and the next step's process
         CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_merged, 0));
-        rc = run_graphed(h, 5, [&]() -> int { return launch_comb(h, cp, nullptr, false, 2); });
+        rc = run_graphed(h, 5, [&]() -> int {
+            if ((rc = launch_comb(h, cp, nullptr, false, 2))) return rc;
+            return dev_out ? enqueue_device_outputs(h, pos, neg, roughness, visibility) : GVOM_OK;
+        });
         if (!rc) CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_stats[cp.nb], 0));  // later calls see whole records
     } else if (pipe == 1) {
         h->st_dirty = true;
         // the trace waits only for the previous process to release the scratch
         // (and for its slots), so it runs beside the previous step's combine
-        rc = run_graphed(h, 3, [&]() -> int { return launch_scans(h, pp, nullptr, false, 1, h->tr); }, h->tr);
+        rc = run_graphed(h, 3, [&]() -> int {
+            if ((rc = launch_scans(h, pp, nullptr, false, 1, h->tr))) return rc;
+            CUDA_TRY(rec_event_external(h->ev_traced, h->tr));
+            return GVOM_OK;
+        }, h->tr);
         if (rc) return rc;
-        CUDA_TRY(cudaEventRecord(h->ev_traced, h->tr));
         CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_traced, 0));
         rc = run_graphed(h, 4, [&]() -> int {
             if ((rc = launch_scans(h, pp, idx, false, 2))) return rc;
             // in graph mode an event-record node of the graph
-            if (h->graphs) CUDA_TRY(cudaEventRecordWithFlags(h->ev_scratch[pp.set], h->st, cudaEventRecordExternal));
-            else CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->st));
-            return launch_comb(h, cp, idx, false);
+            CUDA_TRY(rec_event_external(h->ev_scratch[pp.set], h->st));
+            if ((rc = launch_comb(h, cp, idx, false))) return rc;
+            return dev_out ? enqueue_device_outputs(h, pos, neg, roughness, visibility) : GVOM_OK;
         });
         if (!rc) rc = comb_done(h, h->st);
     } else {
         h->st_dirty = true;
         rc = run_graphed(h, 2, [&]() -> int {
             if ((rc = launch_scans(h, pp, idx, timing))) return rc;
-            return launch_comb(h, cp, idx, timing);
+            if ((rc = launch_comb(h, cp, idx, timing))) return rc;
+            return dev_out ? enqueue_device_outputs(h, pos, neg, roughness, visibility) : GVOM_OK;
         });
         if (!rc) CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->st));
         if (!rc) rc = comb_done(h, h->st);
     }
     if (rc) return rc;
     commit_combine(h, cp);
-    if ((rc = copy_outputs(h, cp, origin, pos, neg, roughness, visibility, !outputs_on_device))) return rc;
+    // device outputs were written by the step's own sequence; host outputs are copied here
+    if (dev_out) rc = copy_outputs(h, cp, origin, nullptr, nullptr, nullptr, nullptr, false);
+    else rc = copy_outputs(h, cp, origin, pos, neg, roughness, visibility, true);
+    if (rc) return rc;
     if (pinned) CUDA_TRY(cudaStreamSynchronize(pipe ? h->tr : h->st));  // the caller may reuse its buffers
     return GVOM_OK;
 }

@@ -16,9 +16,85 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#ifdef __CUDACC__
+#include <type_traits>
+#include <vector>
+#endif
+
 #include "gvom_exact.cuh"
 
 namespace gvom {
+
+#ifdef __CUDACC__  // (the host-compiled kernel tests include this header without the CUDA runtime)
+// ---------------------------------------------------------------------------
+// Stream-ordered work in graph mode.  The launch sequences of a process,
+// combine or step call go through the rec_* helpers below.  Without graphs
+// they launch directly.  The first time a sequence runs in graph mode it is
+// captured (the helpers launch into the capture and note each node they
+// add, in order); later calls of the same shape do not capture again: the
+// helpers write the new parameters (kernel arguments and grid, memset and
+// copy addresses, events) into the executable graph's nodes in the same
+// order.  A call whose sequence differs (another kernel at a position, more
+// or fewer nodes) is captured anew.
+// ---------------------------------------------------------------------------
+struct GraphNodes {
+    cudaGraph_t graph = nullptr;      // the graph `exec` was instantiated from (owns the nodes)
+    cudaGraphExec_t exec = nullptr;
+    std::vector<cudaGraphNode_t> nodes;
+    std::vector<const void *> tags;   // per node: kernel function, or the kind of operation
+    std::vector<cudaMemsetParams> mset;  // per node: memset parameters at capture (other nodes: unused)
+    std::vector<long long> arg;       // per node: memset size and value, copy size, or recorded event
+};
+
+struct Recorder {
+    int mode = 0;             // 0 launch directly, 1 capture (and note nodes), 2 write into g's nodes
+    GraphNodes *g = nullptr;
+    size_t next = 0;          // next node (mode 2)
+    bool ok = true;           // mode 2: every operation matched its node and was written
+};
+
+// the recorder of the calling thread (calls on one instance are serialised)
+Recorder &recorder();
+
+// capture mode: notes the node the last operation on `st` added
+cudaError_t rec_note(cudaStream_t st, const void *tag);
+// update mode: the next node if it carries `tag`, else nullptr (and the update fails)
+cudaGraphNode_t rec_take(const void *tag);
+
+template <typename... P>
+cudaError_t rec_kernel(void (*fn)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       std::decay_t<P>... args) {
+    void *ptrs[] = {static_cast<void *>(&args)...};
+    Recorder &r = recorder();
+    if (r.mode == 2) {
+        cudaGraphNode_t n = rec_take(reinterpret_cast<const void *>(fn));
+        if (!n) return cudaSuccess;
+        cudaKernelNodeParams kp = {};
+        kp.func = reinterpret_cast<void *>(fn);
+        kp.gridDim = grid;
+        kp.blockDim = block;
+        kp.sharedMemBytes = (unsigned)smem;
+        kp.kernelParams = ptrs;
+        if (cudaGraphExecKernelNodeSetParams(r.g->exec, n, &kp) != cudaSuccess) {
+            cudaGetLastError();
+            r.ok = false;
+        }
+        return cudaSuccess;
+    }
+    cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void *>(fn), grid, block, ptrs, smem, st);
+    if (e == cudaSuccess && r.mode == 1) e = rec_note(st, reinterpret_cast<const void *>(fn));
+    return e;
+}
+
+cudaError_t rec_memset(void *p, int value, size_t bytes, cudaStream_t st);
+cudaError_t rec_memcpy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st);
+// an event recorded for waits outside the graph (an event-record node in graph mode)
+cudaError_t rec_event_external(cudaEvent_t ev, cudaStream_t st);
+// a fork / join inside one sequence (edges of the graph, nothing to write in update mode)
+cudaError_t rec_event_internal(cudaEvent_t ev, cudaStream_t st);
+cudaError_t rec_wait_internal(cudaStream_t st, cudaEvent_t ev);
+#endif
+
 
 constexpr int kMaxBatch = 16;         // scans per batched launch
 

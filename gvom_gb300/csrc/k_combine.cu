@@ -1066,85 +1066,90 @@ __global__ void k_debug_maps(DebugMapParams p) {
 // launchers
 // ---------------------------------------------------------------------------
 template <int TX, int TY>
-static void launch_maps2d(const Maps2DParams &m2, cudaStream_t st) {
+static cudaError_t launch_maps2d(const Maps2DParams &m2, cudaStream_t st) {
     const int X = m2.X;
     dim3 g2((X + TY - 1) / TY, (X + TX - 1) / TX);
-    k_maps2d<TX, TY><<<g2, dim3(TY, TX + 32 / TY), 0, st>>>(m2);
+    return rec_kernel(k_maps2d<TX, TY>, g2, dim3(TY, TX + 32 / TY), 0, st, m2);
 }
 template <int NSRC>
-static void launch_merge_idx(const MergeParams &mp, cudaStream_t st) {
+static cudaError_t launch_merge_idx(const MergeParams &mp, cudaStream_t st) {
     const int X = mp.g.X, Z = mp.g.Z, zc = mp.planes;
     dim3 gm((X + 31) / 32, (X + 7) / 8, (Z + zc - 1) / zc);
-    if (zc == 4) k_merge<NSRC, 4><<<gm, dim3(32, 8), 0, st>>>(mp);
-    else if (zc == 16) k_merge<NSRC, 16><<<gm, dim3(32, 8), 0, st>>>(mp);
-    else k_merge<NSRC, 8><<<gm, dim3(32, 8), 0, st>>>(mp);
+    if (zc == 4) return rec_kernel(k_merge<NSRC, 4>, gm, dim3(32, 8), 0, st, mp);
+    if (zc == 16) return rec_kernel(k_merge<NSRC, 16>, gm, dim3(32, 8), 0, st, mp);
+    return rec_kernel(k_merge<NSRC, 8>, gm, dim3(32, 8), 0, st, mp);
 }
 
 template <int NSRC>
-static void launch_merge_stats(const MergeParams &mp, cudaStream_t st) {
-    k_merge_stats<NSRC><<<mp.num_sms * mp.stats_bpsm, 256, 0, st>>>(mp);
+static cudaError_t launch_merge_stats(const MergeParams &mp, cudaStream_t st) {
+    return rec_kernel(k_merge_stats<NSRC>, dim3(mp.num_sms * mp.stats_bpsm), dim3(256), 0, st, mp);
 }
 
 template <int NSRC>
-static void launch_merge_counts(const MergeParams &mp, cudaStream_t st) {
-    k_merge_counts<NSRC><<<mp.num_sms * 8, 256, 0, st>>>(mp);
+static cudaError_t launch_merge_counts(const MergeParams &mp, cudaStream_t st) {
+    return rec_kernel(k_merge_counts<NSRC>, dim3(mp.num_sms * 8), dim3(256), 0, st, mp);
 }
 
 // source-count class of a merge (2, 3, 5, 9 or 17 sources)
 template <template <int> class F>
-static void by_nsrc(const MergeParams &mp, cudaStream_t st) {
-    if (mp.nsrc <= 2) F<2>::run(mp, st);
-    else if (mp.nsrc <= 3) F<3>::run(mp, st);
-    else if (mp.nsrc <= 5) F<5>::run(mp, st);
-    else if (mp.nsrc <= 9) F<9>::run(mp, st);
-    else F<kMaxSources>::run(mp, st);
+static cudaError_t by_nsrc(const MergeParams &mp, cudaStream_t st) {
+    if (mp.nsrc <= 2) return F<2>::run(mp, st);
+    if (mp.nsrc <= 3) return F<3>::run(mp, st);
+    if (mp.nsrc <= 5) return F<5>::run(mp, st);
+    if (mp.nsrc <= 9) return F<9>::run(mp, st);
+    return F<kMaxSources>::run(mp, st);
 }
 template <int N>
 struct MergeIdx {
-    static void run(const MergeParams &mp, cudaStream_t st) { launch_merge_idx<N>(mp, st); }
+    static cudaError_t run(const MergeParams &mp, cudaStream_t st) { return launch_merge_idx<N>(mp, st); }
 };
 template <int N>
 struct MergeStats {
-    static void run(const MergeParams &mp, cudaStream_t st) { launch_merge_stats<N>(mp, st); }
+    static cudaError_t run(const MergeParams &mp, cudaStream_t st) { return launch_merge_stats<N>(mp, st); }
 };
 template <int N>
 struct MergeCounts {
-    static void run(const MergeParams &mp, cudaStream_t st) { launch_merge_counts<N>(mp, st); }
+    static cudaError_t run(const MergeParams &mp, cudaStream_t st) { return launch_merge_counts<N>(mp, st); }
 };
 
 cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st) {
-    by_nsrc<MergeIdx>(mp, st);
-    return cudaGetLastError();
+    const cudaError_t e = by_nsrc<MergeIdx>(mp, st);
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 // count merge, statistics merge, columns and 2-D maps (events ev[1..5] when timing)
 cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
                                 cudaEvent_t *ev, int part) {
     const int X = mp.g.X;
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
     if (part) ev = nullptr;
     if (ev) cudaEventRecord(ev[1], st);
-    if (part == 0 || part == 1) by_nsrc<MergeCounts>(mp, st);
+    if (part == 0 || part == 1) chk(by_nsrc<MergeCounts>(mp, st));
     if (ev) cudaEventRecord(ev[2], st);
-    if (part == 0 || part == 4) by_nsrc<MergeStats>(mp, st);
+    if (part == 0 || part == 4) chk(by_nsrc<MergeStats>(mp, st));
     if (ev) cudaEventRecord(ev[3], st);
     if (part == 0 || part == 2) {
         dim3 gc((X + 31) / 32, (X + 7) / 8);
-        k_columns<<<gc, dim3(32, 8), 0, st>>>(cp);
+        chk(rec_kernel(k_columns, gc, dim3(32, 8), 0, st, cp));
     }
     if (ev) cudaEventRecord(ev[4], st);
     if (part == 0 || part == 3) {
-        if (m2.tile_cells == 64) launch_maps2d<4, 16>(m2, st);
-        else if (m2.tile_cells == 128) launch_maps2d<8, 16>(m2, st);
-        else launch_maps2d<8, 32>(m2, st);
+        if (m2.tile_cells == 64) chk(launch_maps2d<4, 16>(m2, st));
+        else if (m2.tile_cells == 128) chk(launch_maps2d<8, 16>(m2, st));
+        else chk(launch_maps2d<8, 32>(m2, st));
     }
     if (ev) cudaEventRecord(ev[5], st);
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_combine(const MergeParams &mp, const ColumnParams &cp, const Maps2DParams &m2, cudaStream_t st,
                            cudaEvent_t *ev) {  // every kernel in sequence on `st`
     if (ev) cudaEventRecord(ev[0], st);
-    by_nsrc<MergeIdx>(mp, st);
+    const cudaError_t e = by_nsrc<MergeIdx>(mp, st);
+    if (e != cudaSuccess) return e;
     return launch_combine_rest(mp, cp, m2, st, ev);
 }
 

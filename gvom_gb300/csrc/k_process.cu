@@ -815,34 +815,35 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
     auto mark = [&](int i) {
         if (ev) cudaEventRecord(ev[i], st);
     };
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess) e = x;
+    };
     if (part == 0 || part == 1) {
         mark(0);
         if (dtype == 1)
-            k_voxelize_trace<double, NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
+            chk(rec_kernel(k_voxelize_trace<double, NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank));
         else
-            k_voxelize_trace<float, NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
+            chk(rec_kernel(k_voxelize_trace<float, NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank));
         mark(1);
-        if (part == 1) return cudaGetLastError();
+        if (part == 1) return e != cudaSuccess ? e : cudaGetLastError();
     }
-    k_assign<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
-    if (after_assign) {
-        if (assign_external) cudaEventRecordWithFlags(after_assign, st, cudaEventRecordExternal);
-        else cudaEventRecord(after_assign, st);
-    }
+    chk(rec_kernel(k_assign<NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank));
+    if (after_assign) chk(assign_external ? rec_event_external(after_assign, st) : rec_event_internal(after_assign, st));
     mark(2);
-    k_scatter<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank, sorted);
+    chk(rec_kernel(k_scatter<NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank, sorted));
     mark(3);
-    k_cell_moments<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank, sorted, mom);
+    chk(rec_kernel(k_cell_moments<NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank, sorted, mom));
     mark(4);
     const bool e3 = pc.g.exy == 1 && pc.g.ez == 1;  // four lanes per voxel
     const long long want = ((e3 ? 4LL : 1LL) * max_n + 255) / 256;
     dim3 gs((unsigned)std::max<long long>(1, std::min<long long>(want, (long long)pc.num_sms * 8)), pc.nscans);
-    if (e3) k_voxel_stats<NS, 1><<<gs, 256, 0, st>>>(pc, tab, mom);
-    else k_voxel_stats<NS, 0><<<gs, 256, 0, st>>>(pc, tab, mom);
+    if (e3) chk(rec_kernel(k_voxel_stats<NS, 1>, gs, dim3(256), 0, st, pc, tab, mom));
+    else chk(rec_kernel(k_voxel_stats<NS, 0>, gs, dim3(256), 0, st, pc, tab, mom));
     mark(5);
-    k_cleanup<NS><<<total_blocks, bs, 0, st>>>(pc, tab, prec, prank);
+    chk(rec_kernel(k_cleanup<NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank));
     mark(6);
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
