@@ -431,11 +431,40 @@ __global__ void k_gather_records(const VoxelRec *__restrict__ rec, const int *__
 // ring segment of the guess search is one lookup).
 // ---------------------------------------------------------------------------
 constexpr int kHalo = 15;
+constexpr long long kMinus1000Bits = (long long)0xC08F400000000000ULL;  // -1000.0
 
 // h > -1000.0 on the bit pattern (no float64 compare)
 __device__ __forceinline__ bool height_known(double h) {
     const long long b = __double_as_longlong(h);
     return b >= 0 || (b & 0x7fffffffffffffffLL) < 0x408F400000000000LL;  // |h| < 1000
+}
+
+// The cell threads compare and widen doubles on their bit patterns: a
+// float64 instruction holds this part's slow float64 pipe as long as a
+// float64 plane fit step of the queue, which the same pipe runs.
+
+// a == b for doubles that are not NaN: equal bits, or +0 against -0
+__device__ __forceinline__ bool same_double(double a, double b) {
+    const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+    return x == y || ((x | y) << 1) == 0;
+}
+
+// a signed key that orders doubles that are not NaN as < does, except that
+// -0 sorts below +0
+__device__ __forceinline__ long long double_order(double a) {
+    const long long b = __double_as_longlong(a);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
+// (double)f: a normal float's bits moved into place (exponent rebiased by
+// 1023 - 127); zero, subnormals, inf and NaN take the conversion instruction
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)f;
+    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
+                                            ((unsigned long long)(e + 896u) << 52) |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
 // atan2(a, im) with im = RN(1/m), m = sqrt(a0^2 + a1^2 + 1) >= 1: atan2f of
@@ -653,6 +682,7 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
     // 0, a slope component near 0); closed form where every neighbour has
     // the same height
     double rough = -1.0, slx = 0.0, sly = 0.0;
+    float slxf = 0.f, slyf = 0.f;  // the slopes in float32, for the slope gate
     bool need_exact = false;
     {
         const int xl = max(0, x0 - 1), xh = min(X, x0 + 2), yl = max(0, y0 - 1), yh = min(X, y0 + 2);
@@ -674,7 +704,7 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
                         yf = yy;
                     }
                     all_vox = all_vox && szl[sx][sy] >= 0;
-                    all_eq = all_eq && sh[sx][sy] == h0;
+                    all_eq = all_eq && same_double(sh[sx][sy], h0);
                     n_good++;
                     sxi += xx - x0;
                     syi += yy - y0;
@@ -733,15 +763,23 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
                         const int xx = x0 - 1 + a, yy = y0 - 1 + b;
                         const int sx = xx - x0t + kHalo, sy = yy - y0t + kHalo;
                         kk[a][b] = xx >= xl && xx < xh && yy >= yl && yy < yh && kn[sx][sy];
-                        dzs[a][b] = 0.f;
-                        if (kk[a][b]) {
-                            // from voxels: an exact count plus a fraction; with a robot-disc
-                            // height: the float64 difference, rounded once
-                            dzs[a][b] = all_vox ? ((sml[sx][sy] - mr) + (float)(szl[sx][sy] - zr)) * zres
-                                                : (float)__dsub_rn(sh[sx][sy], h0);
-                            zsum += dzs[a][b];
-                        }
+                        // from voxels: an exact count plus a fraction
+                        dzs[a][b] = kk[a][b] ? ((sml[sx][sy] - mr) + (float)(szl[sx][sy] - zr)) * zres : 0.f;
                     }
+                if (!all_vox) {
+                    // with a robot-disc height: the float64 difference, rounded once
+#pragma unroll
+                    for (int a = 0; a < 3; a++)
+#pragma unroll
+                        for (int b = 0; b < 3; b++)
+                            if (kk[a][b])
+                                dzs[a][b] = (float)__dsub_rn(sh[x0 - 1 + a - x0t + kHalo][y0 - 1 + b - y0t + kHalo], h0);
+                }
+#pragma unroll
+                for (int a = 0; a < 3; a++)
+#pragma unroll
+                    for (int b = 0; b < 3; b++)
+                        if (kk[a][b]) zsum += dzs[a][b];
                 const float zm = zsum / nf;
                 float sxx = 0.f, sxy = 0.f, sxz = 0.f, syy = 0.f, syz = 0.f;
 #pragma unroll
@@ -795,9 +833,11 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
                 need_exact = true;
                 qcell[atomicAdd(&qn, 1)] = tid;
             } else {
-                rough = (double)rf;
-                slx = (double)sxf;
-                sly = (double)syf;
+                rough = widen(rf);
+                slx = widen(sxf);
+                sly = widen(syf);
+                slxf = sxf;
+                slyf = syf;
             }
         }
     }
@@ -831,8 +871,9 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
     // included; each ring segment is scanned in increasing order, so its first
     // known cell is one lookup in the next-known tables
     double guess = 0.0;
-    if (valid && !known && !(mp.inferred[cell] == -1000.0)) {
+    if (valid && !known && __double_as_longlong(mp.inferred[cell]) != kMinus1000Bits) {
         bool xpd = false, xnd = false, ypd = false, ynd = false;
+        bool xpf = false, xnf = false, ypf = false, ynf = false;  // a known height found
         int xp = x0, xn = x0, yp = y0, yn = y0;
         double xph = -1000.0, xnh = -1000.0, yph = -1000.0, ynh = -1000.0;
         int i = 0;
@@ -845,7 +886,7 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
                     if (lo < hi) {
                         const int sx = xp - x0t + kHalo;
                         const int f = nky[sx][lo - y0t + kHalo];
-                        if (f < hi - y0t + kHalo) { xph = sh[sx][f]; xpd = true; }
+                        if (f < hi - y0t + kHalo) { xph = sh[sx][f]; xpd = xpf = true; }
                     }
                 } else xpd = true;
             }
@@ -855,7 +896,7 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
                     if (lo < hi) {
                         const int sx = xn - x0t + kHalo;
                         const int f = nky[sx][lo - y0t + kHalo];
-                        if (f < hi - y0t + kHalo) { xnh = sh[sx][f]; xnd = true; }
+                        if (f < hi - y0t + kHalo) { xnh = sh[sx][f]; xnd = xnf = true; }
                     }
                 } else xnd = true;
             }
@@ -865,7 +906,7 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
                     if (lo < hi) {
                         const int sy = yp - y0t + kHalo;
                         const int f = nkx[sy][lo - x0t + kHalo];
-                        if (f < hi - x0t + kHalo) { yph = sh[f][sy]; ypd = true; }
+                        if (f < hi - x0t + kHalo) { yph = sh[f][sy]; ypd = ypf = true; }
                     }
                 } else ypd = true;
             }
@@ -875,18 +916,28 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
                     if (lo < hi) {
                         const int sy = yn - y0t + kHalo;
                         const int f = nkx[sy][lo - x0t + kHalo];
-                        if (f < hi - x0t + kHalo) { ynh = sh[f][sy]; ynd = true; }
+                        if (f < hi - x0t + kHalo) { ynh = sh[f][sy]; ynd = ynf = true; }
                     }
                 } else ynd = true;
             }
         }
+        // a height found is known (> -1000), so each "> -1000" test is its
+        // found flag; the extremes are taken on ordered keys (a -0 / +0 tie
+        // can pick the other zero, which leaves mx - mn > 0 unchanged)
         double mn = 1000.0, mx = mp.inferred[cell];
-        if (xph > -1000.0) { mn = xph < mn ? xph : mn; mx = xph > mx ? xph : mx; }
-        if (xnh > -1000.0) { mn = xnh < mn ? xnh : mn; mx = xnh > mx ? xnh : mx; }
-        if (yph > -1000.0) { mn = yph < mn ? yph : mn; mx = yph > mx ? yph : mx; }
-        if (xnh > -1000.0) { mn = ynh < mn ? ynh : mn; mx = ynh > mx ? ynh : mx; }
+        long long kmn = double_order(mn), kmx = double_order(mx);
+        auto take = [&](double v) {
+            const long long k = double_order(v);
+            if (k < kmn) { kmn = k; mn = v; }
+            if (k > kmx) { kmx = k; mx = v; }
+        };
+        if (xpf) take(xph);
+        if (xnf) take(xnh);
+        if (ypf) take(yph);
+        if (xnf) take(ynh);  // x_nh's test guards y_nh (scripts/gvom.py:704-706); -1000 when not found
         const double dh = __dsub_rn(mx, mn);
-        if (dh > 0.0) guess = dh;
+        const long long db = __double_as_longlong(dh);
+        if (db > 0 && db <= 0x7ff0000000000000LL) guess = dh;  // dh > 0
     }
     // cell warps that finish their search take what the extra warp has not
     __syncwarp();
@@ -897,13 +948,15 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
         rough = qres[tid][0];
         slx = qres[tid][1];
         sly = qres[tid][2];
+        slxf = (float)slx;
+        slyf = (float)sly;
     }
 
     // __make_positive_obstacle_map slope gate (scripts/gvom.py:524-526): in
     // float32 unless |slope| is near the threshold
     bool steep;
     {
-        const float sn = sqrtf((float)slx * (float)slx + (float)sly * (float)sly);
+        const float sn = sqrtf(slxf * slxf + slyf * slyf);
         if (fabsf(sn - mp.slope_thr_f) > 1e-5f * mp.slope_thr_f + 1e-6f) steep = sn >= mp.slope_thr_f;
         else steep = sqrt(__dadd_rn(__dmul_rn(slx, slx), __dmul_rn(sly, sly))) >= mp.slope_thr;
     }

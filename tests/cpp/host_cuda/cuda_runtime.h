@@ -56,6 +56,8 @@ static inline unsigned atomicCAS(unsigned *p, unsigned cmp, unsigned v) {
 }
 static inline int atomicAdd(int *p, int v) { const int o = *p; *p = o + v; return o; }
 static inline long long __double_as_longlong(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
+static inline double __longlong_as_double(long long i) { double d; std::memcpy(&d, &i, 8); return d; }
+static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 static inline int __popc(unsigned v) { return __builtin_popcount(v); }
 static inline float2 make_float2(float a, float b) { return float2{a, b}; }
 static inline int2 make_int2(int a, int b) { return int2{a, b}; }

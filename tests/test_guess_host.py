@@ -21,8 +21,13 @@ KERNEL = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc", "k_combine.cu
 
 PRELUDE = r"""
 #include <algorithm>
+#include <cstring>
 using std::max; using std::min;
 #define __dsub_rn(a, b) ((double)(a) - (double)(b))
+#define __device__
+#define __forceinline__ inline
+static inline long long __double_as_longlong(double d) { long long b; std::memcpy(&b, &d, 8); return b; }
+%(helpers)s
 constexpr int kHalo = %(halo)d;
 constexpr int kS = 250;  // one tile over the whole map: X + 2 kHalo <= kS (next-known indices are bytes)
 static double sh[kS][kS];
@@ -66,6 +71,15 @@ POSTLUDE = r"""
 """
 
 
+def _kernel_helpers():
+    """The kernel's own -1000.0 constant and ordered-key helper."""
+    src = open(KERNEL).read()
+    const = re.search(r"^constexpr long long kMinus1000Bits = .*$", src, re.M).group(0)
+    a = src.index("__device__ __forceinline__ long long double_order(double a) {")
+    b = src.index("\n}\n", a) + 3
+    return const + "\n" + src[a:b]
+
+
 def _kernel_guess_block():
     src = open(KERNEL).read()
     a = src.index("    // __guess_height (scripts/gvom.py:592-714)")
@@ -80,7 +94,7 @@ def guess_lib(tmp_path_factory):
     halo = int(re.search(r"constexpr int kHalo = (\d+);", open(KERNEL).read()).group(1))
     d = tmp_path_factory.mktemp("guess")
     cpp = d / "guess_host.cpp"
-    cpp.write_text(PRELUDE % {"halo": halo} + _kernel_guess_block() + POSTLUDE)
+    cpp.write_text(PRELUDE % {"halo": halo, "helpers": _kernel_helpers()} + _kernel_guess_block() + POSTLUDE)
     so = d / "libguess.so"
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(so), str(cpp)],
                    check=True)

@@ -25,7 +25,7 @@ def _kernel_parts():
     a = src.index("constexpr int kHalo = ")
     b = src.index("template <int kTX, int kTY>", a)
     helpers = src[a:b]
-    c = src.index("    double rough = -1.0, slx = 0.0, sly = 0.0;\n    bool need_exact = false;")
+    c = src.index("    double rough = -1.0, slx = 0.0, sly = 0.0;\n")
     d = src.index("    // cells that need the float64 sequence are compacted", c)
     return helpers, src[c:d]
 
