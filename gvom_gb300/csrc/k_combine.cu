@@ -498,97 +498,124 @@ __device__ __forceinline__ bool axis_mean_exact(int c, double res, int n) {
 }
 
 // __calculate_slope (scripts/gvom.py:717-805) in the reference's float64
-// operation order up to the final log / atan2.  The reference forms every
-// point's x * res, y * res and their offsets from the means point by point;
-// the neighbourhood has at most three distinct x and three distinct y, so
-// those values (and x * x, y * y, a0 * x, a1 * y of the offsets) are formed
-// once per column / row with the same rounded operations and reused -- the
-// same bits in fewer float64 instructions, all in registers.  Sums run over
-// the known neighbours in the reference's order (x major, y minor).
+// operation order up to the final log / atan2, for four queued cells per
+// warp, eight lanes (g = 0..7) per cell.  The reference forms every point's
+// x * res, y * res and their offsets from the means point by point; the
+// neighbourhood has at most three distinct x and three distinct y, so those
+// values (and x * x, y * y, a0 * x, a1 * y of the offsets) are formed once
+// per column / row with the same rounded operations and reused.  Sums run
+// over the known neighbours in the reference's order (x major, y minor).
+//
+// This part's float64 pipe holds a warp instruction as long with one active
+// lane as with 32, so the independent operations of each step are spread
+// over the cell's lanes and one instruction does up to eight of them; values
+// move between lanes by shuffles.  Each value is the same IEEE operation on
+// the same operands as the one-lane sequence.  Lane roles:
+//   coordinates  lanes 0-2: x of column a, (xl + a) res; lanes 3-5: y of row b
+//   means        lane 0: x, lane 1: y, lane 2: z
+//   offsets      lanes 0-2: dx[a] = x[a] - mean x; lanes 3-5: dy[b]
+//   neighbours   lane g: neighbour g = (g / 3, g % 3); neighbour 8 on all lanes
+//   sums         lanes 0-4: sxx, sxy, sxz, syy, syz
+//   solve        lane 0: det, lane 1: a0, lane 2: a1
+// Called by the whole warp, converged.  A group with `active` false has no
+// cell (x0, y0 name a cell of the tile, so its loads stay in bounds) and its
+// result is not used.  Returns, in lane 0 of the group, the roughness, in
+// lane 1 the x slope, in lane 2 the y slope.
 template <int kSY>
-__device__ __forceinline__ void slope_f64(const double (*sh)[kSY], const unsigned char (*kn)[kSY], int x0t, int y0t,
-                                          int x0, int y0, int X, double res, double &rough, double &slx, double &sly) {
+__device__ __forceinline__ double slope_f64_group(const double (*sh)[kSY], const unsigned char (*kn)[kSY], int x0t,
+                                                  int y0t, int x0, int y0, bool active, int X, double res, int g) {
+    constexpr unsigned kFull = 0xffffffffu;
     const int xl = max(0, x0 - 1), xh = min(X, x0 + 2), yl = max(0, y0 - 1), yh = min(X, y0 + 2);
-    bool k[3][3];
-    double hz[3][3];
+    // known neighbours (bit j: neighbour (j / 3, j % 3)) and their heights;
+    // hzg: neighbour g's height
+    unsigned km = 0;
+    double hz[9], hzg = 0.0;
 #pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int b = 0; b < 3; b++) {
-            k[a][b] = xl + a < xh && yl + b < yh && kn[xl + a - x0t + kHalo][yl + b - y0t + kHalo];
-            hz[a][b] = k[a][b] ? sh[xl + a - x0t + kHalo][yl + b - y0t + kHalo] : 0.0;
-        }
+    for (int j = 0; j < 9; j++) {
+        const int sx = xl + j / 3 - x0t + kHalo, sy = yl + j % 3 - y0t + kHalo;
+        const bool k = active && xl + j / 3 < xh && yl + j % 3 < yh && kn[sx][sy];
+        km |= (unsigned)k << j;
+        hz[j] = k ? sh[sx][sy] : 0.0;
+        if (j == g) hzg = hz[j];
+    }
+    const double pv = __dmul_rn(widen((float)(g < 3 ? xl + g : yl + min(g - 3, 2))), res);
     double px[3], py[3];
 #pragma unroll
     for (int a = 0; a < 3; a++) {
-        px[a] = __dmul_rn((double)(xl + a), res);
-        py[a] = __dmul_rn((double)(yl + a), res);
+        px[a] = __shfl_sync(kFull, pv, a, 8);
+        py[a] = __shfl_sync(kFull, pv, 3 + a, 8);
     }
-    double mx = 0.0, my = 0.0, mz = 0.0;
+    double acc = 0.0;
     int n = 0;
 #pragma unroll
-    for (int a = 0; a < 3; a++)
+    for (int j = 0; j < 9; j++)
+        if ((km >> j) & 1u) {
+            acc = __dadd_rn(acc, g == 0 ? px[j / 3] : g == 1 ? py[j % 3] : hz[j]);
+            n++;
+        }
+    // a group without a cell (n = 0) and a singular fit (det = 0) divide by
+    // 1 instead: a zero divisor would send the whole warp's division down its
+    // slow path, and those quotients are not used (a cell has n >= 3)
+    const double dn = widen((float)max(n, 1));
+    const double mean = __ddiv_rn(acc, dn);
+    const double mx = __shfl_sync(kFull, mean, 0, 8), my = __shfl_sync(kFull, mean, 1, 8);
+    const double mz = __shfl_sync(kFull, mean, 2, 8);
+    const double d = __dsub_rn(pv, g < 3 ? mx : my);
+    const double dd = __dmul_rn(d, d);
+    // neighbour g's residual height and products, then neighbour 8's: lane 0
+    // dx dy, lane 1 dx dz, lane 2 dy dz
+    const double dxg = __shfl_sync(kFull, d, g / 3, 8), dyg = __shfl_sync(kFull, d, 3 + g % 3, 8);
+    const double dx2 = __shfl_sync(kFull, d, 2, 8), dy2 = __shfl_sync(kFull, d, 5, 8);
+    const double dzg = __dsub_rn(hzg, mz), dz8 = __dsub_rn(hz[8], mz);
+    const double pxy = __dmul_rn(dxg, dyg), pxz = __dmul_rn(dxg, dzg), pyz = __dmul_rn(dyg, dzg);
+    const double p8 = __dmul_rn(g == 2 ? dy2 : dx2, g == 0 ? dy2 : dz8);
+    double s = 0.0;
 #pragma unroll
-        for (int b = 0; b < 3; b++)
-            if (k[a][b]) {
-                mx = __dadd_rn(mx, px[a]);
-                my = __dadd_rn(my, py[b]);
-                mz = __dadd_rn(mz, hz[a][b]);
-                n++;
-            }
-    const double dn = (double)n;
-    mx = __ddiv_rn(mx, dn);
-    my = __ddiv_rn(my, dn);
-    mz = __ddiv_rn(mz, dn);
-    double dx[3], dy[3], dxx[3], dyy[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        dx[a] = __dsub_rn(px[a], mx);
-        dy[a] = __dsub_rn(py[a], my);
-        dxx[a] = __dmul_rn(dx[a], dx[a]);
-        dyy[a] = __dmul_rn(dy[a], dy[a]);
+    for (int j = 0; j < 9; j++) {
+        const double tsq = __shfl_sync(kFull, dd, g == 0 ? j / 3 : 3 + j % 3, 8);  // dx[a]^2 (lane 0), dy[b]^2 (lane 3)
+        double txy, txz, tyz;
+        if (j < 8) {
+            txy = __shfl_sync(kFull, pxy, j, 8);
+            txz = __shfl_sync(kFull, pxz, j, 8);
+            tyz = __shfl_sync(kFull, pyz, j, 8);
+        } else {
+            txy = txz = tyz = __shfl_sync(kFull, p8, g == 1 ? 0 : g == 2 ? 1 : 2, 8);
+        }
+        const double term = (g == 0 || g == 3) ? tsq : g == 1 ? txy : g == 2 ? txz : tyz;
+        if ((km >> j) & 1u) s = __dadd_rn(s, term);
     }
-    double sxx = 0.0, sxy = 0.0, sxz = 0.0, syy = 0.0, syz = 0.0;
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int b = 0; b < 3; b++)
-            if (k[a][b]) {
-                const double dz = __dsub_rn(hz[a][b], mz);
-                hz[a][b] = dz;  // kept for the residuals
-                sxx = __dadd_rn(sxx, dxx[a]);
-                sxy = __dadd_rn(sxy, __dmul_rn(dx[a], dy[b]));
-                sxz = __dadd_rn(sxz, __dmul_rn(dx[a], dz));
-                syy = __dadd_rn(syy, dyy[b]);
-                syz = __dadd_rn(syz, __dmul_rn(dy[b], dz));
-            }
-    const double det = __dsub_rn(__dmul_rn(sxx, syy), __dmul_rn(sxy, sxy));
-    if (det == 0.0) return;
-    double a0 = __ddiv_rn(__dsub_rn(__dmul_rn(syy, sxz), __dmul_rn(sxy, syz)), det);
-    double a1 = __ddiv_rn(__dsub_rn(__dmul_rn(sxx, syz), __dmul_rn(sxy, sxz)), det);
-    const double m = sqrt(__dadd_rn(__dadd_rn(__dmul_rn(a0, a0), __dmul_rn(a1, a1)), 1.0));
-    a0 = __ddiv_rn(a0, m);
-    a1 = __ddiv_rn(a1, m);
-    double ax[3], ay[3];
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        ax[a] = __dmul_rn(a0, dx[a]);
-        ay[a] = __dmul_rn(a1, dy[a]);
-    }
+    const double sxx = __shfl_sync(kFull, s, 0, 8), sxy = __shfl_sync(kFull, s, 1, 8);
+    const double sxz = __shfl_sync(kFull, s, 2, 8), syy = __shfl_sync(kFull, s, 3, 8);
+    const double syz = __shfl_sync(kFull, s, 4, 8);
+    // det = sxx syy - sxy sxy, a0 = (syy sxz - sxy syz) / det, a1 = (sxx syz - sxy sxz) / det:
+    // the six products on lanes 0-5, the three differences on lanes 0-2
+    const double fa = g == 0 ? sxx : g == 2 ? syy : g == 4 ? sxx : sxy;
+    const double fb = g == 0 ? syy : g == 1 ? sxy : g == 2 ? sxz : g == 3 ? syz : g == 4 ? syz : sxz;
+    const double pr = __dmul_rn(fa, fb);
+    const double r = __dsub_rn(__shfl_sync(kFull, pr, (2 * g) & 7, 8), __shfl_sync(kFull, pr, (2 * g + 1) & 7, 8));
+    const double det = __shfl_sync(kFull, r, 0, 8);
+    const bool singular = ((unsigned long long)__double_as_longlong(det) << 1) == 0;  // det == 0
+    const double a = __ddiv_rn(r, singular ? 1.0 : det);  // lane 1 a0, lane 2 a1
+    const double asq = __dmul_rn(a, a);
+    const double m = sqrt(__dadd_rn(__dadd_rn(__shfl_sync(kFull, asq, 1, 8), __shfl_sync(kFull, asq, 2, 8)), 1.0));
+    const double an = __ddiv_rn(a, m);  // lane 1 a0 / m, lane 2 a1 / m
+    const double a0 = __shfl_sync(kFull, an, 1, 8), a1 = __shfl_sync(kFull, an, 2, 8);
+    const double axy = __dmul_rn(g < 3 ? a0 : a1, d);  // lanes 0-2 a0 dx[a], lanes 3-5 a1 dy[b]
+    const double eg = __dsub_rn(dzg, __dadd_rn(__shfl_sync(kFull, axy, g / 3, 8), __shfl_sync(kFull, axy, 3 + g % 3, 8)));
+    const double e2g = __dmul_rn(eg, eg);
+    const double e8 = __dsub_rn(dz8, __dadd_rn(__shfl_sync(kFull, axy, 2, 8), __shfl_sync(kFull, axy, 5, 8)));
+    const double e28 = __dmul_rn(e8, e8);
     double err = 0.0;
 #pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int b = 0; b < 3; b++)
-            if (k[a][b]) {
-                const double e = __dsub_rn(hz[a][b], __dadd_rn(ax[a], ay[b]));
-                err = __dadd_rn(err, __dmul_rn(e, e));
-            }
-    err = __ddiv_rn(err, dn);
-    rough = rough_of(err);
-    const double im = __ddiv_rn(1.0, m);
-    slx = slope_angle(a0, m, im);
-    sly = slope_angle(a1, m, im);
+    for (int j = 0; j < 9; j++) {
+        const double t = j < 8 ? __shfl_sync(kFull, e2g, j, 8) : e28;
+        if ((km >> j) & 1u) err = __dadd_rn(err, t);
+    }
+    const double qv = __ddiv_rn(g == 0 ? err : 1.0, g == 0 ? dn : m);  // lane 0 err / n, lane 1 1 / m
+    const double im = __shfl_sync(kFull, qv, 1, 8);
+    // det == 0: the reference leaves roughness -1 and the slopes 0 (scripts/gvom.py:769-771)
+    if (singular) return g == 0 ? -1.0 : 0.0;
+    return g == 0 ? rough_of(qv) : slope_angle(g == 1 ? a0 : a1, m, im);
 }
 
 // The block has one thread per cell plus one more warp (kTY = 32: one more
@@ -844,24 +871,22 @@ __global__ void __launch_bounds__(kTX * kTY + 32) k_maps2d(const __grid_constant
     // cells that need the float64 sequence are compacted into a queue so that
     // whole warps run it, instead of one lane in every warp that has one
     __syncthreads();  // queue complete; szl / sml no longer read (qres reuses their space)
-    // the float64 queue, 32 cells per warp: each warp takes the next 32 queued
-    // cells until none are left (called with the warp converged)
+    // the float64 queue, four cells per warp pass (eight lanes each): each
+    // warp takes the next four queued cells until none are left (called with
+    // the warp converged)
     auto drain = [&]() {
         const int nq = qn, lane = tid & 31;
         while (true) {
             int base = 0;
-            if (lane == 0) base = atomicAdd(&qtake, 32);
+            if (lane == 0) base = atomicAdd(&qtake, 4);
             base = __shfl_sync(0xffffffffu, base, 0);
             if (base >= nq) break;
-            const int q = base + lane;
-            if (q < nq) {
-                const int t = qcell[q];
-                double r = -1.0, a = 0.0, b = 0.0;
-                slope_f64<kSY>(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, X, mp.xy_res, r, a, b);
-                qres[t][0] = r;
-                qres[t][1] = a;
-                qres[t][2] = b;
-            }
+            const int q = base + (lane >> 3);
+            const bool act = q < nq;
+            const int t = act ? qcell[q] : 0;
+            const double v = slope_f64_group<kSY>(sh, kn, x0t, y0t, x0t + t / kTY, y0t + t % kTY, act, X, mp.xy_res,
+                                                  lane & 7);
+            if (act && (lane & 7) < 3) qres[t][lane & 7] = v;
             __syncwarp();
         }
     };

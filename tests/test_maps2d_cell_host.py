@@ -1,6 +1,7 @@
 """k_maps2d's slope and roughness path for every cell (gvom_gb300/csrc/
 k_combine.cu: the float32 plane fit with its rules, the two closed forms,
-and the float64 sequence for the cells the rules queue, with the kernel's
+and the float64 sequence for the cells the rules queue (its eight lanes
+emulated), with the kernel's
 float32 log / atan2), compiled for the host from the kernel source with the
 whole map as one tile, against the oracle's float64 maps on every golden
 fixture, at the parity tolerance (1e-3 relative)."""
@@ -62,7 +63,13 @@ extern "C" int cells_all(const double *H, const int *zlow, const float *mlow, in
             int qn = 0;
 %(cell)s
             if (need_exact) {
-                slope_f64<kS>(sh, kn, x0t, y0t, x0, y0, X, mp.xy_res, rough, slx, sly);
+                double out[8];
+                if (!run_group([&](int g) { return slope_f64_group<kS>(sh, kn, x0t, y0t, x0, y0, true, X, mp.xy_res, g); },
+                               out))
+                    return 2;
+                rough = out[0];
+                slx = out[1];
+                sly = out[2];
                 ++*queued;
             }
             (void)qcell;
@@ -83,7 +90,7 @@ def cell_lib(tmp_path_factory):
     d = tmp_path_factory.mktemp("cells")
     cpp = d / "cells_host.cpp"
     cpp.write_text("#include <algorithm>\n#include <cmath>\nusing std::max; using std::min;\n"
-                   '#include "cuda_runtime.h"\n' + helpers + DRIVER % {"cell": cell})
+                   '#include "cuda_runtime.h"\n#include "group_lanes.h"\n' + helpers + DRIVER % {"cell": cell})
     so = d / "libcells.so"
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
                     "-I", os.path.join(HERE, "cpp", "host_cuda"), "-o", str(so), str(cpp)], check=True)

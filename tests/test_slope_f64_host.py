@@ -1,11 +1,13 @@
-"""The float64 plane-fit sequence of k_maps2d (`slope_f64` in
+"""The float64 plane-fit sequence of k_maps2d (`slope_f64_group` in
 gvom_gb300/csrc/k_combine.cu, the path of the cells whose float32 fit cannot
-be trusted), compiled for the host from the kernel source and run on every
-cell of every golden fixture's height maps: its roughness and slopes must
-equal the oracle's __calculate_slope (scripts/gvom.py:717-805) bit for bit.
-The device code uses only correctly rounded float64 operations (no
-contraction), so the host build performs the same arithmetic; only the
-final log / atan2 is taken from the host's libm here, as the oracle does."""
+be trusted; eight lanes per cell), compiled for the host from the kernel
+source with its eight lanes emulated (tests/cpp/host_cuda/group_lanes.h),
+and run on every cell of every golden fixture's height maps: its roughness
+and slopes must equal the oracle's __calculate_slope (scripts/gvom.py:
+717-805) bit for bit.  The device code uses only correctly rounded float64
+operations (no contraction), so the host build performs the same
+arithmetic; only the final log / atan2 is taken from the host's libm here,
+as the oracle does."""
 import ctypes as C
 import os
 import shutil
@@ -24,9 +26,13 @@ KERNEL = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc", "k_combine.cu
 PRELUDE = r"""
 #include <algorithm>
 #include <cmath>
+#include "group_lanes.h"
 using std::max; using std::min; using std::sqrt;
 #define __device__
 #define __forceinline__ inline
+static inline long long __double_as_longlong(double d) { long long b; std::memcpy(&b, &d, 8); return b; }
+static inline double __longlong_as_double(long long b) { double d; std::memcpy(&d, &b, 8); return d; }
+static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
 #define __dadd_rn(a, b) ((double)(a) + (double)(b))
 #define __dsub_rn(a, b) ((double)(a) - (double)(b))
 #define __dmul_rn(a, b) ((double)(a) * (double)(b))
@@ -55,7 +61,14 @@ extern "C" int slope_all(const double *H, int X, double res, double *rough, doub
             int n = 0;
             for (int x = std::max(0, x0 - 1); x < std::min(X, x0 + 2); x++)
                 for (int y = std::max(0, y0 - 1); y < std::min(X, y0 + 2); y++) n += kn[x + kHalo][y + kHalo];
-            if (n >= 3) slope_f64<kS>(sh, kn, 0, 0, x0, y0, X, res, r, a, b);
+            if (n >= 3) {
+                double out[8];
+                if (!run_group([&](int g) { return slope_f64_group<kS>(sh, kn, 0, 0, x0, y0, true, X, res, g); }, out))
+                    return 2;
+                r = out[0];
+                a = out[1];
+                b = out[2];
+            }
             rough[x0 * X + y0] = r;
             sx[x0 * X + y0] = a;
             sy[x0 * X + y0] = b;
@@ -66,10 +79,13 @@ extern "C" int slope_all(const double *H, int X, double res, double *rough, doub
 
 
 def _kernel_slope_source():
+    """The kernel's widen helper and its eight-lane float64 sequence."""
     src = open(KERNEL).read()
-    a = src.index("template <int kSY>\n__device__ __forceinline__ void slope_f64")
+    w = src.index("__device__ __forceinline__ double widen(float f) {")
+    w_end = src.index("\n}\n", w) + 3
+    a = src.index("template <int kSY>\n__device__ __forceinline__ double slope_f64_group")
     b = src.index("template <int kTX, int kTY>", a)
-    return src[a:b]
+    return src[w:w_end] + src[a:b]
 
 
 def _halo():
@@ -89,8 +105,8 @@ def slope_lib(tmp_path_factory):
     cpp = d / "slope_f64_host.cpp"
     cpp.write_text(PRELUDE % {"halo": _halo()} + _kernel_slope_source() + DRIVER)
     so = d / "libslope.so"
-    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-o", str(so), str(cpp)],
-                   check=True)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+                    "-I", os.path.join(HERE, "cpp", "host_cuda"), "-o", str(so), str(cpp)], check=True)
     lib = C.CDLL(str(so))
     P = C.c_void_p
     lib.slope_all.argtypes = [P, C.c_int, C.c_double, P, P, P]
