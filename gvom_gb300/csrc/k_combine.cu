@@ -1,15 +1,17 @@
 // Map-combine kernels: Gvom.combine_maps (scripts/gvom.py:222-393).
 //
-//   k_merge    one thread per (x, y, 8-plane z chunk): merges every ring slot
-//              (slot order) and the previous combined map with their ego
-//              shifts and the clearing rule (scripts/gvom.py:1009-1063) and
-//              Chan-merges the statistics of occupied voxels
-//              (scripts/gvom.py:888-980) and solves their eigenvalues
-//              (scripts/gvom.py:1423-1487).  The combined map addresses its
-//              records by voxel id, so nothing is allocated; each thread
-//              leaves the lowest occupied / known-free z of its chunk.
-//   k_merge_stats  one thread per listed occupied voxel: statistics merge
-//              and eigenvalues
+//   k_merge    one thread per (x, y, z chunk of 4-16 planes): merges every
+//              ring slot (slot order) and the previous combined map with
+//              their ego shifts and the clearing rule (scripts/gvom.py:
+//              1009-1063) into the combined index map, addressed by voxel id
+//              so nothing is allocated; lists the occupied voxels and leaves
+//              the lowest occupied / known-free z of each chunk.
+//   k_merge_counts  one thread per listed occupied voxel: the sources' hit
+//              and total sums and lowest in-voxel height (scripts/gvom.py:
+//              888-980), all the columns pass reads
+//   k_merge_stats  one thread per listed occupied voxel: Chan merge of the
+//              statistics (scripts/gvom.py:926-980) and eigenvalues
+//              (scripts/gvom.py:1423-1487)
 //   k_columns  one thread per column: height (lowest occupied voxel or the
 //              robot disc), inferred height (lowest known-free voxel) and the
 //              positive-obstacle band density (scripts/gvom.py:515-590)
@@ -28,30 +30,38 @@
 namespace gvom {
 
 constexpr int kOcc = 0x7fffffff;
-constexpr int kOutside = INT32_MIN;
+
+// Doubles compared and widened on their bit patterns: a float64 warp
+// instruction holds this part's slow float64 pipe for as long as any other,
+// so conversions and compares stay off it.
+
+// a == b for doubles that are not NaN: equal bits, or +0 against -0
+__device__ __forceinline__ bool same_double(double a, double b) {
+    const unsigned long long x = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long y = (unsigned long long)__double_as_longlong(b);
+    return x == y || ((x | y) << 1) == 0;
+}
+
+// a signed key that orders doubles that are not NaN as < does, except that
+// -0 sorts below +0
+__device__ __forceinline__ long long double_order(double a) {
+    const long long b = __double_as_longlong(a);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
+// (double)f: a normal float's bits moved into place (exponent rebiased by
+// 1023 - 127); zero, subnormals, inf and NaN take the conversion instruction
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu;
+    if (e == 0u || e == 0xffu) return (double)f;
+    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
+                                            ((unsigned long long)(e + 896u) << 52) |
+                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
 
 // ---------------------------------------------------------------------------
 // k_merge
 // ---------------------------------------------------------------------------
-template <int NSRC>
-struct SrcVals {
-    int v[NSRC];
-};
-
-template <int NSRC>
-__device__ __forceinline__ void merge_load_plane(const MergeParams &mp, int x, int y, int z, bool col, int (&v)[NSRC]) {
-    const int X = mp.g.X, Z = mp.g.Z;
-#pragma unroll
-    for (int s = 0; s < NSRC; s++) {
-        v[s] = kOutside;
-        if (s < mp.nsrc && col && z < Z) {
-            const int xs = x + mp.src[s].dx, ys = y + mp.src[s].dy, zs = z + mp.src[s].dz;
-            if ((unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X && (unsigned)zs < (unsigned)Z)
-                v[s] = __ldg(&mp.src[s].idx[xs + ys * X + zs * X * X]);
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // eigenvalues (scripts/gvom.py:1423-1487): cyclic Jacobi in float32, which is
 // backward stable -- every eigenvalue, and the gap between nearly equal ones
@@ -236,14 +246,24 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
     const bool col = x < X && y < X;
     const int plane = X * X;
     if (tid == 0) qn = 0;
-    // index merge, source by source in source order (scripts/gvom.py:242-298):
-    // a source's kZC loads are independent, and the state per plane is one int.
-    // Entries outside a shifted source read as -1, which changes nothing: only
-    // an occupied entry (>= 0) or a free one (<= -2) acts, and only on a
-    // combined value that is not occupied yet (<= -1).
-    int cmb[kZC];
+    // index merge, source by source in source order (scripts/gvom.py:242-298).
+    // The reference's state per plane, c, is -1 (unknown), a pass count <= -2
+    // (free) or occupied: a source's occupied entry (>= 0) makes c occupied,
+    // a free entry o (<= -2) adds o + 1, and neither acts once c is occupied.
+    // A ring slot's step is held here as two ints: occ, the AND of the
+    // entries merged so far (its sign bit clears once an entry was >= 0), and
+    // cnt = -1 + the sum of min(o, -1) + 1 over them (o = -1 and o >= 0 add
+    // nothing).  While no entry was occupied c = cnt, and an occupied c
+    // becomes the voxel id whatever cnt holds -- the same result in three
+    // integer operations per entry.  Entries outside a shifted source read as
+    // -1, which changes neither.  The previous combined map applies its
+    // clearing rule on c itself.  A source's kZC loads are independent.
+    int occ[kZC], cnt[kZC];
 #pragma unroll
-    for (int k = 0; k < kZC; k++) cmb[k] = -1;
+    for (int k = 0; k < kZC; k++) {
+        occ[k] = -1;
+        cnt[k] = -1;
+    }
 #pragma unroll
     for (int s = 0; s < NSRC; s++) {
         if (s >= mp.nsrc) break;
@@ -254,25 +274,36 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
         const int klo = max(0, -(z0 + src.dz)), khi = min(min(kZC, Z - z0), Z - z0 - src.dz);
         const int *colp = src.idx + xs + ys * X;
         int vs[kZC];
+        if (klo == 0 && khi == kZC) {  // the whole chunk inside the shifted source (same for the whole block)
 #pragma unroll
-        for (int k = 0; k < kZC; k++)
-            vs[k] = (k >= klo && k < khi) ? __ldg(colp + (z0 + k + src.dz) * plane) : -1;
+            for (int k = 0; k < kZC; k++) vs[k] = __ldg(colp + (z0 + k + src.dz) * plane);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kZC; k++)
+                vs[k] = (k >= klo && k < khi) ? __ldg(colp + (z0 + k + src.dz) * plane) : -1;
+        }
         if (src.is_last) {
             // previous combined map: an occupied voxel comes back only if at most
             // 10 new rays passed through it (scripts/gvom.py:1058)
 #pragma unroll
             for (int k = 0; k < kZC; k++) {
-                const int o = vs[k], c = cmb[k];
-                if (c <= -1) cmb[k] = (o >= 0) ? (c >= -11 ? kOcc : c) : (o < -1 ? c + o + 1 : c);
+                const int o = vs[k];
+                int c = occ[k] >= 0 ? kOcc : cnt[k];
+                if (c <= -1) c = (o >= 0) ? (c >= -11 ? kOcc : c) : (o < -1 ? c + o + 1 : c);
+                occ[k] = c == kOcc ? 0 : -1;
+                cnt[k] = c;
             }
         } else {
 #pragma unroll
             for (int k = 0; k < kZC; k++) {
-                const int o = vs[k], c = cmb[k];
-                if (c <= -1) cmb[k] = (o >= 0) ? kOcc : (o < -1 ? c + o + 1 : c);
+                occ[k] &= vs[k];
+                cnt[k] += min(vs[k], -1) + 1;
             }
         }
     }
+    int cmb[kZC];  // c: kOcc or the pass count
+#pragma unroll
+    for (int k = 0; k < kZC; k++) cmb[k] = occ[k] >= 0 ? kOcc : cnt[k];
     __syncthreads();
     int occ_z = Z, free_z = Z;
 #pragma unroll
@@ -352,7 +383,7 @@ __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnP
     if (occ_z < Z) {
         // lowest occupied voxel -> height (scripts/gvom.py:572-576)
         const float minh = cp.rec[x + y * X + occ_z * plane].min_h;
-        h = __dmul_rn(__dadd_rn(__dadd_rn((double)minh, (double)occ_z), cp.co[2]), cp.z_res);
+        h = __dmul_rn(__dadd_rn(__dadd_rn(widen(minh), widen((float)occ_z)), cp.co[2]), cp.z_res);
         zl = occ_z;
         ml = minh;
         // positive-obstacle band (scripts/gvom.py:529-555):
@@ -391,8 +422,23 @@ __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnP
                     }
                 }
             }
-            // integer-valued float64 sums are exact, so only the final density needs float64
-            if (nn > 0) pd = (int)__dmul_rn(__ddiv_rn((double)dens, (double)nn), 100.0);
+            // (int)(dens / nn * 100.0) in float64 (integer-valued sums are exact):
+            // the two roundings move the exact value 100 dens / nn by at most
+            // 2.3e-16 of itself.  Below 2^44 a non-integer value lies at least
+            // 1 / nn from every integer, more than that, so its truncation is the
+            // integer quotient; an integer value (and a larger one) takes the
+            // float64 sequence, whose rounding can fall just below it.
+            if (nn > 0) {
+                const long long P = 100 * dens;
+                long long q = -1;
+                if (P < (1LL << 32) && nn < (1LL << 32)) {  // 32-bit division where it fits
+                    const unsigned p32 = (unsigned)P, n32 = (unsigned)nn;
+                    if (p32 % n32 != 0u) q = p32 / n32;
+                } else if (P < (1LL << 44) && P % nn != 0) {
+                    q = P / nn;
+                }
+                pd = q >= 0 ? (int)q : (int)__dmul_rn(__ddiv_rn((double)dens, (double)nn), 100.0);
+            }
         }
     } else {
         // robot disc (scripts/gvom.py:566-570): decided in float32 unless near the rim
@@ -408,7 +454,7 @@ __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnP
         }
         if (in) h = cp.disc_h;
     }
-    const double ih = free_z < Z ? __dmul_rn(__dadd_rn((double)free_z, cp.co[2]), cp.z_res) : -1000.0;
+    const double ih = free_z < Z ? __dmul_rn(__dadd_rn(widen((float)free_z), cp.co[2]), cp.z_res) : -1000.0;
     const int m2d = x * X + y;
     cp.height[m2d] = h;
     cp.inferred[m2d] = ih;
@@ -437,34 +483,6 @@ constexpr long long kMinus1000Bits = (long long)0xC08F400000000000ULL;  // -1000
 __device__ __forceinline__ bool height_known(double h) {
     const long long b = __double_as_longlong(h);
     return b >= 0 || (b & 0x7fffffffffffffffLL) < 0x408F400000000000LL;  // |h| < 1000
-}
-
-// The cell threads compare and widen doubles on their bit patterns: a
-// float64 instruction holds this part's slow float64 pipe as long as a
-// float64 plane fit step of the queue, which the same pipe runs.
-
-// a == b for doubles that are not NaN: equal bits, or +0 against -0
-__device__ __forceinline__ bool same_double(double a, double b) {
-    const unsigned long long x = (unsigned long long)__double_as_longlong(a);
-    const unsigned long long y = (unsigned long long)__double_as_longlong(b);
-    return x == y || ((x | y) << 1) == 0;
-}
-
-// a signed key that orders doubles that are not NaN as < does, except that
-// -0 sorts below +0
-__device__ __forceinline__ long long double_order(double a) {
-    const long long b = __double_as_longlong(a);
-    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-}
-
-// (double)f: a normal float's bits moved into place (exponent rebiased by
-// 1023 - 127); zero, subnormals, inf and NaN take the conversion instruction
-__device__ __forceinline__ double widen(float f) {
-    const unsigned u = __float_as_uint(f), e = (u >> 23) & 0xffu;
-    if (e == 0u || e == 0xffu) return (double)f;
-    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) |
-                                            ((unsigned long long)(e + 896u) << 52) |
-                                            ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
 // atan2(a, im) with im = RN(1/m), m = sqrt(a0^2 + a1^2 + 1) >= 1: atan2f of

@@ -79,13 +79,16 @@ def columns_lib(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     src = open(os.path.join(CSRC, "k_combine.cu")).read()
+    h0 = src.index("// Doubles compared and widened on their bit patterns")
+    h1 = src.index("\n}\n", src.index("__device__ __forceinline__ double widen(float f) {", h0)) + 3
     a = src.index("__device__ __forceinline__ bool near_integer(")
     k = src.index("__global__ void __launch_bounds__(256) k_columns(")
     b = src.index("\n}\n", k) + 3
     d = tmp_path_factory.mktemp("columns")
     cpp = d / "columns_host.cpp"
     cpp.write_text("#include <algorithm>\n#include <cmath>\nusing std::floor; using std::fabs;\n"
-                   '#include "gvom_internal.cuh"\nnamespace gvom {\n' + src[a:b] + "}\n" + DRIVER % {"planes": PLANES})
+                   '#include "gvom_internal.cuh"\nnamespace gvom {\n' + src[h0:h1] + src[a:b] + "}\n" +
+                   DRIVER % {"planes": PLANES})
     so = d / "libcolumns.so"
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I",
                     os.path.join(HERE, "cpp", "host_cuda"), "-I", CSRC, "-o", str(so), str(cpp)], check=True)

@@ -23,9 +23,11 @@ CSRC = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc")
 
 def _kernel_parts():
     src = open(os.path.join(CSRC, "k_combine.cu")).read()
+    h0 = src.index("// Doubles compared and widened on their bit patterns")
+    h1 = src.index("\n}\n", src.index("__device__ __forceinline__ double widen(float f) {", h0)) + 3
     a = src.index("constexpr int kHalo = ")
     b = src.index("template <int kTX, int kTY>", a)
-    helpers = src[a:b]
+    helpers = src[h0:h1] + src[a:b]
     c = src.index("    double rough = -1.0, slx = 0.0, sly = 0.0;\n")
     d = src.index("    // cells that need the float64 sequence are compacted", c)
     return helpers, src[c:d]

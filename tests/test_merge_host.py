@@ -23,16 +23,9 @@ KZC = 16  # z planes per thread
 def _kernel_merge_block():
     src = open(os.path.join(CSRC, "k_combine.cu")).read()
     k = src.index("__global__ void __launch_bounds__(256) k_merge(")
-    a = src.index("    int cmb[kZC];", k)
-    loop = src.index("    for (int s = 0; s < NSRC; s++) {", a)
-    i = src.index("{", loop)
-    depth = 0
-    for j in range(i, len(src)):
-        depth += src[j] == "{"
-        depth -= src[j] == "}"
-        if depth == 0:
-            return src[a:j + 1]
-    raise AssertionError("unbalanced braces")
+    a = src.index("    int occ[kZC], cnt[kZC];", k)
+    end = "    for (int k = 0; k < kZC; k++) cmb[k] = occ[k] >= 0 ? kOcc : cnt[k];\n"
+    return src[a:src.index(end, a) + len(end)]
 
 
 DRIVER = r"""
