@@ -158,6 +158,9 @@ int fail(int code, const std::string &msg) {
     return code;
 }
 
+// combine_maps' four outputs, one block on the device (see gvom_create)
+constexpr size_t kOutBytesPerCell = 8 + 3 * 4;  // roughness (f64), positive, negative, visibility (i32)
+
 #define CUDA_TRY(expr)                                                                         \
     do {                                                                                       \
         cudaError_t e__ = (expr);                                                              \
@@ -329,12 +332,17 @@ struct GvomHandle {
     // the parameters of each later call (see Recorder)
     bool graphs = false;
     // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ the combine
-    // at level 1), [5] its columns and maps, [6] its count and statistics merges (level 2), [7] its index
-    // merge (level 2)
-    GraphNodes gn[8];
+    // at level 1), [5] its columns and maps, [6] its count merge (level 2), [7] its index merge (level 2),
+    // [8] its statistics merge (level 2)
+    GraphNodes gn[9];
     // a step forks the index merge onto `side` once the index maps are done
+    // (ev_idx), and the count merge once the records' hit, total and min
+    // height are (ev_mom, after the cell moments)
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_idx = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_idx = nullptr, ev_mom = nullptr, ev_join = nullptr;
+    // the last call was a process that recorded ev_idx and ev_mom, so a
+    // combine that follows may overlap its tail
+    bool proc_events = false;
     // step pipeline (Tuning::step_pipeline): a step stages its points and
     // runs k_voxelize_trace on `tr` as soon as the process call that last used
     // its scratch set (the one before the previous call) is done with it
@@ -765,7 +773,7 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl,
 // call in two.  The trace part first fills the slots' index maps with -1
 // (unknown): the trace counts pass-throughs down from there.
 int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bool timing, int part = 0,
-                 cudaStream_t st = nullptr, bool assign_external = false) {
+                 cudaStream_t st = nullptr, bool external = false, cudaEvent_t after_moments = nullptr) {
     if (!st) st = h->st;
     ScanCounters *ctr = h->d_ctr + pl.set * kMaxBatch;
     if (part == 0 || part == 1) {
@@ -775,7 +783,7 @@ int launch_scans(GvomHandle *h, const ProcPlan &pl, cudaEvent_t after_assign, bo
     }
     CUDA_TRY(launch_process(pl.pc, pl.table, pl.k, pl.block, pl.max_n, pl.dtype, h->prec[pl.set], h->prank[pl.set], h->sorted,
                             h->moments, st, (timing && !part) ? h->timer.begin(0, kProcessKernels) : nullptr,
-                            h->tun.pts_block, after_assign, part, assign_external));
+                            h->tun.pts_block, after_assign, after_moments, part, external));
     if (part == 1) return GVOM_OK;
     for (int i = 0; i < pl.k; i++)
         CUDA_TRY(rec_memcpy(h->d_slotC + pl.slot_of[i], &ctr[i].C, sizeof(int), cudaMemcpyDeviceToDevice, st));
@@ -805,13 +813,20 @@ int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
     int rc = prepare_scans(h, scans, pl);
     if (rc) return rc;
     if (!rc) rc = wait_slots_free(h, pl.slot_of, pl.k, h->st);
-    if (!rc) rc = run_graphed(h, 0, [&]() -> int { return launch_scans(h, pl, nullptr, !h->graphs); });
+    // events for a combine that follows (see combine_impl)
+    const bool events = h->tun.step_overlap && !h->timer.on;
+    if (!rc)
+        rc = run_graphed(h, 0, [&]() -> int {
+            return launch_scans(h, pl, events ? h->ev_idx : nullptr, !h->graphs, 0, nullptr, true,
+                                events ? h->ev_mom : nullptr);
+        });
     if (rc) {
         release_slots(h, pl);
         return rc;
     }
     CUDA_TRY(cudaEventRecord(h->ev_scratch[pl.set], h->st));  // a later pipelined trace may reuse the set
     commit_scans(h, pl);
+    h->proc_events = events;
     return GVOM_OK;
 }
 
@@ -921,6 +936,7 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         cudaEventCreateWithFlags(&h->ev_cols[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_cols[1], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_idx, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_mom, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_scratch[0], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->ev_scratch[1], cudaEventDisableTiming) != cudaSuccess ||
@@ -953,12 +969,19 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         return bail(rc);
     if ((rc = dalloc_t(h, &h->d_slotC, (size_t)kMaxPhysSlots))) return bail(rc);
     if ((rc = dalloc_t(h, &h->d_combC, 4))) return bail(rc);
-    double **maps[6] = {&h->height, &h->inferred, &h->slope_x, &h->slope_y, &h->rough, &h->guess};
+    double **maps[5] = {&h->height, &h->inferred, &h->slope_x, &h->slope_y, &h->guess};
     for (auto m : maps)
         if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
-    int **imaps[5] = {&h->pos_density, &h->pos, &h->neg, &h->vis, &h->zlow};
+    int **imaps[2] = {&h->pos_density, &h->zlow};
     for (auto m : imaps)
         if ((rc = dalloc_t(h, m, (size_t)X2))) return bail(rc);
+    // combine_maps' four outputs in one block, roughness | positive | negative |
+    // visibility (kOutBytesPerCell bytes a cell), so that a caller whose host
+    // buffers follow the same layout gets them in one copy
+    if ((rc = dalloc(h, reinterpret_cast<void **>(&h->rough), (size_t)X2 * kOutBytesPerCell))) return bail(rc);
+    h->pos = reinterpret_cast<int *>(h->rough + X2);
+    h->neg = h->pos + X2;
+    h->vis = h->neg + X2;
     if ((rc = dalloc_t(h, &h->mlow, (size_t)X2))) return bail(rc);
     for (int b = 0; b < 2; b++)  // chunks of >= 4 planes
         if ((rc = dalloc_t(h, &h->colinfo[b], (size_t)X2 * ((g.Z + 3) / 4)))) return bail(rc);
@@ -1000,6 +1023,7 @@ int gvom_destroy(GvomHandle *h) {
                           h->ev_stats[1]})
         if (e) cudaEventDestroy(e);
     if (h->ev_idx) cudaEventDestroy(h->ev_idx);
+    if (h->ev_mom) cudaEventDestroy(h->ev_mom);
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     for (cudaEvent_t e : h->ev_scratch)
         if (e) cudaEventDestroy(e);
@@ -1029,12 +1053,9 @@ int gvom_destroy(GvomHandle *h) {
     cudaFree(h->inferred);
     cudaFree(h->slope_x);
     cudaFree(h->slope_y);
-    cudaFree(h->rough);
+    cudaFree(h->rough);  // also the positive, negative and visibility maps
     cudaFree(h->guess);
     cudaFree(h->pos_density);
-    cudaFree(h->pos);
-    cudaFree(h->neg);
-    cudaFree(h->vis);
     cudaFree(h->zlow);
     cudaFree(h->mlow);
     cudaFree(h->colinfo[0]);
@@ -1324,20 +1345,21 @@ int prepare_combine(GvomHandle *h, CombPlan &pl) {
     return GVOM_OK;
 }
 
-// stream-ordered work of a prepared combine on h->st.  With `idx_ready`, the
-// index merge runs on the side stream as soon as that event (recorded when
-// the ring's index maps are complete) has fired, overlapping the rest of the
-// process kernels, and joins back before the statistics merge.
-// `part`: 0 the whole combine on h->st; 1 the merge and merge_stats on `st`;
-// 2 columns and maps on h->st, with ev_cols[buffer] recorded between them
-// `part`: 0 the whole combine on h->st (the index merge on `side` after
-// `idx_ready` when given; the statistics merge forked onto `side` after the
-// count merge, beside the columns and maps, and joined at the end); 1 the
-// index and count merges on `st`; 2 columns and maps on h->st, with
-// ev_cols[buffer] recorded between them.  With `timing` every kernel runs in
-// sequence on h->st.
+// stream-ordered work of a prepared combine on h->st.
+// `part`: 0 the whole combine (below); 1 the index and count merges on `st`;
+// 2 columns and maps on h->st, with ev_cols[buffer] recorded between them.
+// part 0: with `timing`, every kernel in sequence on h->st.  Without events,
+// the index and count merges on `st`, then the statistics merge forked onto
+// `side` beside the columns and maps, joined at the end.  With `idx_ready`
+// (recorded once the ring's index maps are complete) the index merge runs on
+// `side` after that event, overlapping the rest of the process kernels.  With
+// `mom_ready` too (recorded once the slots' records hold hit, total and min
+// height, after the cell moments), `side` goes on with the count merge, the
+// columns and the maps after that event, while h->st, after the process
+// tail (neighbourhood statistics, clean-up), runs the statistics merge; h->st
+// joins `side` at the end.
 int launch_comb(GvomHandle *h, const CombPlan &pl, cudaEvent_t idx_ready, bool timing, int part = 0,
-                cudaStream_t st = nullptr) {
+                cudaStream_t st = nullptr, cudaEvent_t mom_ready = nullptr) {
     if (!st) st = h->st;
     if (part == 2) {
         CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 2));
@@ -1348,6 +1370,21 @@ int launch_comb(GvomHandle *h, const CombPlan &pl, cudaEvent_t idx_ready, bool t
     if (timing) {
         CUDA_TRY(rec_memset(pl.mp.out_count, 0, sizeof(int), h->st));
         CUDA_TRY(launch_combine(pl.mp, pl.cp, pl.m2, h->st, h->timer.begin(kProcessKernels, kCombineKernels)));
+        return GVOM_OK;
+    }
+    if (idx_ready && mom_ready && part == 0) {
+        CUDA_TRY(rec_wait_internal(h->side, idx_ready));
+        CUDA_TRY(rec_memset(pl.mp.out_count, 0, sizeof(int), h->side));
+        CUDA_TRY(launch_merge_index(pl.mp, h->side));
+        CUDA_TRY(rec_event_internal(h->ev_join, h->side));
+        CUDA_TRY(rec_wait_internal(h->side, mom_ready));
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->side, nullptr, 1));
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->side, nullptr, 2));
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->side, nullptr, 3));
+        CUDA_TRY(rec_event_internal(h->ev_msj, h->side));
+        CUDA_TRY(rec_wait_internal(h->st, h->ev_join));
+        CUDA_TRY(launch_combine_rest(pl.mp, pl.cp, pl.m2, h->st, nullptr, 4));
+        CUDA_TRY(rec_wait_internal(h->st, h->ev_msj));
         return GVOM_OK;
     }
     if (idx_ready) {
@@ -1381,6 +1418,15 @@ void commit_combine(GvomHandle *h, const CombPlan &pl) {
     h->have_maps = true;
 }
 
+// the caller's four buffers laid out as the device block: roughness, then
+// positive, negative and visibility, back to back
+static bool outputs_in_block(size_t X2, const int32_t *pos, const int32_t *neg, const double *rough,
+                             const int32_t *vis) {
+    if (!pos || !neg || !rough || !vis) return false;
+    const char *r = reinterpret_cast<const char *>(rough);
+    return reinterpret_cast<const char *>(pos) == r + X2 * 8 && neg == pos + X2 && vis == neg + X2;
+}
+
 // origin (scripts/gvom.py:385-388) and the four maps to host or device buffers
 int copy_outputs(GvomHandle *h, const CombPlan &pl, double origin[3], int32_t *pos, int32_t *neg, double *rough,
                  int32_t *vis, bool to_host) {
@@ -1391,6 +1437,11 @@ int copy_outputs(GvomHandle *h, const CombPlan &pl, double origin[3], int32_t *p
     }
     const size_t X2 = (size_t)h->g.X * h->g.X;
     const cudaMemcpyKind kind = to_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (outputs_in_block(X2, pos, neg, rough, vis)) {
+        CUDA_TRY(cudaMemcpyAsync(rough, h->rough, X2 * kOutBytesPerCell, kind, h->st));
+        if (to_host) CUDA_TRY(cudaStreamSynchronize(h->st));
+        return GVOM_OK;
+    }
     if (pos) CUDA_TRY(cudaMemcpyAsync(pos, h->pos, X2 * 4, kind, h->st));
     if (neg) CUDA_TRY(cudaMemcpyAsync(neg, h->neg, X2 * 4, kind, h->st));
     if (rough) CUDA_TRY(cudaMemcpyAsync(rough, h->rough, X2 * 8, kind, h->st));
@@ -1403,6 +1454,10 @@ int copy_outputs(GvomHandle *h, const CombPlan &pl, double origin[3], int32_t *p
 // part of the sequence (graph) that computes them
 static int enqueue_device_outputs(GvomHandle *h, int32_t *pos, int32_t *neg, double *rough, int32_t *vis) {
     const size_t X2 = (size_t)h->g.X * h->g.X;
+    if (outputs_in_block(X2, pos, neg, rough, vis)) {
+        CUDA_TRY(rec_memcpy(rough, h->rough, X2 * kOutBytesPerCell, cudaMemcpyDeviceToDevice, h->st));
+        return GVOM_OK;
+    }
     if (pos) CUDA_TRY(rec_memcpy(pos, h->pos, X2 * 4, cudaMemcpyDeviceToDevice, h->st));
     if (neg) CUDA_TRY(rec_memcpy(neg, h->neg, X2 * 4, cudaMemcpyDeviceToDevice, h->st));
     if (rough) CUDA_TRY(rec_memcpy(rough, h->rough, X2 * 8, cudaMemcpyDeviceToDevice, h->st));
@@ -1419,7 +1474,14 @@ static int combine_impl(GvomHandle *h, double origin[3], int32_t *pos, int32_t *
     CombPlan pl;
     int rc = prepare_combine(h, pl);
     if (rc) return rc;
-    rc = run_graphed(h, 1, [&]() -> int { return launch_comb(h, pl, nullptr, !h->graphs); });
+    // right after a process call: its index merge starts once the index maps
+    // are complete and its count merge, columns and maps once the cell moments
+    // are, beside the process tail (direct launches: the waits name the
+    // process call's events)
+    const bool overlap = h->proc_events && h->tun.step_overlap && !h->timer.on;
+    h->proc_events = false;
+    if (overlap) rc = launch_comb(h, pl, h->ev_idx, false, 0, nullptr, h->ev_mom);
+    else rc = run_graphed(h, 1, [&]() -> int { return launch_comb(h, pl, nullptr, !h->graphs); });
     if (rc) return rc;
     if ((rc = comb_done(h, h->st))) return rc;
     commit_combine(h, pl);
@@ -1472,6 +1534,8 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     CombPlan cp;
     if ((rc = prepare_combine(h, cp))) return rc;
     cudaEvent_t idx = (timing || !h->tun.step_overlap) ? nullptr : h->ev_idx;
+    cudaEvent_t mom = idx ? h->ev_mom : nullptr;
+    h->proc_events = false;
     if (pipe == 2) {
         // tr: the trace
         rc = run_graphed(h, 3, [&]() -> int {
@@ -1481,10 +1545,11 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         }, h->tr);
         if (rc) return rc;
         // bs: the rest of the process, after the trace; ev_idx marks the slots'
-        // index maps complete, ev_scratch[set] the whole process
+        // index maps complete, ev_mom their records' hit, total and min height,
+        // ev_scratch[set] the whole process
         CUDA_TRY(cudaStreamWaitEvent(h->bs, h->ev_traced, 0));
         rc = run_graphed(h, 4, [&]() -> int {
-            if ((rc = launch_scans(h, pp, h->ev_idx, false, 2, h->bs, true))) return rc;
+            if ((rc = launch_scans(h, pp, h->ev_idx, false, 2, h->bs, true, h->ev_mom))) return rc;
             CUDA_TRY(rec_event_external(h->ev_scratch[pp.set], h->bs));
             return GVOM_OK;
         }, h->bs);
@@ -1501,11 +1566,17 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
             return GVOM_OK;
         }, h->side);
         if (rc) return rc;
-        // the count and statistics merges once the slots' records are complete
-        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_scratch[pp.set], 0));
+        // the count merge once the slots' records hold hit, total and min
+        // height; the statistics merge once they are complete
+        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_mom, 0));
         rc = run_graphed(h, 6, [&]() -> int {
             CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->side, nullptr, 1));
             CUDA_TRY(rec_event_external(h->ev_merged, h->side));
+            return GVOM_OK;
+        }, h->side);
+        if (rc) return rc;
+        CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_scratch[pp.set], 0));
+        rc = run_graphed(h, 8, [&]() -> int {
             CUDA_TRY(launch_combine_rest(cp.mp, cp.cp, cp.m2, h->side, nullptr, 4));
             CUDA_TRY(rec_event_external(h->ev_stats[cp.nb], h->side));
             return GVOM_OK;
@@ -1532,18 +1603,18 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
         if (rc) return rc;
         CUDA_TRY(cudaStreamWaitEvent(h->st, h->ev_traced, 0));
         rc = run_graphed(h, 4, [&]() -> int {
-            if ((rc = launch_scans(h, pp, idx, false, 2))) return rc;
+            if ((rc = launch_scans(h, pp, idx, false, 2, nullptr, false, mom))) return rc;
             // in graph mode an event-record node of the graph
             CUDA_TRY(rec_event_external(h->ev_scratch[pp.set], h->st));
-            if ((rc = launch_comb(h, cp, idx, false))) return rc;
+            if ((rc = launch_comb(h, cp, idx, false, 0, nullptr, mom))) return rc;
             return dev_out ? enqueue_device_outputs(h, pos, neg, roughness, visibility) : GVOM_OK;
         });
         if (!rc) rc = comb_done(h, h->st);
     } else {
         h->st_dirty = true;
         rc = run_graphed(h, 2, [&]() -> int {
-            if ((rc = launch_scans(h, pp, idx, timing))) return rc;
-            if ((rc = launch_comb(h, cp, idx, timing))) return rc;
+            if ((rc = launch_scans(h, pp, idx, timing, 0, nullptr, false, mom))) return rc;
+            if ((rc = launch_comb(h, cp, idx, timing, 0, nullptr, mom))) return rc;
             return dev_out ? enqueue_device_outputs(h, pos, neg, roughness, visibility) : GVOM_OK;
         });
         if (!rc) CUDA_TRY(cudaEventRecord(h->ev_scratch[pp.set], h->st));

@@ -283,13 +283,15 @@ constexpr int kCombineKernels = 5;  // merge, merge_counts, merge_stats, columns
 constexpr int kCellMomBytes = 48;  // per point slot (moments stored at each cell's first slot)
 // `part`: 0 every kernel, 1 k_voxelize_trace only, 2 the kernels after it
 // (parts are launched without stage events).  `after_assign` (nullable) is
-// recorded once the slots' index maps are complete; `assign_external`: as an
-// external event (graph capture: for a wait outside the captured graph).
-// The slots' index maps must already hold -1 when the trace starts.
+// recorded once the slots' index maps are complete, `after_moments`
+// (nullable) once the slots' records hold hit, total and min height (what
+// the count merge reads); `external`: as external events (graph capture: for
+// a wait outside the captured graph).  The slots' index maps must already
+// hold -1 when the trace starts.
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part = 0,
-                           bool assign_external = false);
+                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, cudaEvent_t after_moments,
+                           int part = 0, bool external = false);
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
 cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st);
 // `part`: 0 counts, statistics, columns, maps2d in sequence; 1 the count

@@ -239,8 +239,10 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
     __shared__ int queue[256 * kZC];
     __shared__ int qn;
     const int X = mp.g.X, Z = mp.g.Z;
-    const int x = blockIdx.x * 32 + threadIdx.x;
-    const int y = blockIdx.y * 8 + threadIdx.y;
+    // a block: 256 consecutive x of one row (eight warps of 32), so that each
+    // plane of a source is read as one contiguous 1 KB segment
+    const int x = blockIdx.x * 256 + threadIdx.y * 32 + threadIdx.x;
+    const int y = blockIdx.y;
     const int z0 = blockIdx.z * kZC;
     const int tid = threadIdx.y * 32 + threadIdx.x;
     const bool col = x < X && y < X;
@@ -1170,7 +1172,7 @@ static cudaError_t launch_maps2d(const Maps2DParams &m2, cudaStream_t st) {
 template <int NSRC>
 static cudaError_t launch_merge_idx(const MergeParams &mp, cudaStream_t st) {
     const int X = mp.g.X, Z = mp.g.Z, zc = mp.planes;
-    dim3 gm((X + 31) / 32, (X + 7) / 8, (Z + zc - 1) / zc);
+    dim3 gm((X + 255) / 256, X, (Z + zc - 1) / zc);
     if (zc == 4) return rec_kernel(k_merge<NSRC, 4>, gm, dim3(32, 8), 0, st, mp);
     if (zc == 16) return rec_kernel(k_merge<NSRC, 16>, gm, dim3(32, 8), 0, st, mp);
     return rec_kernel(k_merge<NSRC, 8>, gm, dim3(32, 8), 0, st, mp);

@@ -534,11 +534,24 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
+// the record of an in-grid cell's voxel takes the cell's lowest height
+// fraction (__calculate_min_height, scripts/gvom.py:1390-1421: the points of
+// the voxel itself), so the count merge can read it before the neighbourhood
+// statistics are done
+__device__ __forceinline__ void store_min_h(const ScanDesc &sd, const Geom &g, int cell, float mh) {
+    const int XeXe = g.Xe * g.Xe, r = cell % XeXe;
+    const int bx = r % g.Xe - g.exy, by = r / g.Xe - g.exy, bz = cell / XeXe - g.ez;
+    if ((unsigned)bx < (unsigned)g.X && (unsigned)by < (unsigned)g.X && (unsigned)bz < (unsigned)g.Z) {
+        const int ci = sd.idx[bx + g.X * by + g.X * g.X * bz];  // compact index (k_assign)
+        if (ci >= 0 && ci < sd.rec_cap) sd.rec[ci].min_h = mh;
+    }
+}
+
 template <int NS>
 __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
                                                      const float4 *__restrict__ prec, const int *__restrict__ prank,
                                                      const float4 *__restrict__ sorted, CellMom *__restrict__ mom) {
-    __shared__ int hq_off[256], hq_n[256];
+    __shared__ int hq_off[256], hq_n[256], hq_cell[256];
     __shared__ int hq_count;
     const int s = find_scan(tab, pc.nscans, blockIdx.x);
     const ScanDesc &sd = tab.s[s];
@@ -546,10 +559,10 @@ __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, con
     __syncthreads();
     const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
     bool mine = false;
-    int off = 0, n = 0;
+    int off = 0, n = 0, cell = -1;
     if (i < sd.n) {
         const long long gi = sd.pt_base + i;
-        const int cell = __float_as_int(prec[gi].w);
+        cell = __float_as_int(prec[gi].w);
         if (cell >= 0 && prank[gi] == 0) {
             const unsigned long long v = sd.cnt[cell];
             off = (int)(v >> 32);
@@ -558,6 +571,7 @@ __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, con
                 const int q = atomicAdd(&hq_count, 1);
                 hq_off[q] = off;
                 hq_n[q] = n;
+                hq_cell[q] = cell;
             } else {
                 mine = true;
             }
@@ -597,6 +611,7 @@ __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, con
         o[1] = make_float4(__fsub_rn(cxx.s, cxx.c), __fsub_rn(cxy.s, cxy.c), __fsub_rn(cxz.s, cxz.c),
                            __fsub_rn(cyy.s, cyy.c));
         o[2] = make_float4(__fsub_rn(cyz.s, cyz.c), __fsub_rn(czz.s, czz.c), mh, 0.f);
+        store_min_h(sd, pc.g, cell, mh);
     }
     __syncthreads();
     // cells with many points: one warp each, lanes striding over the points with
@@ -642,6 +657,7 @@ __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, con
             o[0] = make_float4(mx, my, mz, nf);
             o[1] = make_float4(c0, c1, c2, c3);
             o[2] = make_float4(c4, c5, mh, 0.f);
+            store_min_h(sd, pc.g, hq_cell[q], mh);
         }
     }
 }
@@ -705,12 +721,12 @@ struct NbAcc {
         o.C5 = __shfl_down_sync(0xffffffffu, C5, delta);
         return o;
     }
-    __device__ __forceinline__ void store(VoxelRec *r, float mh) const {
+    // every field but hit, total (k_assign) and min_h (k_cell_moments)
+    __device__ __forceinline__ void store(VoxelRec *r) const {
         float4 *o = reinterpret_cast<float4 *>(r);
         o[0] = make_float4(__fadd_rn(m0, 0.5f), __fadd_rn(m1, 0.5f), __fadd_rn(m2, 0.5f), __fdiv_rn(C0, n));
         o[1] = make_float4(__fdiv_rn(C1, n), __fdiv_rn(C2, n), __fdiv_rn(C3, n), __fdiv_rn(C4, n));
         reinterpret_cast<float2 *>(r)[4] = make_float2(__fdiv_rn(C5, n), n);
-        r->min_h = mh;
     }
 };
 
@@ -735,7 +751,6 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
             const int c = base + (lane >> 2);
             NbAcc a;
             a.init();
-            float mh = 1.0f;
             if (c < C) {
                 const int gid = __float_as_int(sd.rec[c].aux[0]);
                 const int x = gid % g.X, y = (gid / g.X) % g.X, z = gid / (g.X * g.X);
@@ -752,7 +767,6 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
                     const int k = sub * 7 + j;
                     if (!(v[j] & 0xffffffffull)) continue;
                     const CellMom cm = M[(int)(v[j] >> 32)];
-                    if (k == 13) mh = cm.min_h;
                     a.add(cm, k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1);
                 }
             }
@@ -760,8 +774,7 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
             if (!(sub & 1)) a.merge(o);
             o = a.shfl_down(2);
             if (sub == 0) a.merge(o);
-            mh = __shfl_sync(0xffffffffu, mh, (lane & ~3) | 1);
-            if (c < C && sub == 0) a.store(&sd.rec[c], mh);
+            if (c < C && sub == 0) a.store(&sd.rec[c]);
         }
         return;
     }
@@ -772,17 +785,15 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
         const int e0 = (x + g.exy) + (y + g.exy) * g.Xe + (z + g.ez) * g.Xe * g.Xe;
         NbAcc a;
         a.init();
-        float mh = 1.0f;
         for (int dz = -g.ez; dz <= g.ez; dz++)
             for (int dy = -g.exy; dy <= g.exy; dy++)
                 for (int dx = -g.exy; dx <= g.exy; dx++) {
                     const unsigned long long v = sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe];
                     if (!(v & 0xffffffffull)) continue;
                     const CellMom cm = M[(int)(v >> 32)];
-                    if (dx == 0 && dy == 0 && dz == 0) mh = cm.min_h;
                     a.add(cm, dx, dy, dz);
                 }
-        a.store(r, mh);
+        a.store(r);
     }
 }
 
@@ -808,7 +819,7 @@ __global__ void __launch_bounds__(256) k_cleanup(const ProcessConst pc, const __
 template <int NS>
 static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int total_blocks, int max_n, int dtype,
                              float4 *prec, int *prank, float4 *sorted, CellMom *mom, cudaStream_t st, cudaEvent_t *ev,
-                             int bs, cudaEvent_t after_assign, int part, bool assign_external) {
+                             int bs, cudaEvent_t after_assign, cudaEvent_t after_moments, int part, bool external) {
     ScanTable<NS> tab;
     for (int i = 0; i < NS; i++) tab.s[i] = i < pc.nscans ? table[i] : table[0];
     if (total_blocks < 1) total_blocks = 1;
@@ -829,11 +840,12 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
         if (part == 1) return e != cudaSuccess ? e : cudaGetLastError();
     }
     chk(rec_kernel(k_assign<NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank));
-    if (after_assign) chk(assign_external ? rec_event_external(after_assign, st) : rec_event_internal(after_assign, st));
+    if (after_assign) chk(external ? rec_event_external(after_assign, st) : rec_event_internal(after_assign, st));
     mark(2);
     chk(rec_kernel(k_scatter<NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank, sorted));
     mark(3);
     chk(rec_kernel(k_cell_moments<NS>, dim3(total_blocks), dim3(bs), 0, st, pc, tab, prec, prank, sorted, mom));
+    if (after_moments) chk(external ? rec_event_external(after_moments, st) : rec_event_internal(after_moments, st));
     mark(4);
     const bool e3 = pc.g.exy == 1 && pc.g.ez == 1;  // four lanes per voxel
     const long long want = ((e3 ? 4LL : 1LL) * max_n + 255) / 256;
@@ -848,17 +860,18 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
 
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
-                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, int part, bool assign_external) {
+                           cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, cudaEvent_t after_moments, int part,
+                           bool external) {
     CellMom *mom = static_cast<CellMom *>(moments);
     if (part) ev = nullptr;
     if (nscans == 1)
         return launch_ns<1>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                            after_assign, part, assign_external);
+                            after_assign, after_moments, part, external);
     if (nscans <= 4)
         return launch_ns<4>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                            after_assign, part, assign_external);
+                            after_assign, after_moments, part, external);
     return launch_ns<kMaxBatch>(pc, table, total_blocks, max_n, dtype, prec, prank, sorted, mom, st, ev, pts_block,
-                                after_assign, part, assign_external);
+                                after_assign, after_moments, part, external);
 }
 
 }  // namespace gvom

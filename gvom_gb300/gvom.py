@@ -174,14 +174,24 @@ class Gvom:
 
     process_pointcloud = Process_pointcloud
 
+    def _output_maps(self):
+        """combine_maps' four maps (int32, int32, float64, int32; (X, X)) as
+        views of one fresh host block laid out as the library's device block
+        (roughness, positive, negative, visibility), which it then copies in
+        one transfer."""
+        X2 = self.xy_size * self.xy_size
+        blk = np.empty(20 * X2, np.uint8)
+        sh = (self.xy_size, self.xy_size)
+        rough = blk[:8 * X2].view(np.float64).reshape(sh)
+        pos = blk[8 * X2:12 * X2].view(np.int32).reshape(sh)
+        neg = blk[12 * X2:16 * X2].view(np.int32).reshape(sh)
+        vis = blk[16 * X2:].view(np.int32).reshape(sh)
+        return pos, neg, rough, vis
+
     def combine_maps(self):
         """Merge the ring and build the 2-D maps (scripts/gvom.py:222-393)."""
-        X = self.xy_size
         origin = np.zeros(3, np.float64)
-        pos = np.empty((X, X), np.int32)
-        neg = np.empty((X, X), np.int32)
-        rough = np.empty((X, X), np.float64)
-        vis = np.empty((X, X), np.int32)
+        pos, neg, rough, vis = self._output_maps()
         rc = self._l.gvom_combine(self._h, origin.ctypes.data, pos.ctypes.data, neg.ctypes.data, rough.ctypes.data,
                                   vis.ctypes.data)
         if rc == GVOM_NO_DATA:
@@ -315,11 +325,7 @@ class Gvom:
             check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, P(origin), *ptrs, 1))
             del keep
             return origin
-        X = self.xy_size
-        pos = np.empty((X, X), np.int32)
-        neg = np.empty((X, X), np.int32)
-        rough = np.empty((X, X), np.float64)
-        vis = np.empty((X, X), np.int32)
+        pos, neg, rough, vis = self._output_maps()
         check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, P(origin), P(pos), P(neg), P(rough),
                                 P(vis), 0))
         del keep

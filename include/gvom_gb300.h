@@ -110,7 +110,9 @@ int gvom_process_batch(GvomHandle *h, const GvomScan *scans, int32_t n_scans, in
 /* Replaces Gvom.combine_maps (scripts/gvom.py:222-393).  Writes the world
  * origin of the map (3 doubles) and the positive-obstacle, negative-obstacle,
  * roughness and visibility maps into host buffers.  GVOM_NO_DATA when the
- * last written slot is empty. */
+ * last written slot is empty.  Buffers laid out back to back as roughness
+ * (X*X doubles), pos, neg, visibility (X*X int32 each) -- the library's own
+ * device layout -- come down in one copy; any other layout takes four. */
 int gvom_combine(GvomHandle *h, double origin[3], int32_t *pos, int32_t *neg, double *roughness,
                  int32_t *visibility);
 

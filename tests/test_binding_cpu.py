@@ -100,7 +100,11 @@ def test_combine_maps_outputs(stub):
     out = list(_rec(stub, C.c_void_p * 5, "rec_out"))
     assert out == [origin.ctypes.data, pos.ctypes.data, neg.ctypes.data, rough.ctypes.data, vis.ctypes.data]
     for a, dt in ((pos, np.int32), (neg, np.int32), (rough, np.float64), (vis, np.int32)):
-        assert a.shape == (16, 16) and a.dtype == dt and a.flags.c_contiguous and a.flags.owndata
+        assert a.shape == (16, 16) and a.dtype == dt and a.flags.c_contiguous and a.flags.writeable
+    # one host block in the library's device order, so the four maps come down in one copy
+    X2 = 16 * 16
+    r = rough.ctypes.data
+    assert [pos.ctypes.data, neg.ctypes.data, vis.ctypes.data] == [r + 8 * X2, r + 12 * X2, r + 16 * X2]
 
 
 def _scans(lib):
