@@ -333,8 +333,9 @@ struct GvomHandle {
     bool graphs = false;
     // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ the combine
     // at level 1), [5] its columns and maps, [6] its count merge (level 2), [7] its index merge (level 2),
-    // [8] its statistics merge (level 2)
-    GraphNodes gn[9];
+    // [8] its statistics merge (level 2); each up to kGraphCache executables, one per shape (number of
+    // scans, of merge sources), most recently used first
+    std::vector<GraphNodes> gn[9];
     // a step forks the index merge onto `side` once the index maps are done
     // (ev_idx), and the count merge once the records' hit, total and min
     // height are (ev_mom, after the cell moments)
@@ -400,6 +401,8 @@ long long ext_cells(const Geom &g) { return (long long)g.Xe * g.Xe * g.Ze; }
 // call's parameters into its nodes and the graph is launched; when it does
 // not, or the sequence differs in shape, `enqueue` is captured into a new
 // executable graph, which replaces the old one.
+constexpr size_t kGraphCache = 4;  // executables kept per launch sequence
+
 template <class F>
 int run_graphed(GvomHandle *h, int which, F &&enqueue, cudaStream_t st = nullptr) {
     if (!st) st = h->st;
@@ -408,8 +411,13 @@ int run_graphed(GvomHandle *h, int which, F &&enqueue, cudaStream_t st = nullptr
         r = Recorder{};
         return enqueue();
     }
-    GraphNodes &G = h->gn[which];
-    if (G.exec) {
+    // the first cached executable whose nodes take this call's operations in
+    // order is updated in place and launched (a request loop alternating
+    // between batch sizes keeps one executable per size instead of capturing
+    // again at every change)
+    std::vector<GraphNodes> &cache = h->gn[which];
+    for (size_t i = 0; i < cache.size(); i++) {
+        GraphNodes &G = cache[i];
         r = Recorder{};
         r.mode = 2;
         r.g = &G;
@@ -418,7 +426,8 @@ int run_graphed(GvomHandle *h, int which, F &&enqueue, cudaStream_t st = nullptr
         r = Recorder{};
         if (rc) return rc;
         if (done) {
-            CUDA_TRY(cudaGraphLaunch(G.exec, st));
+            if (i) std::rotate(cache.begin(), cache.begin() + (long)i, cache.begin() + (long)i + 1);
+            CUDA_TRY(cudaGraphLaunch(cache[0].exec, st));
             return GVOM_OK;
         }
     }
@@ -449,10 +458,15 @@ int run_graphed(GvomHandle *h, int which, F &&enqueue, cudaStream_t st = nullptr
         cudaGetLastError();
         return fail(GVOM_ERR_CUDA, std::string("graph instantiation: ") + cudaGetErrorString(ei));
     }
-    // an executable graph still running is freed when it completes
-    if (G.exec) cudaGraphExecDestroy(G.exec);
-    if (G.graph) cudaGraphDestroy(G.graph);
-    G = std::move(fresh);
+    // the least recently used executable beyond the cache's size is freed (an
+    // executable graph still running is freed when it completes)
+    if (cache.size() >= kGraphCache) {
+        if (cache.back().exec) cudaGraphExecDestroy(cache.back().exec);
+        if (cache.back().graph) cudaGraphDestroy(cache.back().graph);
+        cache.pop_back();
+    }
+    cache.insert(cache.begin(), std::move(fresh));
+    GraphNodes &G = cache[0];
     G.graph = g;
     G.exec = x;
     if (!noted) {  // nodes not all noted: later calls capture again
@@ -993,6 +1007,11 @@ int gvom_create(const GvomParams *params, GvomHandle **out) {
         return bail(fail(GVOM_ERR_CUDA, "memset failed"));
     }
     if ((rc = ensure_cnt(h, 1, 0)) || (rc = ensure_cnt(h, 1, 1))) return bail(rc);
+    // every kernel loaded now, not at its first launch inside a later call
+    if (preload_process_kernels() != cudaSuccess || preload_combine_kernels() != cudaSuccess) {
+        cudaGetLastError();
+        return bail(fail(GVOM_ERR_CUDA, "kernel loading failed"));
+    }
     if (cudaStreamSynchronize(h->st) != cudaSuccess) {
         cudaGetLastError();
         return bail(fail(GVOM_ERR_CUDA, "initialisation failed"));
@@ -1006,10 +1025,11 @@ int gvom_destroy(GvomHandle *h) {
     DeviceScope ds(h->dev);
     if (h->st) cudaStreamSynchronize(h->st);
     if (h->own) cudaStreamSynchronize(h->own);
-    for (auto &x : h->gn) {
-        if (x.exec) cudaGraphExecDestroy(x.exec);
-        if (x.graph) cudaGraphDestroy(x.graph);
-    }
+    for (auto &c : h->gn)
+        for (auto &x : c) {
+            if (x.exec) cudaGraphExecDestroy(x.exec);
+            if (x.graph) cudaGraphDestroy(x.graph);
+        }
     if (h->side) {
         cudaStreamSynchronize(h->side);
         cudaStreamDestroy(h->side);

@@ -292,6 +292,10 @@ cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int ns
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
                            cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, cudaEvent_t after_moments,
                            int part = 0, bool external = false);
+// load every kernel of the process / combine path now instead of at its
+// first launch (CUDA's lazy module loading)
+cudaError_t preload_process_kernels();
+cudaError_t preload_combine_kernels();
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st);
 cudaError_t launch_merge_index(const MergeParams &mp, cudaStream_t st);
 // `part`: 0 counts, statistics, columns, maps2d in sequence; 1 the count

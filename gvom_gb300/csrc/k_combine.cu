@@ -1269,6 +1269,40 @@ cudaError_t launch_debug_maps(const DebugMapParams &p, cudaStream_t st) {
 
 int debug_chunk() { return kDbgChunk; }
 
+// Every combine kernel a call can launch, loaded now: with CUDA's lazy module
+// loading a kernel is otherwise loaded at its first launch, which stalls the
+// device for milliseconds in the middle of a request loop (a ring that fills
+// up reaches a new source-count class, a batch a new size).
+template <int N>
+static void add_merge_kernels(std::vector<const void *> &k) {
+    k.push_back(reinterpret_cast<const void *>(k_merge<N, 4>));
+    k.push_back(reinterpret_cast<const void *>(k_merge<N, 8>));
+    k.push_back(reinterpret_cast<const void *>(k_merge<N, 16>));
+    k.push_back(reinterpret_cast<const void *>(k_merge_counts<N>));
+    k.push_back(reinterpret_cast<const void *>(k_merge_stats<N>));
+}
+
+cudaError_t preload_combine_kernels() {
+    std::vector<const void *> k;
+    add_merge_kernels<2>(k);
+    add_merge_kernels<3>(k);
+    add_merge_kernels<5>(k);
+    add_merge_kernels<9>(k);
+    add_merge_kernels<kMaxSources>(k);
+    for (const void *f : {reinterpret_cast<const void *>(k_columns), reinterpret_cast<const void *>(k_maps2d<8, 32>),
+                          reinterpret_cast<const void *>(k_maps2d<8, 16>), reinterpret_cast<const void *>(k_maps2d<4, 16>),
+                          reinterpret_cast<const void *>(k_ros_grids), reinterpret_cast<const void *>(k_debug_count),
+                          reinterpret_cast<const void *>(k_debug_voxels), reinterpret_cast<const void *>(k_debug_maps),
+                          reinterpret_cast<const void *>(k_gather_records)})
+        k.push_back(f);
+    for (const void *f : k) {
+        cudaFuncAttributes a;
+        const cudaError_t e = cudaFuncGetAttributes(&a, f);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_gather_records(const VoxelRec *rec, const int *vids, int n, VoxelRec *out, cudaStream_t st) {
     if (n > 0) k_gather_records<<<(n + 255) / 256, 256, 0, st>>>(rec, vids, n, out);
     return cudaGetLastError();

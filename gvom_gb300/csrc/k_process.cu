@@ -858,6 +858,33 @@ static cudaError_t launch_ns(const ProcessConst &pc, const ScanDesc *table, int 
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
+// Every process kernel a call can launch, loaded now (see
+// preload_combine_kernels).
+template <int NS>
+static void add_process_kernels(std::vector<const void *> &k) {
+    k.push_back(reinterpret_cast<const void *>(k_voxelize_trace<float, NS>));
+    k.push_back(reinterpret_cast<const void *>(k_voxelize_trace<double, NS>));
+    k.push_back(reinterpret_cast<const void *>(k_assign<NS>));
+    k.push_back(reinterpret_cast<const void *>(k_scatter<NS>));
+    k.push_back(reinterpret_cast<const void *>(k_cell_moments<NS>));
+    k.push_back(reinterpret_cast<const void *>(k_voxel_stats<NS, 0>));
+    k.push_back(reinterpret_cast<const void *>(k_voxel_stats<NS, 1>));
+    k.push_back(reinterpret_cast<const void *>(k_cleanup<NS>));
+}
+
+cudaError_t preload_process_kernels() {
+    std::vector<const void *> k;
+    add_process_kernels<1>(k);
+    add_process_kernels<4>(k);
+    add_process_kernels<kMaxBatch>(k);
+    for (const void *f : k) {
+        cudaFuncAttributes a;
+        const cudaError_t e = cudaFuncGetAttributes(&a, f);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_process(const ProcessConst &pc, const ScanDesc *table, int nscans, int total_blocks, int max_n,
                            int dtype, float4 *prec, int *prank, float4 *sorted, void *moments, cudaStream_t st,
                            cudaEvent_t *ev, int pts_block, cudaEvent_t after_assign, cudaEvent_t after_moments, int part,
