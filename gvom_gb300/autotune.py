@@ -7,7 +7,8 @@ the caller's workload:
   merge_planes_per_thread  4 / 8 / 16  k_merge, k_columns
   stats_blocks_per_sm      2 / 4 / 8   k_merge_stats
   step_overlap             0 / 1       gvom_step: the index merge beside the statistics kernels
-  maps_tile_cells          64/128/256  k_maps2d (smaller tiles spread the float64 plane fits)
+  maps_tile_cells          64/128/224/256  k_maps2d (smaller tiles spread the float64 plane fits; 224 =
+                                       14 x 16, two blocks on each of 152 SMs at 256 x 256)
   step_pipeline            0 / 1 / 2   gvom_step: ray tracing beside the previous step's combine (1),
                                        and the process + merge beside its columns and maps (2)
 
@@ -31,7 +32,7 @@ CHOICES = {
     "merge_planes_per_thread": (4, 8, 16),
     "stats_blocks_per_sm": (2, 4, 8),
     "step_overlap": (0, 1),
-    "maps_tile_cells": (64, 128, 256),
+    "maps_tile_cells": (64, 128, 224, 256),
     "step_pipeline": (0, 1, 2),
 }
 AFFECTS = {

@@ -2059,8 +2059,9 @@ int gvom_set_tuning(GvomHandle *h, const GvomTuning *t) {
     if (!(t->stats_blocks_per_sm == 2 || t->stats_blocks_per_sm == 4 || t->stats_blocks_per_sm == 8))
         return fail(GVOM_ERR_ARG, "stats_blocks_per_sm must be 2, 4 or 8");
     if (!(t->step_overlap == 0 || t->step_overlap == 1)) return fail(GVOM_ERR_ARG, "step_overlap must be 0 or 1");
-    if (!(t->maps_tile_cells == 64 || t->maps_tile_cells == 128 || t->maps_tile_cells == 256))
-        return fail(GVOM_ERR_ARG, "maps_tile_cells must be 64, 128 or 256");
+    if (!(t->maps_tile_cells == 64 || t->maps_tile_cells == 128 || t->maps_tile_cells == 224 ||
+          t->maps_tile_cells == 256))
+        return fail(GVOM_ERR_ARG, "maps_tile_cells must be 64, 128, 224 or 256");
     if (!(t->step_pipeline >= 0 && t->step_pipeline <= 2)) return fail(GVOM_ERR_ARG, "step_pipeline must be 0, 1 or 2");
     std::lock_guard<std::mutex> lk(h->mu);
     h->tun.pts_block = t->points_per_block;

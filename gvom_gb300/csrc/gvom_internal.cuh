@@ -104,7 +104,7 @@ struct Tuning {
     int merge_planes;   // z planes per k_merge thread: 4, 8 or 16
     int stats_bpsm;     // k_merge_stats blocks per multiprocessor: 2, 4 or 8
     int step_overlap;   // gvom_step runs the index merge beside the statistics kernels: 0 or 1
-    int maps_tile;      // k_maps2d tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) cells
+    int maps_tile;      // k_maps2d tile: 256 (8 x 32), 224 (14 x 16), 128 (8 x 16) or 64 (4 x 16) cells
     int step_pipeline;  // gvom_step: 0 one stream; 1 the trace beside the previous step's combine; 2 also the
                         // rest of the process and the merge beside the previous step's columns and maps
 };
@@ -243,7 +243,7 @@ struct Maps2DParams {
     const float *mlow;
     double *slope_x, *slope_y, *rough, *guess;
     int *pos, *neg, *vis;
-    int tile_cells;        // Tuning::maps_tile_cells: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16)
+    int tile_cells;        // Tuning::maps_tile_cells: 256 (8 x 32), 224 (14 x 16), 128 (8 x 16) or 64 (4 x 16)
 };
 
 struct RosGridParams {

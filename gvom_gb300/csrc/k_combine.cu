@@ -266,40 +266,53 @@ __global__ void __launch_bounds__(256) k_merge(const __grid_constant__ MergePara
         occ[k] = -1;
         cnt[k] = -1;
     }
+    // up to kG sources' loads are issued together (kG * kZC in flight per
+    // thread), then merged in source order
+    constexpr int kG = NSRC < 5 ? NSRC : 5;
 #pragma unroll
-    for (int s = 0; s < NSRC; s++) {
-        if (s >= mp.nsrc) break;
-        const MergeSrc &src = mp.src[s];
-        const int xs = x + src.dx, ys = y + src.dy;
-        if (!(col && (unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X)) continue;
-        // planes k with 0 <= z0 + k + dz < Z (and z0 + k < Z)
-        const int klo = max(0, -(z0 + src.dz)), khi = min(min(kZC, Z - z0), Z - z0 - src.dz);
-        const int *colp = src.idx + xs + ys * X;
-        int vs[kZC];
-        if (klo == 0 && khi == kZC) {  // the whole chunk inside the shifted source (same for the whole block)
+    for (int s0 = 0; s0 < NSRC; s0 += kG) {
+        if (s0 >= mp.nsrc) break;
+        int vs[kG][kZC];
 #pragma unroll
-            for (int k = 0; k < kZC; k++) vs[k] = __ldg(colp + (z0 + k + src.dz) * plane);
-        } else {
-#pragma unroll
-            for (int k = 0; k < kZC; k++)
-                vs[k] = (k >= klo && k < khi) ? __ldg(colp + (z0 + k + src.dz) * plane) : -1;
-        }
-        if (src.is_last) {
-            // previous combined map: an occupied voxel comes back only if at most
-            // 10 new rays passed through it (scripts/gvom.py:1058)
-#pragma unroll
-            for (int k = 0; k < kZC; k++) {
-                const int o = vs[k];
-                int c = occ[k] >= 0 ? kOcc : cnt[k];
-                if (c <= -1) c = (o >= 0) ? (c >= -11 ? kOcc : c) : (o < -1 ? c + o + 1 : c);
-                occ[k] = c == kOcc ? 0 : -1;
-                cnt[k] = c;
+        for (int j = 0; j < kG; j++) {
+            const int s = s0 + j;
+            bool in = s < NSRC && s < mp.nsrc;
+            int klo = 0, khi = 0, off0 = 0;
+            const int *base = mp.src[0].idx;
+            if (in) {
+                const MergeSrc &src = mp.src[s];
+                const int xs = x + src.dx, ys = y + src.dy;
+                in = col && (unsigned)xs < (unsigned)X && (unsigned)ys < (unsigned)X;
+                // planes k with 0 <= z0 + k + dz < Z (and z0 + k < Z)
+                klo = max(0, -(z0 + src.dz));
+                khi = min(min(kZC, Z - z0), Z - z0 - src.dz);
+                base = src.idx;
+                off0 = xs + ys * X + (z0 + src.dz) * plane;  // plane k at off0 + k plane, read for klo <= k < khi
             }
-        } else {
 #pragma unroll
-            for (int k = 0; k < kZC; k++) {
-                occ[k] &= vs[k];
-                cnt[k] += min(vs[k], -1) + 1;
+            for (int k = 0; k < kZC; k++) vs[j][k] = (in && k >= klo && k < khi) ? __ldg(base + (off0 + k * plane)) : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < kG; j++) {
+            const int s = s0 + j;
+            if (s >= NSRC || s >= mp.nsrc) break;
+            if (mp.src[s].is_last) {
+                // previous combined map: an occupied voxel comes back only if at most
+                // 10 new rays passed through it (scripts/gvom.py:1058)
+#pragma unroll
+                for (int k = 0; k < kZC; k++) {
+                    const int o = vs[j][k];
+                    int c = occ[k] >= 0 ? kOcc : cnt[k];
+                    if (c <= -1) c = (o >= 0) ? (c >= -11 ? kOcc : c) : (o < -1 ? c + o + 1 : c);
+                    occ[k] = c == kOcc ? 0 : -1;
+                    cnt[k] = c;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < kZC; k++) {
+                    occ[k] &= vs[j][k];
+                    cnt[k] += min(vs[j][k], -1) + 1;
+                }
             }
         }
     }
@@ -1237,6 +1250,7 @@ cudaError_t launch_combine_rest(const MergeParams &mp, const ColumnParams &cp, c
     if (part == 0 || part == 3) {
         if (m2.tile_cells == 64) chk(launch_maps2d<4, 16>(m2, st));
         else if (m2.tile_cells == 128) chk(launch_maps2d<8, 16>(m2, st));
+        else if (m2.tile_cells == 224) chk(launch_maps2d<14, 16>(m2, st));
         else chk(launch_maps2d<8, 32>(m2, st));
     }
     if (ev) cudaEventRecord(ev[5], st);
@@ -1291,6 +1305,7 @@ cudaError_t preload_combine_kernels() {
     add_merge_kernels<kMaxSources>(k);
     for (const void *f : {reinterpret_cast<const void *>(k_columns), reinterpret_cast<const void *>(k_maps2d<8, 32>),
                           reinterpret_cast<const void *>(k_maps2d<8, 16>), reinterpret_cast<const void *>(k_maps2d<4, 16>),
+                          reinterpret_cast<const void *>(k_maps2d<14, 16>),
                           reinterpret_cast<const void *>(k_ros_grids), reinterpret_cast<const void *>(k_debug_count),
                           reinterpret_cast<const void *>(k_debug_voxels), reinterpret_cast<const void *>(k_debug_maps),
                           reinterpret_cast<const void *>(k_gather_records)})

@@ -253,7 +253,8 @@ typedef struct GvomTuning {
     int32_t merge_planes_per_thread;  /* index merge: 4, 8 or 16 z planes */
     int32_t stats_blocks_per_sm;      /* statistics merge: 2, 4 or 8 */
     int32_t step_overlap;             /* gvom_step: index merge beside the statistics kernels, 0 or 1 */
-    int32_t maps_tile_cells;          /* 2-D maps tile: 256 (8 x 32), 128 (8 x 16) or 64 (4 x 16) */
+    int32_t maps_tile_cells;          /* 2-D maps tile: 256 (8 x 32), 224 (14 x 16: 304 blocks at 256^2,
+                                         two per SM), 128 (8 x 16) or 64 (4 x 16) */
     int32_t step_pipeline;            /* gvom_step streams: 0 one; 1 the trace beside the previous step's combine;
                                          2 also the process and merge beside the previous step's columns and maps */
 } GvomTuning;
