@@ -44,7 +44,7 @@ AFFECTS = {
     "step_pipeline": None,  # whole steps
 }
 DEFAULT = {"points_per_block": 256, "merge_planes_per_thread": 8,
-           "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 256, "step_pipeline": 2}
+           "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 224, "step_pipeline": 2}
 
 
 def cache_path() -> str:

@@ -108,7 +108,7 @@ struct Tuning {
     int step_pipeline;  // gvom_step: 0 one stream; 1 the trace beside the previous step's combine; 2 also the
                         // rest of the process and the merge beside the previous step's columns and maps
 };
-constexpr Tuning kDefaultTuning = {256, 8, 4, 1, 256, 2};
+constexpr Tuning kDefaultTuning = {256, 8, 4, 1, 224, 2};
 constexpr int kCube = 16;             // shared-memory cube of ray-step counts (cells per axis)
 constexpr int kCubeCells = kCube * kCube * kCube;
 constexpr int kMaxSources = 17;       // ring slots (<= 16) + previous combined map

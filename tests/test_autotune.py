@@ -102,7 +102,9 @@ def test_every_launch_shape_gives_identical_maps(gpu_lib):
               {"points_per_block": 128, "merge_planes_per_thread": 16,
                "stats_blocks_per_sm": 2, "step_overlap": 0, "maps_tile_cells": 64, "step_pipeline": 0},
               {"points_per_block": 256, "merge_planes_per_thread": 4,
-               "stats_blocks_per_sm": 8, "step_overlap": 1, "maps_tile_cells": 128, "step_pipeline": 2}]
+               "stats_blocks_per_sm": 8, "step_overlap": 1, "maps_tile_cells": 128, "step_pipeline": 2},
+              {"points_per_block": 128, "merge_planes_per_thread": 8,
+               "stats_blocks_per_sm": 4, "step_overlap": 1, "maps_tile_cells": 224, "step_pipeline": 1}]
     results = []
     for t in shapes:
         g = Gvom(*params)
