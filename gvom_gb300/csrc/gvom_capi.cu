@@ -334,7 +334,7 @@ struct GvomHandle {
     // [0] process, [1] combine, [2] step, [3] a pipelined step's trace, [4] its process rest (+ the combine
     // at level 1), [5] its columns and maps, [6] its count merge (level 2), [7] its index merge (level 2),
     // [8] its statistics merge (level 2); each up to kGraphCache executables, one per shape (number of
-    // scans, of merge sources), most recently used first
+    // scans, merge source count), most recently used first
     std::vector<GraphNodes> gn[9];
     // a step forks the index merge onto `side` once the index maps are done
     // (ev_idx), and the count merge once the records' hit, total and min
@@ -401,7 +401,9 @@ long long ext_cells(const Geom &g) { return (long long)g.Xe * g.Xe * g.Ze; }
 // call's parameters into its nodes and the graph is launched; when it does
 // not, or the sequence differs in shape, `enqueue` is captured into a new
 // executable graph, which replaces the old one.
-constexpr size_t kGraphCache = 4;  // executables kept per launch sequence
+// executables kept per launch sequence: a step's trace and process graphs hold
+// one fill or copy node per scan, so each batch size (1-16) is its own shape
+constexpr size_t kGraphCache = 16;
 
 template <class F>
 int run_graphed(GvomHandle *h, int which, F &&enqueue, cudaStream_t st = nullptr) {
@@ -1525,8 +1527,11 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     std::lock_guard<std::mutex> lk(h->mu);
     const bool timing = !h->graphs && h->timer.on;
     const bool dev_out = outputs_on_device != 0;
-    // with stage timing the kernels run in sequence so that each interval is one kernel
-    const int pipe = timing ? 0 : h->tun.step_pipeline;
+    // with stage timing the kernels run in sequence so that each interval is one
+    // kernel; a step whose maps go to host memory ends with a host wait, so the
+    // next call cannot overlap it, and one graph (level 0, with the same
+    // overlap inside the step) is cheaper to submit than the pipeline's six
+    const int pipe = (timing || !dev_out) ? 0 : h->tun.step_pipeline;
     if (pipe >= 2 && h->st_dirty) {  // order the pipeline streams after other calls' work
         CUDA_TRY(cudaEventRecord(h->ev_host, h->st));
         CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_host, 0));

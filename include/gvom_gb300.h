@@ -129,7 +129,8 @@ int gvom_combine_device(GvomHandle *h, double origin[3], int32_t *d_pos, int32_t
  * steps submitted back to back overlap: at 1 a step's ray tracing runs on a
  * second stream beside the previous step's combine; at 2 the rest of its
  * process and its merge also run, on a third stream, beside the previous
- * step's columns and 2-D maps.  The maps are complete in stream order of the
+ * step's columns and 2-D maps.  A step with host outputs ends with a host
+ * wait, so it runs as at 0.  The maps are complete in stream order of the
  * instance stream either way; in graph mode each stream's part of a step is
  * one executable graph. */
 int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t points_on_device, double origin[3],
