@@ -435,15 +435,18 @@ __device__ __forceinline__ bool cell_in_grid(unsigned e, const Geom &g, unsigned
     return (unsigned)gx < (unsigned)g.X && (unsigned)gy < (unsigned)g.X && (unsigned)gz < (unsigned)g.Z;
 }
 
+// The owner of an in-grid cell (its point of rank 0) leaves its voxel's
+// compact index in its rank word as -2 - index, for k_cell_moments; readers
+// of the rank take max(rank, 0).
 template <int NS>
 __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
-                                               const float4 *__restrict__ prec, const int *__restrict__ prank) {
+                                               const float4 *__restrict__ prec, int *__restrict__ prank) {
     const int s = find_scan(tab, pc.nscans, blockIdx.x);
     const ScanDesc &sd = tab.s[s];
     const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
     int cell = -1, gid = 0, occ = 0, npts = 0;
+    const long long gi = sd.pt_base + i;
     if (i < sd.n) {
-        const long long gi = sd.pt_base + i;
         const int c = __float_as_int(prec[gi].w);
         if (c >= 0 && prank[gi] == 0) {
             cell = c;
@@ -477,6 +480,7 @@ __global__ void __launch_bounds__(256) k_assign(const ProcessConst pc, const __g
             atomicOr(&sd.ctr->overflow, 1);
         }
         sd.idx[gid] = c;
+        prank[gi] = -2 - c;
     }
     sd.cnt[cell] = ((unsigned long long)(unsigned)(bases[1] + ep) << 32) | (unsigned)npts;
 }
@@ -499,7 +503,7 @@ __global__ void __launch_bounds__(256) k_scatter(const ProcessConst pc, const __
     if (cell < 0) return;
     const unsigned long long v = sd.cnt[cell];
     const int off = (int)(v >> 32);
-    sorted[sd.pt_base + off + prank[gi]] = make_float4(r.x, r.y, r.z, 0.f);
+    sorted[sd.pt_base + off + max(prank[gi], 0)] = make_float4(r.x, r.y, r.z, 0.f);
 }
 
 // ---------------------------------------------------------------------------
@@ -537,21 +541,17 @@ __device__ __forceinline__ float warp_sum(float v) {
 // the record of an in-grid cell's voxel takes the cell's lowest height
 // fraction (__calculate_min_height, scripts/gvom.py:1390-1421: the points of
 // the voxel itself), so the count merge can read it before the neighbourhood
-// statistics are done
-__device__ __forceinline__ void store_min_h(const ScanDesc &sd, const Geom &g, int cell, float mh) {
-    const int XeXe = g.Xe * g.Xe, r = cell % XeXe;
-    const int bx = r % g.Xe - g.exy, by = r / g.Xe - g.exy, bz = cell / XeXe - g.ez;
-    if ((unsigned)bx < (unsigned)g.X && (unsigned)by < (unsigned)g.X && (unsigned)bz < (unsigned)g.Z) {
-        const int ci = sd.idx[bx + g.X * by + g.X * g.X * bz];  // compact index (k_assign)
-        if (ci >= 0 && ci < sd.rec_cap) sd.rec[ci].min_h = mh;
-    }
+// statistics are done; `ci`: the voxel's compact index from the owner's rank
+// word (k_assign), -1 for a cell outside the grid
+__device__ __forceinline__ void store_min_h(const ScanDesc &sd, int ci, float mh) {
+    if (ci >= 0 && ci < sd.rec_cap) sd.rec[ci].min_h = mh;
 }
 
 template <int NS>
 __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, const __grid_constant__ ScanTable<NS> tab,
                                                      const float4 *__restrict__ prec, const int *__restrict__ prank,
                                                      const float4 *__restrict__ sorted, CellMom *__restrict__ mom) {
-    __shared__ int hq_off[256], hq_n[256], hq_cell[256];
+    __shared__ int hq_off[256], hq_n[256], hq_rec[256];
     __shared__ int hq_count;
     const int s = find_scan(tab, pc.nscans, blockIdx.x);
     const ScanDesc &sd = tab.s[s];
@@ -559,11 +559,13 @@ __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, con
     __syncthreads();
     const long long i = (long long)(blockIdx.x - sd.block_begin) * blockDim.x + threadIdx.x;
     bool mine = false;
-    int off = 0, n = 0, cell = -1;
+    int off = 0, n = 0, ci = -1;
     if (i < sd.n) {
         const long long gi = sd.pt_base + i;
-        cell = __float_as_int(prec[gi].w);
-        if (cell >= 0 && prank[gi] == 0) {
+        const int cell = __float_as_int(prec[gi].w);
+        const int rk = prank[gi];
+        if (cell >= 0 && rk <= 0) {  // the cell's owner (rank 0)
+            ci = rk < 0 ? -2 - rk : -1;
             const unsigned long long v = sd.cnt[cell];
             off = (int)(v >> 32);
             n = (int)(v & 0xffffffffull);
@@ -571,7 +573,7 @@ __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, con
                 const int q = atomicAdd(&hq_count, 1);
                 hq_off[q] = off;
                 hq_n[q] = n;
-                hq_cell[q] = cell;
+                hq_rec[q] = ci;
             } else {
                 mine = true;
             }
@@ -611,7 +613,7 @@ __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, con
         o[1] = make_float4(__fsub_rn(cxx.s, cxx.c), __fsub_rn(cxy.s, cxy.c), __fsub_rn(cxz.s, cxz.c),
                            __fsub_rn(cyy.s, cyy.c));
         o[2] = make_float4(__fsub_rn(cyz.s, cyz.c), __fsub_rn(czz.s, czz.c), mh, 0.f);
-        store_min_h(sd, pc.g, cell, mh);
+        store_min_h(sd, ci, mh);
     }
     __syncthreads();
     // cells with many points: one warp each, lanes striding over the points with
@@ -657,7 +659,7 @@ __global__ void __launch_bounds__(256) k_cell_moments(const ProcessConst pc, con
             o[0] = make_float4(mx, my, mz, nf);
             o[1] = make_float4(c0, c1, c2, c3);
             o[2] = make_float4(c4, c5, mh, 0.f);
-            store_min_h(sd, pc.g, hq_cell[q], mh);
+            store_min_h(sd, hq_rec[q], mh);
         }
     }
 }
@@ -810,7 +812,7 @@ __global__ void __launch_bounds__(256) k_cleanup(const ProcessConst pc, const __
     if (i >= sd.n) return;
     const long long gi = sd.pt_base + i;
     const int cell = __float_as_int(prec[gi].w);
-    if (cell >= 0 && prank[gi] == 0) sd.cnt[cell] = 0ull;
+    if (cell >= 0 && prank[gi] <= 0) sd.cnt[cell] = 0ull;  // the owner
 }
 
 // ---------------------------------------------------------------------------
