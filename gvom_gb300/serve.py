@@ -26,6 +26,7 @@ Process_pointcloud from the lidar callback and combine_maps from a timer.
 """
 from __future__ import annotations
 
+import gc
 import threading
 import time
 from collections import deque
@@ -127,10 +128,13 @@ class MapServer:
     `point_budget` fixes the points per batch; by default it is taken at each
     admission as `mem_fraction` of the device's free memory, shared by the
     instances.  `reserve_points`: points per batch whose scratch each instance
-    allocates at start-up (default: `max_scans` scans of 262,144 points)."""
+    allocates at start-up (default: `max_scans` scans of 262,144 points).
+    `freeze_gc`: move every object alive at start-up into the garbage
+    collector's permanent generation (gc.freeze), so that a full collection
+    during serving does not traverse the whole start-up heap."""
 
     def __init__(self, instances: list[tuple], graphs: bool = True, mem_fraction: float = 0.25,
-                 point_budget: int | None = None, reserve_points: int | None = None):
+                 point_budget: int | None = None, reserve_points: int | None = None, freeze_gc: bool = True):
         import torch
         free, _ = torch.cuda.mem_get_info()
         self.free_at_start = free
@@ -147,6 +151,9 @@ class MapServer:
         self._seq = 0
         self._lock = threading.Lock()
         self._running = True
+        if freeze_gc:
+            gc.collect()
+            gc.freeze()
         for inst in self.instances:
             inst.threads = [threading.Thread(target=self._submitter, args=(inst,), daemon=True),
                             threading.Thread(target=self._completer, args=(inst,), daemon=True)]
