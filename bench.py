@@ -896,7 +896,7 @@ def main():
     ap.add_argument("--workload", default="os1_64_veg", help="headline form")
     ap.add_argument("--forms", default="batched_8,served,ros",
                     help="comma-separated other forms measured in the same run")
-    ap.add_argument("--served-seconds", type=float, default=3.0, help="arrival window of the served form")
+    ap.add_argument("--served-seconds", type=float, default=6.0, help="arrival window of the served form")
     ap.add_argument("--form-steps", type=int, default=300, help="timed steps of each other form")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false",
