@@ -802,7 +802,7 @@ def measure_served(args, torch):
     return {"at_load": at_load, "saturated": saturated,
             "loop": f"pipelined: up to {serve.IN_FLIGHT} batches per instance in flight (gvom_step, device "
                     "outputs, asynchronous copies into pinned host memory); point budget from free HBM "
-                    "at each admission; scratch reserved at start-up",
+                    "(read at most every 50 ms); scratch reserved at start-up",
             "note": "latency = submission to combine_maps outputs on the host; the saturated run queues every "
                     "request of the window at once and reports the points/sec the loop sustains"}
 

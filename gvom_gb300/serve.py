@@ -4,7 +4,7 @@ Scans arrive as requests for one of several map instances (a vehicle's
 sensors feed one instance).  Each instance has its own CUDA stream and two
 threads.  The submitter admits every queued request that fits -- at most one
 ring slot per scan (the buffer size, at most 16 per launch) and a point
-budget taken from the device's free memory at each admission -- and submits
+budget taken from the device's free memory (read at most every 50 ms) -- and submits
 them as one step (`gvom_step`: one process launch set over the batch, then
 the combine) with the maps written to a device output set, followed on the
 same stream by an asynchronous copy into pinned host memory and an event.
@@ -131,13 +131,19 @@ class MapServer:
     allocates at start-up (default: `max_scans` scans of 262,144 points).
     `freeze_gc`: move every object alive at start-up into the garbage
     collector's permanent generation (gc.freeze), so that a full collection
-    during serving does not traverse the whole start-up heap."""
+    during serving does not traverse the whole start-up heap.  The free
+    memory behind the budget is read at most every `free_refresh_s` seconds:
+    the query runs with the interpreter lock held, so an occasional slow
+    driver call would stall every thread of the loop."""
 
     def __init__(self, instances: list[tuple], graphs: bool = True, mem_fraction: float = 0.25,
-                 point_budget: int | None = None, reserve_points: int | None = None, freeze_gc: bool = True):
+                 point_budget: int | None = None, reserve_points: int | None = None, freeze_gc: bool = True,
+                 free_refresh_s: float = 0.05):
         import torch
         free, _ = torch.cuda.mem_get_info()
         self.free_at_start = free
+        self.free_refresh_s = free_refresh_s
+        self._free, self._free_t = free, float("-inf")  # read again at the first admission
         self.mem_fraction = mem_fraction
         self.fixed_budget = point_budget
         self.instances: list[_Instance] = []
@@ -169,7 +175,12 @@ class MapServer:
         if self.fixed_budget is not None:
             return self.fixed_budget
         import torch
-        free, _ = torch.cuda.mem_get_info()
+        with self._lock:
+            now = time.perf_counter()
+            if now - self._free_t >= self.free_refresh_s:
+                self._free, _ = torch.cuda.mem_get_info()
+                self._free_t = now
+            free = self._free
         return max(1, int(free * self.mem_fraction / BYTES_PER_POINT / max(1, len(self.instances))))
 
     # ------------------------------------------------------------------
