@@ -349,16 +349,19 @@ struct GvomHandle {
     // its scratch set (the one before the previous call) is done with it
     // (ev_scratch[set]).  At level 1 the rest of the step follows on the
     // instance stream after ev_traced.  At level 2 the rest of the process
-    // and the merge run on `bs` (after ev_traced, and after the columns pass
-    // that last read the combined buffer they write, ev_cols[buffer]) beside
-    // the previous step's columns and maps on the instance stream, which
-    // waits for ev_merged.  Work queued on the instance stream by other calls
-    // sets st_dirty: the next level-2 step first orders `tr` and `bs` after
-    // it (ev_host).
+    // runs on `bs` after ev_traced; on `side`, the index merge after ev_idx
+    // (and after the columns pass that last read the combined buffer it
+    // writes, ev_cols[buffer]), the count merge after ev_mom and the
+    // statistics merge after ev_scratch[set]; the columns and maps on the
+    // instance stream after ev_merged, beside the next step's process.  Work
+    // queued on the instance stream by other calls sets st_dirty: the next
+    // level-2 step first orders `tr`, `bs` and `side` after it (ev_host).
     cudaStream_t tr = nullptr, bs = nullptr;
     // the statistics merge runs beside the columns and maps: on `side` after
     // the count merge (ev_ms) and joined at the end of a combine (ev_msj), or
-    // at level 2 as its own graph, ev_stats[buffer] marking its end
+    // at level 2 as its own graph, ev_stats[buffer] marking its end.  A
+    // combine that follows a process swaps the roles (launch_comb): `side`
+    // runs the merges, columns and maps, and ev_msj joins them back.
     cudaEvent_t ev_ms = nullptr, ev_msj = nullptr, ev_stats[2] = {nullptr, nullptr};
     cudaEvent_t ev_scratch[2] = {nullptr, nullptr};  // the process call that last used the set is done with it
     cudaEvent_t ev_traced = nullptr, ev_merged = nullptr, ev_host = nullptr;

@@ -13,10 +13,15 @@
 //   k_assign          one thread per point-holding cell (its first point):
 //                     compact index and record of occupied voxels, total =
 //                     -(word)-1 read back from the index map
-//                     (scripts/gvom.py:1233-1247), point-group offsets
+//                     (scripts/gvom.py:1233-1247), point-group offsets; the
+//                     owner of an in-grid cell keeps the compact index in its
+//                     rank word
 //   k_scatter         groups points by cell (rank from the hit atomic)
-//   k_voxel_stats     neighbourhood mean / covariance / count and in-voxel
-//                     minimum height (scripts/gvom.py:1249-1421)
+//   k_cell_moments    per point-holding cell: moments of its points and their
+//                     minimum height, which goes into the voxel's record
+//                     (scripts/gvom.py:1390-1421)
+//   k_voxel_stats     neighbourhood mean / covariance / count
+//                     (scripts/gvom.py:1249-1387)
 //   k_cleanup         returns the cell words to zero
 //
 // All float arithmetic that decides an integer result uses the IEEE-rounded
