@@ -154,7 +154,7 @@ def test_request_loop_batches_and_answers(monkeypatch):
     _FakeMapper.reserved = {}
     p4 = (0.2, 0.2, 32, 16, 4, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
     p2 = p4[:4] + (2,) + p4[5:]
-    srv = serve.MapServer([p4, p2], point_budget=1000)
+    srv = serve.MapServer([p4, p2], point_budget=1000, freeze_gc=False)
     pts = lambda n: np.zeros((n, 3), np.float32)  # noqa: E731
     first = srv.submit(0, pts(10), (0, 0, 0))
     assert _FakeMapper.entered[4].wait(10)  # the first scan is on the device alone
@@ -215,7 +215,7 @@ def test_submitter_runs_ahead_of_completion(monkeypatch):
     _FakeMapper.calls = []
     _FakeMapper.reserved = {}
     p = (0.2, 0.2, 32, 16, 1, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)  # one slot: one scan per batch
-    srv = serve.MapServer([p], point_budget=1000, reserve_points=0)
+    srv = serve.MapServer([p], point_budget=1000, reserve_points=0, freeze_gc=False)
     pts = np.zeros((10, 3), np.float32)
     reqs = [srv.submit(0, pts, (0, 0, 0)) for _ in range(3)]
     import time
@@ -253,3 +253,46 @@ def test_instance_refused_when_device_memory_is_short(gpu_lib):
         Gvom(*big)
     g = Gvom(0.2, 0.2, 64, 16, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
     assert g.device_bytes() > 0
+
+
+def test_point_budget_reads_free_memory_at_most_every_refresh(monkeypatch):
+    """Without a fixed budget, the point budget follows the device's free
+    memory, read at most every `free_refresh_s` (the query holds the
+    interpreter lock, so it is not made at every admission)."""
+    import time
+    import types
+
+    import torch
+
+    from gvom_gb300 import serve
+    monkeypatch.setattr(serve, "Gvom", _FakeMapper)
+    monkeypatch.setattr(serve, "OutputSet", _FakeOutputSet)
+    _FakeMapper.gate = None
+    _FakeMapper.reserved = {}
+    reads = []
+    free = [8 << 30]
+
+    def mem_get_info():
+        reads.append(time.perf_counter())
+        return free[0], 16 << 30
+
+    fake_cuda = types.SimpleNamespace(Stream=lambda: types.SimpleNamespace(cuda_stream=0),
+                                      mem_get_info=mem_get_info, set_stream=lambda s: None)
+    monkeypatch.setattr(torch, "cuda", fake_cuda)
+    p = (0.2, 0.2, 32, 16, 4, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    srv = serve.MapServer([p, p], mem_fraction=0.25, free_refresh_s=0.2, freeze_gc=False)
+    try:
+        n0 = len(reads)  # the start-up reading
+        b1 = srv.point_budget  # the first admission reads again
+        assert len(reads) == n0 + 1
+        assert b1 == int((8 << 30) * 0.25 / serve.BYTES_PER_POINT / 2)
+        free[0] = 4 << 30
+        for _ in range(50):  # within the refresh interval: the cached reading
+            assert srv.point_budget == b1
+        assert len(reads) == n0 + 1
+        time.sleep(0.25)
+        b2 = srv.point_budget
+        assert len(reads) == n0 + 2
+        assert b2 == int((4 << 30) * 0.25 / serve.BYTES_PER_POINT / 2)
+    finally:
+        srv.close()
