@@ -93,8 +93,7 @@ def _as_transform(transform):
 
 
 def _ego3(ego_position):
-    e = np.ascontiguousarray(np.asarray(ego_position, dtype=np.float64).reshape(3))
-    return e
+    return np.array(ego_position, np.float64).reshape(3)  # a fresh C-contiguous copy
 
 
 def pose_to_transform(translation, rotation_xyzw) -> np.ndarray:
@@ -178,22 +177,21 @@ class Gvom:
         """combine_maps' four maps (int32, int32, float64, int32; (X, X)) as
         views of one fresh host block laid out as the library's device block
         (roughness, positive, negative, visibility), which it then copies in
-        one transfer."""
+        one transfer; the origin (3 doubles) follows at an 8-byte boundary.
+        Returns (origin, pos, neg, rough, vis, address of the block)."""
         X2 = self.xy_size * self.xy_size
-        blk = np.empty(20 * X2, np.uint8)
+        oo = (20 * X2 + 7) & ~7
+        blk = np.empty(oo + 24, np.uint8)
         sh = (self.xy_size, self.xy_size)
-        rough = blk[:8 * X2].view(np.float64).reshape(sh)
-        pos = blk[8 * X2:12 * X2].view(np.int32).reshape(sh)
-        neg = blk[12 * X2:16 * X2].view(np.int32).reshape(sh)
-        vis = blk[16 * X2:].view(np.int32).reshape(sh)
-        return pos, neg, rough, vis
+        nd = np.ndarray
+        return (nd((3,), np.float64, blk, oo), nd(sh, np.int32, blk, 8 * X2), nd(sh, np.int32, blk, 12 * X2),
+                nd(sh, np.float64, blk, 0), nd(sh, np.int32, blk, 16 * X2), blk.ctypes.data)
 
     def combine_maps(self):
         """Merge the ring and build the 2-D maps (scripts/gvom.py:222-393)."""
-        origin = np.zeros(3, np.float64)
-        pos, neg, rough, vis = self._output_maps()
-        rc = self._l.gvom_combine(self._h, origin.ctypes.data, pos.ctypes.data, neg.ctypes.data, rough.ctypes.data,
-                                  vis.ctypes.data)
+        origin, pos, neg, rough, vis, b = self._output_maps()
+        X2 = self.xy_size * self.xy_size
+        rc = self._l.gvom_combine(self._h, b + ((20 * X2 + 7) & ~7), b + 8 * X2, b + 12 * X2, b, b + 16 * X2)
         if rc == GVOM_NO_DATA:
             print("ERROR: No data in buffer")
             return None
@@ -318,16 +316,16 @@ class Gvom:
         combine_maps()'s tuple, or with `device_outputs` = (pos, neg, rough,
         vis) CUDA tensors fills them stream-ordered and returns the origin."""
         arr, keep, on_dev = self._scan_array(scans)
-        origin = np.zeros(3, np.float64)
-        P = lambda a: a.ctypes.data  # noqa: E731
         if device_outputs is not None:
+            origin = np.zeros(3, np.float64)
             ptrs = [C.c_void_p(t.data_ptr()) for t in device_outputs]
-            check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, P(origin), *ptrs, 1))
+            check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, origin.ctypes.data, *ptrs, 1))
             del keep
             return origin
-        pos, neg, rough, vis = self._output_maps()
-        check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, P(origin), P(pos), P(neg), P(rough),
-                                P(vis), 0))
+        origin, pos, neg, rough, vis, b = self._output_maps()
+        X2 = self.xy_size * self.xy_size
+        check(self._l.gvom_step(self._h, arr, len(scans), 1 if on_dev else 0, b + ((20 * X2 + 7) & ~7), b + 8 * X2,
+                                b + 12 * X2, b, b + 16 * X2, 0))
         del keep
         return origin, pos, neg, rough, vis
 
