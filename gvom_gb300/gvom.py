@@ -96,6 +96,20 @@ def _ego3(ego_position):
     return np.array(ego_position, np.float64).reshape(3)  # a fresh C-contiguous copy
 
 
+_D3 = C.c_double * 3
+
+
+def _ego_c(ego_position):
+    """The ego position as a ctypes double[3] (passed by address without a
+    numpy .ctypes lookup): three numbers directly, any other shape that holds
+    three values through numpy."""
+    try:
+        x, y, z = ego_position
+        return _D3(float(x), float(y), float(z))
+    except (TypeError, ValueError):
+        return _D3(*_ego3(ego_position).tolist())
+
+
 def pose_to_transform(translation, rotation_xyzw) -> np.ndarray:
     """float64 4x4 of tf's fromTranslationRotation (translation, quaternion
     x, y, z, w), as the reference's ROS node builds Process_pointcloud's
@@ -163,9 +177,9 @@ class Gvom:
         """Voxelise one scan into the ring buffer (scripts/gvom.py:105-217)."""
         ptr, code, n, stride, keep, on_dev = _as_points(pointcloud)
         tptr, tcode, tkeep = _as_transform(transform)
-        ego = _ego3(ego_position)
+        ego = _ego_c(ego_position)
         fn = self._l.gvom_process_device if on_dev else self._l.gvom_process
-        check(fn(self._h, ptr, code, n, stride, ego.ctypes.data, tptr, tcode))
+        check(fn(self._h, ptr, code, n, stride, ego, tptr, tcode))
         if on_dev:
             # the library runs on its own stream; keep the tensor alive until the scan is consumed
             self.synchronize()

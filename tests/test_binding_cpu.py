@@ -69,6 +69,12 @@ def test_process_pointcloud_arguments(stub):
     g.Process_pointcloud(pts, [0, 0, 0])
     a = _process_args(stub)
     assert a["transform"] is None and a["tdtype"] == GVOM_NONE
+    # an ego position of shape (1, 3), float32 or integer, becomes three float64
+    for ego in (np.array([[3.0, 4.0, 5.0]]), np.float32([3.0, 4.0, 5.0]), (3, 4, 5)):
+        g.Process_pointcloud(pts, ego)
+        assert _process_args(stub)["ego"] == [3.0, 4.0, 5.0]
+    with pytest.raises(ValueError):
+        g.Process_pointcloud(pts, (1.0, 2.0))
     # a strided view and integer points are copied to contiguous float rows
     g.Process_pointcloud(pts[::2], (0, 0, 0), T)
     a = _process_args(stub)
