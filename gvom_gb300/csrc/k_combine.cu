@@ -378,6 +378,25 @@ __device__ __forceinline__ bool near_integer(float w, float margin) {
     return !(w - f > margin && f + 1.0f - w > margin);
 }
 
+// (int)(dens / nn * 100.0) of the positive-obstacle band (scripts/gvom.py:
+// 548-555) in float64, dens and nn >= 0 integer-valued sums (exact): the two
+// roundings move the exact value 100 dens / nn by at most 2.3e-16 of itself.
+// Below 2^44 a non-integer value lies at least 1 / nn from every integer,
+// more than that, so its truncation is the integer quotient; an integer value
+// (and a larger one) takes the float64 sequence, whose rounding can fall just
+// below it.  nn > 0.
+__device__ __forceinline__ int band_density(long long dens, long long nn) {
+    const long long P = 100 * dens;
+    long long q = -1;
+    if (P < (1LL << 32) && nn < (1LL << 32)) {  // 32-bit division where it fits
+        const unsigned p32 = (unsigned)P, n32 = (unsigned)nn;
+        if (p32 % n32 != 0u) q = p32 / n32;
+    } else if (P < (1LL << 44) && P % nn != 0) {
+        q = P / nn;
+    }
+    return q >= 0 ? (int)q : (int)__dmul_rn(__ddiv_rn((double)dens, (double)nn), 100.0);
+}
+
 __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnParams cp) {
     const int X = cp.X, Z = cp.Z;
     const int x = blockIdx.x * 32 + threadIdx.x;
@@ -437,23 +456,7 @@ __global__ void __launch_bounds__(256) k_columns(const __grid_constant__ ColumnP
                     }
                 }
             }
-            // (int)(dens / nn * 100.0) in float64 (integer-valued sums are exact):
-            // the two roundings move the exact value 100 dens / nn by at most
-            // 2.3e-16 of itself.  Below 2^44 a non-integer value lies at least
-            // 1 / nn from every integer, more than that, so its truncation is the
-            // integer quotient; an integer value (and a larger one) takes the
-            // float64 sequence, whose rounding can fall just below it.
-            if (nn > 0) {
-                const long long P = 100 * dens;
-                long long q = -1;
-                if (P < (1LL << 32) && nn < (1LL << 32)) {  // 32-bit division where it fits
-                    const unsigned p32 = (unsigned)P, n32 = (unsigned)nn;
-                    if (p32 % n32 != 0u) q = p32 / n32;
-                } else if (P < (1LL << 44) && P % nn != 0) {
-                    q = P / nn;
-                }
-                pd = q >= 0 ? (int)q : (int)__dmul_rn(__ddiv_rn((double)dens, (double)nn), 100.0);
-            }
+            if (nn > 0) pd = band_density(dens, nn);
         }
     } else {
         // robot disc (scripts/gvom.py:566-570): decided in float32 unless near the rim
