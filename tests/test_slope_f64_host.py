@@ -135,3 +135,95 @@ def test_kernel_float64_sequence_equals_oracle(slope_lib, name):
         checked += int((r != -1.0).sum())
     # scenes without three known heights around any cell have no plane fit at all
     assert checked > 0 or name.split(".")[0] in ("kat_clear10", "kat_clear11", "kat_rays", "kat_eigen")
+
+
+def _reference_slope(H, X, res, x0, y0):
+    """__calculate_slope (scripts/gvom.py:717-805) for one cell, restated in
+    Python floats (IEEE double, operations in the reference's order):
+    (roughness, slope x, slope y), or None where the reference leaves the
+    cell alone (fewer than three known neighbours, or det == 0)."""
+    import math
+    pts = [(x * res, y * res, H[x][y])
+           for x in range(max(0, x0 - 1), min(X, x0 + 2))
+           for y in range(max(0, y0 - 1), min(X, y0 + 2)) if H[x][y] > -1000]
+    n = len(pts)
+    if n < 3:
+        return None
+    mx = my = mz = 0.0
+    for px, py, pz in pts:
+        mx += px
+        my += py
+        mz += pz
+    mx /= float(n)
+    my /= float(n)
+    mz /= float(n)
+    xx = xy = xz = yy = yz = 0.0
+    for px, py, pz in pts:
+        xx += (px - mx) * (px - mx)
+        xy += (px - mx) * (py - my)
+        xz += (px - mx) * (pz - mz)
+        yy += (py - my) * (py - my)
+        yz += (py - my) * (pz - mz)
+    det = xx * yy - xy * xy
+    if det == 0.0:
+        return None
+    a0 = (yy * xz - xy * yz) / det
+    a1 = (xx * yz - xy * xz) / det
+    m = math.sqrt(a0 * a0 + a1 * a1 + 1)
+    a0 /= m
+    a1 /= m
+    err = 0.0
+    for px, py, pz in pts:
+        e = (pz - mz) - (a0 * (px - mx) + a1 * (py - my))
+        err += e * e
+    err /= float(n)
+    if err > 0:
+        err = math.log(err)
+    return err, math.atan2(a0, 1.0 / m), math.atan2(a1, 1.0 / m)
+
+
+def test_kernel_float64_sequence_on_random_neighbourhoods(slope_lib):
+    """Random height maps -- noise, voxel-quantised heights, flat patches,
+    single known rows and columns, sparse known cells, map edges -- through
+    the kernel's eight-lane sequence and the Python restatement: equal bit
+    for bit on every cell with a plane fit."""
+    rng = np.random.default_rng(17)
+    X, checked = 24, 0
+    for trial in range(24):
+        res = (0.15, 0.2, 0.1, 0.25)[trial % 4]
+        kind = trial % 6
+        if kind == 0:
+            H = rng.normal(0.0, 1.0, (X, X))
+        elif kind == 1:  # voxel-quantised: integer z times a resolution plus a fraction
+            H = rng.integers(-5, 20, (X, X)) * 0.15 + rng.random((X, X)) * 0.15
+        elif kind == 2:  # flat patches
+            H = np.repeat(np.repeat(rng.integers(0, 3, (X // 4, X // 4)) * 0.3, 4, 0), 4, 1).astype(np.float64)
+        elif kind == 3:  # a gentle plane with tiny noise (near-cancellations)
+            xs, ys = np.meshgrid(np.arange(X), np.arange(X), indexing="ij")
+            H = 0.01 * xs + 0.02 * ys + rng.normal(0.0, 1e-9, (X, X))
+        elif kind == 4:  # only some rows known (collinear neighbourhoods)
+            H = rng.normal(0.0, 1.0, (X, X))
+            H[rng.random(X) < 0.6, :] = -1000.0
+        else:  # only some columns known
+            H = rng.normal(0.0, 1.0, (X, X))
+            H[:, rng.random(X) < 0.6] = -1000.0
+        H[rng.random((X, X)) < 0.25] = -1000.0  # unknown cells
+        H = np.ascontiguousarray(H, np.float64)
+        r, sx, sy = (np.empty((X, X)) for _ in range(3))
+        assert slope_lib.slope_all(H.ctypes.data, X, res, r.ctypes.data, sx.ctypes.data, sy.ctypes.data) == 0
+        Hl = H.tolist()
+        for x0 in range(X):
+            for y0 in range(X):
+                ref = _reference_slope(Hl, X, res, x0, y0)
+                if ref is None:
+                    # the kernel leaves the defaults (roughness -1, slopes 0)
+                    n = sum(1 for x in range(max(0, x0 - 1), min(X, x0 + 2))
+                            for y in range(max(0, y0 - 1), min(X, y0 + 2)) if Hl[x][y] > -1000)
+                    if n >= 3:
+                        assert (r[x0, y0], sx[x0, y0], sy[x0, y0]) == (-1.0, 0.0, 0.0), (trial, x0, y0)
+                    continue
+                got = (r[x0, y0], sx[x0, y0], sy[x0, y0])
+                assert np.array(got).view(np.uint64).tolist() == np.array(ref).view(np.uint64).tolist(), \
+                    (trial, x0, y0, got, ref)
+                checked += 1
+    assert checked > 5000
