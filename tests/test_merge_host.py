@@ -113,3 +113,60 @@ def test_kernel_index_merge_equals_oracle(merge_lib, name):
         np.testing.assert_array_equal(np.where(ref >= 0, 0, got), np.where(ref >= 0, 0, ref), f"{name} free map")
         prev = (ref.copy(), co)
         del keep
+
+
+def _reference_merge(srcs, X, Z):
+    """__combine_indices / __combine_old_indices (scripts/gvom.py:1009-1063)
+    restated in numpy, source after source: a voxel becomes occupied (True)
+    where a source holds an occupied entry and the combined value is not
+    occupied yet (the previous combined map only while that value is
+    >= -11); a free entry o <= -2 adds o + 1 while the value is not
+    occupied.  Returns (occupied mask, combined values)."""
+    V = X * X * Z
+    c = np.full(V, -1, np.int64)
+    occ = np.zeros(V, bool)
+    z, y, x = np.meshgrid(np.arange(Z), np.arange(X), np.arange(X), indexing="ij")
+    x, y, z = x.reshape(-1), y.reshape(-1), z.reshape(-1)
+    for idx, (dx, dy, dz), last in srcs:
+        xs, ys, zs = x + dx, y + dy, z + dz
+        inb = (xs >= 0) & (xs < X) & (ys >= 0) & (ys < X) & (zs >= 0) & (zs < Z)
+        o = np.full(V, -1, np.int64)
+        o[inb] = idx[(xs + ys * X + zs * X * X)[inb]]
+        free = ~occ
+        take = free & (o >= 0) & ((c >= -11) if last else True)
+        add = free & ~take & (o < -1)
+        occ |= take
+        c[add] += o[add] + 1
+    return occ, c
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_kernel_index_merge_random_rings(merge_lib, seed):
+    """Random rings of 1-16 slot index maps (occupied entries, unknown ones
+    and free counts around the -11 return threshold) plus, half the time, a
+    previous combined map, with random ego shifts: the kernel's merge block
+    (AND for occupancy, clamped sum for the pass count) against the
+    reference's rule restated source by source."""
+    rng = np.random.default_rng(100 + seed)
+    for _ in range(4):
+        X, Z = int(rng.integers(5, 13)), int(rng.integers(KZC // 2, 2 * KZC + 3))
+        V = X * X * Z
+        nsl = int(rng.integers(1, 17))
+        srcs = []
+        for s in range(nsl + int(rng.integers(0, 2))):
+            u = rng.random(V)
+            idx = np.where(u < 0.15, rng.integers(0, 1000, V),
+                           np.where(u < 0.55, -1, -rng.integers(2, 9, V))).astype(np.int32)
+            shift = tuple(int(v) for v in rng.integers(-3, 4, 3))
+            srcs.append((np.ascontiguousarray(idx), shift, 1 if s == nsl else 0))
+        ptrs = (C.c_void_p * len(srcs))(*[s[0].ctypes.data for s in srcs])
+        ar = lambda v: np.ascontiguousarray(np.array(v, np.int32))  # noqa: E731
+        dx, dy, dz = (ar([s[1][a] for s in srcs]) for a in range(3))
+        last = ar([s[2] for s in srcs])
+        got = np.empty(V, np.int32)
+        assert merge_lib.merge_all(ptrs, dx.ctypes.data, dy.ctypes.data, dz.ctypes.data, last.ctypes.data,
+                                   len(srcs), X, Z, got.ctypes.data) == 0
+        occ, c = _reference_merge([(s[0].astype(np.int64), s[1], s[2]) for s in srcs], X, Z)
+        np.testing.assert_array_equal(got >= 0, occ)
+        np.testing.assert_array_equal(got[~occ], c[~occ])
+        assert occ.any() and (c[~occ] < -11).any()  # both branches of the return rule reached
