@@ -120,3 +120,88 @@ def test_kernel_guess_search_equals_oracle(guess_lib, name):
         got = np.empty((X, X))
         assert guess_lib.guess_all(H.ctypes.data, inf.ctypes.data, X, got.ctypes.data) == 0
         np.testing.assert_array_equal(got, m["guess"], f"{name}")
+
+
+def _reference_guess(H, inf, X, x0, y0):
+    """__guess_height (scripts/gvom.py:592-714) for one cell, restated in
+    Python with its quirks: the loop condition tests x_n_done twice and not
+    x_p_done, the x ranges of the two y directions differ from the y ranges
+    of the two x directions, and x_nh's test guards y_nh.  0.0 where the
+    reference writes nothing."""
+    if H[x0][y0] > -1000 or inf[x0][y0] == -1000.0:
+        return 0.0
+    xpd = xnd = ypd = ynd = False
+    xp = xn = x0
+    yp = yn = y0
+    xph = xnh = yph = ynh = -1000
+    i = 0
+    while i < 15 and not (xnd and xnd and ypd and ynd):
+        xp += 1
+        xn -= 1
+        yp += 1
+        yn -= 1
+        i += 1
+        if not xpd:
+            if xp < X:
+                for dy in range(-i, i):
+                    if 0 <= y0 + dy < X and H[xp][y0 + dy] > -1000:
+                        xph, xpd = H[xp][y0 + dy], True
+                        break
+            else:
+                xpd = True
+        if not xnd:
+            if xn >= 0:
+                for dy in range(-i + 1, i + 1):
+                    if 0 <= y0 + dy < X and H[xn][y0 + dy] > -1000:
+                        xnh, xnd = H[xn][y0 + dy], True
+                        break
+            else:
+                xnd = True
+        if not ypd:
+            if yp < X:
+                for dx in range(-i + 1, i + 1):
+                    if 0 <= x0 + dx < X and H[x0 + dx][yp] > -1000:
+                        yph, ypd = H[x0 + dx][yp], True
+                        break
+            else:
+                ypd = True
+        if not ynd:
+            if yn >= 0:
+                for dx in range(-i, i):
+                    if 0 <= x0 + dx < X and H[x0 + dx][yn] > -1000:
+                        ynh, ynd = H[x0 + dx][yn], True
+                        break
+            else:
+                ynd = True
+    mn, mx = 1000.0, inf[x0][y0]
+    if xph > -1000:
+        mn, mx = min(xph, mn), max(xph, mx)
+    if xnh > -1000:
+        mn, mx = min(xnh, mn), max(xnh, mx)
+    if yph > -1000:
+        mn, mx = min(yph, mn), max(yph, mx)
+    if xnh > -1000:
+        mn, mx = min(ynh, mn), max(ynh, mx)
+    dh = mx - mn
+    return dh if dh > 0 else 0.0
+
+
+@pytest.mark.parametrize("density", [0.02, 0.08, 0.3, 0.7])
+def test_kernel_guess_search_on_random_maps(guess_lib, density):
+    """Random sparse height and inferred-height maps (known cells at several
+    densities, so rings reach from one cell to the 15-cell limit and the map
+    edges): the kernel's search through its next-known tables against the
+    Python restatement, bit for bit on every cell."""
+    rng = np.random.default_rng(int(density * 1000))
+    X = 48
+    for _ in range(3):
+        H = np.where(rng.random((X, X)) < density, rng.normal(1.0, 2.0, (X, X)), -1000.0)
+        inf = np.where(rng.random((X, X)) < 0.8, rng.normal(0.0, 2.0, (X, X)), -1000.0)
+        H = np.ascontiguousarray(H, np.float64)
+        inf = np.ascontiguousarray(inf, np.float64)
+        got = np.empty((X, X))
+        assert guess_lib.guess_all(H.ctypes.data, inf.ctypes.data, X, got.ctypes.data) == 0
+        Hl, il = H.tolist(), inf.tolist()
+        ref = np.array([[_reference_guess(Hl, il, X, x, y) for y in range(X)] for x in range(X)])
+        np.testing.assert_array_equal(got.view(np.uint64), ref.view(np.uint64))
+        assert (ref > 0).any()
