@@ -131,3 +131,84 @@ def test_kernel_columns_equal_oracle(columns_lib, name):
         np.testing.assert_array_equal(inf, m["inferred"], f"{name} inferred")
         steep = np.hypot(m["slope_x"], m["slope_y"]) >= p[8]
         np.testing.assert_array_equal(pd[~steep], out[1][~steep], f"{name} band density")
+
+
+def _reference_columns(idx, hit, total, minh, X, Z, co, ego, xy_res, z_res, robot_r, lidar_h, pos_thr, robot_h):
+    """__make_height_map, __make_inferred_height_map and the band density of
+    __make_positive_obstacle_map (scripts/gvom.py:515-590) restated in Python
+    floats per column, the voxel's record fields given per voxel: (height,
+    inferred height, band density)."""
+    import math
+    H = np.full((X, X), -1000.0)
+    INF = np.full((X, X), -1000.0)
+    PD = np.zeros((X, X), np.int64)
+    for x in range(X):
+        for y in range(X):
+            xp = ((co[0] + x) * xy_res) - ego[0]
+            yp = ((co[1] + y) * xy_res) - ego[1]
+            if xp * xp + yp * yp <= robot_r * robot_r:
+                H[x, y] = ego[2] - lidar_h
+            for z in range(Z):
+                v = x + y * X + z * X * X
+                if idx[v] >= 0:
+                    H[x, y] = (float(minh[v]) + z + co[2]) * z_res
+                    break
+            for z in range(Z):
+                if idx[x + y * X + z * X * X] < -1:
+                    INF[x, y] = (z + co[2]) * z_res
+                    break
+            lo = int(math.floor(((H[x, y] + pos_thr) / z_res) - co[2])) + 1
+            hi = int(math.floor(((H[x, y] + robot_h) / z_res) - co[2]))
+            if not (0 <= lo < Z and 0 <= hi < Z):
+                continue
+            dens = n = 0.0
+            for z in range(lo, hi + 1):
+                v = x + y * X + z * X * X
+                if idx[v] >= 0 and hit[v] > 10:
+                    n += float(total[v])
+                    dens += float(hit[v])
+            if n > 0.0:
+                dens /= n
+            PD[x, y] = int(dens * 100)
+    return H, INF, PD
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_kernel_columns_on_random_maps(columns_lib, seed):
+    """Random combined maps (occupied voxels with hit / total counts and
+    in-voxel heights, some placed so that the band limits fall within 1e-6
+    of a voxel boundary; free and unknown voxels; a robot disc; varied
+    origins and resolutions): heights, inferred heights and band densities
+    equal to the Python restatement, the heights bit for bit."""
+    rng = np.random.default_rng(50 + seed)
+    X, Z = 14, 24
+    V = X * X * Z
+    for trial in range(3):
+        z_res = (0.1, 0.15, 0.2)[trial]
+        xy_res, pos_thr, robot_h = 0.2, (0.3, 0.25, 0.5)[seed % 3], 2.0
+        co = np.ascontiguousarray(np.array([rng.integers(-40, 40), rng.integers(-40, 40), rng.integers(-10, 10)],
+                                           np.float64))
+        ego = np.ascontiguousarray(np.array([(co[0] + X / 2) * xy_res, (co[1] + X / 2) * xy_res, 1.0]))
+        u = rng.random(V)
+        idx = np.where(u < 0.2, 0, np.where(u < 0.6, -1, -2 - rng.integers(0, 5, V))).astype(np.int32)
+        # make most columns have their lowest occupied voxel in the lower half
+        hit = rng.integers(0, 40, V).astype(np.int32)
+        total = (hit + rng.integers(0, 40, V)).astype(np.int32)
+        minh = rng.random(V).astype(np.float32)
+        # in-voxel heights that put minh + pos_thr / z_res within 1e-6 of an integer
+        near = rng.random(V) < 0.3
+        frac = np.float32(pos_thr / z_res - np.floor(pos_thr / z_res))
+        minh[near] = np.clip(np.float32(1.0) - frac + rng.normal(0, 1e-6, near.sum()).astype(np.float32), 0, 0.9999)
+        vidx = np.ascontiguousarray(np.where(idx >= 0, np.arange(V), idx).astype(np.int32))
+        h, inf = np.empty((X, X)), np.empty((X, X))
+        pd = np.empty((X, X), np.int32)
+        robot_r, lidar_h = 0.6, 0.8
+        columns_lib.columns_all(vidx.ctypes.data, hit.ctypes.data, total.ctypes.data, minh.ctypes.data, X, Z,
+                                co.ctypes.data, ego.ctypes.data, xy_res, z_res, robot_r, lidar_h, pos_thr, robot_h,
+                                h.ctypes.data, inf.ctypes.data, pd.ctypes.data)
+        H, INF, PD = _reference_columns(idx, hit, total, minh, X, Z, co, ego, xy_res, z_res, robot_r, lidar_h,
+                                        pos_thr, robot_h)
+        np.testing.assert_array_equal(h.view(np.uint64), H.view(np.uint64))
+        np.testing.assert_array_equal(inf.view(np.uint64), INF.view(np.uint64))
+        np.testing.assert_array_equal(pd, PD)
+        assert (PD > 0).any()
