@@ -134,3 +134,57 @@ def test_kernel_cell_path_within_tolerance(cell_lib, name):
         assert_rel(r, out[3], f"{name} roughness", atol=1e-9)
         assert_rel(sx, m["slope_x"], f"{name} slope x", atol=SLOPE_ATOL)
         assert_rel(sy, m["slope_y"], f"{name} slope y", atol=SLOPE_ATOL)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_kernel_cell_path_on_random_terrain(cell_lib, seed):
+    """Random voxel-quantised terrains -- each height built as the columns
+    pass builds it, (in-voxel fraction + lowest occupied z + origin z) times
+    z_res, from random slopes, steps, noise and flat stretches -- with a
+    robot-disc patch and unknown cells, through the kernel's whole per-cell
+    path (float32 fit, its rules, the closed forms, the queued float64
+    sequence), against a plain-Python restatement of __calculate_slope at the
+    parity tolerance."""
+    from test_slope_f64_host import _reference_slope
+    rng = np.random.default_rng(300 + seed)
+    X = 40
+    for trial in range(3):
+        xy_res, z_res = (0.15, 0.2, 0.1)[trial], (0.15, 0.1, 0.2)[(trial + seed) % 3]
+        oz = int(rng.integers(-30, 30))
+        xs, ys = np.meshgrid(np.arange(X), np.arange(X), indexing="ij")
+        kind = (trial + seed) % 4
+        if kind == 0:  # plane with noise
+            h = 0.05 * xs * xy_res + 0.12 * ys * xy_res + rng.normal(0, 0.02, (X, X))
+        elif kind == 1:  # steps and flat stretches
+            h = np.where(xs < X // 2, 0.0, 0.6) + np.where(ys % 9 < 4, 0.0, 0.3)
+        elif kind == 2:  # rough ground
+            h = rng.normal(0, 0.3, (X, X))
+        else:  # a gentle ramp (small slopes, near-cancelling residuals)
+            h = 0.002 * xs + 0.001 * ys + rng.normal(0, 1e-4, (X, X))
+        w = h / z_res - oz  # in voxel units above the origin
+        zl = np.floor(w).astype(np.int32)
+        ml = (w - zl).astype(np.float32)
+        H = (ml.astype(np.float64) + zl + oz) * z_res  # the columns pass's height
+        disc = (xs - X // 3) ** 2 + (ys - X // 3) ** 2 <= 9  # robot disc: one float64 height, no voxel
+        H[disc] = 0.7
+        zl[disc] = -1
+        ml[disc] = 0.0
+        unknown = rng.random((X, X)) < 0.15
+        H[unknown] = -1000.0
+        zl[unknown] = -1
+        ml[unknown] = 0.0
+        H, zl, ml = (np.ascontiguousarray(a) for a in (H, zl, ml))
+        r, sx, sy = (np.empty((X, X)) for _ in range(3))
+        q = C.c_int()
+        assert cell_lib.cells_all(H.ctypes.data, zl.ctypes.data, ml.ctypes.data, X, xy_res, z_res, r.ctypes.data,
+                                  sx.ctypes.data, sy.ctypes.data, C.byref(q)) == 0
+        Hl = H.tolist()
+        rr, rx, ry = np.full((X, X), -1.0), np.zeros((X, X)), np.zeros((X, X))
+        for x0 in range(X):
+            for y0 in range(X):
+                ref = _reference_slope(Hl, X, xy_res, x0, y0)
+                if ref is not None:
+                    rr[x0, y0], rx[x0, y0], ry[x0, y0] = ref
+        assert_rel(r, rr, f"seed {seed} trial {trial} roughness", atol=1e-9)
+        assert_rel(sx, rx, f"seed {seed} trial {trial} slope x", atol=SLOPE_ATOL)
+        assert_rel(sy, ry, f"seed {seed} trial {trial} slope y", atol=SLOPE_ATOL)
