@@ -78,3 +78,39 @@ def test_kernel_eigen_solve_within_tolerance_of_reference(eigen_lib, name):
         assert_eigen(got, st["eigen"], f"{name} eigenvalues")
         n_checked += len(cov)
     assert n_checked > 0
+
+
+def test_kernel_eigen_solve_on_random_covariances(eigen_lib):
+    """Random symmetric covariances in float32 -- generic, isotropic, two equal
+    eigenvalues, planar and linear (the smallest one or two eigenvalues 1e-9
+    to 1e-4 of the largest), scales from 1e-6 to 1e2 -- against float64
+    eigenvalues of the same float32 matrices (numpy), at the parity
+    tolerance."""
+    rng = np.random.default_rng(8)
+    covs, ref = [], []
+    for i in range(6000):
+        Q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        s = 10.0 ** rng.uniform(-6, 2)
+        kind = i % 6
+        if kind == 0:
+            lam = rng.random(3)
+        elif kind == 1:
+            lam = np.ones(3)
+        elif kind == 2:
+            lam = np.array([1.0, 1.0, rng.random()])
+        elif kind == 3:
+            lam = np.array([1.0, rng.random(), rng.random()])
+            lam[2] = lam[0] * 10.0 ** rng.uniform(-9, -4)
+        elif kind == 4:
+            lam = np.array([1.0, 10.0 ** rng.uniform(-9, -4), 10.0 ** rng.uniform(-9, -4)])
+        else:
+            lam = np.array([1.0, 1.0 - 10.0 ** rng.uniform(-7, -2), rng.random()])
+        A = (Q * (lam * s)) @ Q.T
+        c = np.array([A[0, 0], A[0, 1], A[0, 2], A[1, 1], A[1, 2], A[2, 2]], np.float32)
+        B = np.array([[c[0], c[1], c[2]], [c[1], c[3], c[4]], [c[2], c[4], c[5]]], np.float64)
+        covs.append(c)
+        ref.append(np.sort(np.linalg.eigvalsh(B))[::-1])
+    cov = np.ascontiguousarray(np.array(covs, np.float32))
+    got = np.empty((len(cov), 3), np.float32)
+    eigen_lib.eigen_all(cov.ctypes.data, len(cov), got.ctypes.data)
+    assert_eigen(np.sort(got, axis=1)[:, ::-1], np.array(ref), "random covariances")
