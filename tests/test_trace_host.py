@@ -279,3 +279,89 @@ def test_kernel_trace_reads_pointcloud2_bytes(trace_lib, name):
                                     hit.ctypes.data, total.ctypes.data, 1, off.ctypes.data, None) == 0
         np.testing.assert_array_equal(hit, ref_hit, f"{name} scan {pi} hits")
         np.testing.assert_array_equal(total, ref_total, f"{name} scan {pi} totals")
+
+
+def _adversarial_scan(rng, res, zres, X, Z, ego, n):
+    """Points around `ego`: uniform in and beyond the map, on voxel
+    boundaries, in the float sliver just below zero, inside the minimum
+    distance, and non-finite."""
+    half = X * res / 2
+    p = [ego + rng.uniform(-1.3 * half, 1.3 * half, (n, 3)) * [1, 1, 0.2]]
+    k = rng.integers(-X, X, (n // 4, 3)).astype(np.float64)
+    p.append(np.floor(ego / [res, res, zres]) * [res, res, zres] + k * [res, res, zres])  # on boundaries
+    s = ego + rng.uniform(-half, half, (n // 8, 3)) * [1, 1, 0.2]
+    s[:, rng.integers(0, 3)] = -rng.choice([1e-7, 2.0 ** -21, 2.0 ** -24, 1e-30, 0.0], n // 8)  # the sliver
+    p.append(s)
+    p.append(ego + rng.normal(0, 0.3, (n // 16, 3)))  # within the minimum distance
+    bad = ego + rng.uniform(-1, 1, (8, 3))
+    bad[:3, 0] = [np.nan, np.inf, -np.inf]
+    p.append(bad)
+    return np.concatenate(p)
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_kernel_trace_counts_on_adversarial_scans(trace_lib, seed):
+    """Random scans built to reach the exact paths of the per-point code --
+    points on voxel boundaries, coordinates in (-2^-20, 0), rays leaving the
+    grid, points inside the minimum distance, non-finite points; float32 and
+    float64 points and transforms; maps near the world origin and 1e4 m away;
+    rays whose every step lies in the sliver -- against the oracle: hits,
+    totals and min heights equal."""
+    rng = np.random.default_rng(900 + seed)
+    res, zres = (0.2, 0.15)[seed % 2], (0.2, 0.1, 0.15)[seed % 3]
+    X, Z = int(rng.integers(20, 34)), int(rng.integers(10, 18))
+    p = (res, zres, X, Z, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    far = 1e4 if seed >= 4 else 0.0
+    ego = np.array([far + rng.uniform(-3, 3), far / 2 + rng.uniform(-3, 3), rng.uniform(-1, 1)])
+    V = X * X * Z
+    o = OracleGvom(*p)
+    for scan in range(3 if far == 0.0 else 2):
+        pts = _adversarial_scan(rng, res, zres, X, Z, ego, 3000)
+        dt = np.float32 if (seed + scan) % 2 == 0 else np.float64
+        if scan == 2:
+            # rays in the plane x = ego x, ego x just below zero: every step of
+            # them lies in the sliver (-2^-20, 0) voxels
+            ego = np.array([float(np.float32(-1e-21)), rng.uniform(-1, 1), 1.0])
+            pts = np.empty((3000, 3))
+            pts[:, 0] = ego[0]
+            pts[:, 1] = ego[1] + rng.uniform(-X * res / 2, X * res / 2, 3000)
+            pts[:, 2] = rng.uniform(-1.5, 2.5, 3000)
+            pts[:1000, 0] = -1e-9 * rng.random(1000)  # small negative x ends
+            dt, T = np.float32, None
+        elif scan == 0:
+            T = None
+        else:  # a sensor pose: rotation about z, translation to the ego; points in the sensor frame
+            a = rng.uniform(-0.2, 0.2)
+            R = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+            T = np.eye(4)
+            T[:3, :3] = R
+            T[:3, 3] = ego
+            T = T.astype(dt)
+            with np.errstate(invalid="ignore"):  # the non-finite rows stay non-finite
+                pts = (pts - ego) @ R  # R^T (w - ego), row by row
+        pts = np.ascontiguousarray(pts.astype(dt))
+        o.Process_pointcloud(pts, ego, T)
+        _, last = o.ring_state()
+        st = o.slot_state(last)
+        idx = np.asarray(st["index"]).reshape(-1)
+        ref_hit = np.zeros(V, np.int64)
+        ref_total = np.zeros(V, np.int64)
+        occ = idx >= 0
+        ref_hit[occ] = np.asarray(st["hit"])[idx[occ]]
+        ref_total[occ] = np.asarray(st["total"])[idx[occ]]
+        ref_total[~occ] = -idx[~occ].astype(np.int64) - 1
+        Td = None if T is None else np.ascontiguousarray(np.asarray(T, np.float64).reshape(4, 4))
+        tmode = 0 if T is None else (1 if T.dtype == np.float32 else 2)
+        e = np.ascontiguousarray(ego)
+        hit = np.empty(V, np.int32)
+        total = np.empty(V, np.int32)
+        minh = np.empty(V, np.float32)
+        rc = trace_lib.trace_scan(pts.ctypes.data, 0 if pts.dtype == np.float32 else 1, pts.shape[0], pts.shape[1],
+                                  e.ctypes.data, None if Td is None else Td.ctypes.data, tmode, res, zres, X, Z,
+                                  1, 1, p[5], hit.ctypes.data, total.ctypes.data, 0, None, minh.ctypes.data)
+        assert rc == 0
+        np.testing.assert_array_equal(hit, ref_hit, f"seed {seed} scan {scan} hits")
+        np.testing.assert_array_equal(total, ref_total, f"seed {seed} scan {scan} totals")
+        np.testing.assert_array_equal(minh[occ], np.asarray(st["min_h"], np.float32)[idx[occ]],
+                                      f"seed {seed} scan {scan} min height")
+        assert occ.sum() > 50
