@@ -749,7 +749,7 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
     const Geom g = pc.g;
     const int C = min(*(volatile int *)&sd.ctr->C, (int)sd.rec_cap);
     const CellMom *__restrict__ M = mom + sd.pt_base;
-    if (E3) {
+    if constexpr (E3 != 0) {
         const int lane = (int)lane_id(), sub = lane & 3;
         const int warp = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
         const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
@@ -783,24 +783,24 @@ __global__ void __launch_bounds__(256) k_voxel_stats(const ProcessConst pc, cons
             if (sub == 0) a.merge(o);
             if (c < C && sub == 0) a.store(&sd.rec[c]);
         }
-        return;
-    }
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
-        VoxelRec *r = &sd.rec[c];
-        const int gid = __float_as_int(r->aux[0]);
-        const int x = gid % g.X, y = (gid / g.X) % g.X, z = gid / (g.X * g.X);
-        const int e0 = (x + g.exy) + (y + g.exy) * g.Xe + (z + g.ez) * g.Xe * g.Xe;
-        NbAcc a;
-        a.init();
-        for (int dz = -g.ez; dz <= g.ez; dz++)
-            for (int dy = -g.exy; dy <= g.exy; dy++)
-                for (int dx = -g.exy; dx <= g.exy; dx++) {
-                    const unsigned long long v = sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe];
-                    if (!(v & 0xffffffffull)) continue;
-                    const CellMom cm = M[(int)(v >> 32)];
-                    a.add(cm, dx, dy, dz);
-                }
-        a.store(r);
+    } else {
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+            VoxelRec *r = &sd.rec[c];
+            const int gid = __float_as_int(r->aux[0]);
+            const int x = gid % g.X, y = (gid / g.X) % g.X, z = gid / (g.X * g.X);
+            const int e0 = (x + g.exy) + (y + g.exy) * g.Xe + (z + g.ez) * g.Xe * g.Xe;
+            NbAcc a;
+            a.init();
+            for (int dz = -g.ez; dz <= g.ez; dz++)
+                for (int dy = -g.exy; dy <= g.exy; dy++)
+                    for (int dx = -g.exy; dx <= g.exy; dx++) {
+                        const unsigned long long v = sd.cnt[e0 + dx + dy * g.Xe + dz * g.Xe * g.Xe];
+                        if (!(v & 0xffffffffull)) continue;
+                        const CellMom cm = M[(int)(v >> 32)];
+                        a.add(cm, dx, dy, dz);
+                    }
+            a.store(r);
+        }
     }
 }
 
