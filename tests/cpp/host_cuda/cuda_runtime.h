@@ -2,7 +2,9 @@
  * be compiled by a host compiler for the CPU tests (tests/test_trace_host.py):
  * qualifiers become nothing, the correctly rounded intrinsics become plain
  * IEEE operations (compile with -ffp-contract=off -frounding-math), atomics
- * become sequential updates.  Not part of the library. */
+ * become host atomics, and the thread and block indices are per host thread
+ * (block_threads.h runs a block's threads on host threads).  Not part of the
+ * library. */
 #pragma once
 #include <cfenv>
 #include <climits>
@@ -26,7 +28,7 @@ typedef int cudaError_t;
 typedef struct CUstream_st *cudaStream_t;
 typedef struct CUevent_st *cudaEvent_t;
 struct HostDim3 { unsigned x, y, z; };
-static HostDim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1};
+static thread_local HostDim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1}, gridDim = {1, 1, 1};
 
 static inline float __fadd_rn(float a, float b) { return a + b; }
 static inline float __fsub_rn(float a, float b) { return a - b; }
@@ -48,13 +50,15 @@ static inline int __float2int_rd(float f) { return (int)std::floor(f); }
 static inline int __float_as_int(float f) { int i; std::memcpy(&i, &f, 4); return i; }
 static inline float __int_as_float(int i) { float f; std::memcpy(&f, &i, 4); return f; }
 static inline unsigned long long atomicAdd(unsigned long long *p, unsigned long long v) {
-    const unsigned long long o = *p; *p = o + v; return o;
+    return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST);
 }
-static inline unsigned atomicAdd(unsigned *p, unsigned v) { const unsigned o = *p; *p = o + v; return o; }
+static inline unsigned atomicAdd(unsigned *p, unsigned v) { return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST); }
 static inline unsigned atomicCAS(unsigned *p, unsigned cmp, unsigned v) {
-    const unsigned o = *p; if (o == cmp) *p = v; return o;
+    __atomic_compare_exchange_n(p, &cmp, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
+    return cmp;  // the old value
 }
-static inline int atomicAdd(int *p, int v) { const int o = *p; *p = o + v; return o; }
+static inline int atomicAdd(int *p, int v) { return __atomic_fetch_add(p, v, __ATOMIC_SEQ_CST); }
+static inline int atomicOr(int *p, int v) { return __atomic_fetch_or(p, v, __ATOMIC_SEQ_CST); }
 static inline long long __double_as_longlong(double d) { long long i; std::memcpy(&i, &d, 8); return i; }
 static inline double __longlong_as_double(long long i) { double d; std::memcpy(&d, &i, 8); return d; }
 static inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
