@@ -32,7 +32,7 @@ struct dim3 {
 
 namespace block_threads {
 
-constexpr int kPoolThreads = 256;  // the largest block this emulates
+constexpr int kPoolThreads = 1024;  // the largest block this emulates
 
 struct BlockState {
     std::unique_ptr<std::barrier<>> bar;
@@ -129,6 +129,31 @@ inline void launch(dim3 grid, dim3 blk, const std::function<void()> &fn) {
 
 static inline void __syncthreads() { block_threads::cur->bar->arrive_and_wait(); }
 
+static inline void __syncwarp(unsigned = 0xffffffffu) {
+    block_threads::cur->warp[block_threads::linear_tid() >> 5]->arrive_and_wait();
+}
+
+// the lanes of the caller's warp whose predicate is non-zero (every lane
+// of the warp takes part)
+static inline unsigned __ballot_sync(unsigned, int pred) {
+    using namespace block_threads;
+    const int t = linear_tid(), w = t >> 5;
+    unsigned long long *x = cur->xchg[parity];
+    parity ^= 1u;
+    x[t] = pred != 0;
+    cur->warp[w]->arrive_and_wait();
+    unsigned m = 0;
+    for (int l = 0; l < 32; l++)
+        if (x[(w << 5) + l]) m |= 1u << l;
+    return m;
+}
+
+// lane `src` of the caller's `width`-lane segment of the warp
+template <class T>
+static inline T __shfl_sync(unsigned, T v, int src, int width = 32) {
+    const int lane = block_threads::linear_tid() & 31;
+    return block_threads::exchange(v, (lane & ~(width - 1)) + (src & (width - 1)), true);
+}
 template <class T>
 static inline T __shfl_up_sync(unsigned, T v, unsigned d) {
     const int lane = block_threads::linear_tid() & 31;

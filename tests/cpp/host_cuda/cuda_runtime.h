@@ -16,7 +16,7 @@
 #define __host__
 #define __global__
 #define __forceinline__ inline
-#define __align__(n) alignas(n)
+#define __align__(n) __attribute__((aligned(n)))
 #define __launch_bounds__(...)
 #define __grid_constant__
 
@@ -28,7 +28,7 @@ typedef int cudaError_t;
 typedef struct CUstream_st *cudaStream_t;
 typedef struct CUevent_st *cudaEvent_t;
 struct HostDim3 { unsigned x, y, z; };
-static thread_local HostDim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1}, gridDim = {1, 1, 1};
+inline thread_local HostDim3 threadIdx = {0, 0, 0}, blockIdx = {0, 0, 0}, blockDim = {1, 1, 1}, gridDim = {1, 1, 1};
 
 static inline float __fadd_rn(float a, float b) { return a + b; }
 static inline float __fsub_rn(float a, float b) { return a - b; }

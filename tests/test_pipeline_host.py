@@ -1,0 +1,483 @@
+"""The library's scan->map path end to end on the CPU: every process and
+combine kernel (gvom_gb300/csrc/k_process.cu, k_combine.cu) compiled
+unchanged for the host and launched through the library's own launchers
+(launch_process, launch_combine), each block run with one host thread per
+CUDA thread (tests/cpp/host_cuda/block_threads.h).  A small host mapper
+keeps what the library's instance keeps -- the ring of slots, the
+double-buffered combined map addressed by voxel id, the 2-D maps -- and
+fills the launch parameters as prepare_scans / prepare_combine in
+gvom_gb300/csrc/gvom_capi.cu do.  It is replayed through every golden fixture
+with the comparison the GPU parity tests use (replay.replay_and_compare):
+every slot, every combined map with its eigenvalues, and every combine's
+maps, against the outputs of the reference itself."""
+import ctypes as C
+import os
+import re
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_files
+from replay import load, params_of, replay_and_compare
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc")
+
+PRELUDE = r"""
+#include <algorithm>
+#include <cmath>
+using std::isfinite; using std::isnan; using std::max; using std::min;
+#include "cuda_runtime.h"
+#include "block_threads.h"
+// CUDA's integer min / max take their operands by value (a volatile read
+// included)
+static inline int min(int a, int b) { return a < b ? a : b; }
+static inline int max(int a, int b) { return a > b ? a : b; }
+static inline long long min(long long a, long long b) { return a < b ? a : b; }
+static inline long long max(long long a, long long b) { return a > b ? a : b; }
+template <class T> static inline T __ldg(const T *p) { return *p; }
+static inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
+    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+}
+static inline float __fdividef(float a, float b) { return a / b; }
+static inline float __frcp_rn(float x) { return 1.0f / x; }
+static inline float rsqrtf(float x) { return 1.0f / std::sqrt(x); }
+static inline int __ffs(int x) { return __builtin_ffs(x); }
+constexpr cudaError_t cudaSuccess = 0;
+static inline cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
+static inline cudaError_t cudaGetLastError() { return cudaSuccess; }
+struct cudaFuncAttributes { int unused; };
+static inline cudaError_t cudaFuncGetAttributes(cudaFuncAttributes *, const void *) { return cudaSuccess; }
+#include "gvom_internal.cuh"
+namespace gvom {
+// a launch runs every block of the grid under the block emulator
+template <typename... P>
+cudaError_t rec_kernel(void (*fn)(P...), dim3 grid, dim3 block, size_t, cudaStream_t, std::decay_t<P>... args) {
+    block_threads::launch(grid, block, [&] { fn(args...); });
+    return cudaSuccess;
+}
+static inline cudaError_t rec_event_external(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
+static inline cudaError_t rec_event_internal(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
+}  // namespace gvom
+"""
+
+MAPPER = r"""
+#include "host_scan.h"
+#include <vector>
+
+using namespace gvom;
+
+namespace {
+
+struct Slot {
+    std::vector<int> idx;
+    std::vector<VoxelRec> rec;
+    int C = 0;
+    double od[3] = {0, 0, 0};
+    bool valid = false;
+};
+
+// what a library instance keeps (gvom_create in gvom_capi.cu), in host memory
+struct HostMap {
+    double p[14];  // the constructor's parameters, in order
+    Geom g;
+    int B;
+    int buffer_index = 0, last_buffer_index = 0;
+    std::vector<Slot> slots;
+    std::vector<int> cidx[2], occ_list[2];
+    std::vector<VoxelRec> crec[2];
+    std::vector<int2> colinfo[2];
+    int combC[2] = {0, 0};
+    double cod[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    int cur = 0;
+    bool have_comb = false;
+    std::vector<double> height, inferred, slope_x, slope_y, guess;
+    std::vector<int> pos_density, zlow;
+    std::vector<float> mlow;
+    std::vector<double> out;  // roughness | positive | negative | visibility, as the device block
+    double ego[3] = {0, 0, 0};
+    Tuning tun = kDefaultTuning;
+    int num_sms = 2;
+    double *rough() { return out.data(); }
+    int *pos() { return reinterpret_cast<int *>(out.data() + (size_t)g.X * g.X); }
+    int *neg() { return pos() + (size_t)g.X * g.X; }
+    int *vis() { return neg() + (size_t)g.X * g.X; }
+};
+
+}  // namespace
+
+extern "C" HostMap *hm_create(const double *params, int maps_tile, int merge_planes, int num_sms) {
+    HostMap *h = new HostMap;
+    for (int i = 0; i < 14; i++) h->p[i] = params[i];
+    Geom &g = h->g;
+    g.X = (int)params[2]; g.Z = (int)params[3]; g.exy = (int)params[12]; g.ez = (int)params[13];
+    g.Xe = g.X + 2 * g.exy; g.Ze = g.Z + 2 * g.ez;
+    g.V = (long long)g.X * g.X * g.Z; g.Vext = (long long)g.Xe * g.Xe * g.Ze;
+    h->B = (int)params[4];
+    h->slots.resize(h->B);
+    const size_t X2 = (size_t)g.X * g.X;
+    for (int b = 0; b < 2; b++) {
+        h->cidx[b].assign(g.V, 0);
+        h->occ_list[b].assign(g.V, 0);
+        h->crec[b].assign(g.V, VoxelRec{});
+        h->colinfo[b].assign(X2 * ((g.Z + 3) / 4), int2{0, 0});
+    }
+    for (auto *m : {&h->height, &h->inferred, &h->slope_x, &h->slope_y, &h->guess}) m->assign(X2, 0.0);
+    h->pos_density.assign(X2, 0);
+    h->zlow.assign(X2, 0);
+    h->mlow.assign(X2, 0.f);
+    h->out.assign((X2 * 20 + 7) / 8, 0.0);
+    h->tun.maps_tile = maps_tile;
+    h->tun.merge_planes = merge_planes;
+    h->num_sms = num_sms;
+    return h;
+}
+
+extern "C" void hm_destroy(HostMap *h) { delete h; }
+
+// Process_pointcloud into the ring slot at buffer_index (prepare_scans,
+// launch_scans, commit_scans); tdtype -1 none, 0 float32, 1 float64; T 16
+// doubles
+extern "C" int hm_process(HostMap *h, const void *pts, int dtype, long long n, long long stride, const double *ego,
+                          const double *T, int tdtype) {
+    const Geom &g = h->g;
+    const ProcessConst pc = host_scan::process_const(g.X, g.Z, g.exy, g.ez, h->p[0], h->p[1], h->p[5], 1, h->num_sms);
+    Slot &s = h->slots[h->buffer_index];
+    s.idx.assign(g.V, -1);  // the slot's index map before the scan
+    s.rec.assign(std::max<long long>(n, 1), VoxelRec{});
+    std::vector<unsigned long long> cnt(g.Vext, 0ull);
+    ScanCounters ctr;
+    std::memset(&ctr, 0, sizeof ctr);
+    double Tr[12] = {0};
+    if (T)
+        for (int r = 0; r < 12; r++) Tr[r] = T[r];
+    ScanDesc d;
+    host_scan::scan_desc(d, pc, pts, n, stride, T ? (tdtype == 0 ? 1 : 2) : 0, ego, Tr);
+    d.block_begin = 0;
+    d.nblocks = (int)((n + h->tun.pts_block - 1) / h->tun.pts_block);
+    d.pt_base = 0;
+    d.cnt = cnt.data();
+    d.idx = s.idx.data();
+    d.rec = s.rec.data();
+    d.rec_cap = (long long)s.rec.size();
+    d.ctr = &ctr;
+    const long long np = std::max<long long>(n, 1);
+    std::vector<float4> prec(np), sorted(np);
+    std::vector<int> prank(np);
+    std::vector<unsigned char> mom((size_t)np * kCellMomBytes);
+    if (launch_process(pc, &d, 1, std::max(d.nblocks, 1), (int)std::min<long long>(n, g.V), dtype, prec.data(),
+                       prank.data(), sorted.data(), mom.data(), nullptr, nullptr, h->tun.pts_block, nullptr, nullptr,
+                       0, false) != cudaSuccess)
+        return 4;
+    if (ctr.overflow) return 4;
+    s.C = ctr.C;
+    for (int a = 0; a < 3; a++) s.od[a] = d.od[a];
+    s.valid = true;
+    for (int a = 0; a < 3; a++) h->ego[a] = ego[a];
+    h->last_buffer_index = h->buffer_index;
+    h->buffer_index = (h->buffer_index + 1) % h->B;
+    return 0;
+}
+
+// combine_maps (prepare_combine, launch_combine, commit_combine, copy_outputs)
+extern "C" int hm_combine(HostMap *h, double *origin, int *pos, int *neg, double *rough, int *vis) {
+    const Slot &ls = h->slots[h->last_buffer_index];
+    if (!ls.valid) return 1;
+    const Geom &g = h->g;
+    const int nb = h->have_comb ? 1 - h->cur : 0;
+    MergeParams mp;
+    std::memset(&mp, 0, sizeof mp);
+    mp.g = g;
+    for (int a = 0; a < 3; a++) mp.co[a] = ls.od[a];
+    int ns = 0;
+    for (int i = 0; i < h->B; i++) {  // ring order
+        const Slot &s = h->slots[i];
+        if (!s.valid) continue;
+        MergeSrc &m = mp.src[ns++];
+        m.idx = s.idx.data();
+        m.rec = s.rec.data();
+        m.dx = (int)(mp.co[0] - s.od[0]);
+        m.dy = (int)(mp.co[1] - s.od[1]);
+        m.dz = (int)(mp.co[2] - s.od[2]);
+        m.is_last = 0;
+    }
+    if (h->have_comb) {
+        MergeSrc &m = mp.src[ns++];
+        m.idx = h->cidx[h->cur].data();
+        m.rec = h->crec[h->cur].data();
+        m.dx = (int)(mp.co[0] - h->cod[h->cur][0]);
+        m.dy = (int)(mp.co[1] - h->cod[h->cur][1]);
+        m.dz = (int)(mp.co[2] - h->cod[h->cur][2]);
+        m.is_last = 1;
+    }
+    mp.nsrc = ns;
+    mp.out_idx = h->cidx[nb].data();
+    mp.out_rec = h->crec[nb].data();
+    mp.out_count = &h->combC[nb];
+    mp.list = h->occ_list[nb].data();
+    mp.num_sms = h->num_sms;
+    mp.planes = h->tun.merge_planes;
+    mp.stats_bpsm = h->tun.stats_bpsm;
+    mp.colinfo = h->colinfo[nb].data();
+    const double *p = h->p;
+    ColumnParams cp;
+    std::memset(&cp, 0, sizeof cp);
+    cp.X = g.X;
+    cp.Z = g.Z;
+    cp.planes = h->tun.merge_planes;
+    cp.idx = mp.out_idx;
+    cp.rec = mp.out_rec;
+    cp.colinfo = mp.colinfo;
+    for (int a = 0; a < 3; a++) {
+        cp.co[a] = mp.co[a];
+        cp.ego[a] = h->ego[a];
+    }
+    cp.xy_res = p[0];
+    cp.z_res = p[1];
+    cp.robot_r2 = p[10] * p[10];
+    cp.disc_h = h->ego[2] - p[11];
+    cp.pos_thr = p[6];
+    cp.robot_h = p[9];
+    cp.pthr_v = (float)(p[6] / p[1]);
+    cp.robh_v = (float)(p[9] / p[1]);
+    cp.base_xf = (float)(mp.co[0] * p[0] - h->ego[0]);
+    cp.base_yf = (float)(mp.co[1] * p[0] - h->ego[1]);
+    cp.res_f = (float)p[0];
+    cp.r2_f = (float)cp.robot_r2;
+    cp.height = h->height.data();
+    cp.inferred = h->inferred.data();
+    cp.pos_density = h->pos_density.data();
+    cp.zlow = h->zlow.data();
+    cp.mlow = h->mlow.data();
+    Maps2DParams m2;
+    std::memset(&m2, 0, sizeof m2);
+    m2.X = g.X;
+    m2.xy_res = p[0];
+    m2.z_res = p[1];
+    m2.slope_thr = p[8];
+    m2.slope_thr_f = (float)p[8];
+    m2.neg_thr = p[7];
+    m2.height = h->height.data();
+    m2.inferred = h->inferred.data();
+    m2.pos_density = h->pos_density.data();
+    m2.zlow = h->zlow.data();
+    m2.mlow = h->mlow.data();
+    m2.slope_x = h->slope_x.data();
+    m2.slope_y = h->slope_y.data();
+    m2.rough = h->rough();
+    m2.guess = h->guess.data();
+    m2.pos = h->pos();
+    m2.neg = h->neg();
+    m2.vis = h->vis();
+    m2.tile_cells = h->tun.maps_tile;
+    h->combC[nb] = 0;
+    if (launch_combine(mp, cp, m2, nullptr, nullptr) != cudaSuccess) return 4;
+    for (int a = 0; a < 3; a++) h->cod[nb][a] = mp.co[a];
+    h->cur = nb;
+    h->have_comb = true;
+    origin[0] = mp.co[0] * p[0];
+    origin[1] = mp.co[1] * p[0];
+    origin[2] = mp.co[2] * p[1];
+    const size_t X2 = (size_t)g.X * g.X;
+    std::memcpy(rough, h->rough(), X2 * 8);
+    std::memcpy(pos, h->pos(), X2 * 4);
+    std::memcpy(neg, h->neg(), X2 * 4);
+    std::memcpy(vis, h->vis(), X2 * 4);
+    return 0;
+}
+
+extern "C" void hm_ring_state(HostMap *h, long long *bi, long long *lbi) {
+    *bi = h->buffer_index;
+    *lbi = h->last_buffer_index;
+}
+
+static void unpack(const VoxelRec &v, long long c, int *hit, int *total, float *min_h, float *metrics, float *eigen) {
+    hit[c] = v.hit;
+    total[c] = v.total;
+    min_h[c] = v.min_h;
+    float *m = metrics + c * 10;
+    for (int a = 0; a < 3; a++) m[a] = v.mean[a];
+    for (int t = 0; t < 6; t++) m[3 + t] = v.cov[t];
+    m[9] = v.count;
+    if (eigen)
+        for (int a = 0; a < 3; a++) eigen[c * 3 + a] = v.aux[a];
+}
+
+// gvom_slot_count / gvom_get_slot
+extern "C" int hm_slot_count(HostMap *h, int slot) { return h->slots[slot].valid ? h->slots[slot].C : -1; }
+extern "C" void hm_get_slot(HostMap *h, int slot, int *index, int *hit, int *total, float *min_h, float *metrics,
+                            double *origin) {
+    const Slot &s = h->slots[slot];
+    std::memcpy(index, s.idx.data(), sizeof(int) * h->g.V);
+    for (int c = 0; c < s.C; c++) unpack(s.rec[c], c, hit, total, min_h, metrics, nullptr);
+    for (int a = 0; a < 3; a++) origin[a] = s.od[a];
+}
+
+// gvom_combined_count / gvom_get_combined: records in ascending voxel-id
+// order, the index map renumbered to match
+extern "C" int hm_combined_count(HostMap *h) {
+    if (!h->have_comb) return -1;
+    return h->combC[h->cur];
+}
+extern "C" void hm_get_combined(HostMap *h, int *index, int *hit, int *total, float *min_h, float *metrics,
+                                float *eigen, double *origin) {
+    const std::vector<int> &idx = h->cidx[h->cur];
+    long long c = 0;
+    for (long long v = 0; v < h->g.V; v++) {
+        if (idx[v] >= 0) {
+            unpack(h->crec[h->cur][v], c, hit, total, min_h, metrics, eigen);
+            index[v] = (int)c++;
+        } else {
+            index[v] = idx[v];
+        }
+    }
+    for (int a = 0; a < 3; a++) origin[a] = h->cod[h->cur][a];
+}
+
+// gvom_get_maps
+extern "C" void hm_get_maps(HostMap *h, double *height, double *inferred, double *slope_x, double *slope_y,
+                            double *rough, double *guess) {
+    const size_t b = (size_t)h->g.X * h->g.X * 8;
+    std::memcpy(height, h->height.data(), b);
+    std::memcpy(inferred, h->inferred.data(), b);
+    std::memcpy(slope_x, h->slope_x.data(), b);
+    std::memcpy(slope_y, h->slope_y.data(), b);
+    std::memcpy(rough, h->rough(), b);
+    std::memcpy(guess, h->guess.data(), b);
+}
+"""
+
+
+def _chevrons_to_launches(src):
+    """k_combine.cu's direct launches (`k<<<grid, block, smem, stream>>>(args)`)
+    as rec_kernel calls, which a host compiler parses."""
+    def sub(m):
+        parts = [s.strip() for s in m.group(2).split(",")]
+        assert len(parts) == 4, m.group(0)
+        return f"rec_kernel({m.group(1)}, dim3({parts[0]}), dim3({parts[1]}), {parts[2]}, {parts[3]}, "
+    out, n = re.subn(r"(\w+(?:<[^<>;]*>)?)<<<(.*?)>>>\(", sub, src)
+    assert n > 0
+    return out
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    d = tmp_path_factory.mktemp("pipeline")
+    comb = _chevrons_to_launches(open(os.path.join(CSRC, "k_combine.cu")).read())
+    units = {"proc.cpp": PRELUDE + '#include "k_process.cu"\n', "comb.cpp": PRELUDE + comb,
+             "mapper.cpp": PRELUDE + MAPPER}
+    flags = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-frounding-math", "-fPIC", "-pthread",
+             "-Wno-unknown-pragmas", "-I", os.path.join(HERE, "cpp", "host_cuda"), "-I", CSRC]
+    for name, text in units.items():
+        (d / name).write_text(text)
+
+    def compile_unit(name):
+        subprocess.run(flags + ["-c", str(d / name), "-o", str(d / (name + ".o"))], check=True)
+
+    with ThreadPoolExecutor(3) as ex:
+        list(ex.map(compile_unit, units))
+    so = d / "libpipeline.so"
+    subprocess.run(["g++", "-shared", "-pthread", "-o", str(so)] + [str(d / (n + ".o")) for n in units], check=True)
+    lib = C.CDLL(str(so))
+    P = C.c_void_p
+    lib.hm_create.restype = P
+    lib.hm_create.argtypes = [P, C.c_int, C.c_int, C.c_int]
+    lib.hm_destroy.argtypes = [P]
+    lib.hm_process.argtypes = [P, P, C.c_int, C.c_longlong, C.c_longlong, P, P, C.c_int]
+    lib.hm_combine.argtypes = [P, P, P, P, P, P]
+    lib.hm_ring_state.argtypes = [P, P, P]
+    lib.hm_slot_count.argtypes = [P, C.c_int]
+    lib.hm_get_slot.argtypes = [P, C.c_int, P, P, P, P, P, P]
+    lib.hm_combined_count.argtypes = [P]
+    lib.hm_get_combined.argtypes = [P, P, P, P, P, P, P, P]
+    lib.hm_get_maps.argtypes = [P, P, P, P, P, P, P]
+    return lib
+
+
+def _ptr(a):
+    return a.ctypes.data
+
+
+class HostMapper:
+    """The reference surface and the parity accessors over the host build
+    (the methods replay.replay_and_compare drives)."""
+
+    def __init__(self, lib, params, maps_tile=224, merge_planes=8, num_sms=2):
+        self._l = lib
+        self.params = np.asarray(params, np.float64)
+        self.X, self.Z = int(params[2]), int(params[3])
+        self.V = self.X * self.X * self.Z
+        self._h = lib.hm_create(_ptr(self.params), maps_tile, merge_planes, num_sms)
+
+    def close(self):
+        if self._h:
+            self._l.hm_destroy(self._h)
+            self._h = None
+
+    def Process_pointcloud(self, pts, ego, T=None):
+        pts = np.ascontiguousarray(pts)
+        e = np.ascontiguousarray(np.asarray(ego, np.float64).reshape(3))
+        Td = None if T is None else np.ascontiguousarray(np.asarray(T, np.float64).reshape(4, 4))
+        tdt = -1 if T is None else (0 if np.asarray(T).dtype == np.float32 else 1)
+        rc = self._l.hm_process(self._h, _ptr(pts), 0 if pts.dtype == np.float32 else 1, pts.shape[0], pts.shape[1],
+                                _ptr(e), None if Td is None else _ptr(Td), tdt)
+        assert rc == 0, rc
+
+    def combine_maps(self):
+        X = self.X
+        origin = np.zeros(3)
+        pos, neg, vis = (np.empty((X, X), np.int32) for _ in range(3))
+        rough = np.empty((X, X), np.float64)
+        rc = self._l.hm_combine(self._h, _ptr(origin), _ptr(pos), _ptr(neg), _ptr(rough), _ptr(vis))
+        if rc == 1:
+            return None
+        assert rc == 0, rc
+        return origin, pos, neg, rough, vis
+
+    def ring_state(self):
+        a, b = C.c_longlong(), C.c_longlong()
+        self._l.hm_ring_state(self._h, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def slot_state(self, slot):
+        c = self._l.hm_slot_count(self._h, int(slot))
+        if c < 0:
+            return None
+        st = dict(index=np.empty(self.V, np.int32), hit=np.empty(c, np.int32), total=np.empty(c, np.int32),
+                  min_h=np.empty(c, np.float32), metrics=np.empty((c, 10), np.float32), origin=np.zeros(3))
+        self._l.hm_get_slot(self._h, int(slot), *[_ptr(st[k]) for k in ("index", "hit", "total", "min_h", "metrics",
+                                                                        "origin")])
+        return st
+
+    def combined_state(self):
+        c = self._l.hm_combined_count(self._h)
+        if c < 0:
+            return None
+        st = dict(index=np.empty(self.V, np.int32), hit=np.empty(c, np.int32), total=np.empty(c, np.int32),
+                  min_h=np.empty(c, np.float32), metrics=np.empty((c, 10), np.float32),
+                  eigen=np.empty((c, 3), np.float32), origin=np.zeros(3))
+        self._l.hm_get_combined(self._h, *[_ptr(st[k]) for k in ("index", "hit", "total", "min_h", "metrics", "eigen",
+                                                                 "origin")])
+        return st
+
+    def maps_state(self):
+        X = self.X
+        keys = ("height", "inferred", "slope_x", "slope_y", "roughness", "guess")
+        st = {k: np.empty((X, X), np.float64) for k in keys}
+        self._l.hm_get_maps(self._h, *[_ptr(st[k]) for k in keys])
+        return st
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_host_build_replays_every_fixture(lib, name):
+    fx = load(os.path.join(GOLDEN, name))
+    m = HostMapper(lib, params_of(fx))
+    try:
+        replay_and_compare(m, fx, stats=True, debug=False)
+    finally:
+        m.close()

@@ -19,7 +19,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_files
+from conftest import GOLDEN
 from oracle.canonical import canonical_state
 from oracle.oracle import OracleGvom
 from replay import compare_slot, load, ops_of, params_of
@@ -60,6 +60,7 @@ static inline cudaError_t rec_event_external(cudaEvent_t, cudaStream_t) { return
 static inline cudaError_t rec_event_internal(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
 }  // namespace gvom
 #include "k_process.cu"
+#include "host_scan.h"
 
 using namespace gvom;
 
@@ -71,42 +72,14 @@ struct HostScan {
     double T[12];      // rows 0..2 of the 4x4
 };
 
-static ExactRes exact_res_of(double r) {
-    int e;
-    const double f = std::frexp(r, &e);
-    ExactRes R;
-    R.mr = (unsigned long long)std::ldexp(f, 53);
-    R.er = e - 53;
-    unsigned __int128 w = ((unsigned __int128)1 << 116) / R.mr;
-    if (w >> 64) w = ~0ull;
-    R.W = (unsigned long long)w;
-    R.pad = 0;
-    return R;
-}
-
 // One process call over k scans (prepare_scans + launch_scans of the
 // library): idx[i] (V ints) and rec[i] (rec_cap records) are scan i's slot,
 // ctr[i] its counters.  Returns the number of cell words left non-zero.
 extern "C" long long process_scans(const HostScan *scans, int k, int dtype, double xy_res, double z_res, int X,
                                    int Z, int exy, int ez, double min_distance, int num_sms, int pts_block,
                                    int *const *idx, VoxelRec *const *rec, long long rec_cap, ScanCounters *ctr) {
-    ProcessConst pc;
-    std::memset(&pc, 0, sizeof pc);
-    Geom &g = pc.g;
-    g.X = X; g.Z = Z; g.exy = exy; g.ez = ez; g.Xe = X + 2 * exy; g.Ze = Z + 2 * ez;
-    g.V = (long long)X * X * Z; g.Vext = (long long)g.Xe * g.Xe * g.Ze;
-    pc.xy_res = xy_res; pc.z_res = z_res;
-    pc.md2 = min_distance * min_distance;
-    float f = (float)pc.md2;
-    if ((double)f < pc.md2) f = std::nextafter(f, INFINITY);
-    while ((double)std::nextafter(f, -INFINITY) >= pc.md2) f = std::nextafter(f, -INFINITY);
-    pc.md2_f32 = f;
-    pc.rxy = exact_res_of(xy_res);
-    pc.rz = exact_res_of(z_res);
-    pc.step_cap = 2 * std::max(X, Z) + 8;
-    pc.num_sms = num_sms;
-    pc.xe_magic = ~0ull / (unsigned long long)g.Xe + 1ull;
-    pc.nscans = k;
+    const ProcessConst pc = host_scan::process_const(X, Z, exy, ez, xy_res, z_res, min_distance, k, num_sms);
+    const Geom &g = pc.g;
     std::vector<ScanDesc> table(k);
     std::vector<std::vector<unsigned long long>> cnt(k, std::vector<unsigned long long>(g.Vext, 0ull));
     long long base = 0, max_n = 0;
@@ -114,32 +87,7 @@ extern "C" long long process_scans(const HostScan *scans, int k, int dtype, doub
     for (int i = 0; i < k; i++) {
         const HostScan &s = scans[i];
         ScanDesc &d = table[i];
-        std::memset(&d, 0, sizeof d);
-        d.pts = s.pts; d.n = s.n; d.stride = s.stride; d.tmode = s.tmode;
-        for (int r = 0; r < 12; r++) { d.T[r] = s.T[r]; d.Tf[r] = (float)s.T[r]; }
-        d.od[0] = std::floor((s.ego[0] / xy_res) - (double)X / 2.0);
-        d.od[1] = std::floor((s.ego[1] / xy_res) - (double)X / 2.0);
-        d.od[2] = std::floor((s.ego[2] / z_res) - (double)Z / 2.0);
-        bool fast = true, exact = true;
-        const double lim = 4194304.0 - (double)std::max(X, Z) - 2.0;
-        for (int a = 0; a < 3; a++) {
-            if (!(std::fabs(d.od[a]) < 2147483648.0)) exact = false;
-            if (!(std::fabs(d.od[a]) < lim)) fast = false;
-        }
-        for (int a = 0; a < 3; a++) d.oi[a] = exact ? (int)d.od[a] : 0;
-        d.fast_floor = fast; d.exact_ok = exact;
-        d.pt0[0] = (float)(s.ego[0] / xy_res); d.pt0[1] = (float)(s.ego[1] / xy_res);
-        d.pt0[2] = (float)(s.ego[2] / z_res);
-        d.cube_on = (fast && X >= kCube && Z >= kCube) ? 1 : 0;
-        for (int a = 0; a < 3; a++) {
-            const int dim = a < 2 ? X : Z;
-            int c = 0;
-            if (d.cube_on) {
-                const double ev = std::floor((double)d.pt0[a] - d.od[a]);
-                c = (int)std::min(std::max(ev - kCube / 2, 0.0), (double)(dim - kCube));
-            }
-            d.cube0[a] = c;
-        }
+        host_scan::scan_desc(d, pc, s.pts, s.n, s.stride, s.tmode, s.ego, s.T);
         d.block_begin = block;
         d.nblocks = (int)((s.n + pts_block - 1) / pts_block);
         block += d.nblocks;
@@ -260,9 +208,18 @@ def _oracle_slots(fx):
     return p, res
 
 
-@pytest.mark.parametrize("name", golden_files())
+# every scan of every fixture also runs through the whole host build in
+# tests/test_pipeline_host.py; here the scan counters and the cell words'
+# clean-up are checked too, on fixtures of each kind (float32 / float64
+# points and transforms, voxel boundaries, rays, eigen distances (2, 0) and
+# (1, 2), the 128 x 128 x 32 grid)
+PROCESS_FIXTURES = ["kat_boundaries.npz", "kat_rays.npz", "synth_f64T_veg.npz", "synth_f64pts_eig20.npz",
+                    "synth_aniso_z.npz", "small_32x512.npz"]
+
+
+@pytest.mark.parametrize("name", PROCESS_FIXTURES)
 def test_process_kernels_equal_oracle(lib, name):
-    """The first and the last scan of every fixture, one scan per call."""
+    """The first and the last scan of the fixture, one scan per call."""
     p, res = _oracle_slots(load(os.path.join(GOLDEN, name)))
     for scan, ref, stats, pi in (res[:1] + res[-1:] if len(res) > 1 else res):
         (got, ctr), = _run(lib, p, [scan])
