@@ -1,26 +1,31 @@
-/* Host emulation of whole CUDA kernel launches with one host thread per CUDA
- * thread, for host builds of kernels that synchronise inside a block
- * (tests/test_process_host.py).  Include after cuda_runtime.h (this
- * directory), whose thread and block indices are per host thread and whose
- * atomics are host atomics.
+/* Host emulation of whole CUDA kernel launches, one fiber per CUDA thread,
+ * for host builds of kernels that synchronise inside a block
+ * (tests/test_process_host.py, tests/test_pipeline_host.py).  Include after
+ * cuda_runtime.h (this directory).
  *
- * Blocks run one after another on a pool of host threads; the threads of a
- * block run at the same time.  __syncthreads is a barrier of the block's
- * threads; a warp shuffle writes the caller's value into the warp's exchange
- * slots, waits at a barrier of the warp's lanes and reads its source lane's
- * slot.  __shared__ variables become statics, which is sound
- * because one block runs at a time.  A thread that returns leaves its
- * block's and its warp's barriers, as an exited CUDA thread stops counting
- * at a block barrier.  Kernels whose shuffles run with lanes missing (a lane
- * that returned) are outside what this emulates.  Not part of the library. */
+ * Blocks run one after another on the calling thread.  Each CUDA thread of a
+ * block is a fiber (POSIX ucontext) with its own stack; a fiber runs until it
+ * waits at a barrier or returns, and a scheduler then resumes the next ready
+ * fiber.  __syncthreads is a barrier of the block's live threads; a warp
+ * shuffle writes the caller's value into the warp's exchange slots, waits at
+ * a barrier of the warp's live lanes and reads its source lane's slot.  A
+ * barrier's waiters become ready again when its last live participant
+ * arrives; a thread that returns leaves its block's and its warp's barriers,
+ * as an exited CUDA thread stops counting at a block barrier.  __shared__
+ * variables become statics (one block runs at a time).  The schedule is
+ * deterministic, so atomics resolve in the same order on every run.  Kernels
+ * whose shuffles run with lanes missing (a lane that returned) and kernels
+ * that spin on memory another thread writes are outside what this emulates;
+ * a block whose fibers all wait ends the program.  Not part of the library. */
 #pragma once
+#include <ucontext.h>
+
 #include <algorithm>
-#include <barrier>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <functional>
-#include <memory>
-#include <thread>
 #include <vector>
 
 #define __shared__ static
@@ -32,105 +37,143 @@ struct dim3 {
 
 namespace block_threads {
 
-constexpr int kPoolThreads = 1024;  // the largest block this emulates
+constexpr int kMaxThreads = 1024;          // the largest block this emulates
+constexpr size_t kStackBytes = 256 << 10;  // per fiber
 
-struct BlockState {
-    std::unique_ptr<std::barrier<>> bar;
-    std::vector<std::unique_ptr<std::barrier<>>> warp;
-    unsigned long long xchg[2][kPoolThreads];  // by shuffle parity
-    explicit BlockState(int nt) : bar(new std::barrier<>(nt)) {
-        for (int w = 0; w * 32 < nt; w++) warp.emplace_back(new std::barrier<>(std::min(32, nt - w * 32)));
-    }
+struct Barrier {
+    int expected = 0, arrived = 0;
+    std::vector<int> waiters;
 };
-inline BlockState *cur = nullptr;
-inline thread_local unsigned parity = 0;  // the calling thread's shuffles so far, mod 2
+
+struct Sched {
+    ucontext_t main_ctx;
+    std::vector<ucontext_t> ctx;
+    std::vector<char *> stacks;
+    std::vector<HostDim3> tidx;
+    std::vector<unsigned> par;
+    std::vector<char> done;
+    std::deque<int> ready;
+    int cur = -1;
+    const std::function<void()> *fn = nullptr;
+    Barrier bar;
+    std::vector<Barrier> warp;
+    unsigned long long xchg[2][kMaxThreads];  // by shuffle parity
+};
+inline Sched *sched = nullptr;
+inline unsigned parity = 0;  // the running fiber's shuffles so far, mod 2
 
 inline int linear_tid() { return (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z)); }
 
+inline void release(Barrier &b) {
+    b.arrived = 0;
+    for (int w : b.waiters) sched->ready.push_back(w);
+    b.waiters.clear();
+}
+
+inline void arrive_and_wait(Barrier &b) {
+    Sched &s = *sched;
+    if (b.arrived + 1 == b.expected) {
+        release(b);
+        return;
+    }
+    b.arrived++;
+    const int me = s.cur;
+    b.waiters.push_back(me);
+    swapcontext(&s.ctx[me], &s.main_ctx);  // back when the barrier is complete
+}
+
+inline void arrive_and_drop(Barrier &b) {
+    b.expected--;
+    if (b.arrived > 0 && b.arrived == b.expected) release(b);
+}
+
+inline void fiber_entry() {
+    Sched &s = *sched;
+    const int me = s.cur;
+    (*s.fn)();
+    arrive_and_drop(s.bar);
+    arrive_and_drop(s.warp[me >> 5]);
+    s.done[me] = 1;
+}  // returns to the scheduler (uc_link)
+
 // value of lane `src` of the caller's warp (`take`), else the caller's own.
 // One barrier per shuffle: consecutive shuffles use alternate slot arrays,
-// and a lane can reach the next shuffle of the same parity only after every
+// and a lane reaches the next shuffle of the same parity only after every
 // lane has passed the barrier of the shuffle in between, that is, after
 // every lane has read this one.
 template <class T>
 inline T exchange(T v, int src, bool take) {
     static_assert(sizeof(T) <= 8, "shuffles move at most 8 bytes");
     const int t = linear_tid(), w = t >> 5;
-    unsigned long long *x = cur->xchg[parity];
+    unsigned long long *x = sched->xchg[parity];
     parity ^= 1u;
     unsigned long long b = 0;
     std::memcpy(&b, &v, sizeof(T));
     x[t] = b;
-    cur->warp[w]->arrive_and_wait();
+    arrive_and_wait(sched->warp[w]);
     T r = v;
     if (take) std::memcpy(&r, &x[(w << 5) + src], sizeof(T));
     return r;
 }
 
-// as many host threads as the blocks it runs have threads
-class Pool {
-public:
-    explicit Pool(int n) : go_(n + 1), done_(n + 1) {
-        for (int i = 0; i < n; i++) th_.emplace_back([this, i] { run(i); });
-    }
-    // runs block `idx` of the launch; returns when its threads have finished
-    void block(dim3 grid, dim3 blk, dim3 idx, const std::function<void()> *fn) {
-        grid_ = grid;
-        blk_ = blk;
-        idx_ = idx;
-        fn_ = fn;
-        go_.arrive_and_wait();
-        done_.arrive_and_wait();
-    }
-
-private:
-    void run(int i) {
-        for (;;) {
-            go_.arrive_and_wait();
-            const int nt = (int)(blk_.x * blk_.y * blk_.z);
-            if (i < nt) {
-                threadIdx = {i % blk_.x, (i / blk_.x) % blk_.y, i / (blk_.x * blk_.y)};
-                parity = 0;
-                blockIdx = {idx_.x, idx_.y, idx_.z};
-                blockDim = {blk_.x, blk_.y, blk_.z};
-                gridDim = {grid_.x, grid_.y, grid_.z};
-                (*fn_)();
-                cur->bar->arrive_and_drop();
-                cur->warp[i >> 5]->arrive_and_drop();
-            }
-            done_.arrive_and_wait();
-        }
-    }
-    std::barrier<> go_, done_;
-    std::vector<std::thread> th_;
-    dim3 grid_, blk_, idx_;
-    const std::function<void()> *fn_ = nullptr;
-};
-
-// Every block of the grid, x fastest, on the pool of the block's size.  The
-// pools live for the process (their threads wait between launches).
+// Every block of the grid, x fastest.
 inline void launch(dim3 grid, dim3 blk, const std::function<void()> &fn) {
-    static Pool *pools[kPoolThreads + 1] = {};
+    static Sched *s = new Sched();
+    sched = s;
     const int nt = (int)(blk.x * blk.y * blk.z);
-    if (nt < 1 || nt > kPoolThreads) std::abort();
-    if (!pools[nt]) pools[nt] = new Pool(nt);
-    Pool *pool = pools[nt];
-    for (unsigned z = 0; z < grid.z; z++)
-        for (unsigned y = 0; y < grid.y; y++)
-            for (unsigned x = 0; x < grid.x; x++) {
-                BlockState st(nt);
-                cur = &st;
-                pool->block(grid, blk, dim3(x, y, z), &fn);
-                cur = nullptr;
+    if (nt < 1 || nt > kMaxThreads) std::abort();
+    while ((int)s->stacks.size() < nt) s->stacks.push_back(static_cast<char *>(std::malloc(kStackBytes)));
+    s->ctx.resize(nt);
+    s->tidx.resize(nt);
+    s->par.resize(nt);
+    s->done.resize(nt);
+    s->fn = &fn;
+    blockDim = {blk.x, blk.y, blk.z};
+    gridDim = {grid.x, grid.y, grid.z};
+    for (unsigned bz = 0; bz < grid.z; bz++)
+        for (unsigned by = 0; by < grid.y; by++)
+            for (unsigned bx = 0; bx < grid.x; bx++) {
+                blockIdx = {bx, by, bz};
+                s->bar = Barrier{nt, 0, {}};
+                s->warp.assign((nt + 31) / 32, Barrier{});
+                for (int w = 0; w * 32 < nt; w++) s->warp[w].expected = std::min(32, nt - w * 32);
+                s->ready.clear();
+                for (int i = 0; i < nt; i++) {
+                    getcontext(&s->ctx[i]);
+                    s->ctx[i].uc_stack.ss_sp = s->stacks[i];
+                    s->ctx[i].uc_stack.ss_size = kStackBytes;
+                    s->ctx[i].uc_link = &s->main_ctx;
+                    makecontext(&s->ctx[i], fiber_entry, 0);
+                    s->tidx[i] = {i % blk.x, (i / blk.x) % blk.y, i / (blk.x * blk.y)};
+                    s->par[i] = 0;
+                    s->done[i] = 0;
+                    s->ready.push_back(i);
+                }
+                while (!s->ready.empty()) {
+                    const int i = s->ready.front();
+                    s->ready.pop_front();
+                    s->cur = i;
+                    threadIdx = s->tidx[i];
+                    parity = s->par[i];
+                    swapcontext(&s->main_ctx, &s->ctx[i]);
+                    s->par[i] = parity;
+                }
+                for (int i = 0; i < nt; i++)
+                    if (!s->done[i]) {
+                        std::fprintf(stderr, "block_threads: block (%u, %u, %u): thread %d waits forever\n", bx, by,
+                                     bz, i);
+                        std::abort();
+                    }
             }
+    s->cur = -1;
 }
 
 }  // namespace block_threads
 
-static inline void __syncthreads() { block_threads::cur->bar->arrive_and_wait(); }
+static inline void __syncthreads() { block_threads::arrive_and_wait(block_threads::sched->bar); }
 
 static inline void __syncwarp(unsigned = 0xffffffffu) {
-    block_threads::cur->warp[block_threads::linear_tid() >> 5]->arrive_and_wait();
+    block_threads::arrive_and_wait(block_threads::sched->warp[block_threads::linear_tid() >> 5]);
 }
 
 // the lanes of the caller's warp whose predicate is non-zero (every lane
@@ -138,10 +181,10 @@ static inline void __syncwarp(unsigned = 0xffffffffu) {
 static inline unsigned __ballot_sync(unsigned, int pred) {
     using namespace block_threads;
     const int t = linear_tid(), w = t >> 5;
-    unsigned long long *x = cur->xchg[parity];
+    unsigned long long *x = sched->xchg[parity];
     parity ^= 1u;
     x[t] = pred != 0;
-    cur->warp[w]->arrive_and_wait();
+    arrive_and_wait(sched->warp[w]);
     unsigned m = 0;
     for (int l = 0; l < 32; l++)
         if (x[(w << 5) + l]) m |= 1u << l;

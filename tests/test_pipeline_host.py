@@ -1,8 +1,8 @@
 """The library's scan->map path end to end on the CPU: every process and
 combine kernel (gvom_gb300/csrc/k_process.cu, k_combine.cu) compiled
 unchanged for the host and launched through the library's own launchers
-(launch_process, launch_combine), each block run with one host thread per
-CUDA thread (tests/cpp/host_cuda/block_threads.h).  A small host mapper
+(launch_process, launch_combine), each block run with one fiber per CUDA
+thread (tests/cpp/host_cuda/block_threads.h).  A small host mapper
 keeps what the library's instance keeps -- the ring of slots, the
 double-buffered combined map addressed by voxel id, the 2-D maps -- and
 fills the launch parameters as prepare_scans / prepare_combine in
@@ -21,7 +21,11 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, golden_files
-from replay import load, params_of, replay_and_compare
+from oracle.canonical import canonical_state
+from oracle.oracle import OracleGvom
+from replay import compare_slot, load, params_of, replay_and_compare
+# the GPU parity tests' own drivers (a mapper and the oracle side by side)
+from test_parity_gpu import _compare_runs, _run_both
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc")
@@ -99,6 +103,7 @@ struct HostMap {
     std::vector<float> mlow;
     std::vector<double> out;  // roughness | positive | negative | visibility, as the device block
     double ego[3] = {0, 0, 0};
+    long long last_stats[3] = {0, 0, 0};  // the last scan's valid points, hits, ray steps
     Tuning tun = kDefaultTuning;
     int num_sms = 2;
     double *rough() { return out.data(); }
@@ -173,6 +178,9 @@ extern "C" int hm_process(HostMap *h, const void *pts, int dtype, long long n, l
                        0, false) != cudaSuccess)
         return 4;
     if (ctr.overflow) return 4;
+    h->last_stats[0] = (long long)ctr.valid;
+    h->last_stats[1] = (long long)ctr.hits;
+    h->last_stats[2] = (long long)ctr.steps;
     s.C = ctr.C;
     for (int a = 0; a < 3; a++) s.od[a] = d.od[a];
     s.valid = true;
@@ -289,6 +297,11 @@ extern "C" int hm_combine(HostMap *h, double *origin, int *pos, int *neg, double
     return 0;
 }
 
+// gvom_last_process_stats
+extern "C" void hm_last_stats(HostMap *h, long long *out) {
+    for (int i = 0; i < 3; i++) out[i] = h->last_stats[i];
+}
+
 extern "C" void hm_ring_state(HostMap *h, long long *bi, long long *lbi) {
     *bi = h->buffer_index;
     *lbi = h->last_buffer_index;
@@ -371,7 +384,7 @@ def lib(tmp_path_factory):
     comb = _chevrons_to_launches(open(os.path.join(CSRC, "k_combine.cu")).read())
     units = {"proc.cpp": PRELUDE + '#include "k_process.cu"\n', "comb.cpp": PRELUDE + comb,
              "mapper.cpp": PRELUDE + MAPPER}
-    flags = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-frounding-math", "-fPIC", "-pthread",
+    flags = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-frounding-math", "-fPIC",
              "-Wno-unknown-pragmas", "-I", os.path.join(HERE, "cpp", "host_cuda"), "-I", CSRC]
     for name, text in units.items():
         (d / name).write_text(text)
@@ -382,7 +395,7 @@ def lib(tmp_path_factory):
     with ThreadPoolExecutor(3) as ex:
         list(ex.map(compile_unit, units))
     so = d / "libpipeline.so"
-    subprocess.run(["g++", "-shared", "-pthread", "-o", str(so)] + [str(d / (n + ".o")) for n in units], check=True)
+    subprocess.run(["g++", "-shared", "-o", str(so)] + [str(d / (n + ".o")) for n in units], check=True)
     lib = C.CDLL(str(so))
     P = C.c_void_p
     lib.hm_create.restype = P
@@ -391,6 +404,7 @@ def lib(tmp_path_factory):
     lib.hm_process.argtypes = [P, P, C.c_int, C.c_longlong, C.c_longlong, P, P, C.c_int]
     lib.hm_combine.argtypes = [P, P, P, P, P, P]
     lib.hm_ring_state.argtypes = [P, P, P]
+    lib.hm_last_stats.argtypes = [P, P]
     lib.hm_slot_count.argtypes = [P, C.c_int]
     lib.hm_get_slot.argtypes = [P, C.c_int, P, P, P, P, P, P]
     lib.hm_combined_count.argtypes = [P]
@@ -439,6 +453,11 @@ class HostMapper:
         assert rc == 0, rc
         return origin, pos, neg, rough, vis
 
+    def last_process_stats(self):
+        v = np.zeros(3, np.int64)
+        self._l.hm_last_stats(self._h, _ptr(v))
+        return dict(valid_points=int(v[0]), hits=int(v[1]), ray_steps=int(v[2]))
+
     def ring_state(self):
         a, b = C.c_longlong(), C.c_longlong()
         self._l.hm_ring_state(self._h, C.byref(a), C.byref(b))
@@ -481,3 +500,86 @@ def test_host_build_replays_every_fixture(lib, name):
         replay_and_compare(m, fx, stats=True, debug=False)
     finally:
         m.close()
+
+
+def _host(lib, **tuning):
+    """A constructor with the reference's signature for the host build."""
+    return lambda *params: HostMapper(lib, params, **tuning)
+
+
+def _terrain_scans(n, beams, columns, extent, seed=0, offset=(0.0, 0.0, 0.0), **kw):
+    from gvom_gb300.synthetic import Lidar, Terrain, make_scan, make_trajectory
+    t = Terrain.make(seed, extent=extent, path_len=n * 0.4, offset=offset)
+    lid = Lidar(beams=beams, columns=columns)
+    return [make_scan(t, lid, p, i, **kw) for i, p in enumerate(make_trajectory(n))]
+
+
+@pytest.mark.parametrize("tile,planes", [(256, 4), (128, 16), (64, 8)])
+def test_launch_shapes_vs_oracle(lib, tile, planes):
+    """The autotuner's other launch shapes against the oracle: k_maps2d tiles
+    of 8 x 32 (288-thread blocks), 8 x 16 and 4 x 16 cells, k_merge chunks of
+    4 and 16 planes, a combine after every scan."""
+    params = (0.2, 0.2, 48, 16, 3, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    _run_both(_host(lib, maps_tile=tile, merge_planes=planes), params,
+              _terrain_scans(4, 16, 256, 9.6, dropout=0.2))
+
+
+@pytest.mark.parametrize("B", [1, 4, 8, 16])
+def test_ring_sizes_every_source_class_vs_oracle(lib, B):
+    """Rings of 1 to 16 slots, a combine after every scan: every source-count
+    class of the merges (2, 3, 5, 9 and 17 sources), the ring full and after
+    it wraps (scripts/gvom.py:242-298)."""
+    params = (0.25, 0.25, 24, 8, B, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    _run_both(_host(lib), params, _terrain_scans(B + 3, 8, 128, 6.0, dropout=0.25))
+
+
+def test_odd_grid_and_row_length(lib):
+    """xy_size 63 (extended rows of 65 cells) and eigen distances (1, 2)."""
+    params = (0.2, 0.2, 63, 21, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 2)
+    _compare_runs(_host(lib), params, [(s.points, s.ego, s.transform) for s in _terrain_scans(2, 16, 256, 12.6)])
+
+
+def test_eigen_distances_and_far_world_offset(lib):
+    """Eigen distances (2, 0) and a 1e4 m world offset."""
+    params = (0.1, 0.1, 64, 24, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 2, 0)
+    _run_both(_host(lib), params, _terrain_scans(3, 16, 256, 6.4, offset=(1.0e4, 0.0, 0.0)))
+
+
+def test_origin_beyond_float32_floor_range(lib):
+    """A world origin past 2^22 voxels: ray indices take the float64 path."""
+    params = (0.1, 0.1, 64, 24, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    runs = [(s.points, s.ego, s.transform) for s in
+            _terrain_scans(2, 16, 256, 6.4, offset=(5.0e5, -2.0e5, 0.0), transform_dtype=np.float64)]
+    _compare_runs(_host(lib), params, runs)
+
+
+def test_empty_and_out_of_grid_scans(lib):
+    params = (0.2, 0.2, 32, 16, 2, 1.0, 0.5, 0.5, 0.3, 2.0, 4.0, 1.0, 1, 1)
+    g, o = _host(lib)(*params), OracleGvom(*params)
+    assert g.combine_maps() is None
+    empty = np.zeros((0, 3), np.float32)
+    far = np.array([[500.0, 0.0, 0.0], [0.0, -400.0, 3.0]], np.float32)  # no hit inside the grid
+    for pts in (empty, far, empty):
+        g.Process_pointcloud(pts, (0.1, 0.2, 1.0))
+        o.Process_pointcloud(pts, (0.1, 0.2, 1.0))
+        _, last = g.ring_state()
+        compare_slot(canonical_state(g.slot_state(last)), canonical_state(o.slot_state(last)), "scan")
+        out, ref = g.combine_maps(), o.combine_maps()
+        for a, b in zip(out, ref):
+            np.testing.assert_array_equal(a, b)
+
+
+def test_rays_inside_the_sliver_below_zero(lib):
+    """Ray positions in (-2^-20, 0) voxels with a non-zero grid origin."""
+    params = (0.2, 0.2, 32, 16, 2, 0.1, 0.5, 0.5, 0.3, 2.0, 1.0, 1.0, 1, 1)
+    rng = np.random.default_rng(11)
+    ex = np.float32(-1.0e-21)
+    n = 1500
+    pts = np.empty((n, 3), np.float32)
+    pts[:, 0] = ex  # rays in the plane x = ego x stay inside the sliver for every step
+    pts[:, 1] = rng.uniform(-3, 3, n)
+    pts[:, 2] = rng.uniform(-1.5, 2.5, n)
+    pts[: n // 3, 0] = np.float32(-1e-9) * rng.uniform(0, 1, n // 3).astype(np.float32)
+    pts2 = pts.copy()
+    pts2[:, 0] = np.float32(-4.0e-7)
+    _compare_runs(_host(lib), params, [(pts, (float(ex), 0.05, 1.0), None), (pts2, (-2.0e-7, -0.03, 0.8), None)])

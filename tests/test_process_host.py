@@ -1,8 +1,8 @@
 """The whole process launch sequence (launch_process in
 gvom_gb300/csrc/k_process.cu: k_voxelize_trace, k_assign, k_scatter,
 k_cell_moments, k_voxel_stats, k_cleanup, with the launcher's own grids),
-compiled unchanged for the host and run block by block with one host thread
-per CUDA thread (tests/cpp/host_cuda/block_threads.h: block barriers, warp
+compiled unchanged for the host and run block by block with one fiber per
+CUDA thread (tests/cpp/host_cuda/block_threads.h: block barriers, warp
 shuffles, shared memory, atomics).  Scan descriptors are filled the way the
 library's host code fills them (prepare_scans in
 gvom_gb300/csrc/gvom_capi.cu).  On every scan of every golden fixture the
@@ -19,7 +19,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import GOLDEN
+from conftest import GOLDEN, golden_files
 from oracle.canonical import canonical_state
 from oracle.oracle import OracleGvom
 from replay import compare_slot, load, ops_of, params_of
@@ -139,7 +139,7 @@ def lib(tmp_path_factory):
     cpp.write_text(SOURCE)
     so = d / "libprocess.so"
     subprocess.run(["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-frounding-math", "-fPIC", "-shared",
-                    "-pthread", "-Wno-unknown-pragmas", "-I", os.path.join(HERE, "cpp", "host_cuda"), "-I", CSRC,
+                    "-Wno-unknown-pragmas", "-I", os.path.join(HERE, "cpp", "host_cuda"), "-I", CSRC,
                     "-o", str(so), str(cpp)], check=True)
     lib = C.CDLL(str(so))
     P = C.c_void_p
@@ -208,20 +208,11 @@ def _oracle_slots(fx):
     return p, res
 
 
-# every scan of every fixture also runs through the whole host build in
-# tests/test_pipeline_host.py; here the scan counters and the cell words'
-# clean-up are checked too, on fixtures of each kind (float32 / float64
-# points and transforms, voxel boundaries, rays, eigen distances (2, 0) and
-# (1, 2), the 128 x 128 x 32 grid)
-PROCESS_FIXTURES = ["kat_boundaries.npz", "kat_rays.npz", "synth_f64T_veg.npz", "synth_f64pts_eig20.npz",
-                    "synth_aniso_z.npz", "small_32x512.npz"]
-
-
-@pytest.mark.parametrize("name", PROCESS_FIXTURES)
+@pytest.mark.parametrize("name", golden_files())
 def test_process_kernels_equal_oracle(lib, name):
-    """The first and the last scan of the fixture, one scan per call."""
+    """Every scan of the fixture, one scan per call."""
     p, res = _oracle_slots(load(os.path.join(GOLDEN, name)))
-    for scan, ref, stats, pi in (res[:1] + res[-1:] if len(res) > 1 else res):
+    for scan, ref, stats, pi in res:
         (got, ctr), = _run(lib, p, [scan])
         what = f"{name} scan {pi}"
         compare_slot(canonical_state(got), canonical_state(ref), what)
@@ -229,8 +220,8 @@ def test_process_kernels_equal_oracle(lib, name):
             (stats["valid_points"], stats["hits"], stats["ray_steps"]), what
 
 
-@pytest.mark.parametrize("name,k,pts_block", [("synth_ring16.npz", 6, 256), ("synth_f64T_veg.npz", 5, 256),
-                                              ("synth_longrun.npz", 3, 128)])
+@pytest.mark.parametrize("name,k,pts_block", [("synth_ring16.npz", 16, 256), ("synth_f64T_veg.npz", 5, 128),
+                                              ("synth_longrun.npz", 3, 256)])
 def test_batched_launch_equals_oracle(lib, name, k, pts_block):
     """k scans of a fixture in one launch set (the batched form's scan table:
     the 4-scan and 16-scan launch templates, 128- and 256-thread blocks):
