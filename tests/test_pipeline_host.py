@@ -8,8 +8,9 @@ double-buffered combined map addressed by voxel id, the 2-D maps -- and
 fills the launch parameters as prepare_scans / prepare_combine in
 gvom_gb300/csrc/gvom_capi.cu do.  It is replayed through every golden fixture
 with the comparison the GPU parity tests use (replay.replay_and_compare):
-every slot, every combined map with its eigenvalues, and every combine's
-maps, against the outputs of the reference itself."""
+every slot, every combined map with its eigenvalues, every combine's maps
+and the three debug exports, against the outputs of the reference
+itself."""
 import ctypes as C
 import os
 import re
@@ -350,6 +351,58 @@ extern "C" void hm_get_combined(HostMap *h, int *index, int *hit, int *total, fl
     for (int a = 0; a < 3; a++) origin[a] = h->cod[h->cur][a];
 }
 
+// gvom_debug_voxel_map: per-block counts, their exclusive prefix on the
+// host, then the rows in ascending voxel-id order; returns the row count
+// (rows written when `out` holds `cap` rows)
+extern "C" long long hm_debug_voxel_map(HostMap *h, float *out, long long cap) {
+    if (!h->have_comb) return -1;
+    const long long V = h->g.V;
+    const int chunk = debug_chunk();
+    const int nblocks = (int)((V + chunk - 1) / chunk);
+    std::vector<int> offs(nblocks + 1, 0);
+    if (launch_debug_count(h->cidx[h->cur].data(), V, offs.data(), nblocks, nullptr) != cudaSuccess) return -2;
+    long long tot = 0;
+    for (int b = 0; b < nblocks; b++) {
+        const int c = offs[b];
+        offs[b] = (int)tot;
+        tot += c;
+    }
+    if (!out || tot == 0) return tot;
+    DebugVoxParams p;
+    std::memset(&p, 0, sizeof p);
+    p.idx = h->cidx[h->cur].data();
+    p.rec = h->crec[h->cur].data();
+    p.block_off = offs.data();
+    p.V = V;
+    p.X = h->g.X;
+    for (int a = 0; a < 3; a++) p.co[a] = h->cod[h->cur][a];
+    p.xy_res = h->p[0];
+    p.z_res = h->p[1];
+    p.out = out;
+    p.cap = std::min(tot, cap);
+    if (launch_debug_voxels(p, nblocks, nullptr) != cudaSuccess) return -2;
+    return tot;
+}
+
+// gvom_debug_height_map (out_h, X*X rows of 7) / gvom_debug_inferred_height_map (out_i, X*X rows of 3)
+extern "C" int hm_debug_maps(HostMap *h, float *out_h, float *out_i) {
+    if (!h->have_comb) return 1;
+    DebugMapParams p;
+    std::memset(&p, 0, sizeof p);
+    p.X = h->g.X;
+    for (int a = 0; a < 3; a++) p.co[a] = h->cod[h->cur][a];
+    p.xy_res = h->p[0];
+    p.z_res = h->p[1];
+    p.height = h->height.data();
+    p.rough = h->rough();
+    p.slope_x = h->slope_x.data();
+    p.slope_y = h->slope_y.data();
+    p.guess = h->guess.data();
+    p.out_h = out_h;
+    p.out_i = out_i;
+    return launch_debug_maps(p, nullptr) == cudaSuccess ? 0 : 4;
+}
+
 // gvom_get_maps
 extern "C" void hm_get_maps(HostMap *h, double *height, double *inferred, double *slope_x, double *slope_y,
                             double *rough, double *guess) {
@@ -410,6 +463,9 @@ def lib(tmp_path_factory):
     lib.hm_combined_count.argtypes = [P]
     lib.hm_get_combined.argtypes = [P, P, P, P, P, P, P, P]
     lib.hm_get_maps.argtypes = [P, P, P, P, P, P, P]
+    lib.hm_debug_voxel_map.restype = C.c_longlong
+    lib.hm_debug_voxel_map.argtypes = [P, P, C.c_longlong]
+    lib.hm_debug_maps.argtypes = [P, P, P]
     return lib
 
 
@@ -484,6 +540,24 @@ class HostMapper:
                                                                  "origin")])
         return st
 
+    def make_debug_voxel_map(self):
+        n = self._l.hm_debug_voxel_map(self._h, None, 0)
+        assert n >= 0, n
+        out = np.zeros((n, 8), np.float32)
+        if n:
+            assert self._l.hm_debug_voxel_map(self._h, _ptr(out), n) == n
+        return out
+
+    def make_debug_height_map(self):
+        out = np.zeros((self.X * self.X, 7), np.float32)
+        assert self._l.hm_debug_maps(self._h, _ptr(out), None) == 0
+        return out
+
+    def make_debug_inferred_height_map(self):
+        out = np.zeros((self.X * self.X, 3), np.float32)
+        assert self._l.hm_debug_maps(self._h, None, _ptr(out)) == 0
+        return out
+
     def maps_state(self):
         X = self.X
         keys = ("height", "inferred", "slope_x", "slope_y", "roughness", "guess")
@@ -497,7 +571,7 @@ def test_host_build_replays_every_fixture(lib, name):
     fx = load(os.path.join(GOLDEN, name))
     m = HostMapper(lib, params_of(fx))
     try:
-        replay_and_compare(m, fx, stats=True, debug=False)
+        replay_and_compare(m, fx, stats=True, debug=True)
     finally:
         m.close()
 
