@@ -709,9 +709,6 @@ int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl,
     pc.step_cap = 2 * std::max(h->g.X, h->g.Z) + 8;
     pc.num_sms = h->num_sms;
     pc.xe_magic = ~0ull / (unsigned long long)h->g.Xe + 1ull;
-    pc.adv[0] = 256 % h->g.Xe;
-    pc.adv[1] = (256 / h->g.Xe) % h->g.Xe;
-    pc.adv[2] = 256 / (h->g.Xe * h->g.Xe);
     pc.nscans = k;
     ScanDesc *table = pl.table;
     std::memset(pl.table, 0, sizeof(pl.table));

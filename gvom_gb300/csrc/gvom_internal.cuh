@@ -187,7 +187,6 @@ struct ProcessConst {
     int nscans;
     int num_sms;           // multiprocessors of the device (persistent grids)
     unsigned long long xe_magic;  // floor((2^64 - 1) / Xe) + 1 (divisions by the extended row length)
-    int adv[3];            // extended coordinates (x, y, z) of cell index 256
 };
 
 struct MergeSrc {
