@@ -10,6 +10,8 @@ is rejected by range()).
 GPU: gvom_expand_binary / gvom_lowpass_binary / gvom_convolve through the C
 ABI equal the fixtures and the oracle bit for bit, on the shared-memory
 staged path and on the direct path of radii too large to stage.
+Host build: the same kernel file compiled for the host (tests/hostbuild.py)
+gives the same outputs on the same cases.
 """
 import ctypes as C
 import os
@@ -116,3 +118,70 @@ def test_device_image_kernels_equal_reference_and_oracle(gpu_lib):
     assert lib.gvom_expand_binary(None, None, 8, 1.0, None) == 2
     assert lib.gvom_lowpass_binary(P(img), P(out), 8, -1, 0.5, None) == 2
     assert lib.gvom_convolve(P(img), P(out), P(kd), 8, 0, None) == 2
+
+
+MORPH_DRIVER = r"""
+extern "C" int run_expand(const int32_t *in, int32_t *out, int X, double r) {
+    return gvom::launch_expand_binary(in, out, X, r, nullptr);
+}
+extern "C" int run_lowpass(const int32_t *in, int32_t *out, int X, int fs, double frac) {
+    return gvom::launch_lowpass_binary(in, out, X, fs, frac, nullptr);
+}
+extern "C" int run_convolve(const double *in, double *out, const double *kern, int X, int ks) {
+    return gvom::launch_convolve(in, out, kern, X, ks, nullptr);
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def morph_host(tmp_path_factory):
+    import shutil
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    from hostbuild import CSRC, PRELUDE, compile_units, host_source
+    src = host_source(open(os.path.join(CSRC, "k_morph.cu")).read())
+    so = compile_units({"morph.cpp": PRELUDE + src + MORPH_DRIVER}, tmp_path_factory.mktemp("morph"), "libmorph.so")
+    lib = C.CDLL(str(so))
+    P = C.c_void_p
+    lib.run_expand.argtypes = [P, P, C.c_int, C.c_double]
+    lib.run_lowpass.argtypes = [P, P, C.c_int, C.c_int, C.c_double]
+    lib.run_convolve.argtypes = [P, P, P, C.c_int, C.c_int]
+    return lib
+
+
+def test_host_build_image_kernels_equal_reference_and_oracle(morph_host):
+    """k_morph.cu compiled unchanged for the host (its launches and dynamic
+    shared staging rewritten for a host compiler, blocks run one fiber per
+    CUDA thread): the reference's own outputs on every fixture case, and the
+    oracle on the staged and direct paths of the GPU test's sizes."""
+    lib = morph_host
+    fx = _fixture()
+    P = lambda a: a.ctypes.data  # noqa: E731
+    for n in _cases(fx, "expand"):
+        img = np.ascontiguousarray(fx[f"expand{n}_img"], np.int32)
+        out = np.full_like(img, -7)
+        assert lib.run_expand(P(img), P(out), img.shape[0], float(fx[f"expand{n}_r"])) == 0
+        np.testing.assert_array_equal(out, fx[f"expand{n}_out"], f"expand case {n}")
+    for n in _cases(fx, "lowpass"):
+        img = np.ascontiguousarray(fx[f"lowpass{n}_img"], np.int32)
+        out = np.full_like(img, -7)
+        assert lib.run_lowpass(P(img), P(out), img.shape[0], int(fx[f"lowpass{n}_fs"]),
+                               float(fx[f"lowpass{n}_frac"])) == 0
+        np.testing.assert_array_equal(out, fx[f"lowpass{n}_out"], f"lowpass case {n}")
+    rng = np.random.default_rng(9)
+    for X, r in ((100, 60.0), (64, 3.3), (70, 45.5)):
+        a = (rng.uniform(size=(X, X)) < 0.003).astype(np.int32)
+        out = np.full_like(a, -7)
+        assert lib.run_expand(P(a), P(out), X, r) == 0
+        np.testing.assert_array_equal(out, expand_binary(a, r), f"expand {X} {r}")
+    for X, fs, frac in ((100, 45, 0.5), (64, 2, 0.6)):
+        a = (rng.uniform(size=(X, X)) < 0.5).astype(np.int32)
+        out = np.full_like(a, -7)
+        assert lib.run_lowpass(P(a), P(out), X, fs, frac) == 0
+        np.testing.assert_array_equal(out, lowpass_binary(a, fs, frac), f"lowpass {X} {fs}")
+    for X, ks in ((64, 5), (33, 4), (40, 1)):
+        a = rng.normal(size=(X, X))
+        k = rng.normal(size=(ks, ks))
+        out = np.full_like(a, np.nan)
+        assert lib.run_convolve(P(a), P(out), P(k), X, ks) == 0
+        np.testing.assert_array_equal(out, convolve(a, k), f"convolve {X} {ks}")

@@ -13,61 +13,18 @@ and the three debug exports, against the outputs of the reference
 itself."""
 import ctypes as C
 import os
-import re
 import shutil
-import subprocess
-from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 import pytest
 
 from conftest import GOLDEN, golden_files
+from hostbuild import CSRC, PRELUDE, compile_units, host_source
 from oracle.canonical import canonical_state
 from oracle.oracle import OracleGvom
 from replay import compare_slot, load, params_of, replay_and_compare
 # the GPU parity tests' own drivers (a mapper and the oracle side by side)
 from test_parity_gpu import _compare_runs, _run_both
-
-HERE = os.path.dirname(os.path.abspath(__file__))
-CSRC = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc")
-
-PRELUDE = r"""
-#include <algorithm>
-#include <cmath>
-using std::isfinite; using std::isnan; using std::max; using std::min;
-#include "cuda_runtime.h"
-#include "block_threads.h"
-// CUDA's integer min / max take their operands by value (a volatile read
-// included)
-static inline int min(int a, int b) { return a < b ? a : b; }
-static inline int max(int a, int b) { return a > b ? a : b; }
-static inline long long min(long long a, long long b) { return a < b ? a : b; }
-static inline long long max(long long a, long long b) { return a > b ? a : b; }
-template <class T> static inline T __ldg(const T *p) { return *p; }
-static inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
-    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
-}
-static inline float __fdividef(float a, float b) { return a / b; }
-static inline float __frcp_rn(float x) { return 1.0f / x; }
-static inline float rsqrtf(float x) { return 1.0f / std::sqrt(x); }
-static inline int __ffs(int x) { return __builtin_ffs(x); }
-constexpr cudaError_t cudaSuccess = 0;
-static inline cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
-static inline cudaError_t cudaGetLastError() { return cudaSuccess; }
-struct cudaFuncAttributes { int unused; };
-static inline cudaError_t cudaFuncGetAttributes(cudaFuncAttributes *, const void *) { return cudaSuccess; }
-#include "gvom_internal.cuh"
-namespace gvom {
-// a launch runs every block of the grid under the block emulator
-template <typename... P>
-cudaError_t rec_kernel(void (*fn)(P...), dim3 grid, dim3 block, size_t, cudaStream_t, std::decay_t<P>... args) {
-    block_threads::launch(grid, block, [&] { fn(args...); });
-    return cudaSuccess;
-}
-static inline cudaError_t rec_event_external(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
-static inline cudaError_t rec_event_internal(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
-}  // namespace gvom
-"""
 
 MAPPER = r"""
 #include "host_scan.h"
@@ -417,38 +374,14 @@ extern "C" void hm_get_maps(HostMap *h, double *height, double *inferred, double
 """
 
 
-def _chevrons_to_launches(src):
-    """k_combine.cu's direct launches (`k<<<grid, block, smem, stream>>>(args)`)
-    as rec_kernel calls, which a host compiler parses."""
-    def sub(m):
-        parts = [s.strip() for s in m.group(2).split(",")]
-        assert len(parts) == 4, m.group(0)
-        return f"rec_kernel({m.group(1)}, dim3({parts[0]}), dim3({parts[1]}), {parts[2]}, {parts[3]}, "
-    out, n = re.subn(r"(\w+(?:<[^<>;]*>)?)<<<(.*?)>>>\(", sub, src)
-    assert n > 0
-    return out
-
-
 @pytest.fixture(scope="module")
 def lib(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     d = tmp_path_factory.mktemp("pipeline")
-    comb = _chevrons_to_launches(open(os.path.join(CSRC, "k_combine.cu")).read())
-    units = {"proc.cpp": PRELUDE + '#include "k_process.cu"\n', "comb.cpp": PRELUDE + comb,
-             "mapper.cpp": PRELUDE + MAPPER}
-    flags = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-frounding-math", "-fPIC",
-             "-Wno-unknown-pragmas", "-I", os.path.join(HERE, "cpp", "host_cuda"), "-I", CSRC]
-    for name, text in units.items():
-        (d / name).write_text(text)
-
-    def compile_unit(name):
-        subprocess.run(flags + ["-c", str(d / name), "-o", str(d / (name + ".o"))], check=True)
-
-    with ThreadPoolExecutor(3) as ex:
-        list(ex.map(compile_unit, units))
-    so = d / "libpipeline.so"
-    subprocess.run(["g++", "-shared", "-o", str(so)] + [str(d / (n + ".o")) for n in units], check=True)
+    comb = host_source(open(os.path.join(CSRC, "k_combine.cu")).read())
+    so = compile_units({"proc.cpp": PRELUDE + '#include "k_process.cu"\n', "comb.cpp": PRELUDE + comb,
+                        "mapper.cpp": PRELUDE + MAPPER}, d, "libpipeline.so")
     lib = C.CDLL(str(so))
     P = C.c_void_p
     lib.hm_create.restype = P

@@ -14,51 +14,17 @@ the scans one at a time."""
 import ctypes as C
 import os
 import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
 from conftest import GOLDEN, golden_files
+from hostbuild import PRELUDE, compile_units
 from oracle.canonical import canonical_state
 from oracle.oracle import OracleGvom
 from replay import compare_slot, load, ops_of, params_of
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-CSRC = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc")
-
 SOURCE = r"""
-#include <algorithm>
-#include <cmath>
-using std::isfinite; using std::max; using std::min;
-#include "cuda_runtime.h"
-#include "block_threads.h"
-// CUDA's integer min / max take their operands by value (a volatile read
-// included)
-static inline int min(int a, int b) { return a < b ? a : b; }
-static inline int max(int a, int b) { return a > b ? a : b; }
-static inline long long min(long long a, long long b) { return a < b ? a : b; }
-static inline long long max(long long a, long long b) { return a > b ? a : b; }
-template <class T> static inline T __ldg(const T *p) { return *p; }
-static inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
-    return (unsigned long long)(((unsigned __int128)a * b) >> 64);
-}
-constexpr cudaError_t cudaSuccess = 0;
-static inline cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
-static inline cudaError_t cudaGetLastError() { return cudaSuccess; }
-struct cudaFuncAttributes { int unused; };
-static inline cudaError_t cudaFuncGetAttributes(cudaFuncAttributes *, const void *) { return cudaSuccess; }
-#include "gvom_internal.cuh"
-namespace gvom {
-// a launch runs every block of the grid under the block emulator
-template <typename... P>
-cudaError_t rec_kernel(void (*fn)(P...), dim3 grid, dim3 block, size_t, cudaStream_t, std::decay_t<P>... args) {
-    block_threads::launch(grid, block, [&] { fn(args...); });
-    return cudaSuccess;
-}
-static inline cudaError_t rec_event_external(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
-static inline cudaError_t rec_event_internal(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
-}  // namespace gvom
 #include "k_process.cu"
 #include "host_scan.h"
 
@@ -135,12 +101,7 @@ def lib(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("g++ not available")
     d = tmp_path_factory.mktemp("process")
-    cpp = d / "process_host.cpp"
-    cpp.write_text(SOURCE)
-    so = d / "libprocess.so"
-    subprocess.run(["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-frounding-math", "-fPIC", "-shared",
-                    "-Wno-unknown-pragmas", "-I", os.path.join(HERE, "cpp", "host_cuda"), "-I", CSRC,
-                    "-o", str(so), str(cpp)], check=True)
+    so = compile_units({"process_host.cpp": PRELUDE + SOURCE}, d, "libprocess.so")
     lib = C.CDLL(str(so))
     P = C.c_void_p
     lib.process_scans.restype = C.c_longlong
