@@ -648,13 +648,17 @@ struct ProcPlan {
     ScanDesc table[kMaxBatch];
     int k = 0, block = 0, max_n = 0, dtype = GVOM_F32;
     int set = 0;  // scratch set
+    // ring positions of a batch's dropped scans (those a later scan of the
+    // same batch overwrites): the plan's scans take the positions after them,
+    // where one call per scan would have put them
+    int skip = 0;
     int slot_of[kMaxBatch];
     double last_ego[3];
     std::deque<int> free_before;  // the free queue before this plan took its slots
 };
 
 // Physical slots for the plan's scans.  Scan i overwrites ring position
-// (buffer_index + i) mod B: the slot that position held joins the back of
+// (buffer_index + skip + i) mod B: the slot that position held joins the back of
 // the free queue, and the scan takes the head (the slot unreferenced the
 // longest).  While fewer than `spare` + 1 slots are free, a spare slot is
 // added first (up to kMaxPhysSlots; without memory the plan goes on with
@@ -663,7 +667,7 @@ struct ProcPlan {
 void take_slots(GvomHandle *h, ProcPlan &pl, int spare) {
     pl.free_before = h->free_q;
     for (int i = 0; i < pl.k; i++) {
-        const int pos = (int)((h->buffer_index + i) % h->B);
+        const int pos = (int)((h->buffer_index + pl.skip + i) % h->B);
         if (h->phys_of[pos] >= 0) h->free_q.push_back(h->phys_of[pos]);
         while ((int)h->free_q.size() < spare + 1 && (int)h->slots.size() < kMaxPhysSlots) {
             if (add_slot(h)) {
@@ -679,9 +683,10 @@ void take_slots(GvomHandle *h, ProcPlan &pl, int spare) {
 // undoes take_slots when the plan is dropped before commit_scans
 void release_slots(GvomHandle *h, ProcPlan &pl) { h->free_q = pl.free_before; }
 
-int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl, int spare = 0) {
+int prepare_scans(GvomHandle *h, const std::vector<ScanIn> &scans, ProcPlan &pl, int spare = 0, int skip = 0) {
     const int k = (int)scans.size();
     pl.k = k;
+    pl.skip = skip;
     if (k == 0) return GVOM_OK;
     int rc;
     pl.set = h->sset;
@@ -814,19 +819,20 @@ void commit_scans(GvomHandle *h, const ProcPlan &pl) {
         sl.valid = true;
     }
     for (int a = 0; a < 3; a++) h->ego[a] = pl.last_ego[a];
-    for (int i = 0; i < pl.k; i++) h->phys_of[(h->buffer_index + i) % h->B] = pl.slot_of[i];
-    h->last_buffer_index = (h->buffer_index + pl.k - 1) % h->B;
-    h->buffer_index = (h->buffer_index + pl.k) % h->B;
-    h->scans_total += pl.k;
+    const long long b0 = h->buffer_index + pl.skip;
+    for (int i = 0; i < pl.k; i++) h->phys_of[(b0 + i) % h->B] = pl.slot_of[i];
+    h->last_buffer_index = (b0 + pl.k - 1) % h->B;
+    h->buffer_index = (b0 + pl.k) % h->B;
+    h->scans_total += pl.skip + pl.k;
     h->last_ctr = pl.set * kMaxBatch + pl.k - 1;
     h->sset = pl.set ^ 1;
 }
 
-int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans) {
+int enqueue_scans(GvomHandle *h, const std::vector<ScanIn> &scans, int skip = 0) {
     h->st_dirty = true;  // work on the instance stream: see the step pipeline
     if (scans.empty()) return GVOM_OK;
     ProcPlan pl;
-    int rc = prepare_scans(h, scans, pl);
+    int rc = prepare_scans(h, scans, pl, 0, skip);
     if (rc) return rc;
     if (!rc) rc = wait_slots_free(h, pl.slot_of, pl.k, h->st);
     // events for a combine that follows (see combine_impl)
@@ -1162,12 +1168,14 @@ int gvom_process_device(GvomHandle *h, const void *d_points, int32_t dtype, int6
 
 // Validates a scan list and stages host points into the device staging
 // buffer (stream-ordered on h->st).  Scans that a later scan of the same batch
-// overwrites (ring wrap) are dropped; `pinned` tells whether a host buffer
-// was page-locked (the copy must then finish before the call returns).
+// overwrites (ring wrap) are dropped, their count in `skipped` (the kept
+// scans go to the ring positions after theirs); `pinned` tells whether a host
+// buffer was page-locked (the copy must then finish before the call returns).
 static int stage_batch(GvomHandle *h, const GvomScan *scans, int n_scans, int points_on_device,
-                       std::vector<ScanIn> &v, bool &pinned, cudaStream_t st = nullptr) {
+                       std::vector<ScanIn> &v, bool &pinned, int &skipped, cudaStream_t st = nullptr) {
     if (!st) st = h->st;
     const int first = std::max(0, n_scans - std::min(h->B, kMaxBatch));
+    skipped = first;
     const int dt = scans[first].dtype;
     size_t total_bytes = 0;
     pinned = false;
@@ -1256,9 +1264,10 @@ int gvom_process_batch(GvomHandle *h, const GvomScan *scans, int32_t n_scans, in
     std::lock_guard<std::mutex> lk(h->mu);
     std::vector<ScanIn> v;
     bool pinned = false;
+    int skipped = 0;
     int rc;
-    if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned))) return rc;
-    if ((rc = enqueue_scans(h, v))) return rc;
+    if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned, skipped))) return rc;
+    if ((rc = enqueue_scans(h, v, skipped))) return rc;
     if (pinned) CUDA_TRY(cudaStreamSynchronize(h->st));
     for (int a = 0; a < 3; a++) h->ego[a] = scans[n_scans - 1].ego[a];
     return GVOM_OK;
@@ -1544,11 +1553,12 @@ int gvom_step(GvomHandle *h, const GvomScan *scans, int32_t n_scans, int32_t poi
     if (pipe) CUDA_TRY(cudaStreamWaitEvent(h->tr, h->ev_scratch[h->sset], 0));
     std::vector<ScanIn> v;
     bool pinned = false;
+    int skipped = 0;
     int rc;
-    if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned, pipe ? h->tr : h->st))) return rc;
+    if ((rc = stage_batch(h, scans, n_scans, points_on_device, v, pinned, skipped, pipe ? h->tr : h->st))) return rc;
     ProcPlan pp;
     // pipelined: spare slots for two steps, so the trace never waits for a combine in flight
-    if ((rc = prepare_scans(h, v, pp, pipe ? 2 * (int)v.size() : 0))) return rc;
+    if ((rc = prepare_scans(h, v, pp, pipe ? 2 * (int)v.size() : 0, skipped))) return rc;
     // the trace stream waits until no combine in flight reads the slots it fills
     if ((rc = wait_slots_free(h, pp.slot_of, pp.k, pipe ? h->tr : h->st))) {
         release_slots(h, pp);

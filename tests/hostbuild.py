@@ -12,6 +12,7 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(os.path.dirname(HERE), "gvom_gb300", "csrc")
 HOST_CUDA = os.path.join(HERE, "cpp", "host_cuda")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 PRELUDE = r"""
 #include <algorithm>
@@ -38,6 +39,10 @@ static inline cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cu
 static inline cudaError_t cudaGetLastError() { return cudaSuccess; }
 struct cudaFuncAttributes { int unused; };
 static inline cudaError_t cudaFuncGetAttributes(cudaFuncAttributes *, const void *) { return cudaSuccess; }
+template <class T> static inline cudaError_t cudaGetSymbolAddress(void **p, const T &symbol) {
+    *p = (void *)&symbol;  // a file-scope device array is a host array here
+    return cudaSuccess;
+}
 #include "gvom_internal.cuh"
 namespace gvom {
 // a launch runs every block of the grid under the block emulator
@@ -86,7 +91,7 @@ def compile_units(units, out_dir, name):
     """Compile {file name: source text} in parallel and link them into one
     shared library; returns its path."""
     flags = ["g++", "-O2", "-std=c++20", "-ffp-contract=off", "-frounding-math", "-fPIC", "-Wno-unknown-pragmas",
-             "-I", HOST_CUDA, "-I", CSRC]
+             "-I", HOST_CUDA, "-I", CSRC, "-I", INCLUDE]
     for fname, text in units.items():
         (out_dir / fname).write_text(text)
 

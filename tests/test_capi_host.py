@@ -1,0 +1,223 @@
+"""The library's C ABI on the CPU: gvom_capi.cu compiled for the host over a
+stand-in of the CUDA runtime calls it makes (tests/cpp/host_cuda/
+host_runtime.h: device memory is tracked host memory, launches complete when
+issued, graph capture is refused), with every kernel file compiled unchanged
+and run block by block under tests/cpp/host_cuda/block_threads.h, loaded
+through the package's own binding (gvom_gb300.Gvom over gvom_gb300/_lib.py).
+So the host code the GPU tests run -- the ring of physical slots and its
+spares, the scan tables, batches, the step pipeline at every level, the
+device-output path, the free-memory admission, the debug exports -- runs here
+against the golden fixtures and the oracle."""
+import ctypes as C
+import os
+import shutil
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_files
+from oracle.canonical import canonical_state
+from oracle.oracle import OracleGvom
+from replay import compare_combine, compare_slot, load, ops_of, params_of, replay_and_compare
+
+CAPI_PRELUDE = r"""
+#define __CUDACC__ 1
+#include <algorithm>
+#include <cmath>
+#include "cuda_runtime.h"
+#include "host_runtime.h"
+"""
+
+# settable device memory of the stand-in runtime, for the admission tests
+CAPI_TAIL = r"""
+extern "C" void host_runtime_set_total(unsigned long long bytes) { host_runtime::total = bytes; }
+extern "C" unsigned long long host_runtime_used() { return host_runtime::used; }
+"""
+
+
+@pytest.fixture(scope="module")
+def host_lib(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    from hostbuild import CSRC, PRELUDE, compile_units, host_source
+    read = lambda f: open(os.path.join(CSRC, f)).read()  # noqa: E731
+    capi = read("gvom_capi.cu").replace('#include "../../include/gvom_gb300.h"', '#include "gvom_gb300.h"')
+    units = {"proc.cpp": PRELUDE + '#include "k_process.cu"\n',
+             "comb.cpp": PRELUDE + host_source(read("k_combine.cu")),
+             "morph.cpp": PRELUDE + host_source(read("k_morph.cu")),
+             "dbg.cpp": PRELUDE + host_source(read("k_debug_static.cu")),
+             "capi.cpp": CAPI_PRELUDE + capi + CAPI_TAIL}
+    so = compile_units(units, tmp_path_factory.mktemp("capi"), "libgvom_host.so")
+    from gvom_gb300 import _lib
+    saved = _lib._lib
+    lib = _lib.load(str(so))
+    raw = C.CDLL(str(so))
+    raw.host_runtime_set_total.argtypes = [C.c_ulonglong]
+    raw.host_runtime_used.restype = C.c_ulonglong
+    _lib._lib = lib
+    try:
+        yield lib, raw
+    finally:
+        _lib._lib = saved
+
+
+def _gvom(params):
+    from gvom_gb300 import Gvom
+    return Gvom(*params)
+
+
+@pytest.mark.parametrize("name", golden_files())
+def test_c_abi_replays_every_fixture(host_lib, name):
+    """gvom_gb300.Gvom over the host-built library through every fixture:
+    slots, combined maps, maps and debug exports against the reference."""
+    fx = load(os.path.join(GOLDEN, name))
+    replay_and_compare(_gvom(params_of(fx)), fx)
+
+
+def _scans_of(fx):
+    return [(op[2], op[3], op[4]) for op in ops_of(fx) if op[0] == "P"]
+
+
+def _compare_ring(g, o, what):
+    assert g.ring_state() == o.ring_state(), what
+    B = int(g.params[4])
+    for s in range(B):
+        a, b = g.slot_state(s), o.slot_state(s)
+        assert (a is None) == (b is None), (what, s)
+        if a is not None:
+            compare_slot(canonical_state(a), canonical_state(b), f"{what} slot {s}")
+
+
+def _compare_combine(out, o, g, params, what):
+    ref = o.combine_maps()
+    refd = dict(origin=ref[0], pos=ref[1], neg=ref[2], rough=ref[3], vis=ref[4], **o.maps_state())
+    compare_combine(out, refd, g.maps_state(), params, what)
+    compare_slot(canonical_state(g.combined_state()), canonical_state(o.combined_state()), f"{what} combined")
+
+
+@pytest.mark.parametrize("name,k", [("synth_ring16.npz", 16), ("synth_ring16.npz", 5), ("synth_longrun.npz", 3)])
+def test_process_batch_equals_oracle(host_lib, name, k):
+    """gvom_process_batch: the fixture's scans k at a time (the ring wraps
+    inside a batch for the 16-slot ring), each batch then combined; every
+    ring slot and every combine equal the oracle's sequential calls."""
+    fx = load(os.path.join(GOLDEN, name))
+    params = params_of(fx)
+    g, o = _gvom(params), OracleGvom(*params)
+    scans = _scans_of(fx)
+    for b0 in range(0, len(scans), k):
+        batch = scans[b0:b0 + k]
+        g.process_batch(batch)
+        for pts, ego, T in batch:
+            o.Process_pointcloud(pts, ego, T)
+        _compare_ring(g, o, f"batch at {b0}")
+        _compare_combine(g.combine_maps(), o, g, params, f"combine after batch at {b0}")
+
+
+class _HostTensor:
+    """A buffer of the stand-in runtime's "device" (host memory) with the one
+    method the binding reads from a device tensor."""
+
+    def __init__(self, shape, dtype):
+        self.a = np.zeros(shape, dtype)
+
+    def data_ptr(self):
+        return self.a.ctypes.data
+
+
+@pytest.mark.parametrize("pipeline", [0, 1, 2])
+def test_steps_at_every_pipeline_level_equal_oracle(host_lib, pipeline):
+    """gvom_step back to back with device outputs, at step-pipeline levels 0,
+    1 and 2 (the trace of a step beside the previous step's combine, the
+    process and merges beside its maps; spare slots taken and released), and
+    with host outputs: every step's maps equal the oracle's process +
+    combine."""
+    fx = load(os.path.join(GOLDEN, "synth_ring16.npz"))
+    params = params_of(fx)
+    g, o = _gvom(params), OracleGvom(*params)
+    g.set_tuning({"step_pipeline": pipeline})
+    X = int(params[2])
+    scans = _scans_of(fx)
+    for i in range(0, len(scans), 2):
+        batch = scans[i:i + 2]
+        for pts, ego, T in batch:
+            o.Process_pointcloud(pts, ego, T)
+        if i % 4 == 0:
+            outs = [_HostTensor((X, X), d) for d in (np.int32, np.int32, np.float64, np.int32)]
+            origin = g.step(batch, device_outputs=outs)
+            g.synchronize()
+            out = (origin, outs[0].a, outs[1].a, outs[2].a, outs[3].a)
+        else:
+            out = g.step(batch)
+        _compare_combine(out, o, g, params, f"step {i // 2} (level {pipeline})")
+    _compare_ring(g, o, "after the steps")
+
+
+def test_admission_refuses_what_does_not_fit(host_lib):
+    """The free-memory admission: an instance larger than the device is
+    refused with GVOM_ERR_OOM before it allocates; a scan whose scratch does
+    not fit is refused with GVOM_ERR_OOM and leaves the instance usable."""
+    from gvom_gb300._lib import GVOM_ERR_OOM, GvomError
+    _, raw = host_lib
+    fx = load(os.path.join(GOLDEN, "synth_f32.npz"))
+    params = params_of(fx)
+    raw.host_runtime_set_total(256 << 20)
+    try:
+        big = (0.1, 0.1, 512, 96) + tuple(params[4:])
+        used = raw.host_runtime_used()
+        with pytest.raises(GvomError) as e:
+            _gvom(big)
+        assert e.value.code == GVOM_ERR_OOM and raw.host_runtime_used() == used
+        g, o = _gvom(params), OracleGvom(*params)
+        scans = _scans_of(fx)
+        pts, ego, T = scans[0]
+        g.Process_pointcloud(pts, ego, T)
+        o.Process_pointcloud(pts, ego, T)
+        huge = np.zeros((8_000_000, 3), np.float32)
+        with pytest.raises(GvomError) as e:
+            g.Process_pointcloud(huge, ego, T)
+        assert e.value.code == GVOM_ERR_OOM
+        pts, ego, T = scans[1]
+        g.Process_pointcloud(pts, ego, T)
+        o.Process_pointcloud(pts, ego, T)
+        _compare_ring(g, o, "after the refusal")
+        _compare_combine(g.combine_maps(), o, g, params, "combine after the refusal")
+    finally:
+        raw.host_runtime_set_total(8 << 30)
+
+
+def test_allocation_free_debug_export_and_reserve(host_lib):
+    """gvom_reserve allocates up front; the allocation-free voxel export
+    (file-scope scratch, caller-owned output) gives the regular export's
+    rows; neither allocates during the calls."""
+    lib, raw = host_lib
+    fx = load(os.path.join(GOLDEN, "synth_f64T_veg.npz"))
+    params = params_of(fx)
+    g = _gvom(params)
+    scans = _scans_of(fx)
+    g.reserve(2, max(s[0].shape[0] for s in scans) * 2)
+    before = raw.host_runtime_used()
+    for pts, ego, T in scans:
+        g.Process_pointcloud(pts, ego, T)
+    assert raw.host_runtime_used() == before  # nothing allocated after the reservation
+    g.combine_maps()
+    rows = g.make_debug_voxel_map()
+    out = np.zeros((rows.shape[0] + 5, 8), np.float32)
+    n = C.c_int64()
+    assert lib.gvom_debug_voxel_map_noalloc(g._h, out.ctypes.data_as(C.c_void_p), out.shape[0], C.byref(n)) == 0
+    assert n.value == rows.shape[0]
+    np.testing.assert_array_equal(out[:n.value], rows)
+
+
+def test_error_codes(host_lib):
+    """The C ABI's argument and state errors, on the host build."""
+    from gvom_gb300._lib import GVOM_ERR_ARG, GVOM_NO_DATA
+    lib, _ = host_lib
+    fx = load(os.path.join(GOLDEN, "kat_shift.npz"))
+    g = _gvom(params_of(fx))
+    assert g.combine_maps() is None  # an empty ring: the reference's None
+    origin = np.zeros(3)
+    assert lib.gvom_combine(g._h, origin.ctypes.data_as(C.c_void_p), None, None, None, None) == GVOM_NO_DATA
+    assert lib.gvom_process(None, None, 0, 0, 3, None, None, -1) == GVOM_ERR_ARG
+    bad = np.zeros((4, 3), np.float32)
+    ego = (C.c_double * 3)(0, 0, 0)
+    assert lib.gvom_process(g._h, bad.ctypes.data_as(C.c_void_p), 7, 4, 3, ego, None, -1) == GVOM_ERR_ARG
