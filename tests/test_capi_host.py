@@ -221,3 +221,33 @@ def test_error_codes(host_lib):
     bad = np.zeros((4, 3), np.float32)
     ego = (C.c_double * 3)(0, 0, 0)
     assert lib.gvom_process(g._h, bad.ctypes.data_as(C.c_void_p), 7, 4, 3, ego, None, -1) == GVOM_ERR_ARG
+
+
+# the GPU parity tests whose inputs are host arrays, at their own sizes,
+# against the host build (the others need CUDA tensors, graph capture, or
+# grids of millions of voxels per step)
+GPU_TESTS_ON_HOST = ["test_small_32x512_vs_oracle", "test_float64_ros_style_inputs",
+                     "test_empty_and_out_of_grid_scans", "test_nonfinite_points_dropped_like_oracle",
+                     "test_batch_equals_sequential", "test_debug_exports_vs_oracle",
+                     "test_repeated_combines_accumulate_like_reference", "test_rays_inside_the_sliver_below_zero",
+                     "test_origin_beyond_float32_floor_range", "test_odd_grid_and_row_length"]
+
+
+@pytest.mark.parametrize("name", GPU_TESTS_ON_HOST)
+def test_gpu_parity_tests_on_the_host_build(host_lib, name):
+    import test_parity_gpu
+    from gvom_gb300 import Gvom
+    getattr(test_parity_gpu, name)(Gvom)
+
+
+@pytest.mark.parametrize("B", [1, 16])
+def test_gpu_ring_size_test_on_the_host_build(host_lib, B):
+    import test_parity_gpu
+    from gvom_gb300 import Gvom
+    test_parity_gpu.test_ring_sizes_every_source_class_vs_oracle(Gvom, B)
+
+
+def test_gpu_far_world_offset_test_on_the_host_build(host_lib):
+    import test_parity_gpu
+    from gvom_gb300 import Gvom
+    test_parity_gpu.test_eigen_distances_and_far_world_offset(Gvom)
