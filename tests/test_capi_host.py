@@ -251,3 +251,21 @@ def test_gpu_far_world_offset_test_on_the_host_build(host_lib):
     import test_parity_gpu
     from gvom_gb300 import Gvom
     test_parity_gpu.test_eigen_distances_and_far_world_offset(Gvom)
+
+
+@pytest.mark.parametrize("layout", [0, 2])
+def test_gpu_pointcloud2_tests_on_the_host_build(host_lib, layout):
+    """The ROS ingestion test's host-memory layouts (float32 x, y, z at 0, 4,
+    8 of 16-byte points; float64 at 8, 16, 24 of 40-byte points) and its
+    argument checks, against the host build."""
+    import test_ros_ingest
+    marks = test_ros_ingest.test_pointcloud2_equals_process_pointcloud.pytestmark
+    layouts = next(m.args[1] for m in marks if m.name == "parametrize")
+    assert not layouts[layout]["device"]
+    test_ros_ingest.test_pointcloud2_equals_process_pointcloud(host_lib[0], layouts[layout])
+    test_ros_ingest.test_pointcloud2_argument_checks(host_lib[0])
+
+
+def test_gpu_ros_grids_test_on_the_host_build(host_lib):
+    import test_ros_grids
+    test_ros_grids.test_device_payloads_equal_oracle(host_lib[0])
