@@ -269,3 +269,85 @@ def test_gpu_pointcloud2_tests_on_the_host_build(host_lib, layout):
 def test_gpu_ros_grids_test_on_the_host_build(host_lib):
     import test_ros_grids
     test_ros_grids.test_device_payloads_equal_oracle(host_lib[0])
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_call_sequences_equal_oracle(host_lib, seed):
+    """Seeded random sequences of the library's calls on a small map -- single
+    scans, batches of 1 to 20 scans (longer than the ring too), steps at a
+    random pipeline level with host or device outputs, combines, debug
+    exports, empty and out-of-grid scans -- against the oracle's sequential
+    calls, compared after every call: ring state, every slot, every combine's
+    maps and combined map."""
+    from gvom_gb300.synthetic import Lidar, Terrain, make_scan, make_trajectory
+    rng = np.random.default_rng(1000 + seed)
+    B = int(rng.integers(1, 7))
+    X, Z = int(rng.choice([20, 24, 31])), int(rng.choice([8, 12]))
+    exy, ez = [(1, 1), (2, 0), (0, 1), (1, 2)][int(rng.integers(4))]
+    params = (0.3, 0.25, X, Z, B, 0.8, 0.5, 0.5, 0.3, 2.0, 1.5, 1.0, exy, ez)
+    t = Terrain.make(seed, extent=X * 0.3, path_len=12.0)
+    lid = Lidar(beams=8, columns=128)
+    poses = make_trajectory(40)
+    pool = []
+    for i, p in enumerate(poses):
+        s = make_scan(t, lid, p, i, dropout=float(rng.uniform(0, 0.5)),
+                      transform_dtype=np.float64 if i % 3 == 0 else np.float32)
+        pts = s.points if i % 4 else s.points.astype(np.float64)
+        pool.append((pts, s.ego, s.transform))
+    pool.append((np.zeros((0, 3), np.float32), poses[0].ego if hasattr(poses[0], "ego") else pool[0][1], None))
+    pool.append((np.array([[500.0, 0.0, 0.0]], np.float32), pool[1][1], None))
+    g, o = _gvom(params), OracleGvom(*params)
+    nxt = 0
+
+    def take(n):
+        nonlocal nxt
+        out = []
+        for _ in range(n):
+            out.append(pool[nxt % len(pool)] if rng.random() > 0.08 else pool[-1 - int(rng.integers(2))])
+            nxt += 1
+        return out
+
+    combined = False
+    for step in range(20):
+        what = f"seed {seed} call {step}"
+        op = rng.choice(["scan", "batch", "step", "combine", "debug"], p=[0.3, 0.25, 0.25, 0.15, 0.05])
+        if op == "scan":
+            (pts, ego, T), = take(1)
+            g.Process_pointcloud(pts, ego, T)
+            o.Process_pointcloud(pts, ego, T)
+        elif op == "batch":
+            batch = take(int(rng.integers(1, 21)))
+            if len({b[0].dtype for b in batch}) > 1:
+                batch = [(b[0].astype(np.float32), b[1], b[2]) for b in batch]
+            g.process_batch(batch)
+            for pts, ego, T in batch:
+                o.Process_pointcloud(pts, ego, T)
+        elif op == "step":
+            batch = take(int(rng.integers(1, 5)))
+            if len({b[0].dtype for b in batch}) > 1:
+                batch = [(b[0].astype(np.float32), b[1], b[2]) for b in batch]
+            g.set_tuning({"step_pipeline": int(rng.integers(0, 3))})
+            for pts, ego, T in batch:
+                o.Process_pointcloud(pts, ego, T)
+            if rng.random() < 0.5:
+                outs = [_HostTensor((X, X), d) for d in (np.int32, np.int32, np.float64, np.int32)]
+                origin = g.step(batch, device_outputs=outs)
+                g.synchronize()
+                out = (origin, outs[0].a, outs[1].a, outs[2].a, outs[3].a)
+            else:
+                out = g.step(batch)
+            _compare_combine(out, o, g, params, what)
+            combined = True
+        elif op == "combine":
+            out = g.combine_maps()
+            if out is None:
+                assert o.combine_maps() is None, what
+            else:
+                _compare_combine(out, o, g, params, what)
+                combined = True
+        elif op == "debug" and combined:
+            from oracle.canonical import sort_debug_voxels
+            from replay import assert_exact
+            dv, rv = sort_debug_voxels(g.make_debug_voxel_map()), sort_debug_voxels(o.make_debug_voxel_map())
+            assert_exact(dv[:, :5], rv[:, :5], what)
+        _compare_ring(g, o, what)
