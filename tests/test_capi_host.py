@@ -351,3 +351,11 @@ def test_random_call_sequences_equal_oracle(host_lib, seed):
             dv, rv = sort_debug_voxels(g.make_debug_voxel_map()), sort_debug_voxels(o.make_debug_voxel_map())
             assert_exact(dv[:, :5], rv[:, :5], what)
         _compare_ring(g, o, what)
+
+
+def test_gpu_launch_shape_test_on_the_host_build(host_lib):
+    """The autotuner's test that every launch shape (points per block,
+    merge planes, statistics blocks, index-merge overlap, maps tile, step
+    pipeline) gives identical maps, against the host build."""
+    import test_autotune
+    test_autotune.test_every_launch_shape_gives_identical_maps(host_lib[0])
