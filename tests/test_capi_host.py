@@ -359,3 +359,54 @@ def test_gpu_launch_shape_test_on_the_host_build(host_lib):
     pipeline) gives identical maps, against the host build."""
     import test_autotune
     test_autotune.test_every_launch_shape_gives_identical_maps(host_lib[0])
+
+
+def _adversarial_scan(rng, params, ego):
+    """Points on voxel boundaries and corners, piles of hundreds to
+    thousands in one voxel, points inside the minimum distance, outside the
+    grid and non-finite, around `ego`."""
+    xy, zr, X, Z = params[0], params[1], params[2], params[3]
+    n = int(rng.integers(200, 3000))
+    half = np.array([X * xy / 2, X * xy / 2, Z * zr / 2])
+    p = ego + rng.uniform(-1.2, 1.2, (n, 3)) * half
+    k = rng.random(n)
+    snap = k < 0.3  # onto voxel faces / corners
+    p[snap] = np.round(p[snap] / [xy, xy, zr]) * [xy, xy, zr]
+    pile = (k >= 0.3) & (k < 0.45)  # one voxel, many points
+    c = ego + rng.uniform(-0.4, 0.4, 3) * half
+    p[pile] = c + rng.uniform(0, 1, (int(pile.sum()), 3)) * [xy, xy, zr] * 0.999
+    near = (k >= 0.45) & (k < 0.5)  # inside the minimum distance
+    p[near] = ego + rng.normal(size=(int(near.sum()), 3)) * params[5] * 0.3
+    far = (k >= 0.5) & (k < 0.55)
+    p[far] = ego + rng.uniform(-1, 1, (int(far.sum()), 3)) * half * 20
+    bad = rng.random(n) < 0.01
+    p[bad, int(rng.integers(3))] = np.nan
+    return p.astype(np.float64 if rng.random() < 0.4 else np.float32)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_adversarial_scans_equal_oracle(host_lib, seed):
+    """Adversarial scans (voxel boundaries, piles in one voxel, minimum
+    distance, outside the grid, non-finite) through process and combine on
+    small maps, against the oracle after every call."""
+    rng = np.random.default_rng(2000 + seed)
+    B = int(rng.integers(1, 5))
+    X, Z = int(rng.choice([16, 21, 32])), int(rng.choice([8, 10]))
+    exy, ez = [(1, 1), (2, 1), (0, 0), (1, 2)][seed % 4]
+    params = (float(rng.choice([0.2, 0.25, 0.3])), float(rng.choice([0.2, 0.4])), X, Z, B, 0.5, 0.5, 0.5, 0.3,
+              2.0, 1.0, 1.0, exy, ez)
+    g, o = _gvom(params), OracleGvom(*params)
+    ego = np.array([0.05, -0.1, 0.9])
+    for i in range(6):
+        ego = ego + rng.uniform(-0.5, 0.5, 3) * [1, 1, 0.1]
+        pts = _adversarial_scan(rng, params, ego)
+        T = None
+        if i % 2:
+            a = rng.uniform(-0.3, 0.3)
+            T = np.array([[np.cos(a), -np.sin(a), 0, 0.1], [np.sin(a), np.cos(a), 0, -0.2], [0, 0, 1, 0.05],
+                          [0, 0, 0, 1]], np.float64 if i % 4 == 1 else np.float32)
+        g.Process_pointcloud(pts, tuple(ego), T)
+        o.Process_pointcloud(pts, tuple(ego), T)
+        assert g.last_process_stats() == o.last_process_stats(), f"seed {seed} scan {i}"
+        _compare_ring(g, o, f"seed {seed} scan {i}")
+        _compare_combine(g.combine_maps(), o, g, params, f"seed {seed} combine {i}")
