@@ -13,7 +13,10 @@
  * arrives; a thread that returns leaves its block's and its warp's barriers,
  * as an exited CUDA thread stops counting at a block barrier.  __shared__
  * variables become statics (one block runs at a time).  The schedule is
- * deterministic, so atomics resolve in the same order on every run.  Kernels
+ * deterministic, so atomics resolve in the same order on every run, unless
+ * shuffle_seed is set: then blocks run in a random order and a random ready
+ * fiber resumes next, so that a read which only a missing barrier separates
+ * from its write, or an assumption about block order, shows.  Kernels
  * whose shuffles run with lanes missing (a lane that returned) and kernels
  * that spin on memory another thread writes are outside what this emulates;
  * a block whose fibers all wait ends the program.  Not part of the library. */
@@ -61,6 +64,16 @@ struct Sched {
 };
 inline Sched *sched = nullptr;
 inline unsigned parity = 0;  // the running fiber's shuffles so far, mod 2
+// 0: blocks in grid order and ready fibers first in, first out; otherwise
+// the seed of a shuffled schedule
+inline unsigned long long shuffle_seed = 0;
+inline unsigned long long shuffle_state = 0;
+inline unsigned long long shuffle_next() {  // splitmix64
+    unsigned long long z = (shuffle_state += 0x9e3779b97f4a7c15ull);
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
 
 inline int linear_tid() { return (int)(threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z)); }
 
@@ -116,7 +129,7 @@ inline T exchange(T v, int src, bool take) {
     return r;
 }
 
-// Every block of the grid, x fastest.
+// Every block of the grid, x fastest (or shuffled, see shuffle_seed).
 inline void launch(dim3 grid, dim3 blk, const std::function<void()> &fn) {
     static Sched *s = new Sched();
     sched = s;
@@ -130,41 +143,55 @@ inline void launch(dim3 grid, dim3 blk, const std::function<void()> &fn) {
     s->fn = &fn;
     blockDim = {blk.x, blk.y, blk.z};
     gridDim = {grid.x, grid.y, grid.z};
-    for (unsigned bz = 0; bz < grid.z; bz++)
-        for (unsigned by = 0; by < grid.y; by++)
-            for (unsigned bx = 0; bx < grid.x; bx++) {
-                blockIdx = {bx, by, bz};
-                s->bar = Barrier{nt, 0, {}};
-                s->warp.assign((nt + 31) / 32, Barrier{});
-                for (int w = 0; w * 32 < nt; w++) s->warp[w].expected = std::min(32, nt - w * 32);
-                s->ready.clear();
-                for (int i = 0; i < nt; i++) {
-                    getcontext(&s->ctx[i]);
-                    s->ctx[i].uc_stack.ss_sp = s->stacks[i];
-                    s->ctx[i].uc_stack.ss_size = kStackBytes;
-                    s->ctx[i].uc_link = &s->main_ctx;
-                    makecontext(&s->ctx[i], fiber_entry, 0);
-                    s->tidx[i] = {i % blk.x, (i / blk.x) % blk.y, i / (blk.x * blk.y)};
-                    s->par[i] = 0;
-                    s->done[i] = 0;
-                    s->ready.push_back(i);
-                }
-                while (!s->ready.empty()) {
-                    const int i = s->ready.front();
-                    s->ready.pop_front();
-                    s->cur = i;
-                    threadIdx = s->tidx[i];
-                    parity = s->par[i];
-                    swapcontext(&s->main_ctx, &s->ctx[i]);
-                    s->par[i] = parity;
-                }
-                for (int i = 0; i < nt; i++)
-                    if (!s->done[i]) {
-                        std::fprintf(stderr, "block_threads: block (%u, %u, %u): thread %d waits forever\n", bx, by,
-                                     bz, i);
-                        std::abort();
-                    }
+    const unsigned long long nb = (unsigned long long)grid.x * grid.y * grid.z;
+    std::vector<unsigned long long> order(nb);
+    for (unsigned long long b = 0; b < nb; b++) order[b] = b;
+    if (shuffle_seed) {
+        if (!shuffle_state) shuffle_state = shuffle_seed;
+        for (unsigned long long b = nb; b > 1; b--) std::swap(order[b - 1], order[shuffle_next() % b]);
+    }
+    for (unsigned long long ob : order) {
+        const unsigned bx = (unsigned)(ob % grid.x), by = (unsigned)(ob / grid.x % grid.y),
+                       bz = (unsigned)(ob / grid.x / grid.y);
+        blockIdx = {bx, by, bz};
+        s->bar = Barrier{nt, 0, {}};
+        s->warp.assign((nt + 31) / 32, Barrier{});
+        for (int w = 0; w * 32 < nt; w++) s->warp[w].expected = std::min(32, nt - w * 32);
+        s->ready.clear();
+        for (int i = 0; i < nt; i++) {
+            getcontext(&s->ctx[i]);
+            s->ctx[i].uc_stack.ss_sp = s->stacks[i];
+            s->ctx[i].uc_stack.ss_size = kStackBytes;
+            s->ctx[i].uc_link = &s->main_ctx;
+            makecontext(&s->ctx[i], fiber_entry, 0);
+            s->tidx[i] = {i % blk.x, (i / blk.x) % blk.y, i / (blk.x * blk.y)};
+            s->par[i] = 0;
+            s->done[i] = 0;
+            s->ready.push_back(i);
+        }
+        while (!s->ready.empty()) {
+            int i;
+            if (shuffle_seed) {
+                const size_t j = (size_t)(shuffle_next() % s->ready.size());
+                i = s->ready[j];
+                s->ready.erase(s->ready.begin() + (long)j);
+            } else {
+                i = s->ready.front();
+                s->ready.pop_front();
             }
+            s->cur = i;
+            threadIdx = s->tidx[i];
+            parity = s->par[i];
+            swapcontext(&s->main_ctx, &s->ctx[i]);
+            s->par[i] = parity;
+        }
+        for (int i = 0; i < nt; i++)
+            if (!s->done[i]) {
+                std::fprintf(stderr, "block_threads: block (%u, %u, %u): thread %d waits forever\n", bx, by,
+                             bz, i);
+                std::abort();
+            }
+    }
     s->cur = -1;
 }
 

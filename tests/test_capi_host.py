@@ -32,6 +32,10 @@ CAPI_PRELUDE = r"""
 CAPI_TAIL = r"""
 extern "C" void host_runtime_set_total(unsigned long long bytes) { host_runtime::total = bytes; }
 extern "C" unsigned long long host_runtime_used() { return host_runtime::used; }
+extern "C" void block_threads_shuffle(unsigned long long seed) {
+    block_threads::shuffle_seed = seed;
+    block_threads::shuffle_state = seed;
+}
 """
 
 
@@ -54,6 +58,7 @@ def host_lib(tmp_path_factory):
     raw = C.CDLL(str(so))
     raw.host_runtime_set_total.argtypes = [C.c_ulonglong]
     raw.host_runtime_used.restype = C.c_ulonglong
+    raw.block_threads_shuffle.argtypes = [C.c_ulonglong]
     _lib._lib = lib
     try:
         yield lib, raw
@@ -410,3 +415,21 @@ def test_adversarial_scans_equal_oracle(host_lib, seed):
         assert g.last_process_stats() == o.last_process_stats(), f"seed {seed} scan {i}"
         _compare_ring(g, o, f"seed {seed} scan {i}")
         _compare_combine(g.combine_maps(), o, g, params, f"seed {seed} combine {i}")
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+@pytest.mark.parametrize("name", ["kat_boundaries.npz", "kat_guess.npz", "kat_eigen.npz", "synth_f64T_veg.npz",
+                                  "synth_ring16.npz", "small_32x512.npz"])
+def test_shuffled_schedules_replay_fixtures(host_lib, name, seed):
+    """Fixture replays with a shuffled schedule: blocks in a random order and
+    a random ready thread resumed at every barrier phase, so a read that only
+    a missing barrier separates from its write, or code that counts on block
+    order, would change the results.  Integer outputs stay exact, statistics
+    within the parity tolerance."""
+    _, raw = host_lib
+    raw.block_threads_shuffle(seed)
+    try:
+        fx = load(os.path.join(GOLDEN, name))
+        replay_and_compare(_gvom(params_of(fx)), fx)
+    finally:
+        raw.block_threads_shuffle(0)
