@@ -499,7 +499,12 @@ class HostMapper:
         return st
 
 
-@pytest.mark.parametrize("name", golden_files())
+# the known-answer fixtures and the 16-slot ring; every fixture also replays
+# through the host-built C ABI in tests/test_capi_host.py
+MAPPER_FIXTURES = [n for n in golden_files() if n.startswith("kat_")] + ["synth_ring16.npz"]
+
+
+@pytest.mark.parametrize("name", MAPPER_FIXTURES)
 def test_host_build_replays_every_fixture(lib, name):
     fx = load(os.path.join(GOLDEN, name))
     m = HostMapper(lib, params_of(fx))

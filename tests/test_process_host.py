@@ -18,7 +18,7 @@ import shutil
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, golden_files
+from conftest import GOLDEN
 from hostbuild import PRELUDE, compile_units
 from oracle.canonical import canonical_state
 from oracle.oracle import OracleGvom
@@ -169,7 +169,15 @@ def _oracle_slots(fx):
     return p, res
 
 
-@pytest.mark.parametrize("name", golden_files())
+# fixtures of each kind (float32 / float64 points and transforms, voxel
+# boundaries, rays, eigen distances (2, 0) and (1, 2), the 128 x 128 x 32
+# grid); every fixture also replays through tests/test_pipeline_host.py and
+# tests/test_capi_host.py
+PROCESS_FIXTURES = ["kat_boundaries.npz", "kat_rays.npz", "synth_f64T_veg.npz", "synth_f64pts_eig20.npz",
+                    "synth_aniso_z.npz", "small_32x512.npz"]
+
+
+@pytest.mark.parametrize("name", PROCESS_FIXTURES)
 def test_process_kernels_equal_oracle(lib, name):
     """Every scan of the fixture, one scan per call."""
     p, res = _oracle_slots(load(os.path.join(GOLDEN, name)))
