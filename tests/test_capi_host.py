@@ -233,7 +233,8 @@ def test_error_codes(host_lib):
 # grids of millions of voxels per step)
 GPU_TESTS_ON_HOST = ["test_small_32x512_vs_oracle", "test_float64_ros_style_inputs",
                      "test_empty_and_out_of_grid_scans", "test_nonfinite_points_dropped_like_oracle",
-                     "test_batch_equals_sequential", "test_debug_exports_vs_oracle",
+                     "test_batch_equals_sequential", "test_batch_longer_than_ring_equals_sequential",
+                     "test_debug_exports_vs_oracle",
                      "test_repeated_combines_accumulate_like_reference", "test_rays_inside_the_sliver_below_zero",
                      "test_origin_beyond_float32_floor_range", "test_odd_grid_and_row_length"]
 

@@ -151,6 +151,29 @@ def test_batch_equals_sequential(Gvom):
         np.testing.assert_array_equal(x, y)
 
 
+def test_batch_longer_than_ring_equals_sequential(Gvom):
+    """process_batch of 7 scans into a 3-slot ring keeps the last 3 scans at
+    the ring positions one call per scan gives them: the same ring state,
+    slots and maps as the scans one by one."""
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["small_32x512"]
+    scans = make_workload_scans(w, 7)
+    params = w.gvom_args()[:4] + (3,) + w.gvom_args()[5:]
+    a, b = Gvom(*params), Gvom(*params)
+    for s in scans[:2]:
+        for m in (a, b):
+            m.Process_pointcloud(s.points, s.ego, s.transform)
+    for s in scans[2:]:
+        a.Process_pointcloud(s.points, s.ego, s.transform)
+    b.process_batch([(s.points, s.ego, s.transform) for s in scans[2:]])
+    assert a.ring_state() == b.ring_state()
+    for slot in range(3):
+        compare_slot(canonical_state(a.slot_state(slot)), canonical_state(b.slot_state(slot)), f"slot {slot}")
+    ra, rb = a.combine_maps(), b.combine_maps()
+    for x, y in zip(ra, rb):
+        np.testing.assert_array_equal(x, y)
+
+
 def test_torch_device_input_and_device_outputs(Gvom):
     import torch
     from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
