@@ -421,3 +421,11 @@ def test_shuffled_schedules_replay_fixtures(host_lib, name, seed):
         replay_and_compare(_gvom(params_of(fx)), fx)
     finally:
         raw.block_threads_shuffle(0)
+
+
+def test_gpu_step_test_on_the_host_build(host_lib):
+    """The GPU test that gvom_step equals process_batch + combine_maps, with
+    graphs off (the host runtime refuses capture), against the host build."""
+    import test_parity_gpu
+    from gvom_gb300 import Gvom
+    test_parity_gpu.test_step_equals_process_then_combine(Gvom, False)
