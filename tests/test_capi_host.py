@@ -429,3 +429,15 @@ def test_gpu_step_test_on_the_host_build(host_lib):
     import test_parity_gpu
     from gvom_gb300 import Gvom
     test_parity_gpu.test_step_equals_process_then_combine(Gvom, False)
+
+
+def test_headline_workload_step_on_the_host_build(host_lib):
+    """One step of the headline workload (os1_64_veg: 256 x 256 x 64 voxels
+    at 0.15 m, about 95K points of an OS1-64 scan with vegetation) through
+    the host build, against the oracle: the grid sizes, block counts, hash
+    table and large-cell paths of the measured configuration."""
+    import test_parity_gpu
+    from gvom_gb300 import Gvom
+    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
+    w = WORKLOADS["os1_64_veg"]
+    test_parity_gpu._run_both(Gvom, w.gvom_args(), make_workload_scans(w, 1))
