@@ -4,7 +4,8 @@
  * cuda_runtime.h (this directory).
  *
  * Blocks run one after another on the calling thread.  Each CUDA thread of a
- * block is a fiber (POSIX ucontext) with its own stack; a fiber runs until it
+ * block is a fiber with its own stack, entered once through a POSIX ucontext
+ * and afterwards switched with _setjmp / _longjmp; a fiber runs until it
  * waits at a barrier or returns, and a scheduler then resumes the next ready
  * fiber.  __syncthreads is a barrier of the block's live threads; a warp
  * shuffle writes the caller's value into the warp's exchange slots, waits at
@@ -21,7 +22,12 @@
  * that spin on memory another thread writes are outside what this emulates;
  * a block whose fibers all wait ends the program.  Not part of the library. */
 #pragma once
+#include <setjmp.h>
 #include <ucontext.h>
+
+#if defined(_FORTIFY_SOURCE) && _FORTIFY_SOURCE > 0
+#error "build without _FORTIFY_SOURCE: fibers switch stacks with _longjmp, which its check refuses"
+#endif
 
 #include <algorithm>
 #include <cstdio>
@@ -48,9 +54,16 @@ struct Barrier {
     std::vector<int> waiters;
 };
 
+struct JmpBuf {
+    jmp_buf b;
+};
+
 struct Sched {
-    ucontext_t main_ctx;
+    ucontext_t main_ctx;  // the scheduler, as a fiber's first entry left it
+    jmp_buf main_jb;      // the scheduler, as the last resume left it
     std::vector<ucontext_t> ctx;
+    std::vector<JmpBuf> jb;  // each started fiber, as it last waited
+    std::vector<char> started;
     std::vector<char *> stacks;
     std::vector<HostDim3> tidx;
     std::vector<unsigned> par;
@@ -92,7 +105,7 @@ inline void arrive_and_wait(Barrier &b) {
     b.arrived++;
     const int me = s.cur;
     b.waiters.push_back(me);
-    swapcontext(&s.ctx[me], &s.main_ctx);  // back when the barrier is complete
+    if (!_setjmp(s.jb[me].b)) _longjmp(s.main_jb, 1);  // back here when the barrier is complete
 }
 
 inline void arrive_and_drop(Barrier &b) {
@@ -107,7 +120,8 @@ inline void fiber_entry() {
     arrive_and_drop(s.bar);
     arrive_and_drop(s.warp[me >> 5]);
     s.done[me] = 1;
-}  // returns to the scheduler (uc_link)
+    _longjmp(s.main_jb, 1);  // never returns
+}
 
 // value of lane `src` of the caller's warp (`take`), else the caller's own.
 // One barrier per shuffle: consecutive shuffles use alternate slot arrays,
@@ -137,6 +151,8 @@ inline void launch(dim3 grid, dim3 blk, const std::function<void()> &fn) {
     if (nt < 1 || nt > kMaxThreads) std::abort();
     while ((int)s->stacks.size() < nt) s->stacks.push_back(static_cast<char *>(std::malloc(kStackBytes)));
     s->ctx.resize(nt);
+    s->jb.resize(nt);
+    s->started.resize(nt);
     s->tidx.resize(nt);
     s->par.resize(nt);
     s->done.resize(nt);
@@ -167,6 +183,7 @@ inline void launch(dim3 grid, dim3 blk, const std::function<void()> &fn) {
             s->tidx[i] = {i % blk.x, (i / blk.x) % blk.y, i / (blk.x * blk.y)};
             s->par[i] = 0;
             s->done[i] = 0;
+            s->started[i] = 0;
             s->ready.push_back(i);
         }
         while (!s->ready.empty()) {
@@ -182,7 +199,14 @@ inline void launch(dim3 grid, dim3 blk, const std::function<void()> &fn) {
             s->cur = i;
             threadIdx = s->tidx[i];
             parity = s->par[i];
-            swapcontext(&s->main_ctx, &s->ctx[i]);
+            // a started fiber resumes where it waited (no signal-mask system
+            // call, unlike swapcontext); a new one enters once through its
+            // ucontext; either comes back here with _longjmp
+            if (!_setjmp(s->main_jb)) {
+                if (s->started[i]) _longjmp(s->jb[i].b, 1);
+                s->started[i] = 1;
+                swapcontext(&s->main_ctx, &s->ctx[i]);
+            }
             s->par[i] = parity;
         }
         for (int i = 0; i < nt; i++)

@@ -253,12 +253,11 @@ def test_gpu_ring_size_test_on_the_host_build(host_lib, B):
     test_parity_gpu.test_ring_sizes_every_source_class_vs_oracle(Gvom, B)
 
 
-@pytest.mark.parametrize("layout", [2])
+@pytest.mark.parametrize("layout", [0, 2])
 def test_gpu_pointcloud2_tests_on_the_host_build(host_lib, layout):
-    """The ROS ingestion test's float64 host-memory layout (x, y, z at 8, 16,
-    24 of 40-byte points, widened as the node does) and its argument checks,
-    against the host build (float32 fields at byte offsets also run through
-    the trace kernel's host build, tests/test_trace_host.py)."""
+    """The ROS ingestion test's host-memory layouts (float32 x, y, z at 0, 4,
+    8 of 16-byte points; float64 at 8, 16, 24 of 40-byte points, widened as
+    the node does) and its argument checks, against the host build."""
     import test_ros_ingest
     marks = test_ros_ingest.test_pointcloud2_equals_process_pointcloud.pytestmark
     layouts = next(m.args[1] for m in marks if m.name == "parametrize")
@@ -441,3 +440,18 @@ def test_headline_workload_step_on_the_host_build(host_lib):
     from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
     w = WORKLOADS["os1_64_veg"]
     test_parity_gpu._run_both(Gvom, w.gvom_args(), make_workload_scans(w, 1))
+
+
+def test_gpu_far_world_offset_test_on_the_host_build(host_lib):
+    """Eigen distances (2, 0) at a 1e4 m world offset on 256 x 256 x 48."""
+    import test_parity_gpu
+    from gvom_gb300 import Gvom
+    test_parity_gpu.test_eigen_distances_and_far_world_offset(Gvom)
+
+
+def test_gpu_launch_shape_test_on_the_host_build(host_lib):
+    """The autotuner's test that every launch shape (points per block,
+    merge planes, statistics blocks, index-merge overlap, maps tile, step
+    pipeline) gives identical maps, against the host build."""
+    import test_autotune
+    test_autotune.test_every_launch_shape_gives_identical_maps(host_lib[0])
