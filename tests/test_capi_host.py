@@ -430,16 +430,28 @@ def test_gpu_step_test_on_the_host_build(host_lib):
     test_parity_gpu.test_step_equals_process_then_combine(Gvom, False)
 
 
-def test_headline_workload_step_on_the_host_build(host_lib):
-    """One step of the headline workload (os1_64_veg: 256 x 256 x 64 voxels
-    at 0.15 m, about 95K points of an OS1-64 scan with vegetation) through
-    the host build, against the oracle: the grid sizes, block counts, hash
-    table and large-cell paths of the measured configuration."""
+def test_headline_workload_on_the_host_build(host_lib):
+    """The GPU test of the headline workload's trajectory (os1_64_veg: 256 x
+    256 x 64 voxels at 0.15 m, six OS1-64 scans with vegetation, about 95K
+    points each, a combine after each) against the host build: the grid
+    sizes, block counts, hash table and large-cell paths of the measured
+    configuration."""
     import test_parity_gpu
     from gvom_gb300 import Gvom
-    from gvom_gb300.synthetic import WORKLOADS, make_workload_scans
-    w = WORKLOADS["os1_64_veg"]
-    test_parity_gpu._run_both(Gvom, w.gvom_args(), make_workload_scans(w, 1))
+    test_parity_gpu.test_os1_64_vegetation_trajectory_vs_oracle(Gvom)
+
+
+@pytest.mark.skipif(os.environ.get("GVOM_HOST_FULL_SIZE") != "1",
+                    reason="full-size forms on the host take minutes (GVOM_HOST_FULL_SIZE=1 runs them)")
+@pytest.mark.parametrize("name", ["test_batched_8_shape_vs_oracle",
+                                  "test_precision_form_os1_128_far_vs_float64_oracle"])
+def test_full_size_gpu_tests_on_the_host_build(host_lib, name):
+    """The batched_8 shape (8 sensors, 16 slots) and the precision form
+    (512 x 512 x 96, two OS1-128 scans, 1e4 m offset) against the host
+    build."""
+    import test_parity_gpu
+    from gvom_gb300 import Gvom
+    getattr(test_parity_gpu, name)(Gvom)
 
 
 def test_gpu_far_world_offset_test_on_the_host_build(host_lib):
