@@ -222,8 +222,10 @@ def float_errors(got_out, ref: dict, got_maps: dict) -> dict:
 def stat_errors(got_state: dict, ref_state: dict) -> dict:
     """Largest deviations of the combined per-voxel statistics from the oracle,
     on canonical states with the same occupied set: absolute for the mean and
-    the covariance (voxel units), and for the eigenvalues relative to each
-    voxel's largest eigenvalue magnitude."""
+    the covariance (voxel units); for the eigenvalues relative to each
+    voxel's largest eigenvalue magnitude where that is at least EIG_ATOL,
+    and absolute in the voxels below it (a single point, or points on one
+    spot, whose eigenvalues are rounding noise around 0)."""
     g = canonical_state(got_state)
     r = canonical_state(ref_state)
     assert_exact(g["occ"], r["occ"], "occupied set")
@@ -235,6 +237,9 @@ def stat_errors(got_state: dict, ref_state: dict) -> dict:
     if "eigen" in g and "eigen" in r and len(rm):
         ge = np.asarray(g["eigen"], np.float64)
         re = np.asarray(r["eigen"], np.float64)
-        scale = np.maximum(np.abs(re).max(axis=1, keepdims=True), 1e-30)
-        out["eigen_rel_to_max"] = float(np.max(np.abs(ge - re) / scale))
+        scale = np.abs(re).max(axis=1)
+        err = np.abs(ge - re).max(axis=1)
+        big = scale >= EIG_ATOL
+        out["eigen_rel_to_max"] = float(np.max(err[big] / scale[big])) if big.any() else 0.0
+        out["eigen_abs_below_atol"] = float(np.max(err[~big])) if (~big).any() else 0.0
     return out
