@@ -6,7 +6,10 @@
  * Device memory is host memory: allocations are tracked (a pointer query
  * tells them from other memory) against a settable device total, so the
  * library's free-memory admission can be driven; fresh allocations hold a
- * junk pattern, as device memory holds whatever was there.  Kernels run to
+ * junk pattern, as device memory holds whatever was there.  Each allocation
+ * sits between two guard zones whose pattern is checked when it is freed and
+ * on request, so a write past either end by a kernel or by the host code is
+ * counted (guard_faults).  Kernels run to
  * completion when they are launched, so work is done in issue order and
  * streams and events need no state.  Graph capture is refused.  Not part of
  * the library. */
@@ -73,18 +76,38 @@ inline size_t total = (size_t)8 << 30;         // the device's memory
 inline size_t used = 0;
 inline int num_sms = 4;
 inline char handle_bytes[1];  // streams and events: any non-null address
+constexpr size_t kGuard = 256;  // bytes before and after each allocation
+constexpr unsigned char kGuardByte = 0x5a;
+inline unsigned long long guard_faults = 0;
+inline bool guards_intact(const char *p, size_t bytes) {
+    for (size_t i = 0; i < kGuard; i++)
+        if ((unsigned char)p[-1 - (long)i] != kGuardByte || (unsigned char)p[bytes + i] != kGuardByte) return false;
+    return true;
+}
+// live allocations whose guard zones were overwritten (counted in guard_faults)
+inline unsigned long long check_live() {
+    std::lock_guard<std::mutex> lk(mu);
+    unsigned long long bad = 0;
+    for (auto &a : allocs)
+        if (!guards_intact(a.first, a.second)) bad++;
+    guard_faults += bad;
+    return bad;
+}
 }  // namespace host_runtime
 
 static inline cudaError_t cudaMalloc(void **p, size_t bytes) {
     std::lock_guard<std::mutex> lk(host_runtime::mu);
     *p = nullptr;
     if (host_runtime::used + bytes > host_runtime::total) return cudaErrorMemoryAllocation;
-    char *m = static_cast<char *>(std::malloc(bytes ? bytes : 1));
+    using host_runtime::kGuard;
+    char *m = static_cast<char *>(std::malloc(bytes + 2 * kGuard));
     if (!m) return cudaErrorMemoryAllocation;
-    std::memset(m, 0xa5, bytes);
-    host_runtime::allocs[m] = bytes;
+    std::memset(m, host_runtime::kGuardByte, kGuard);
+    std::memset(m + kGuard, 0xa5, bytes);
+    std::memset(m + kGuard + bytes, host_runtime::kGuardByte, kGuard);
+    host_runtime::allocs[m + kGuard] = bytes;
     host_runtime::used += bytes;
-    *p = m;
+    *p = m + kGuard;
     return cudaSuccess;
 }
 static inline cudaError_t cudaFree(void *p) {
@@ -92,9 +115,10 @@ static inline cudaError_t cudaFree(void *p) {
     std::lock_guard<std::mutex> lk(host_runtime::mu);
     auto it = host_runtime::allocs.find(static_cast<const char *>(p));
     if (it == host_runtime::allocs.end()) std::abort();  // not a device allocation
+    if (!host_runtime::guards_intact(it->first, it->second)) host_runtime::guard_faults++;
     host_runtime::used -= it->second;
     host_runtime::allocs.erase(it);
-    std::free(p);
+    std::free(static_cast<char *>(p) - host_runtime::kGuard);
     return cudaSuccess;
 }
 static inline cudaError_t cudaMemGetInfo(size_t *fr, size_t *tot) {

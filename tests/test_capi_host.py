@@ -7,7 +7,8 @@ through the package's own binding (gvom_gb300.Gvom over gvom_gb300/_lib.py).
 So the host code the GPU tests run -- the ring of physical slots and its
 spares, the scan tables, batches, the step pipeline at every level, the
 device-output path, the free-memory admission, the debug exports -- runs here
-against the golden fixtures and the oracle."""
+against the golden fixtures and the oracle.  Every device allocation sits
+between guard zones; after each test no write may have landed in one."""
 import ctypes as C
 import os
 import shutil
@@ -32,6 +33,11 @@ CAPI_PRELUDE = r"""
 CAPI_TAIL = r"""
 extern "C" void host_runtime_set_total(unsigned long long bytes) { host_runtime::total = bytes; }
 extern "C" unsigned long long host_runtime_used() { return host_runtime::used; }
+// guard zones overwritten so far (freed allocations, and live ones now)
+extern "C" unsigned long long host_runtime_guard_faults() {
+    host_runtime::check_live();
+    return host_runtime::guard_faults;
+}
 extern "C" void block_threads_shuffle(unsigned long long seed) {
     block_threads::shuffle_seed = seed;
     block_threads::shuffle_state = seed;
@@ -59,11 +65,23 @@ def host_lib(tmp_path_factory):
     raw.host_runtime_set_total.argtypes = [C.c_ulonglong]
     raw.host_runtime_used.restype = C.c_ulonglong
     raw.block_threads_shuffle.argtypes = [C.c_ulonglong]
+    raw.host_runtime_guard_faults.restype = C.c_ulonglong
     _lib._lib = lib
     try:
         yield lib, raw
     finally:
         _lib._lib = saved
+
+
+@pytest.fixture(autouse=True)
+def _no_write_out_of_bounds(host_lib):
+    """After every test, with its instances freed: no guard zone around any
+    device allocation was overwritten (a write past either end of a buffer,
+    by a kernel or by the host code)."""
+    yield
+    import gc
+    gc.collect()
+    assert host_lib[1].host_runtime_guard_faults() == 0
 
 
 def _gvom(params):
