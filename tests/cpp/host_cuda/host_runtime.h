@@ -7,13 +7,18 @@
  * tells them from other memory) against a settable device total, so the
  * library's free-memory admission can be driven; fresh allocations hold a
  * junk pattern, as device memory holds whatever was there.  Each allocation
- * sits between two guard zones whose pattern is checked when it is freed and
- * on request, so a write past either end by a kernel or by the host code is
- * counted (guard_faults).  Kernels run to
+ * (rounded up to 256 bytes, the alignment cudaMalloc gives) ends against an
+ * inaccessible page and starts after one, so a read or write past its end
+ * stops the process; the bytes between the requested size and those pages
+ * hold a guard pattern checked when the allocation is freed and on request,
+ * so a write just past either end is counted (guard_faults).  Kernels run to
  * completion when they are launched, so work is done in issue order and
  * streams and events need no state.  Graph capture is refused.  Not part of
  * the library. */
 #pragma once
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -76,12 +81,22 @@ inline size_t total = (size_t)8 << 30;         // the device's memory
 inline size_t used = 0;
 inline int num_sms = 4;
 inline char handle_bytes[1];  // streams and events: any non-null address
-constexpr size_t kGuard = 256;  // bytes before and after each allocation
 constexpr unsigned char kGuardByte = 0x5a;
 inline unsigned long long guard_faults = 0;
+struct Mapping {
+    char *base;   // start of the mapping (an inaccessible page)
+    size_t len;   // bytes mapped
+    char *lo;     // first byte of the readable pages
+    char *end;    // one past the readable pages (an inaccessible page follows)
+};
+inline std::map<const char *, Mapping> maps;  // allocation -> its mapping
+// the guard bytes around [p, p + bytes) within the readable pages
 inline bool guards_intact(const char *p, size_t bytes) {
-    for (size_t i = 0; i < kGuard; i++)
-        if ((unsigned char)p[-1 - (long)i] != kGuardByte || (unsigned char)p[bytes + i] != kGuardByte) return false;
+    const Mapping &m = maps.at(p);
+    for (const char *q = m.lo; q < p; q++)
+        if ((unsigned char)*q != kGuardByte) return false;
+    for (const char *q = p + bytes; q < m.end; q++)
+        if ((unsigned char)*q != kGuardByte) return false;
     return true;
 }
 // live allocations whose guard zones were overwritten (counted in guard_faults)
@@ -99,15 +114,23 @@ static inline cudaError_t cudaMalloc(void **p, size_t bytes) {
     std::lock_guard<std::mutex> lk(host_runtime::mu);
     *p = nullptr;
     if (host_runtime::used + bytes > host_runtime::total) return cudaErrorMemoryAllocation;
-    using host_runtime::kGuard;
-    char *m = static_cast<char *>(std::malloc(bytes + 2 * kGuard));
-    if (!m) return cudaErrorMemoryAllocation;
-    std::memset(m, host_runtime::kGuardByte, kGuard);
-    std::memset(m + kGuard, 0xa5, bytes);
-    std::memset(m + kGuard + bytes, host_runtime::kGuardByte, kGuard);
-    host_runtime::allocs[m + kGuard] = bytes;
+    const size_t pg = (size_t)sysconf(_SC_PAGESIZE);
+    const size_t rounded = bytes ? (bytes + 255) & ~(size_t)255 : 256;
+    const size_t data = (rounded + pg - 1) / pg * pg;
+    char *base = static_cast<char *>(mmap(nullptr, data + 2 * pg, PROT_READ | PROT_WRITE,
+                                          MAP_PRIVATE | MAP_ANONYMOUS, -1, 0));
+    if (base == MAP_FAILED) return cudaErrorMemoryAllocation;
+    mprotect(base, pg, PROT_NONE);
+    mprotect(base + pg + data, pg, PROT_NONE);
+    char *lo = base + pg, *end = base + pg + data;
+    char *m = end - rounded;  // the rounded allocation ends against the inaccessible page
+    std::memset(lo, host_runtime::kGuardByte, (size_t)(m - lo));
+    std::memset(m, 0xa5, bytes);
+    std::memset(m + bytes, host_runtime::kGuardByte, rounded - bytes);
+    host_runtime::allocs[m] = bytes;
+    host_runtime::maps[m] = host_runtime::Mapping{base, data + 2 * pg, lo, end};
     host_runtime::used += bytes;
-    *p = m + kGuard;
+    *p = m;
     return cudaSuccess;
 }
 static inline cudaError_t cudaFree(void *p) {
@@ -117,8 +140,10 @@ static inline cudaError_t cudaFree(void *p) {
     if (it == host_runtime::allocs.end()) std::abort();  // not a device allocation
     if (!host_runtime::guards_intact(it->first, it->second)) host_runtime::guard_faults++;
     host_runtime::used -= it->second;
+    const host_runtime::Mapping mp = host_runtime::maps.at(it->first);
+    host_runtime::maps.erase(it->first);
     host_runtime::allocs.erase(it);
-    std::free(static_cast<char *>(p) - host_runtime::kGuard);
+    munmap(mp.base, mp.len);
     return cudaSuccess;
 }
 static inline cudaError_t cudaMemGetInfo(size_t *fr, size_t *tot) {
