@@ -81,6 +81,7 @@ inline size_t total = (size_t)8 << 30;         // the device's memory
 inline size_t used = 0;
 inline int num_sms = 4;
 inline char handle_bytes[1];  // streams and events: any non-null address
+inline unsigned char junk = 0xa5;  // the contents of a fresh allocation
 constexpr unsigned char kGuardByte = 0x5a;
 inline unsigned long long guard_faults = 0;
 struct Mapping {
@@ -125,7 +126,7 @@ static inline cudaError_t cudaMalloc(void **p, size_t bytes) {
     char *lo = base + pg, *end = base + pg + data;
     char *m = end - rounded;  // the rounded allocation ends against the inaccessible page
     std::memset(lo, host_runtime::kGuardByte, (size_t)(m - lo));
-    std::memset(m, 0xa5, bytes);
+    std::memset(m, host_runtime::junk, bytes);
     std::memset(m + bytes, host_runtime::kGuardByte, rounded - bytes);
     host_runtime::allocs[m] = bytes;
     host_runtime::maps[m] = host_runtime::Mapping{base, data + 2 * pg, lo, end};

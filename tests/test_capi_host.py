@@ -38,6 +38,7 @@ extern "C" unsigned long long host_runtime_guard_faults() {
     host_runtime::check_live();
     return host_runtime::guard_faults;
 }
+extern "C" void host_runtime_set_junk(unsigned char v) { host_runtime::junk = v; }
 extern "C" void block_threads_shuffle(unsigned long long seed) {
     block_threads::shuffle_seed = seed;
     block_threads::shuffle_state = seed;
@@ -66,6 +67,7 @@ def host_lib(tmp_path_factory):
     raw.host_runtime_used.restype = C.c_ulonglong
     raw.block_threads_shuffle.argtypes = [C.c_ulonglong]
     raw.host_runtime_guard_faults.restype = C.c_ulonglong
+    raw.host_runtime_set_junk.argtypes = [C.c_ubyte]
     _lib._lib = lib
     try:
         yield lib, raw
@@ -485,3 +487,18 @@ def test_gpu_launch_shape_test_on_the_host_build(host_lib):
     pipeline) gives identical maps, against the host build."""
     import test_autotune
     test_autotune.test_every_launch_shape_gives_identical_maps(host_lib[0])
+
+
+@pytest.mark.parametrize("junk", [0x00, 0xff])
+@pytest.mark.parametrize("name", ["kat_guess.npz", "synth_ring16.npz", "synth_f64T_veg.npz"])
+def test_results_do_not_depend_on_fresh_memory(host_lib, name, junk):
+    """Fixture replays with fresh device allocations holding 0x00 or 0xff
+    instead of the usual pattern: a result that read memory before it was
+    written would change with what fresh memory holds."""
+    _, raw = host_lib
+    raw.host_runtime_set_junk(junk)
+    try:
+        fx = load(os.path.join(GOLDEN, name))
+        replay_and_compare(_gvom(params_of(fx)), fx)
+    finally:
+        raw.host_runtime_set_junk(0xa5)
