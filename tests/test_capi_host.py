@@ -69,6 +69,8 @@ def host_lib(tmp_path_factory):
     raw.host_runtime_guard_faults.restype = C.c_ulonglong
     raw.host_runtime_set_junk.argtypes = [C.c_ubyte]
     _lib._lib = lib
+    # GVOM_HOST_SHUFFLE=<seed>: every test of the module under a shuffled schedule
+    raw.block_threads_shuffle(int(os.environ.get("GVOM_HOST_SHUFFLE", "0")))
     try:
         yield lib, raw
     finally:
@@ -439,7 +441,7 @@ def test_shuffled_schedules_replay_fixtures(host_lib, name, seed):
         fx = load(os.path.join(GOLDEN, name))
         replay_and_compare(_gvom(params_of(fx)), fx)
     finally:
-        raw.block_threads_shuffle(0)
+        raw.block_threads_shuffle(int(os.environ.get("GVOM_HOST_SHUFFLE", "0")))
 
 
 def test_gpu_step_test_on_the_host_build(host_lib):
