@@ -504,3 +504,45 @@ def test_results_do_not_depend_on_fresh_memory(host_lib, name, junk):
         replay_and_compare(_gvom(params_of(fx)), fx)
     finally:
         raw.host_runtime_set_junk(0xa5)
+
+
+def test_image_kernel_entry_points_on_the_host_build(host_lib):
+    """gvom_expand_binary / gvom_lowpass_binary / gvom_convolve through the C
+    ABI of the host build (buffers are the host runtime's device memory):
+    the reference's own outputs on the fixture cases, the oracle on staged
+    and unstaged sizes, and the argument refusals."""
+    from oracle.oracle import convolve, expand_binary, lowpass_binary
+    from gvom_gb300._lib import GVOM_ERR_ARG
+    lib, _ = host_lib
+    P = lambda a: C.c_void_p(a.ctypes.data)  # noqa: E731
+    with np.load(os.path.join(GOLDEN, "morph_binary.npz")) as z:
+        fx = {k: z[k] for k in z.files}
+    n = 0
+    while f"expand{n}_img" in fx:
+        img = np.ascontiguousarray(fx[f"expand{n}_img"], np.int32)
+        out = np.full_like(img, -7)
+        assert lib.gvom_expand_binary(P(img), P(out), img.shape[0], float(fx[f"expand{n}_r"]), None) == 0
+        np.testing.assert_array_equal(out, fx[f"expand{n}_out"])
+        n += 1
+    n = 0
+    while f"lowpass{n}_img" in fx:
+        img = np.ascontiguousarray(fx[f"lowpass{n}_img"], np.int32)
+        out = np.full_like(img, -7)
+        assert lib.gvom_lowpass_binary(P(img), P(out), img.shape[0], int(fx[f"lowpass{n}_fs"]),
+                                       float(fx[f"lowpass{n}_frac"]), None) == 0
+        np.testing.assert_array_equal(out, fx[f"lowpass{n}_out"])
+        n += 1
+    rng = np.random.default_rng(9)
+    a = (rng.uniform(size=(100, 100)) < 0.003).astype(np.int32)
+    out = np.full_like(a, -7)
+    assert lib.gvom_expand_binary(P(a), P(out), 100, 60.0, None) == 0  # beyond the shared staging
+    np.testing.assert_array_equal(out, expand_binary(a, 60.0))
+    d = rng.normal(size=(33, 33))
+    k = rng.normal(size=(4, 4))
+    outd = np.full_like(d, np.nan)
+    assert lib.gvom_convolve(P(d), P(outd), P(k), 33, 4, None) == 0
+    np.testing.assert_array_equal(outd, convolve(d, k))
+    b = np.zeros((8, 8), np.int32)
+    assert lib.gvom_expand_binary(None, None, 8, 1.0, None) == GVOM_ERR_ARG
+    assert lib.gvom_lowpass_binary(P(b), P(b), 8, -1, 0.5, None) == GVOM_ERR_ARG
+    assert lib.gvom_convolve(P(d), P(outd), P(k), 8, 0, None) == GVOM_ERR_ARG
